@@ -1,0 +1,282 @@
+"""Python binding of the amressif_gb300 C ABI (include/amressif_gpu.h).
+
+The solver itself is C++/CUDA; this module only loads the in-tree shared
+library with ctypes and mirrors the entry points, for the tests and bench.py.
+Loading fails loudly when the library has not been built: there is no CPU
+fallback.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libamressif_gb300.so")
+
+NS_OK = 0
+NS_WARN_PSEUDO_MAXITER = 1
+NS_WARN_PSEUDO_DIVERGED = 2
+NS_ERR_ARG = -1
+NS_ERR_BC = -2
+NS_ERR_CUDA = -3
+NS_ERR_MG_STALL = -4
+NS_ERR_NOMEM = -5
+NS_ERR_STATE = -6
+NS_ERR_UNSUPPORTED = -7
+
+PREC_FP64_EXACT, PREC_FP64, PREC_MIXED = 0, 1, 2
+INIT_CAVITY, INIT_TGV = 0, 1
+FIELD_VEL, FIELD_VEL_PREV, FIELD_PRESSURE, FIELD_PHI, FIELD_VEL_STAR, FIELD_POISSON_RHS, FIELD_CART = range(7)
+
+# every symbol declared in include/amressif_gpu.h
+EXPORTS = [
+    "ns_params_default", "ns_params_parse_file", "ns_ctx_create", "ns_ctx_destroy", "ns_last_error",
+    "ns_get_dt", "ns_get_time", "ns_init_fields", "ns_put_box", "ns_get_box", "ns_set_state",
+    "ns_get_state", "ns_step_begin", "ns_rk_stage", "ns_pseudo_norm", "ns_explicit_predictor",
+    "ns_poisson_rhs", "ns_poisson_solve", "ns_project", "ns_step", "ns_step_host", "ns_sync",
+]
+
+
+class NsError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s (status %d)" % (msg, code))
+        self.code = code
+
+
+class NsParams(ctypes.Structure):
+    _fields_ = [
+        ("dim", ctypes.c_int),
+        ("n_cell", ctypes.c_int),
+        ("max_grid_size", ctypes.c_int * 3),
+        ("prob_lo", ctypes.c_double * 3),
+        ("prob_hi", ctypes.c_double * 3),
+        ("ren", ctypes.c_double),
+        ("vis", ctypes.c_double),
+        ("cfl", ctypes.c_double),
+        ("fixed_dt", ctypes.c_double),
+        ("iter_num", ctypes.c_int),
+        ("momentum_tolerance", ctypes.c_double),
+        ("pseudo_timestepping", ctypes.c_int),
+        ("bc_lo", ctypes.c_int * 3),
+        ("bc_hi", ctypes.c_int * 3),
+        ("inflow_waveform", ctypes.c_double * 3),
+        ("nsteps", ctypes.c_int),
+        ("precision", ctypes.c_int),
+        ("fix_quirks", ctypes.c_int),
+        ("poisson_tol_rel", ctypes.c_double),
+        ("poisson_tol_div", ctypes.c_double),
+        ("poisson_max_cycles", ctypes.c_int),
+        ("dtau_clip", ctypes.c_int),
+    ]
+
+
+class NsStepStats(ctypes.Structure):
+    _fields_ = [
+        ("pseudo_iters", ctypes.c_int),
+        ("norm_error", ctypes.c_double),
+        ("div_before", ctypes.c_double),
+        ("rhs_sum", ctypes.c_double),
+        ("poisson_cycles", ctypes.c_int),
+        ("poisson_res", ctypes.c_double),
+        ("div_after", ctypes.c_double),
+        ("status", ctypes.c_int),
+        ("ms_predictor", ctypes.c_double),
+        ("ms_poisson", ctypes.c_double),
+        ("ms_project", ctypes.c_double),
+    ]
+
+
+_lib = None
+
+
+def lib():
+    """Load the CUDA library (raises if it is missing: no CPU fallback)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("libamressif_gb300.so is not built; run __graft_entry__.build()")
+        L = ctypes.CDLL(LIB_PATH)
+        P = ctypes.POINTER
+        dp = P(ctypes.c_double)
+        vp = ctypes.c_void_p
+        i3 = P(ctypes.c_int)
+        L.ns_params_default.argtypes = [P(NsParams)]
+        L.ns_params_default.restype = None
+        L.ns_params_parse_file.argtypes = [P(NsParams), ctypes.c_char_p]
+        L.ns_ctx_create.argtypes = [P(NsParams), vp, P(vp)]
+        L.ns_ctx_destroy.argtypes = [vp]
+        L.ns_ctx_destroy.restype = None
+        L.ns_last_error.argtypes = [vp]
+        L.ns_last_error.restype = ctypes.c_char_p
+        L.ns_get_dt.argtypes = [vp]
+        L.ns_get_dt.restype = ctypes.c_double
+        L.ns_get_time.argtypes = [vp]
+        L.ns_get_time.restype = ctypes.c_double
+        L.ns_init_fields.argtypes = [vp, ctypes.c_int]
+        L.ns_put_box.argtypes = [vp, ctypes.c_int, ctypes.c_int, dp, i3, i3, ctypes.c_longlong, ctypes.c_longlong, ctypes.c_int]
+        L.ns_get_box.argtypes = [vp, ctypes.c_int, ctypes.c_int, dp, i3, i3, ctypes.c_longlong, ctypes.c_longlong, ctypes.c_int]
+        L.ns_set_state.argtypes = [vp, P(dp), P(dp), dp, ctypes.c_double]
+        L.ns_get_state.argtypes = [vp, P(dp), P(dp), dp, dp]
+        L.ns_step_begin.argtypes = [vp]
+        L.ns_rk_stage.argtypes = [vp, ctypes.c_int]
+        L.ns_pseudo_norm.argtypes = [vp, dp]
+        L.ns_explicit_predictor.argtypes = [vp, dp]
+        L.ns_poisson_rhs.argtypes = [vp, dp, dp]
+        L.ns_poisson_solve.argtypes = [vp, ctypes.c_int, P(ctypes.c_int), dp]
+        L.ns_project.argtypes = [vp, dp]
+        L.ns_step.argtypes = [vp, P(NsStepStats)]
+        L.ns_step_host.argtypes = [vp, P(dp), P(dp), dp, P(NsStepStats)]
+        L.ns_sync.argtypes = [vp]
+        _lib = L
+    return _lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def default_params(**kw):
+    p = NsParams()
+    lib().ns_params_default(ctypes.byref(p))
+    for k, v in kw.items():
+        f = getattr(p, k)
+        if isinstance(f, ctypes.Array):
+            for i, x in enumerate(v):
+                f[i] = x
+        else:
+            setattr(p, k, v)
+    return p
+
+
+def stats_dict(st):
+    return {k: getattr(st, k) for k, _ in NsStepStats._fields_}
+
+
+class Solver:
+    """One device context (ns_ctx). Arrays are dense float64, x fastest."""
+
+    def __init__(self, params, stream=None):
+        self.params = params
+        self.n = params.n_cell
+        self.dim = params.dim
+        h = ctypes.c_void_p()
+        rc = lib().ns_ctx_create(ctypes.byref(params), stream, ctypes.byref(h))
+        if rc != NS_OK:
+            raise NsError(rc, "ns_ctx_create failed")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().ns_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc, what, allow_warn=False):
+        if rc < 0 or (rc > 0 and not allow_warn):
+            msg = lib().ns_last_error(self.h)
+            raise NsError(rc, "%s: %s" % (what, msg.decode() if msg else ""))
+        return rc
+
+    @property
+    def dt(self):
+        return lib().ns_get_dt(self.h)
+
+    @property
+    def time(self):
+        return lib().ns_get_time(self.h)
+
+    def face_shape(self, d):
+        return (self.n + (1 if d == 1 else 0), self.n + (1 if d == 0 else 0))
+
+    def init(self, case):
+        self._check(lib().ns_init_fields(self.h, case), "ns_init_fields")
+
+    def set_state(self, u, u_prev, p, time=0.0):
+        u = [np.ascontiguousarray(a, dtype=np.float64) for a in u]
+        up = [np.ascontiguousarray(a, dtype=np.float64) for a in u_prev]
+        p = np.ascontiguousarray(p, dtype=np.float64)
+        au = (ctypes.POINTER(ctypes.c_double) * 2)(*[_dp(a) for a in u])
+        aup = (ctypes.POINTER(ctypes.c_double) * 2)(*[_dp(a) for a in up])
+        self._check(lib().ns_set_state(self.h, au, aup, _dp(p), time), "ns_set_state")
+
+    def get_state(self):
+        u = [np.zeros(self.face_shape(d)) for d in range(2)]
+        up = [np.zeros(self.face_shape(d)) for d in range(2)]
+        p = np.zeros((self.n, self.n))
+        phi = np.zeros((self.n, self.n))
+        au = (ctypes.POINTER(ctypes.c_double) * 2)(*[_dp(a) for a in u])
+        aup = (ctypes.POINTER(ctypes.c_double) * 2)(*[_dp(a) for a in up])
+        self._check(lib().ns_get_state(self.h, au, aup, _dp(p), _dp(phi)), "ns_get_state")
+        return u, up, p, phi
+
+    def put_field(self, field, comp, arr):
+        arr = np.ascontiguousarray(arr, dtype=np.float64)
+        lo = (ctypes.c_int * 3)(0, 0, 0)
+        hi = (ctypes.c_int * 3)(arr.shape[1] - 1, arr.shape[0] - 1, 0)
+        self._check(lib().ns_put_box(self.h, field, comp, _dp(arr), lo, hi, arr.shape[1], 0, 0), "ns_put_box")
+
+    def get_field(self, field, comp=0):
+        if field in (FIELD_VEL, FIELD_VEL_PREV, FIELD_VEL_STAR):
+            out = np.zeros(self.face_shape(comp))
+        else:
+            out = np.zeros((self.n, self.n))
+        lo = (ctypes.c_int * 3)(0, 0, 0)
+        hi = (ctypes.c_int * 3)(out.shape[1] - 1, out.shape[0] - 1, 0)
+        self._check(lib().ns_get_box(self.h, field, comp, _dp(out), lo, hi, out.shape[1], 0, 0), "ns_get_box")
+        return out
+
+    def step(self, allow_warn=True):
+        st = NsStepStats()
+        rc = lib().ns_step(self.h, ctypes.byref(st))
+        self._check(rc, "ns_step", allow_warn=allow_warn)
+        d = stats_dict(st)
+        d["rc"] = rc
+        return d
+
+    def step_host(self, u, u_prev, p):
+        """End-to-end step from/to host arrays (modified in place)."""
+        au = (ctypes.POINTER(ctypes.c_double) * 2)(*[_dp(a) for a in u])
+        aup = (ctypes.POINTER(ctypes.c_double) * 2)(*[_dp(a) for a in u_prev])
+        st = NsStepStats()
+        rc = lib().ns_step_host(self.h, au, aup, _dp(p), ctypes.byref(st))
+        self._check(rc, "ns_step_host", allow_warn=True)
+        return stats_dict(st)
+
+    def step_begin(self):
+        self._check(lib().ns_step_begin(self.h), "ns_step_begin")
+
+    def rk_stage(self, sub):
+        self._check(lib().ns_rk_stage(self.h, sub), "ns_rk_stage")
+
+    def pseudo_norm(self):
+        v = ctypes.c_double()
+        self._check(lib().ns_pseudo_norm(self.h, ctypes.byref(v)), "ns_pseudo_norm")
+        return v.value
+
+    def explicit_predictor(self):
+        v = ctypes.c_double()
+        self._check(lib().ns_explicit_predictor(self.h, ctypes.byref(v)), "ns_explicit_predictor")
+        return v.value
+
+    def poisson_rhs(self):
+        a, b = ctypes.c_double(), ctypes.c_double()
+        self._check(lib().ns_poisson_rhs(self.h, ctypes.byref(a), ctypes.byref(b)), "ns_poisson_rhs")
+        return a.value, b.value
+
+    def poisson_solve(self, precision=PREC_FP64):
+        it, res = ctypes.c_int(), ctypes.c_double()
+        self._check(lib().ns_poisson_solve(self.h, precision, ctypes.byref(it), ctypes.byref(res)), "ns_poisson_solve")
+        return it.value, res.value
+
+    def project(self):
+        v = ctypes.c_double()
+        self._check(lib().ns_project(self.h, ctypes.byref(v)), "ns_project")
+        return v.value
+
+    def sync(self):
+        self._check(lib().ns_sync(self.h), "ns_sync")

@@ -1,0 +1,38 @@
+// Exact-arithmetic instantiations: compiled with -fmad=false so that every
+// product and sum is rounded separately, in the reference's order.
+#include "launch.h"
+
+namespace ns {
+
+static inline dim3 stage_grid(const Geom& g) {
+  return dim3((g.N + kStageTX - 1) / kStageTX, (g.N + kStageTY - 1) / kStageTY, 1);
+}
+
+cudaError_t launch_stage_exact(int mode, const StageArgs& a, cudaStream_t s) {
+  if (mode == kExactRK)
+    k_stage2d<ArithExact, kExactRK, kStageTX, kStageTY><<<stage_grid(a.g), 256, 0, s>>>(a);
+  else if (mode == kExplicit)
+    k_stage2d<ArithExact, kExplicit, kStageTX, kStageTY><<<stage_grid(a.g), 256, 0, s>>>(a);
+  else
+    return cudaErrorInvalidValue;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_step_begin_exact(const ProjArgs& a, cudaStream_t s) {
+  k_step_begin2d<ArithExact, false><<<1024, 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+static inline dim3 cell_grid(const Geom& g) { return dim3((g.N + 31) / 32, (g.N + 7) / 8, 1); }
+
+cudaError_t launch_poisson_rhs_exact(const ProjArgs& a, cudaStream_t s) {
+  k_poisson_rhs2d<ArithExact><<<cell_grid(a.g), 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_project_exact(const ProjArgs& a, cudaStream_t s) {
+  k_project2d<ArithExact><<<cell_grid(a.g), 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+}  // namespace ns

@@ -1,0 +1,54 @@
+// Host-side launchers of the device kernels. The exact-arithmetic kernels
+// live in kernels_exact.cu (compiled with -fmad=false), the others in
+// kernels_fast.cu.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "mg2d.cuh"
+#include "project2d.cuh"
+#include "stage2d.cuh"
+
+namespace ns {
+
+constexpr int kStageTX = 32, kStageTY = 16;
+
+// kernels_exact.cu
+cudaError_t launch_stage_exact(int mode, const StageArgs& a, cudaStream_t s);
+cudaError_t launch_step_begin_exact(const ProjArgs& a, cudaStream_t s);
+cudaError_t launch_poisson_rhs_exact(const ProjArgs& a, cudaStream_t s);
+cudaError_t launch_project_exact(const ProjArgs& a, cudaStream_t s);
+
+// kernels_fast.cu
+cudaError_t launch_stage_fast(int mode, const StageArgs& a, cudaStream_t s);
+cudaError_t launch_step_begin_fast(const ProjArgs& a, cudaStream_t s);
+cudaError_t launch_poisson_rhs_fast(const ProjArgs& a, cudaStream_t s);
+cudaError_t launch_project_fast(const ProjArgs& a, cudaStream_t s);
+
+template <typename T>
+cudaError_t launch_mg_smooth(const MGLevels<T>& M, int l, int mode, int x_zero, cudaStream_t s);
+template <typename T>
+cudaError_t launch_mg_restrict(const MGLevels<T>& M, int l, cudaStream_t s);
+template <typename T>
+cudaError_t launch_mg_bottom(const MGLevels<T>& M, int lb, int x_zero, cudaStream_t s);
+template <typename T>
+cudaError_t launch_mg_resnorm(const MGLevels<T>& M, double* part, unsigned* counter, double* out, cudaStream_t s);
+
+struct DCArgs {
+  int n;
+  long pitch;
+  int periodic[2];
+  double invh2[2];
+  const double* phi_in;
+  double* phi_out;
+  const float* e;      // FP32 correction (level-0 x of the FP32 hierarchy)
+  float* r32;          // FP32 residual (level-0 f of the FP32 hierarchy)
+  const double* f;
+  const double* fmean;
+  int first;           // phi_in is zero and e is absent
+  double* part;
+  unsigned* counter;
+  double* red_out;     // {max |r|}
+};
+cudaError_t launch_dc_update(const DCArgs& a, cudaStream_t s);
+
+}  // namespace ns

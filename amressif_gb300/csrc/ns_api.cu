@@ -1,0 +1,845 @@
+// C ABI and host driver of the GB300 fractional-step advance.
+//
+// The host side restates main_main's time loop (main.cpp:875-1202) over
+// device-resident fields: one fused kernel per RK pseudo-stage, an 8-byte
+// read-back of the pseudo-increment norm per pseudo-iteration (the loop
+// condition of main.cpp:898), then the Poisson right-hand side, the
+// multigrid solve and the projection.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "../../include/amressif_gpu.h"
+#include "launch.h"
+
+using namespace ns;
+
+struct ns_ctx {
+  ns_params P;
+  Geom g;
+  int N = 0;
+  long pitch = 0;
+  size_t fbytes = 0;  // bytes of one FP64 field
+  cudaStream_t st = nullptr;
+  bool own_stream = false;
+  double dt = 0, time = 0, rk[4] = {0, 0, 0, 0};
+  // FP64 fields
+  double* U[2] = {nullptr, nullptr};
+  double* UP[2] = {nullptr, nullptr};
+  double* DU[2] = {nullptr, nullptr};
+  double* B[3][2] = {{nullptr, nullptr}, {nullptr, nullptr}, {nullptr, nullptr}};
+  double* S[2] = {nullptr, nullptr};
+  double* Pp = nullptr;
+  double* PHI[2] = {nullptr, nullptr};
+  double* F = nullptr;
+  double* CART[2] = {nullptr, nullptr};
+  bool cart_pending = false;
+  // pseudo-iteration state: buffer ids, -1 = UP, 0..2 = B[i]
+  int base = -1, cur = -1;
+  bool in_step = false;
+  bool norm_ready = false;
+  // mixed predictor
+  float* SH[2] = {nullptr, nullptr};
+  float* G0[2] = {nullptr, nullptr};
+  float* E[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+  // multigrid
+  MGLevels<double> M64;
+  MGLevels<float> M32;
+  int lb = 0;
+  int phi_cur = 0;
+  // reductions
+  double* part = nullptr;
+  unsigned* counter = nullptr;
+  double* red = nullptr;    // device scalars
+  double* red_h = nullptr;  // pinned mirror
+  cudaEvent_t ev[4];
+  bool ev_ok = false;
+  std::string err;
+};
+
+namespace {
+
+enum RedSlot { kRedNorm = 0, kRedDivBefore = 1, kRedSum = 2, kRedMean = 3, kRedRes = 4, kRedDivAfter = 5, kRedF = 6 };
+
+int fail(ns_ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+int cuda_check(ns_ctx* c, cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return NS_OK;
+  return fail(c, NS_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(expr, what)                                  \
+  do {                                                  \
+    int _r = cuda_check(c, (expr), what);               \
+    if (_r != NS_OK) return _r;                         \
+  } while (0)
+
+double* face_ptr(ns_ctx* c, int id, int m) { return id < 0 ? c->UP[m] : c->B[id][m]; }
+
+// ghost rule table of one velCart side (utilities.cpp:62-349)
+int make_cart_bc(const ns_params& P, int d, int side, CartBC& b) {
+  const int code = side == 0 ? P.bc_lo[d] : P.bc_hi[d];
+  for (int m = 0; m < 3; ++m) { b.rule[m] = kNeg; b.add[m] = 0.0; }
+  if (code == 111 || code == 135) return NS_OK;
+  bool slip = (code == -135);
+  if (d == 0 && side == 1) {
+    // east wall: the reference tests slip as "== 1" (utilities.cpp:152)
+    if (!P.fix_quirks && code == -135) return NS_ERR_UNSUPPORTED;
+    slip = (code == 1) || (P.fix_quirks && code == -135);
+  }
+  if (slip) {
+    for (int m = 0; m < 3; ++m) b.rule[m] = (m == d) ? kNeg : kPos;
+    return NS_OK;
+  }
+  if (code == 165 || (code == -165 && d == 0 && side == 0)) {
+    for (int m = 0; m < 3; ++m) { b.rule[m] = kInlet; b.add[m] = 2.0; }
+    if (d == 1 && side == 1)
+      for (int m = 0; m < 3; ++m) b.add[m] = 2 * P.inflow_waveform[m];
+    return NS_OK;
+  }
+  return NS_ERR_BC;
+}
+
+long round_up(long x, long a) { return (x + a - 1) / a * a; }
+
+void free_all(ns_ctx* c) {
+  auto F = [](void* p) { if (p) cudaFree(p); };
+  for (int m = 0; m < 2; ++m) {
+    F(c->U[m]); F(c->UP[m]); F(c->DU[m]); F(c->S[m]); F(c->CART[m]); F(c->PHI[m]);
+    for (int i = 0; i < 3; ++i) F(c->B[i][m]);
+    F(c->SH[m]); F(c->G0[m]); F(c->E[0][m]); F(c->E[1][m]);
+  }
+  F(c->Pp); F(c->F);
+  for (int l = 1; l < c->M64.L; ++l) { F(c->M64.x[l]); F(c->M64.f[l]); }
+  for (int l = 0; l < c->M32.L; ++l) { F(c->M32.x[l]); F(c->M32.f[l]); }
+  F(c->part); F(c->counter); F(c->red);
+  if (c->red_h) cudaFreeHost(c->red_h);
+  if (c->ev_ok) for (auto& e : c->ev) cudaEventDestroy(e);
+  if (c->own_stream && c->st) cudaStreamDestroy(c->st);
+}
+
+int alloc_field(ns_ctx* c, double** p) {
+  if (cudaMalloc(p, c->fbytes) != cudaSuccess) return fail(c, NS_ERR_NOMEM, "cudaMalloc failed");
+  if (cudaMemsetAsync(*p, 0, c->fbytes, c->st) != cudaSuccess) return fail(c, NS_ERR_CUDA, "memset failed");
+  return NS_OK;
+}
+
+template <typename T>
+int alloc_levels(ns_ctx* c, MGLevels<T>& M, bool own_level0) {
+  int n = c->N;
+  M.L = 0;
+  M.periodic[0] = c->g.periodic[0];
+  M.periodic[1] = c->g.periodic[1];
+  M.fmean = nullptr;
+  double hx = c->g.dx[0], hy = c->g.dx[1];
+  while (true) {
+    const int l = M.L;
+    if (l >= kMaxLevels) return fail(c, NS_ERR_ARG, "too many multigrid levels");
+    M.n[l] = n;
+    // level 0 shares the row pitch of the velocity / pressure fields
+    M.pitch[l] = (l == 0) ? c->pitch : round_up(n, 32);
+    M.invh2[l][0] = 1.0 / (hx * hx);
+    M.invh2[l][1] = 1.0 / (hy * hy);
+    M.x[l] = nullptr;
+    M.f[l] = nullptr;
+    if (l > 0 || own_level0) {
+      const size_t bytes = (size_t)M.pitch[l] * (n + 1) * sizeof(T);
+      if (cudaMalloc(&M.x[l], bytes) != cudaSuccess || cudaMalloc(&M.f[l], bytes) != cudaSuccess)
+        return fail(c, NS_ERR_NOMEM, "cudaMalloc (multigrid) failed");
+      cudaMemsetAsync(M.x[l], 0, bytes, c->st);
+      cudaMemsetAsync(M.f[l], 0, bytes, c->st);
+    }
+    M.L++;
+    if (!(n % 4 == 0 && n > 4)) break;
+    n /= 2;
+    hx *= 2;
+    hy *= 2;
+  }
+  return NS_OK;
+}
+
+int sync_red(ns_ctx* c, int first, int count) {
+  CK(cudaMemcpyAsync(c->red_h + first, c->red + first, count * sizeof(double), cudaMemcpyDeviceToHost, c->st), "readback");
+  CK(cudaStreamSynchronize(c->st), "stream sync");
+  return NS_OK;
+}
+
+StageArgs base_stage_args(ns_ctx* c) {
+  StageArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.g = c->g;
+  a.p = c->Pp;
+  for (int m = 0; m < 2; ++m) {
+    a.un[m] = c->UP[m];
+    a.du[m] = c->DU[m];
+    a.S[m] = c->S[m];
+  }
+  a.part = c->part;
+  a.counter = c->counter;
+  a.norm_out = c->red + kRedNorm;
+  return a;
+}
+
+int pick_out(int base, int in) {
+  for (int i = 0; i < 3; ++i)
+    if (i != base && i != in) return i;
+  return -2;
+}
+
+}  // namespace
+
+extern "C" {
+
+void ns_params_default(ns_params* p) {
+  std::memset(p, 0, sizeof(*p));
+  p->dim = 2;
+  p->n_cell = 32;
+  p->max_grid_size[0] = 32; p->max_grid_size[1] = 16; p->max_grid_size[2] = 16;
+  for (int d = 0; d < 3; ++d) { p->prob_lo[d] = 0.0; p->prob_hi[d] = 1.0; }
+  p->ren = 100.0;
+  p->vis = 1.0;
+  p->cfl = 0.9;
+  p->fixed_dt = 1.0e-3;
+  p->iter_num = 100;
+  p->momentum_tolerance = 1.e-10;
+  p->pseudo_timestepping = 1;
+  p->bc_lo[0] = 135; p->bc_lo[1] = 135; p->bc_lo[2] = 135;
+  p->bc_hi[0] = 135; p->bc_hi[1] = 165; p->bc_hi[2] = 135;
+  p->inflow_waveform[0] = 1.0;
+  p->nsteps = 11;
+  p->precision = NS_PREC_FP64_EXACT;
+  p->fix_quirks = 0;
+  p->poisson_tol_rel = 1.0e-10;
+  p->poisson_tol_div = 0.0;
+  p->poisson_max_cycles = 200;
+  p->dtau_clip = 0;
+}
+
+int ns_params_parse_file(ns_params* p, const char* path) {
+  std::ifstream in(path);
+  if (!in) return NS_ERR_ARG;
+  std::string line;
+  while (std::getline(in, line)) {
+    const size_t h = line.find('#');
+    if (h != std::string::npos) line = line.substr(0, h);
+    const size_t eq = line.find('=');
+    if (eq == std::string::npos) continue;
+    std::string key = line.substr(0, eq), val = line.substr(eq + 1);
+    key.erase(0, key.find_first_not_of(" \t"));
+    key.erase(key.find_last_not_of(" \t") + 1);
+    std::istringstream vs(val);
+    std::vector<double> v;
+    std::string tok;
+    bool bad = false;
+    while (vs >> tok) {
+      char* end = nullptr;
+      const double x = std::strtod(tok.c_str(), &end);
+      if (end == tok.c_str() || *end != '\0') { bad = true; break; }
+      v.push_back(x);
+    }
+    if (bad || v.empty()) continue;  // e.g. "chk_int = = 10" of the shipped inputs
+    auto I = [&](int k) { return (int)v[std::min<size_t>(k, v.size() - 1)]; };
+    auto D = [&](int k) { return v[std::min<size_t>(k, v.size() - 1)]; };
+    if (key == "n_cell") p->n_cell = I(0);
+    else if (key == "max_grid_size_x") p->max_grid_size[0] = I(0);
+    else if (key == "max_grid_size_y") p->max_grid_size[1] = I(0);
+    else if (key == "max_grid_size_z") p->max_grid_size[2] = I(0);
+    else if (key == "nsteps") p->nsteps = I(0);
+    else if (key == "fixed_dt") p->fixed_dt = D(0);
+    else if (key == "cfl") p->cfl = D(0);
+    else if (key == "IterNum") p->iter_num = I(0);
+    else if (key == "ren") p->ren = D(0);
+    else if (key == "vis") p->vis = D(0);
+    else if (key == "momentum_tolerance") p->momentum_tolerance = D(0);
+    else if (key == "PSEUDO_TIMESTEPPING") p->pseudo_timestepping = I(0);
+    else if (key == "phy_bc_lo") for (int d = 0; d < 3 && d < (int)v.size(); ++d) p->bc_lo[d] = I(d);
+    else if (key == "phy_bc_hi") for (int d = 0; d < 3 && d < (int)v.size(); ++d) p->bc_hi[d] = I(d);
+    else if (key == "inflow_waveform") for (int d = 0; d < 3 && d < (int)v.size(); ++d) p->inflow_waveform[d] = D(d);
+    else if (key == "lo_phy_dim") for (int d = 0; d < 3 && d < (int)v.size(); ++d) p->prob_lo[d] = D(d);
+    else if (key == "hi_phy_dim") for (int d = 0; d < 3 && d < (int)v.size(); ++d) p->prob_hi[d] = D(d);
+  }
+  return NS_OK;
+}
+
+int ns_ctx_create(const ns_params* p, void* stream, ns_ctx** out) {
+  if (!p || !out) return NS_ERR_ARG;
+  *out = nullptr;
+  if (p->dim != 2) return NS_ERR_UNSUPPORTED;
+  if (p->n_cell < 8 || p->n_cell % 8 != 0) return NS_ERR_ARG;
+  if (p->ren <= 0) return NS_ERR_ARG;
+  ns_ctx* c = new ns_ctx();
+  c->P = *p;
+  const int N = p->n_cell;
+  c->N = N;
+  c->pitch = round_up(N + 1, 32);
+  c->fbytes = (size_t)c->pitch * (N + 1) * sizeof(double);
+  Geom& g = c->g;
+  std::memset(&g, 0, sizeof(g));
+  g.N = N;
+  g.dim = 2;
+  g.pitch = c->pitch;
+  g.plane = c->pitch * (N + 1);
+  for (int d = 0; d < 3; ++d) g.dx[d] = (p->prob_hi[d] - p->prob_lo[d]) / (double)N;
+  for (int d = 0; d < 2; ++d) {
+    const bool lo111 = p->bc_lo[d] == 111, hi111 = p->bc_hi[d] == 111;
+    if (lo111 != hi111) { delete c; return NS_ERR_BC; }
+    g.periodic[d] = lo111 && hi111;
+    if (p->pseudo_timestepping == 0)
+      g.flux_ghost[d] = g.periodic[d] ? kWrap : kZero;  // explicit mode: no reflection (quirk Q3)
+    else
+      g.flux_ghost[d] = (g.periodic[d] && p->fix_quirks) ? kWrap : kReflect;
+    g.ctx_mirror[d] = (g.periodic[d] && p->fix_quirks) ? 0 : 1;
+    for (int side = 0; side < 2; ++side) {
+      const int r = make_cart_bc(*p, d, side, g.bc[2 * d + side]);
+      if (r != NS_OK) {
+        delete c;
+        return r;
+      }
+    }
+  }
+  // dt rule of main.cpp:285-294
+  const double coeff = 1.0 / (g.dx[0] * g.dx[0]) + 1.0 / (g.dx[1] * g.dx[1]);
+  c->dt = p->fixed_dt != -1.0 ? p->fixed_dt : p->cfl / (2.0 * coeff);
+  g.dt = c->dt;
+  g.ren = p->ren;
+  // RK coefficients (main.cpp:861-870), optionally clipped to 0.9 x the RK4
+  // real-axis stability limit of the stiffest mode
+  double d_tau = 0.4 * c->dt;
+  if (p->dtau_clip) {
+    const double lam = 4.0 / p->ren * coeff + 1.5 / c->dt;
+    d_tau = std::min(d_tau, 0.9 * 2.785 / lam);
+  }
+  c->rk[0] = d_tau * 0.25;
+  c->rk[1] = d_tau * (1.0 / 3.0);
+  c->rk[2] = d_tau * 0.5;
+  c->rk[3] = d_tau * 1.0;
+
+  if (stream) {
+    c->st = (cudaStream_t)stream;
+  } else {
+    if (cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) != cudaSuccess) { delete c; return NS_ERR_CUDA; }
+    c->own_stream = true;
+  }
+  int r = NS_OK;
+  for (int m = 0; m < 2 && r == NS_OK; ++m) {
+    r = alloc_field(c, &c->U[m]);
+    if (r == NS_OK) r = alloc_field(c, &c->UP[m]);
+    if (r == NS_OK) r = alloc_field(c, &c->DU[m]);
+    if (r == NS_OK) r = alloc_field(c, &c->S[m]);
+    if (r == NS_OK) r = alloc_field(c, &c->PHI[m]);
+    for (int i = 0; i < 3 && r == NS_OK; ++i) r = alloc_field(c, &c->B[i][m]);
+  }
+  if (r == NS_OK) r = alloc_field(c, &c->Pp);
+  if (r == NS_OK) r = alloc_field(c, &c->F);
+  if (r == NS_OK) r = alloc_levels<double>(c, c->M64, false);
+  if (r == NS_OK) r = alloc_levels<float>(c, c->M32, true);
+  if (r == NS_OK) {
+    // reduction scratch: 2 partials per block of the largest launch
+    const size_t nb = (size_t)((N + 31) / 32) * ((N + 7) / 8) + 1024;
+    if (cudaMalloc(&c->part, 4 * nb * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&c->counter, 64 * sizeof(unsigned)) != cudaSuccess ||
+        cudaMalloc(&c->red, 16 * sizeof(double)) != cudaSuccess ||
+        cudaMallocHost(&c->red_h, 16 * sizeof(double)) != cudaSuccess)
+      r = fail(c, NS_ERR_NOMEM, "cudaMalloc (reductions) failed");
+    else {
+      cudaMemsetAsync(c->counter, 0, 64 * sizeof(unsigned), c->st);
+      cudaMemsetAsync(c->red, 0, 16 * sizeof(double), c->st);
+    }
+  }
+  if (r == NS_OK) {
+    bool ok = true;
+    for (auto& e : c->ev) ok = ok && cudaEventCreate(&e) == cudaSuccess;
+    c->ev_ok = ok;
+    c->M64.x[0] = c->PHI[0];
+    c->M64.f[0] = c->F;
+    c->M64.fmean = c->red + kRedMean;
+    c->lb = 0;
+    while (c->lb < c->M64.L && c->M64.n[c->lb] > kBottomN) c->lb++;
+    if (cudaStreamSynchronize(c->st) != cudaSuccess) r = fail(c, NS_ERR_CUDA, "init sync failed");
+  }
+  if (r != NS_OK) {
+    free_all(c);
+    delete c;
+    return r;
+  }
+  *out = c;
+  return NS_OK;
+}
+
+void ns_ctx_destroy(ns_ctx* c) {
+  if (!c) return;
+  if (c->st) cudaStreamSynchronize(c->st);
+  free_all(c);
+  delete c;
+}
+
+const char* ns_last_error(const ns_ctx* c) { return c ? c->err.c_str() : "null context"; }
+double ns_get_dt(const ns_ctx* c) { return c ? c->dt : 0.0; }
+double ns_get_time(const ns_ctx* c) { return c ? c->time : 0.0; }
+
+int ns_sync(ns_ctx* c) {
+  if (!c) return NS_ERR_ARG;
+  CK(cudaStreamSynchronize(c->st), "stream sync");
+  return NS_OK;
+}
+
+// ---- field movement -----------------------------------------------------------
+
+static double* field_ptr(ns_ctx* c, int field, int comp, bool* is_face) {
+  *is_face = false;
+  switch (field) {
+    case NS_FIELD_VEL: *is_face = true; return comp < 2 ? c->U[comp] : nullptr;
+    case NS_FIELD_VEL_PREV: *is_face = true; return comp < 2 ? c->UP[comp] : nullptr;
+    case NS_FIELD_VEL_STAR: *is_face = true; return comp < 2 ? face_ptr(c, c->cur, comp) : nullptr;
+    case NS_FIELD_PRESSURE: return c->Pp;
+    case NS_FIELD_PHI: return c->PHI[c->phi_cur];
+    case NS_FIELD_POISSON_RHS: return c->F;
+    case NS_FIELD_CART: return nullptr;
+    default: return nullptr;
+  }
+}
+
+static int box_copy(ns_ctx* c, int field, int comp, double* data, const int lo[3], const int hi[3], long long jstride,
+                    long long kstride, int where_device, bool put) {
+  (void)kstride;
+  if (!c || !data || !lo || !hi || comp < 0 || comp > 1) return NS_ERR_ARG;
+  if (field == NS_FIELD_CART) {
+    if (!put) return NS_ERR_ARG;
+    for (int m = 0; m < 2; ++m)
+      if (!c->CART[m]) {
+        int r = alloc_field(c, &c->CART[m]);
+        if (r != NS_OK) return r;
+      }
+    c->cart_pending = true;
+  }
+  bool face = false;
+  double* dev = (field == NS_FIELD_CART) ? c->CART[comp] : field_ptr(c, field, comp, &face);
+  if (!dev) return NS_ERR_ARG;
+  const int ni = c->N + ((face && comp == 0) ? 1 : 0);
+  const int nj = c->N + ((face && comp == 1) ? 1 : 0);
+  if (lo[0] < 0 || lo[1] < 0 || hi[0] >= ni || hi[1] >= nj || hi[0] < lo[0] || hi[1] < lo[1]) return NS_ERR_ARG;
+  const size_t w = (size_t)(hi[0] - lo[0] + 1) * sizeof(double);
+  const size_t h = (size_t)(hi[1] - lo[1] + 1);
+  double* d = dev + (long)lo[1] * c->pitch + lo[0];
+  const cudaMemcpyKind kind = where_device ? cudaMemcpyDeviceToDevice : (put ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost);
+  cudaError_t e = put ? cudaMemcpy2DAsync(d, c->pitch * sizeof(double), data, (size_t)jstride * sizeof(double), w, h, kind, c->st)
+                      : cudaMemcpy2DAsync(data, (size_t)jstride * sizeof(double), d, c->pitch * sizeof(double), w, h, kind, c->st);
+  return cuda_check(c, e, "box copy");
+}
+
+int ns_put_box(ns_ctx* c, int field, int comp, const double* data, const int lo[3], const int hi[3], long long jstride,
+               long long kstride, int where_device) {
+  int r = box_copy(c, field, comp, const_cast<double*>(data), lo, hi, jstride, kstride, where_device, true);
+  if (r == NS_OK && !where_device) r = ns_sync(c);  // the caller may reuse its buffer on return
+  return r;
+}
+
+int ns_get_box(ns_ctx* c, int field, int comp, double* data, const int lo[3], const int hi[3], long long jstride,
+               long long kstride, int where_device) {
+  int r = box_copy(c, field, comp, data, lo, hi, jstride, kstride, where_device, false);
+  if (r == NS_OK) r = ns_sync(c);
+  return r;
+}
+
+int ns_set_state(ns_ctx* c, const double* const* u, const double* const* u_prev, const double* p, double time) {
+  if (!c || !u || !u_prev || !p) return NS_ERR_ARG;
+  const int N = c->N;
+  for (int m = 0; m < 2; ++m) {
+    const int lo[3] = {0, 0, 0};
+    const int hi[3] = {N - 1 + (m == 0), N - 1 + (m == 1), 0};
+    const long long js = N + (m == 0);
+    int r = box_copy(c, NS_FIELD_VEL, m, const_cast<double*>(u[m]), lo, hi, js, 0, 0, true);
+    if (r == NS_OK) r = box_copy(c, NS_FIELD_VEL_PREV, m, const_cast<double*>(u_prev[m]), lo, hi, js, 0, 0, true);
+    if (r != NS_OK) return r;
+  }
+  const int lo[3] = {0, 0, 0}, hi[3] = {N - 1, N - 1, 0};
+  int r = box_copy(c, NS_FIELD_PRESSURE, 0, const_cast<double*>(p), lo, hi, N, 0, 0, true);
+  if (r != NS_OK) return r;
+  for (int m = 0; m < 2; ++m) CK(cudaMemsetAsync(c->PHI[m], 0, c->fbytes, c->st), "memset phi");
+  c->time = time;
+  c->in_step = false;
+  c->cart_pending = false;
+  return ns_sync(c);
+}
+
+int ns_get_state(ns_ctx* c, double* const* u, double* const* u_prev, double* p, double* phi) {
+  if (!c) return NS_ERR_ARG;
+  const int N = c->N;
+  for (int m = 0; m < 2; ++m) {
+    const int lo[3] = {0, 0, 0};
+    const int hi[3] = {N - 1 + (m == 0), N - 1 + (m == 1), 0};
+    const long long js = N + (m == 0);
+    if (u && u[m]) { int r = box_copy(c, NS_FIELD_VEL, m, u[m], lo, hi, js, 0, 0, false); if (r) return r; }
+    if (u_prev && u_prev[m]) { int r = box_copy(c, NS_FIELD_VEL_PREV, m, u_prev[m], lo, hi, js, 0, 0, false); if (r) return r; }
+  }
+  const int lo[3] = {0, 0, 0}, hi[3] = {N - 1, N - 1, 0};
+  if (p) { int r = box_copy(c, NS_FIELD_PRESSURE, 0, p, lo, hi, N, 0, 0, false); if (r) return r; }
+  if (phi) { int r = box_copy(c, NS_FIELD_PHI, 0, phi, lo, hi, N, 0, 0, false); if (r) return r; }
+  return ns_sync(c);
+}
+
+int ns_init_fields(ns_ctx* c, int init_case) {
+  if (!c || (init_case != NS_INIT_CAVITY && init_case != NS_INIT_TGV)) return NS_ERR_ARG;
+  // hybrid_grid_init (fn_init.cpp:61-229, kn_init.H:8-37), evaluated on the
+  // host with the C library's sin/cos/exp and uploaded.
+  const int N = c->N;
+  const double* lo = c->P.prob_lo;
+  const double dx = c->g.dx[0], dy = c->g.dx[1], dt = c->dt, t0 = 0.0;
+  const double nu_decay = c->P.fix_quirks ? 1.0 / c->P.ren : 1.0;  // the reference hard-codes nu = 1
+  std::vector<double> u((size_t)(N + 1) * N), v((size_t)N * (N + 1)), up(u.size()), vp(v.size());
+  std::vector<double> p((size_t)N * N, 0.0), cu((size_t)N * N, 0.0), cv((size_t)N * N, 0.0);
+  const bool tgv = init_case == NS_INIT_TGV;
+  for (int j = 0; j < N; ++j)
+    for (int i = 0; i <= N; ++i) {
+      const double x = lo[0] + (i + 0.0) * dx, y = lo[1] + (j + 0.5) * dy;
+      u[(size_t)j * (N + 1) + i] = tgv ? std::sin(x) * std::cos(y) : 0.0;
+      up[(size_t)j * (N + 1) + i] = tgv ? std::sin(x) * std::cos(y) * std::exp(-2.0 * nu_decay * (t0 - dt)) : 0.0;
+    }
+  for (int j = 0; j <= N; ++j)
+    for (int i = 0; i < N; ++i) {
+      const double x = lo[0] + (i + 0.5) * dx, y = lo[1] + (j + 0.0) * dy;
+      v[(size_t)j * N + i] = tgv ? -std::cos(x) * std::sin(y) : 0.0;
+      vp[(size_t)j * N + i] = tgv ? -std::cos(x) * std::sin(y) * std::exp(-2.0 * nu_decay * (t0 - dt)) : 0.0;
+    }
+  for (int j = 0; j < N; ++j)
+    for (int i = 0; i < N; ++i) {
+      const double x = lo[0] + (i + 0.5) * dx, y = lo[1] + (j + 0.5) * dy;
+      if (tgv) {
+        cu[(size_t)j * N + i] = std::sin(x) * std::cos(y);
+        cv[(size_t)j * N + i] = -std::cos(x) * std::sin(y);
+        p[(size_t)j * N + i] = 0.25 * (std::cos(2.0 * x) + std::cos(2.0 * y));
+      }
+    }
+  const double* uu[2] = {u.data(), v.data()};
+  const double* uup[2] = {up.data(), vp.data()};
+  int r = ns_set_state(c, uu, uup, p.data(), 0.0);
+  if (r != NS_OK) return r;
+  // the reference sets velCart analytically at init (not by cont2cart)
+  const int l0[3] = {0, 0, 0}, h0[3] = {N - 1, N - 1, 0};
+  r = ns_put_box(c, NS_FIELD_CART, 0, cu.data(), l0, h0, N, 0, 0);
+  if (r == NS_OK) r = ns_put_box(c, NS_FIELD_CART, 1, cv.data(), l0, h0, N, 0, 0);
+  return r;
+}
+
+// ---- building blocks --------------------------------------------------------
+
+int ns_step_begin(ns_ctx* c) {
+  if (!c) return NS_ERR_ARG;
+  ProjArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.g = c->g;
+  for (int m = 0; m < 2; ++m) {
+    a.u[m] = c->U[m];
+    a.uprev[m] = c->UP[m];
+    a.du[m] = c->DU[m];
+    a.S[m] = c->S[m];
+  }
+  a.p = c->Pp;
+  cudaError_t e = (c->P.precision == NS_PREC_FP64_EXACT) ? launch_step_begin_exact(a, c->st) : launch_step_begin_fast(a, c->st);
+  CK(e, "step_begin");
+  // velContPrev <- velCont, velStar <- velCont: the old u^{n-1} buffer becomes
+  // the target of the projection
+  for (int m = 0; m < 2; ++m) std::swap(c->U[m], c->UP[m]);
+  c->base = -1;
+  c->cur = -1;
+  c->time += c->dt;
+  c->in_step = true;
+  c->norm_ready = false;
+  return NS_OK;
+}
+
+static int launch_rk(ns_ctx* c, int sub, bool use_cart) {
+  const int in = c->cur;
+  const int outb = pick_out(c->base, in);
+  StageArgs a = base_stage_args(c);
+  for (int m = 0; m < 2; ++m) {
+    a.us[m] = face_ptr(c, in, m);
+    a.ub[m] = face_ptr(c, c->base, m);
+    a.out[m] = c->B[outb][m];
+    a.cart[m] = use_cart ? c->CART[m] : nullptr;
+  }
+  a.rk = c->rk[sub];
+  a.do_norm = (sub == 3);
+  const int mode = (c->P.precision == NS_PREC_FP64_EXACT) ? kExactRK : kFastRK;
+  cudaError_t e = (mode == kExactRK) ? launch_stage_exact(mode, a, c->st) : launch_stage_fast(mode, a, c->st);
+  CK(e, "rk stage");
+  c->cur = outb;
+  return NS_OK;
+}
+
+int ns_rk_stage(ns_ctx* c, int sub) {
+  if (!c || sub < 0 || sub > 3) return NS_ERR_ARG;
+  if (!c->in_step) return fail(c, NS_ERR_STATE, "ns_rk_stage before ns_step_begin");
+  const bool use_cart = c->cart_pending;
+  int r = launch_rk(c, sub, use_cart);
+  if (r == NS_OK && use_cart) c->cart_pending = false;
+  if (r == NS_OK && sub == 3) c->norm_ready = true;
+  return r;
+}
+
+int ns_pseudo_norm(ns_ctx* c, double* norm) {
+  if (!c) return NS_ERR_ARG;
+  if (!c->norm_ready) return fail(c, NS_ERR_STATE, "ns_pseudo_norm needs stage 3 first");
+  int r = sync_red(c, kRedNorm, 1);
+  if (r != NS_OK) return r;
+  if (norm) *norm = c->red_h[kRedNorm];
+  c->base = c->cur;  // velCont <- velStar (main.cpp:1023-1026)
+  c->norm_ready = false;
+  return NS_OK;
+}
+
+int ns_explicit_predictor(ns_ctx* c, double* norm) {
+  if (!c) return NS_ERR_ARG;
+  if (!c->in_step) return fail(c, NS_ERR_STATE, "explicit predictor before ns_step_begin");
+  const int in = c->cur;
+  const int outb = pick_out(c->base, in);
+  StageArgs a = base_stage_args(c);
+  for (int m = 0; m < 2; ++m) {
+    a.us[m] = face_ptr(c, in, m);
+    a.ub[m] = face_ptr(c, c->base, m);
+    a.out[m] = c->B[outb][m];
+    a.cart[m] = c->cart_pending ? c->CART[m] : nullptr;
+  }
+  a.do_norm = 1;
+  CK(launch_stage_exact(kExplicit, a, c->st), "explicit stage");
+  c->cart_pending = false;
+  c->cur = outb;
+  int r = sync_red(c, kRedNorm, 1);
+  if (r != NS_OK) return r;
+  if (norm) *norm = c->red_h[kRedNorm];
+  c->base = c->cur;
+  return NS_OK;
+}
+
+static int poisson_rhs_async(ns_ctx* c) {
+  ProjArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.g = c->g;
+  for (int m = 0; m < 2; ++m) a.u[m] = face_ptr(c, c->cur, m);
+  a.f = c->F;
+  a.part = c->part;
+  a.counter = c->counter;
+  a.red_out = c->red + kRedDivBefore;  // {max|div|, sum}
+  cudaError_t e = (c->P.precision == NS_PREC_FP64_EXACT) ? launch_poisson_rhs_exact(a, c->st) : launch_poisson_rhs_fast(a, c->st);
+  return cuda_check(c, e, "poisson rhs");
+}
+
+int ns_poisson_rhs(ns_ctx* c, double* divmax, double* sum) {
+  if (!c) return NS_ERR_ARG;
+  int r = poisson_rhs_async(c);
+  if (r == NS_OK) r = sync_red(c, kRedDivBefore, 2);
+  if (r != NS_OK) return r;
+  if (divmax) *divmax = c->red_h[kRedDivBefore];
+  if (sum) *sum = c->red_h[kRedSum];
+  return NS_OK;
+}
+
+}  // extern "C"
+
+template <typename T>
+static int vcycle(ns_ctx* c, MGLevels<T>& M, int x0_zero) {
+  for (int l = 0; l < c->lb; ++l) {
+    CK(launch_mg_smooth<T>(M, l, 0, (l > 0) ? 1 : x0_zero, c->st), "mg smooth");
+    CK(launch_mg_restrict<T>(M, l, c->st), "mg restrict");
+  }
+  CK(launch_mg_bottom<T>(M, c->lb, (c->lb > 0) ? 1 : x0_zero, c->st), "mg bottom");
+  for (int l = c->lb - 1; l >= 0; --l) CK(launch_mg_smooth<T>(M, l, 1, 0, c->st), "mg prolong+smooth");
+  return NS_OK;
+}
+
+// mean of f (singular problem, AMReX makes the RHS solvable) written to red[kRedMean]
+__global__ void k_set_mean(double* red, double inv_n) { red[kRedMean] = red[kRedSum] * inv_n; }
+
+extern "C" {
+
+int ns_poisson_solve(ns_ctx* c, int precision, int* cycles, double* res) {
+  if (!c) return NS_ERR_ARG;
+  const double nn = (double)c->N * (double)c->N;
+  k_set_mean<<<1, 1, 0, c->st>>>(c->red, 1.0 / nn);
+  CK(cudaGetLastError(), "set mean");
+  const int maxc = std::max(1, c->P.poisson_max_cycles);
+  const double div_tol_res = c->P.poisson_tol_div > 0 ? c->P.poisson_tol_div * 1.5 / c->dt : 0.0;
+  double rnorm0 = 0.0, rn = 0.0;
+  int ncyc = 0;
+  int status = NS_OK;
+  if (precision == NS_PREC_MIXED) {
+    // FP32 V-cycles inside an FP64 defect correction
+    DCArgs d;
+    std::memset(&d, 0, sizeof(d));
+    d.n = c->N;
+    d.pitch = c->pitch;
+    d.periodic[0] = c->g.periodic[0];
+    d.periodic[1] = c->g.periodic[1];
+    d.invh2[0] = c->M64.invh2[0][0];
+    d.invh2[1] = c->M64.invh2[0][1];
+    d.f = c->F;
+    d.fmean = c->red + kRedMean;
+    d.part = c->part;
+    d.counter = c->counter;
+    d.red_out = c->red + kRedRes;
+    d.e = c->M32.x[0];
+    d.r32 = c->M32.f[0];
+    // M32 level 0 uses the FP64 pitch of the context (allocated with round_up(N,32))
+    int pc = c->phi_cur;
+    d.phi_in = c->PHI[pc];
+    d.phi_out = c->PHI[pc];
+    d.first = 1;
+    CK(launch_dc_update(d, c->st), "dc update");
+    int r = sync_red(c, kRedRes, 1);
+    if (r != NS_OK) return r;
+    rnorm0 = c->red_h[kRedRes];
+    rn = rnorm0;
+    const double tol = std::max(c->P.poisson_tol_rel * rnorm0, 0.0);
+    auto done = [&](double x) { return x <= tol && (div_tol_res <= 0 || x <= div_tol_res); };
+    double best = rn;
+    int stall = 0;
+    while (!done(rn) && rnorm0 > 0) {
+      if (ncyc >= maxc) { status = NS_ERR_MG_STALL; break; }
+      int r2 = vcycle<float>(c, c->M32, 1);
+      if (r2 != NS_OK) return r2;
+      d.first = 0;
+      d.phi_in = c->PHI[pc];
+      d.phi_out = c->PHI[1 - pc];
+      CK(launch_dc_update(d, c->st), "dc update");
+      pc = 1 - pc;
+      ++ncyc;
+      r2 = sync_red(c, kRedRes, 1);
+      if (r2 != NS_OK) return r2;
+      rn = c->red_h[kRedRes];
+      if (rn < 0.5 * best) { best = rn; stall = 0; } else if (++stall >= 6) { status = NS_ERR_MG_STALL; break; }
+    }
+    c->phi_cur = pc;
+  } else {
+    c->phi_cur = 0;
+    c->M64.x[0] = c->PHI[0];
+    CK(cudaMemsetAsync(c->PHI[0], 0, c->fbytes, c->st), "memset phi");  // poisson.cpp:63
+    CK(launch_mg_resnorm<double>(c->M64, c->part, c->counter, c->red + kRedRes, c->st), "resnorm");
+    int r = sync_red(c, kRedRes, 1);
+    if (r != NS_OK) return r;
+    rnorm0 = c->red_h[kRedRes];
+    rn = rnorm0;
+    const double tol = c->P.poisson_tol_rel * rnorm0;
+    auto done = [&](double x) { return x <= tol && (div_tol_res <= 0 || x <= div_tol_res); };
+    double best = rn;
+    int stall = 0;
+    while (!done(rn) && rnorm0 > 0) {
+      if (ncyc >= maxc) { status = NS_ERR_MG_STALL; break; }
+      int r2 = vcycle<double>(c, c->M64, ncyc == 0 ? 1 : 0);
+      if (r2 != NS_OK) return r2;
+      ++ncyc;
+      CK(launch_mg_resnorm<double>(c->M64, c->part, c->counter, c->red + kRedRes, c->st), "resnorm");
+      r2 = sync_red(c, kRedRes, 1);
+      if (r2 != NS_OK) return r2;
+      rn = c->red_h[kRedRes];
+      if (rn < 0.5 * best) { best = rn; stall = 0; } else if (++stall >= 6) { status = NS_ERR_MG_STALL; break; }
+    }
+  }
+  if (cycles) *cycles = ncyc;
+  if (res) *res = rnorm0 > 0 ? rn / rnorm0 : 0.0;
+  if (status != NS_OK) c->err = "Poisson residual stalled before the tolerance";
+  return status;
+}
+
+static int project_async(ns_ctx* c) {
+  ProjArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.g = c->g;
+  for (int m = 0; m < 2; ++m) {
+    a.u[m] = face_ptr(c, c->cur, m);
+    a.uout[m] = c->U[m];
+  }
+  a.p = c->Pp;
+  a.pw = c->Pp;
+  a.phi = c->PHI[c->phi_cur];
+  a.part = c->part;
+  a.counter = c->counter;
+  a.red_out = c->red + kRedDivAfter;
+  cudaError_t e = (c->P.precision == NS_PREC_FP64_EXACT) ? launch_project_exact(a, c->st) : launch_project_fast(a, c->st);
+  return cuda_check(c, e, "project");
+}
+
+int ns_project(ns_ctx* c, double* divmax) {
+  if (!c) return NS_ERR_ARG;
+  int r = project_async(c);
+  if (r == NS_OK) r = sync_red(c, kRedDivAfter, 1);
+  if (r != NS_OK) return r;
+  if (divmax) *divmax = c->red_h[kRedDivAfter];
+  c->in_step = false;
+  return NS_OK;
+}
+
+int ns_step(ns_ctx* c, ns_step_stats* stats) {
+  if (!c) return NS_ERR_ARG;
+  ns_step_stats s;
+  std::memset(&s, 0, sizeof(s));
+  if (c->ev_ok) cudaEventRecord(c->ev[0], c->st);
+  int r = ns_step_begin(c);
+  if (r != NS_OK) return r;
+  int countIter = 0;
+  double normError = 1.e9;
+  while (normError > c->P.momentum_tolerance) {
+    if (c->P.pseudo_timestepping == 0) {
+      r = ns_explicit_predictor(c, &normError);
+      if (r != NS_OK) return r;
+      countIter = 1;
+      break;
+    }
+    for (int sub = 0; sub < 4; ++sub) {
+      r = ns_rk_stage(c, sub);
+      if (r != NS_OK) return r;
+    }
+    r = ns_pseudo_norm(c, &normError);
+    if (r != NS_OK) return r;
+    countIter++;
+    if (countIter > c->P.iter_num) { s.status = NS_WARN_PSEUDO_MAXITER; break; }
+    if (normError > 1.e2) { s.status = NS_WARN_PSEUDO_DIVERGED; break; }
+  }
+  s.pseudo_iters = countIter;
+  s.norm_error = normError;
+  if (c->ev_ok) cudaEventRecord(c->ev[1], c->st);
+  r = ns_poisson_rhs(c, &s.div_before, &s.rhs_sum);
+  if (r != NS_OK) return r;
+  const int prec = (c->P.precision == NS_PREC_MIXED) ? NS_PREC_MIXED : NS_PREC_FP64;
+  r = ns_poisson_solve(c, prec, &s.poisson_cycles, &s.poisson_res);
+  if (r != NS_OK && r != NS_ERR_MG_STALL) return r;
+  const int mg_status = r;
+  if (c->ev_ok) cudaEventRecord(c->ev[2], c->st);
+  r = ns_project(c, &s.div_after);
+  if (r != NS_OK) return r;
+  if (c->ev_ok) {
+    cudaEventRecord(c->ev[3], c->st);
+    cudaEventSynchronize(c->ev[3]);
+    float a = 0, b = 0, d = 0;
+    cudaEventElapsedTime(&a, c->ev[0], c->ev[1]);
+    cudaEventElapsedTime(&b, c->ev[1], c->ev[2]);
+    cudaEventElapsedTime(&d, c->ev[2], c->ev[3]);
+    s.ms_predictor = a; s.ms_poisson = b; s.ms_project = d;
+  }
+  if (stats) *stats = s;
+  if (mg_status != NS_OK) return mg_status;
+  return s.status;
+}
+
+int ns_step_host(ns_ctx* c, double* const* u, double* const* u_prev, double* p, ns_step_stats* stats) {
+  if (!c || !u || !u_prev || !p) return NS_ERR_ARG;
+  const double t = c->time;
+  int r = ns_set_state(c, u, u_prev, p, t);
+  if (r != NS_OK) return r;
+  const int st = ns_step(c, stats);
+  if (st < 0) return st;
+  r = ns_get_state(c, u, u_prev, p, nullptr);
+  return r != NS_OK ? r : st;
+}
+
+}  // extern "C"

@@ -1,0 +1,126 @@
+// Shared definitions of the GB300 fractional-step kernels (2D MAC grid).
+//
+// Layout in HBM: every level-0 field is a dense row-major array with one row
+// pitch `pitch` (elements, a multiple of 32 so that rows start on 256-byte
+// boundaries). x-face velocity u(i,j): i in [0,N], j in [0,N); y-face
+// velocity v(i,j): i in [0,N), j in [0,N]; cell fields (p, phi, f): [0,N)^2.
+// Element (i,j) lives at j*pitch + i. No ghost cells are stored: boundary
+// rules are applied while a tile is staged in shared memory.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace ns {
+
+// Ghost rule of the cell-centred velocity on one domain side for one
+// component (utilities.cpp:62-349): ghost = -q, +q, or add - q (inlets), with
+// q the mirror cell value.
+enum CartRule : int { kNeg = 0, kPos = 1, kInlet = 2 };
+
+// Ghost rule of the cell-centred total flux across a domain side.
+enum FluxGhost : int { kReflect = 0, kWrap = 1, kZero = 2 };
+
+struct CartBC {
+  int rule[3];
+  double add[3];
+};
+
+struct Geom {
+  int N;          // cells per side
+  int dim;        // 2 (3D kernels use the same struct)
+  long pitch;     // row pitch of level-0 arrays (elements)
+  long plane;     // plane stride (3D); pitch * (N+1)
+  double dx[3];
+  double dt, ren;
+  int periodic[3];
+  int flux_ghost[3];  // per direction: kReflect (quirk Q1), kWrap, kZero
+  int ctx_mirror[3];  // 1: p/phi ghosts mirrored (quirk Q2), 0: periodic wrap
+  CartBC bc[6];       // xlo, xhi, ylo, yhi, zlo, zhi
+};
+
+// periodic index in [0, n) for any a (tiles of small grids reach past one period)
+__host__ __device__ __forceinline__ int wrapi(int a, int n) {
+  if (a >= 0 && a < n) return a;
+  const int r = a % n;
+  return r < 0 ? r + n : r;
+}
+
+__device__ __forceinline__ double cart_ghost(const CartBC& b, int m, double q) {
+  const int r = b.rule[m];
+  return r == kInlet ? b.add[m] - q : (r == kNeg ? -q : q);
+}
+
+__device__ __forceinline__ float cart_ghost_f(const CartBC& b, int m, float q, bool homogeneous) {
+  const int r = b.rule[m];
+  if (r == kInlet) return homogeneous ? -q : (float)b.add[m] - q;
+  return r == kNeg ? -q : q;
+}
+
+// Deterministic grid reduction: every block writes its partials, the last
+// block to finish reduces them in block order.
+// max_mask: bit q set => entry q is reduced with max, else with +.
+template <int NV>
+__device__ __forceinline__ bool grid_reduce_last(double (&v)[NV], double* part, unsigned* counter, unsigned max_mask) {
+  __shared__ double red[NV][32];
+  __shared__ bool last;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nwarps = (blockDim.x + 31) >> 5;
+#pragma unroll
+  for (int q = 0; q < NV; ++q) {
+    const bool is_max = (max_mask >> q) & 1u;
+    double x = v[q];
+    for (int o = 16; o > 0; o >>= 1) {
+      double y = __shfl_down_sync(0xffffffffu, x, o);
+      x = is_max ? fmax(x, y) : x + y;
+    }
+    if (lane == 0) red[q][warp] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const int nb = gridDim.x * gridDim.y * gridDim.z;
+    const int bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+    for (int q = 0; q < NV; ++q) {
+      const bool is_max = (max_mask >> q) & 1u;
+      double x = red[q][0];
+      for (int w = 1; w < nwarps; ++w) x = is_max ? fmax(x, red[q][w]) : x + red[q][w];
+      part[(long)q * nb + bid] = x;
+    }
+    __threadfence();
+    const unsigned done = atomicAdd(counter, 1u);
+    last = (done == (unsigned)(nb - 1));
+  }
+  __syncthreads();
+  if (!last) return false;
+  // The whole last block reduces the partials: thread t takes blocks
+  // t, t+blockDim, ... in order, then a fixed shuffle/shared-memory tree.
+  __threadfence();
+  const int nb = gridDim.x * gridDim.y * gridDim.z;
+#pragma unroll
+  for (int q = 0; q < NV; ++q) {
+    const bool is_max = (max_mask >> q) & 1u;
+    volatile const double* pv = part + (long)q * nb;
+    double x = 0.0;
+    bool first = true;
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+      const double y = pv[b];
+      x = first ? y : (is_max ? fmax(x, y) : x + y);
+      first = false;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      double y = __shfl_down_sync(0xffffffffu, x, o);
+      x = is_max ? fmax(x, y) : x + y;
+    }
+    __syncthreads();
+    if (lane == 0) red[q][warp] = x;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double s = red[q][0];
+      for (int w = 1; w < nwarps; ++w) s = is_max ? fmax(s, red[q][w]) : s + red[q][w];
+      v[q] = s;
+    }
+  }
+  if (threadIdx.x == 0) *counter = 0u;
+  return true;
+}
+
+}  // namespace ns

@@ -1,0 +1,149 @@
+/*
+ * amressif_gb300 — C ABI of the GB300 (sm_103a) fractional-step advance of
+ * AMRESSIF (milk-white-way/AMRESSIF, Source/src1_rever).
+ *
+ * The reference has no plugin layer: main_main (main.cpp:51-1213) calls free
+ * functions over amrex::MultiFab. Each entry point below replaces one of
+ * those call sites (cited per function, paths relative to
+ * Source/src1_rever). The library owns its device buffers (an opaque
+ * ns_ctx); an AMReX host moves MultiFab boxes in and out with
+ * ns_put_box / ns_get_box, which take Array4-style strided views.
+ *
+ * All functions return an int status (NS_OK = 0, negative = error,
+ * positive = warning) and never abort the process. All work is enqueued on
+ * the stream given at creation.
+ */
+#ifndef AMRESSIF_GPU_H
+#define AMRESSIF_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define NS_OK 0
+#define NS_WARN_PSEUDO_MAXITER 1  /* main.cpp:1030-1033: countIter > IterNum, step continued */
+#define NS_WARN_PSEUDO_DIVERGED 2 /* main.cpp:1035-1038: normError > 1e2, step continued */
+#define NS_ERR_ARG -1             /* bad argument or parameter */
+#define NS_ERR_BC -2              /* BC code the reference aborts on (main.cpp:822,832, utilities.cpp:135-179) */
+#define NS_ERR_CUDA -3            /* CUDA runtime error (message in ns_last_error) */
+#define NS_ERR_MG_STALL -4        /* Poisson residual stopped decreasing before the tolerance */
+#define NS_ERR_NOMEM -5           /* device allocation failed */
+#define NS_ERR_STATE -6           /* call out of sequence (e.g. stage before step_begin) */
+#define NS_ERR_UNSUPPORTED -7     /* valid reference input this build does not implement */
+
+/* ---- precision modes ----------------------------------------------------- */
+#define NS_PREC_FP64_EXACT 0 /* reference operation order, no FMA: bit-exact stages */
+#define NS_PREC_FP64 1       /* FP64 everywhere, FMA and reciprocal multiplies */
+#define NS_PREC_MIXED 2      /* FP64 anchors + FP32 increments; FP32 V-cycles in FP64 defect correction */
+
+/* ---- initial conditions of hybrid_grid_init (fn_init.cpp:30-631) ------- */
+#define NS_INIT_CAVITY 0 /* all zero (the shipped source) */
+#define NS_INIT_TGV 1    /* u = sin x cos y, v = -cos x sin y, p = (cos 2x + cos 2y)/4 */
+
+/* ---- field identifiers for ns_put_box / ns_get_box ---------------------- */
+#define NS_FIELD_VEL 0      /* velCont[comp] (face-centred) */
+#define NS_FIELD_VEL_PREV 1 /* velContPrev[comp] */
+#define NS_FIELD_PRESSURE 2 /* userCtx comp 0 */
+#define NS_FIELD_PHI 3      /* userCtx comp 1 / poisson_sol */
+#define NS_FIELD_VEL_STAR 4 /* velStar[comp] (current pseudo-iterate) */
+#define NS_FIELD_POISSON_RHS 5
+#define NS_FIELD_CART 6     /* velCart[comp] override for the first stage (cell-centred) */
+
+/* Inputs-file keys of the reference (main.cpp:89-157) plus GPU options. */
+typedef struct ns_params {
+  int dim;                   /* AMREX_SPACEDIM: 2 */
+  int n_cell;
+  int max_grid_size[3];      /* accepted for drop-in; the GPU runs one box */
+  double prob_lo[3];         /* lo_phy_dim (default 0) */
+  double prob_hi[3];         /* hi_phy_dim (default 1) */
+  double ren;                /* Reynolds number */
+  double vis;                /* read but unused, as in the reference */
+  double cfl;                /* dt = cfl / (2 sum 1/dx^2) unless fixed_dt > 0 (main.cpp:285-294) */
+  double fixed_dt;           /* -1 = use cfl rule */
+  int iter_num;              /* IterNum */
+  double momentum_tolerance; /* 1e-10 */
+  int pseudo_timestepping;   /* 1 dual-time RK4, 0 explicit */
+  int bc_lo[3], bc_hi[3];    /* phy_bc_lo / phy_bc_hi codes */
+  double inflow_waveform[3];
+  int nsteps;
+  /* GPU options */
+  int precision;             /* NS_PREC_* */
+  int fix_quirks;            /* 0 = reproduce reference quirks (flux / pressure ghost mirroring in periodic directions) */
+  double poisson_tol_rel;    /* max-norm residual relative to the RHS (MLMG tol_rel, 1e-10) */
+  double poisson_tol_div;    /* additionally require max|div u| <= this after projection (0 = off) */
+  int poisson_max_cycles;    /* V-cycle / defect-correction cap (MLMG maxiter 2000) */
+  int dtau_clip;             /* 0: dtau = 0.4 dt (main.cpp:861); 1: also clip to 0.9 x RK4 stability limit */
+} ns_params;
+
+typedef struct ns_step_stats {
+  int pseudo_iters;   /* K (countIter at exit) */
+  double norm_error;  /* last pseudo-increment norm */
+  double div_before;  /* max|div u*| (fn_rhs.cpp:103-104) */
+  double rhs_sum;     /* sum of the Poisson RHS (fn_rhs.cpp:123-124) */
+  int poisson_cycles; /* V-cycles (FP64) or defect-correction sweeps (mixed) */
+  double poisson_res; /* final max-norm residual / max-norm RHS */
+  double div_after;   /* post-step max|div u| (main.cpp:1180) */
+  int status;         /* NS_OK or NS_WARN_* */
+  double ms_predictor, ms_poisson, ms_project; /* device time of the phases */
+} ns_step_stats;
+
+typedef struct ns_ctx ns_ctx;
+
+/* Defaults: the shipped Exec/inputs physics with a valid chk_int (no restart). */
+void ns_params_default(ns_params* p);
+
+/* Parse a reference inputs file (ParmParse key = value lines, '#' comments)
+ * into p (keys it does not know are ignored). Returns NS_OK or NS_ERR_ARG. */
+int ns_params_parse_file(ns_params* p, const char* path);
+
+/* main.cpp:267-383 (geometry, BoxArray, MultiFab allocation). stream is a
+ * cudaStream_t (NULL = the context creates its own). */
+int ns_ctx_create(const ns_params* p, void* stream, ns_ctx** out);
+void ns_ctx_destroy(ns_ctx* c);
+const char* ns_last_error(const ns_ctx* c);
+double ns_get_dt(const ns_ctx* c);
+double ns_get_time(const ns_ctx* c);
+
+/* hybrid_grid_init (fn_init.cpp:30-631) for init_case NS_INIT_*. */
+int ns_init_fields(ns_ctx* c, int init_case);
+
+/* Move one box of a field between the caller and the device
+ * (MultiFab::array(mfi) views). data is indexed
+ *   data[(i-lo[0]) + (j-lo[1])*jstride + (k-lo[2])*kstride]
+ * over the inclusive index box [lo, hi] in the field's own index space
+ * (face fields extend to n_cell along their direction). where_device = 1 if
+ * data is device memory. */
+int ns_put_box(ns_ctx* c, int field, int comp, const double* data, const int lo[3], const int hi[3],
+               long long jstride, long long kstride, int where_device);
+int ns_get_box(ns_ctx* c, int field, int comp, double* data, const int lo[3], const int hi[3],
+               long long jstride, long long kstride, int where_device);
+
+/* Whole-state convenience (dense host arrays, x fastest): u[d] are face
+ * arrays of extent n_cell+1 along d, p is a cell array. */
+int ns_set_state(ns_ctx* c, const double* const* u, const double* const* u_prev, const double* p, double time);
+int ns_get_state(ns_ctx* c, double* const* u, double* const* u_prev, double* p, double* phi);
+
+/* ---- building blocks, one per reference call site ------------------------ */
+int ns_step_begin(ns_ctx* c);                              /* main.cpp:879-887 */
+int ns_rk_stage(ns_ctx* c, int sub);                       /* main.cpp:931-1017 (fused) */
+int ns_pseudo_norm(ns_ctx* c, double* norm);               /* Error_Computation, main.cpp:1019-1026 */
+int ns_explicit_predictor(ns_ctx* c, double* norm);        /* main.cpp:902-925 */
+int ns_poisson_rhs(ns_ctx* c, double* divmax, double* sum);/* fn_rhs.cpp:71-125 on velStar */
+int ns_poisson_solve(ns_ctx* c, int precision, int* cycles, double* res); /* poisson.cpp:41-186 */
+int ns_project(ns_ctx* c, double* divmax);                 /* main.cpp:1078-1164 + main.cpp:1180 */
+
+/* One full time step (main.cpp:877-1180); stats may be NULL. */
+int ns_step(ns_ctx* c, ns_step_stats* stats);
+
+/* End-to-end host call: upload (u, u_prev, p) from host memory, advance one
+ * step, download (u, p). The arrays are dense as in ns_set_state. */
+int ns_step_host(ns_ctx* c, double* const* u, double* const* u_prev, double* p, ns_step_stats* stats);
+
+/* Synchronise the context's stream. */
+int ns_sync(ns_ctx* c);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,1056 @@
+// CPU oracle for the AMRESSIF fractional-step advance — TEST INFRASTRUCTURE ONLY.
+//
+// Parity status: UNPINNED (the reference has no golden vectors and cannot be
+// built here; see ns_oracle.h). Each function below restates one reference
+// function and cites the file:line it follows (paths are relative to
+// Source/src1_rever of milk-white-way/AMRESSIF). Operation order inside every
+// expression follows the reference so that, compiled with -ffp-contract=off,
+// the oracle reproduces the reference's FP64 rounding for the explicit
+// stencils. The Poisson solve replaces AMReX MLMG by a PCG solve of the same
+// discrete problem to a tighter tolerance (MLMG stops at rel 1e-10).
+#include "ns_oracle.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+struct Box {
+  int lo[3], hi[3];
+};
+
+// Dense array over an inclusive index box, x fastest (AMReX FArrayBox order).
+struct Arr {
+  int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+  long nx = 1, ny = 1, nz = 1;
+  std::vector<double> v;
+  void define(int l0, int l1, int l2, int h0, int h1, int h2) {
+    lo[0] = l0; lo[1] = l1; lo[2] = l2; hi[0] = h0; hi[1] = h1; hi[2] = h2;
+    nx = h0 - l0 + 1; ny = h1 - l1 + 1; nz = h2 - l2 + 1;
+    v.assign((size_t)(nx * ny * nz), 0.0);
+  }
+  inline double& operator()(int i, int j, int k) {
+    return v[(size_t)((i - lo[0]) + nx * ((j - lo[1]) + ny * (long)(k - lo[2])))];
+  }
+  inline double operator()(int i, int j, int k) const {
+    return v[(size_t)((i - lo[0]) + nx * ((j - lo[1]) + ny * (long)(k - lo[2])))];
+  }
+  void setVal(double x) { std::fill(v.begin(), v.end(), x); }
+};
+
+// Geometric multigrid level for the exact Poisson solve.
+struct MGLevel {
+  int n[3];
+  double h[3];
+  double scale;   // Galerkin factor of the rediscretised operator
+  Arr x, f, r;
+};
+
+}  // namespace
+
+struct orc_ctx {
+  orc_params P;
+  int D = 2, N = 0, nk = 1;
+  double dx[3] = {1, 1, 1};
+  bool periodic[3] = {false, false, false};
+  std::vector<Box> boxes;
+
+  Arr velCont[3], velContPrev[3], velContDiff[3], velStar[3], velStarDiff[3], mrhs[3];
+  Arr gradp[3], gradphi[3];
+  Arr half[3][3];  // half[comp][face direction]: QUICK half-node fluxes
+  Arr cart[3];     // velCart, 2 ghosts
+  Arr conv[3], visc[3];
+  Arr total[3];    // fluxTotal, 1 ghost
+  Arr ctx[2];      // userCtx: pressure, phi; 1 ghost
+  Arr prhs, psol;  // poisson_rhs, poisson_sol; 1 ghost
+  double time = 0.0;
+  double rk[4] = {0, 0, 0, 0};
+  std::vector<MGLevel> mg;
+  std::string err;
+};
+
+namespace {
+
+inline int face_hi(const orc_ctx* c, int d, int dim) {
+  // highest face index along `dim` of the face array of direction d
+  int n = (dim < c->D) ? c->N - 1 : 0;
+  return n + ((d == dim) ? 1 : 0);
+}
+
+void define_face(orc_ctx* c, Arr& a, int d) {
+  a.define(0, 0, 0, face_hi(c, d, 0), face_hi(c, d, 1), c->D == 3 ? face_hi(c, d, 2) : 0);
+}
+
+void define_cell(orc_ctx* c, Arr& a, int g) {
+  int gz = (c->D == 3) ? g : 0;
+  a.define(-g, -g, -gz, c->N - 1 + g, c->N - 1 + g, c->D == 3 ? c->N - 1 + gz : 0);
+}
+
+// Box split of BoxArray::maxSize (main.cpp:317-320): each direction of length L
+// is cut into ceil(L/m) chunks whose sizes differ by at most one.
+void split_boxes(orc_ctx* c) {
+  std::vector<int> cuts[3];
+  for (int d = 0; d < 3; ++d) {
+    int L = (d < c->D) ? c->N : 1;
+    int m = (d < c->D) ? std::max(1, c->P.max_grid_size[d]) : 1;
+    int nb = (L + m - 1) / m;
+    int sz = L / nb, ex = L % nb, pos = 0;
+    for (int b = 0; b < nb; ++b) {
+      cuts[d].push_back(pos);
+      pos += sz + (b < ex ? 1 : 0);
+    }
+    cuts[d].push_back(L);
+  }
+  c->boxes.clear();
+  for (size_t bk = 0; bk + 1 < cuts[2].size(); ++bk)
+    for (size_t bj = 0; bj + 1 < cuts[1].size(); ++bj)
+      for (size_t bi = 0; bi + 1 < cuts[0].size(); ++bi) {
+        Box b;
+        b.lo[0] = cuts[0][bi]; b.hi[0] = cuts[0][bi + 1] - 1;
+        b.lo[1] = cuts[1][bj]; b.hi[1] = cuts[1][bj + 1] - 1;
+        b.lo[2] = cuts[2][bk]; b.hi[2] = cuts[2][bk + 1] - 1;
+        c->boxes.push_back(b);
+      }
+}
+
+// Parallel loop over the valid cells: rows (j,k) are distributed.
+template <typename F>
+void par_cells(const orc_ctx* c, F&& f) {
+  const int N = c->N, nk = c->nk;
+  const long rows = (long)N * nk;
+#pragma omp parallel for schedule(static)
+  for (long r = 0; r < rows; ++r) {
+    int j = (int)(r % N), k = (int)(r / N);
+    for (int i = 0; i < N; ++i) f(i, j, k);
+  }
+}
+
+// Parallel loop over the faces of direction d.
+template <typename F>
+void par_faces(const orc_ctx* c, int d, F&& f) {
+  const int ni = face_hi(c, d, 0) + 1, nj = face_hi(c, d, 1) + 1;
+  const int nkk = (c->D == 3) ? face_hi(c, d, 2) + 1 : 1;
+  const long rows = (long)nj * nkk;
+#pragma omp parallel for schedule(static)
+  for (long r = 0; r < rows; ++r) {
+    int j = (int)(r % nj), k = (int)(r / nj);
+    for (int i = 0; i < ni; ++i) f(i, j, k);
+  }
+}
+
+inline void shift(int d, int s, int& i, int& j, int& k) {
+  if (d == 0) i += s; else if (d == 1) j += s; else k += s;
+}
+
+// FillBoundary restricted to periodic wrap over one global array with ghosts
+// (single level, so the only non-trivial part is the periodic image copy).
+void fill_periodic(const orc_ctx* c, Arr& a, int g) {
+  const int N = c->N;
+  const int gz = (c->D == 3) ? g : 0;
+  for (int k = -gz; k <= (c->D == 3 ? N - 1 + gz : 0); ++k)
+    for (int j = -g; j <= N - 1 + g; ++j)
+      for (int i = -g; i <= N - 1 + g; ++i) {
+        int ii = i, jj = j, kk = k;
+        bool ghost = false, ok = true;
+        int idx[3] = {i, j, k};
+        for (int d = 0; d < c->D; ++d) {
+          if (idx[d] < 0 || idx[d] > N - 1) {
+            ghost = true;
+            if (c->periodic[d]) idx[d] = (idx[d] + N) % N;
+            else ok = false;
+          }
+        }
+        if (!ghost || !ok) continue;
+        ii = idx[0]; jj = idx[1]; kk = idx[2];
+        a(i, j, k) = a(ii, jj, kk);
+      }
+}
+
+// gradient_calc_approach2 (fn_flux_calc.cpp:825-911)
+void gradient_calc(orc_ctx* c) {
+  for (int d = 0; d < c->D; ++d) {
+    const double h = c->dx[d];
+    par_faces(c, d, [&](int i, int j, int k) {
+      int im = i, jm = j, km = k;
+      shift(d, -1, im, jm, km);
+      c->gradp[d](i, j, k) = (c->ctx[0](i, j, k) - c->ctx[0](im, jm, km)) / h;
+      c->gradphi[d](i, j, k) = (c->ctx[1](i, j, k) - c->ctx[1](im, jm, km)) / h;
+    });
+  }
+}
+
+// convective_flux_calc_new_quick (fn_flux_calc.cpp:11-202); the advecting
+// velocity is velStar (main.cpp:936), the transported field velCart.
+void convective_flux(orc_ctx* c) {
+  for (int d = 0; d < c->D; ++d) {
+    par_faces(c, d, [&](int i, int j, int k) {
+      const double ucon = 0.5 * c->velStar[d](i, j, k);
+      const double ud = ucon + std::fabs(ucon);
+      const double up = ucon - std::fabs(ucon);
+      int ip = i, jp = j, kp = k; shift(d, 1, ip, jp, kp);
+      int im = i, jm = j, km = k; shift(d, -1, im, jm, km);
+      int imm = i, jmm = j, kmm = k; shift(d, -2, imm, jmm, kmm);
+      for (int m = 0; m < c->D; ++m) {
+        const Arr& q = c->cart[m];
+        const double a = q(ip, jp, kp), b = q(i, j, k), cm = q(im, jm, km), e = q(imm, jmm, kmm);
+        c->half[m][d](i, j, k) = up * (0.125 * (-a - 2 * b + 3 * cm) + b) +
+                                 ud * (0.125 * (-e - 2 * cm + 3 * b) + cm);
+      }
+    });
+  }
+  // cell divergence of the half-node fluxes (fn_flux_calc.cpp:161-180)
+  par_cells(c, [&](int i, int j, int k) {
+    for (int m = 0; m < c->D; ++m) {
+      double s = (c->half[m][0](i + 1, j, k) - c->half[m][0](i, j, k)) / c->dx[0] +
+                 (c->half[m][1](i, j + 1, k) - c->half[m][1](i, j, k)) / c->dx[1];
+      if (c->D == 3) s = s + (c->half[m][2](i, j, k + 1) - c->half[m][2](i, j, k)) / c->dx[2];
+      c->conv[m](i, j, k) = s;
+    }
+  });
+  // total -= conv (fn_flux_calc.cpp:194-200)
+  par_cells(c, [&](int i, int j, int k) {
+    for (int m = 0; m < c->D; ++m) c->total[m](i, j, k) = c->total[m](i, j, k) - c->conv[m](i, j, k);
+  });
+}
+
+// viscous_flux_calc (fn_flux_calc.cpp:695-766)
+void viscous_flux(orc_ctx* c) {
+  const double ren = c->P.ren;
+  const double* dx = c->dx;
+  par_cells(c, [&](int i, int j, int k) {
+    for (int m = 0; m < c->D; ++m) {
+      const Arr& q = c->cart[m];
+      const double ce = q(i, j, k), s = q(i, j - 1, k), n = q(i, j + 1, k);
+      const double w = q(i - 1, j, k), e = q(i + 1, j, k);
+      double v = ((e - 2 * ce + w) / (dx[0] * dx[0]) + (n - 2 * ce + s) / (dx[1] * dx[1])) / ren;
+      if (c->D == 3) {
+        const double f = q(i, j, k - 1), b = q(i, j, k + 1);
+        v = v + ((b - 2 * ce + f) / (dx[2] * dx[2])) / ren;
+      }
+      c->visc[m](i, j, k) = v;
+    }
+  });
+  par_cells(c, [&](int i, int j, int k) {
+    for (int m = 0; m < c->D; ++m) c->total[m](i, j, k) = c->total[m](i, j, k) + c->visc[m](i, j, k);
+  });
+}
+
+// fluxTotal.FillBoundary + odd reflection of the normal component at every
+// domain edge (main.cpp:939-1014, quirk Q1). With fix_quirks the reflection
+// is skipped in periodic directions.
+void flux_ghosts(orc_ctx* c, bool reflect) {
+  for (int m = 0; m < c->D; ++m) fill_periodic(c, c->total[m], 1);
+  if (!reflect) return;
+  const int N = c->N;
+  for (int d = 0; d < c->D; ++d) {
+    if (c->P.fix_quirks && c->periodic[d]) continue;
+    Arr& t = c->total[d];
+    const int gz = (c->D == 3) ? 1 : 0;
+    for (int side = 0; side < 2; ++side)
+      for (int k = -gz; k <= (c->D == 3 ? N : 0); ++k)
+        for (int j = -1; j <= N; ++j)
+          for (int i = -1; i <= N; ++i) {
+            int idx[3] = {i, j, k};
+            if (side == 0 && !(idx[d] < 0)) continue;
+            if (side == 1 && !(idx[d] > N - 1)) continue;
+            int mi[3] = {i, j, k};
+            mi[d] = (side == 0) ? -idx[d] - 1 : (N - idx[d]) + (N - 1);
+            t(i, j, k) = -t(mi[0], mi[1], mi[2]);
+          }
+  }
+}
+
+// momentum_righthand_side_calc (fn_rhs.cpp:8-68)
+void momentum_rhs(orc_ctx* c) {
+  for (int d = 0; d < c->D; ++d) {
+    par_faces(c, d, [&](int i, int j, int k) {
+      int im = i, jm = j, km = k; shift(d, -1, im, jm, km);
+      c->mrhs[d](i, j, k) = -c->gradp[d](i, j, k) + 0.5 * (c->total[d](im, jm, km) + c->total[d](i, j, k));
+    });
+  }
+}
+
+// Ghost fill of velCart for one side (utilities.cpp:62-349). Returns false for
+// codes the reference aborts on or leaves unset.
+bool cart_bc_side(orc_ctx* c, int d, int side) {
+  const int N = c->N;
+  const int code = side == 0 ? c->P.bc_lo[d] : c->P.bc_hi[d];
+  if (code == 111) return true;  // handled by the periodic fill
+  double sgn[3] = {-1, -1, -1}, add[3] = {0, 0, 0};
+  bool slip = (code == -135), inlet = false;
+  if (d == 0 && side == 1) {
+    // east wall: slip is tested as "== 1" (utilities.cpp:152, quirk Q5)
+    slip = c->P.fix_quirks ? (code == -135 || code == 1) : (code == 1);
+    if (!c->P.fix_quirks && code == -135) return false;
+  }
+  if (code == 135) {
+  } else if (slip) {
+    for (int m = 0; m < c->D; ++m) sgn[m] = (m == d) ? -1.0 : 1.0;
+  } else if (code == 165 || (code == -165 && d == 0 && side == 0)) {
+    inlet = true;
+    for (int m = 0; m < c->D; ++m) add[m] = 2.0;
+    if (d == 1 && side == 1)
+      for (int m = 0; m < c->D; ++m) add[m] = 2 * c->P.inflow[m];
+  } else {
+    return false;
+  }
+  const int gz = (c->D == 3) ? 2 : 0;
+  for (int k = -gz; k <= (c->D == 3 ? N + 1 : 0); ++k)
+    for (int j = -2; j <= N + 1; ++j)
+      for (int i = -2; i <= N + 1; ++i) {
+        int idx[3] = {i, j, k};
+        if (side == 0 && !(idx[d] < 0)) continue;
+        if (side == 1 && !(idx[d] > N - 1)) continue;
+        int mi[3] = {i, j, k};
+        mi[d] = (side == 0) ? -idx[d] - 1 : (N - idx[d]) + (N - 1);
+        for (int m = 0; m < c->D; ++m) {
+          const double q = c->cart[m](mi[0], mi[1], mi[2]);
+          // no-slip: -q; slip: -q normal, +q tangential; inlet: 2 - q or 2*inflow - q
+          c->cart[m](i, j, k) = inlet ? add[m] - q : (sgn[m] < 0 ? -q : q);
+        }
+      }
+  return true;
+}
+
+// cont2cart (utilities.cpp:16-350)
+bool cont2cart(orc_ctx* c, Arr* vel) {
+  par_cells(c, [&](int i, int j, int k) {
+    c->cart[0](i, j, k) = 0.5 * (vel[0](i, j, k) + vel[0](i + 1, j, k));
+    c->cart[1](i, j, k) = 0.5 * (vel[1](i, j, k) + vel[1](i, j + 1, k));
+    if (c->D == 3) c->cart[2](i, j, k) = 0.5 * (vel[2](i, j, k) + vel[2](i, j, k + 1));
+  });
+  for (int m = 0; m < c->D; ++m) fill_periodic(c, c->cart[m], 2);
+  for (int d = 0; d < c->D; ++d)
+    for (int side = 0; side < 2; ++side)
+      if (!cart_bc_side(c, d, side)) return false;
+  return true;
+}
+
+// FillBoundary + unconditional mirror of the userCtx ghosts (main.cpp:1079-1158,
+// poisson.cpp:312-391, quirk Q2). With fix_quirks periodic directions keep the wrap.
+void ctx_ghosts(orc_ctx* c) {
+  const int N = c->N;
+  for (int n = 0; n < 2; ++n) fill_periodic(c, c->ctx[n], 1);
+  for (int d = 0; d < c->D; ++d) {
+    if (c->P.fix_quirks && c->periodic[d]) continue;
+    const int gz = (c->D == 3) ? 1 : 0;
+    for (int side = 0; side < 2; ++side)
+      for (int k = -gz; k <= (c->D == 3 ? N : 0); ++k)
+        for (int j = -1; j <= N; ++j)
+          for (int i = -1; i <= N; ++i) {
+            int idx[3] = {i, j, k};
+            if (side == 0 && !(idx[d] < 0)) continue;
+            if (side == 1 && !(idx[d] > N - 1)) continue;
+            int mi[3] = {i, j, k};
+            mi[d] = (side == 0) ? -idx[d] - 1 : (N - idx[d]) + (N - 1);
+            for (int n = 0; n < 2; ++n) c->ctx[n](i, j, k) = c->ctx[n](mi[0], mi[1], mi[2]);
+          }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Exact discrete Poisson solve: PCG on -L with a symmetric V-cycle
+// preconditioner (red-black Gauss-Seidel, cell averaging, constant
+// prolongation, Galerkin-scaled coarse operators). Replaces AMReX MLMG
+// (poisson.cpp:41-186), which solves the same problem to rel 1e-10.
+// ---------------------------------------------------------------------------
+
+void mg_build(orc_ctx* c) {
+  c->mg.clear();
+  int n = c->N;
+  double h[3] = {c->dx[0], c->dx[1], c->dx[2]};
+  double scale = 1.0;
+  while (true) {
+    MGLevel L;
+    for (int d = 0; d < 3; ++d) { L.n[d] = (d < c->D) ? n : 1; L.h[d] = h[d]; }
+    L.scale = scale;
+    int gz = (c->D == 3) ? 1 : 0;
+    L.x.define(-1, -1, -gz, n, n, c->D == 3 ? n : 0);
+    L.f.define(0, 0, 0, n - 1, n - 1, c->D == 3 ? n - 1 : 0);
+    L.r.define(0, 0, 0, n - 1, n - 1, c->D == 3 ? n - 1 : 0);
+    c->mg.push_back(L);
+    if (n % 2 != 0 || n <= 4) break;
+    n /= 2;
+    for (int d = 0; d < 3; ++d) h[d] *= 2;
+    scale *= 2.0;
+  }
+}
+
+// ghost of a level array: Neumann = mirror, periodic = wrap
+void mg_ghost(const orc_ctx* c, MGLevel& L, Arr& x) {
+  const int n = L.n[0];
+  for (int d = 0; d < c->D; ++d) {
+    for (int k = 0; k < L.n[2]; ++k)
+      for (int j = 0; j < L.n[1]; ++j)
+        for (int i = 0; i < L.n[0]; ++i) {
+          int idx[3] = {i, j, k};
+          if (idx[d] != 0 && idx[d] != n - 1) continue;
+          if (idx[d] == 0) {
+            int g[3] = {i, j, k}; g[d] = -1;
+            int s[3] = {i, j, k}; s[d] = c->periodic[d] ? n - 1 : 0;
+            x(g[0], g[1], g[2]) = x(s[0], s[1], s[2]);
+          }
+          if (idx[d] == n - 1) {
+            int g[3] = {i, j, k}; g[d] = n;
+            int s[3] = {i, j, k}; s[d] = c->periodic[d] ? 0 : n - 1;
+            x(g[0], g[1], g[2]) = x(s[0], s[1], s[2]);
+          }
+        }
+  }
+}
+
+// y = -scale * L x (x must have ghosts filled)
+inline double mg_apply_pt(const orc_ctx* c, const MGLevel& L, const Arr& x, int i, int j, int k) {
+  double s = 0.0;
+  for (int d = 0; d < c->D; ++d) {
+    int p[3] = {i, j, k}, m[3] = {i, j, k};
+    p[d] += 1; m[d] -= 1;
+    s += (2.0 * x(i, j, k) - x(p[0], p[1], p[2]) - x(m[0], m[1], m[2])) / (L.h[d] * L.h[d]);
+  }
+  return L.scale * s;
+}
+
+void mg_smooth(const orc_ctx* c, MGLevel& L, int color_first, int sweeps) {
+  for (int s = 0; s < sweeps; ++s)
+    for (int cc = 0; cc < 2; ++cc) {
+      const int color = (color_first + cc) & 1;
+      mg_ghost(c, L, L.x);
+      const long rows = (long)L.n[1] * L.n[2];
+#pragma omp parallel for schedule(static)
+      for (long r = 0; r < rows; ++r) {
+        int j = (int)(r % L.n[1]), k = (int)(r / L.n[1]);
+        for (int i = 0; i < L.n[0]; ++i) {
+          if (((i + j + k) & 1) != color) continue;
+          // local diagonal accounts for mirrored (Neumann) neighbours
+          double off = 0.0, diag = 0.0;
+          int idx[3] = {i, j, k};
+          for (int d = 0; d < c->D; ++d) {
+            const double w = L.scale / (L.h[d] * L.h[d]);
+            int p[3] = {i, j, k}, m[3] = {i, j, k};
+            p[d] += 1; m[d] -= 1;
+            const int n = L.n[d];
+            if (c->periodic[d]) {
+              p[d] = (p[d] + n) % n; m[d] = (m[d] + n) % n;
+              if (p[d] == idx[d]) { continue; }
+              off += w * (L.x(p[0], p[1], p[2]) + L.x(m[0], m[1], m[2]));
+              diag += 2 * w;
+            } else {
+              if (idx[d] < n - 1) { off += w * L.x(p[0], p[1], p[2]); diag += w; }
+              if (idx[d] > 0) { off += w * L.x(m[0], m[1], m[2]); diag += w; }
+            }
+          }
+          if (diag > 0) L.x(i, j, k) = (L.f(i, j, k) + off) / diag;
+        }
+      }
+    }
+}
+
+void mg_residual(const orc_ctx* c, MGLevel& L) {
+  mg_ghost(c, L, L.x);
+  const long rows = (long)L.n[1] * L.n[2];
+#pragma omp parallel for schedule(static)
+  for (long r = 0; r < rows; ++r) {
+    int j = (int)(r % L.n[1]), k = (int)(r / L.n[1]);
+    for (int i = 0; i < L.n[0]; ++i) L.r(i, j, k) = L.f(i, j, k) - mg_apply_pt(c, L, L.x, i, j, k);
+  }
+}
+
+void mg_vcycle(orc_ctx* c, size_t l) {
+  MGLevel& L = c->mg[l];
+  if (l + 1 == c->mg.size()) {
+    // bottom: many symmetric sweeps with the constant mode projected out
+    for (int it = 0; it < 50; ++it) {
+      mg_smooth(c, L, 0, 1);
+      mg_smooth(c, L, 1, 1);
+    }
+    return;
+  }
+  mg_smooth(c, L, 0, 2);
+  mg_residual(c, L);
+  MGLevel& C = c->mg[l + 1];
+  const double inv = 1.0 / (c->D == 3 ? 8.0 : 4.0);
+  for (int k = 0; k < C.n[2]; ++k)
+    for (int j = 0; j < C.n[1]; ++j)
+      for (int i = 0; i < C.n[0]; ++i) {
+        double s = 0.0;
+        for (int dk = 0; dk < (c->D == 3 ? 2 : 1); ++dk)
+          for (int dj = 0; dj < 2; ++dj)
+            for (int di = 0; di < 2; ++di) s += L.r(2 * i + di, 2 * j + dj, c->D == 3 ? 2 * k + dk : 0);
+        C.f(i, j, k) = s * inv;
+      }
+  C.x.setVal(0.0);
+  mg_vcycle(c, l + 1);
+  for (int k = 0; k < L.n[2]; ++k)
+    for (int j = 0; j < L.n[1]; ++j)
+      for (int i = 0; i < L.n[0]; ++i) L.x(i, j, k) += C.x(i / 2, j / 2, c->D == 3 ? k / 2 : 0);
+  mg_smooth(c, L, 1, 2);
+}
+
+double dot_valid(const orc_ctx* c, const Arr& a, const Arr& b) {
+  const int N = c->N;
+  const long rows = (long)N * c->nk;
+  std::vector<double> part((size_t)rows, 0.0);
+#pragma omp parallel for schedule(static)
+  for (long r = 0; r < rows; ++r) {
+    int j = (int)(r % N), k = (int)(r / N);
+    double s = 0.0;
+    for (int i = 0; i < N; ++i) s += a(i, j, k) * b(i, j, k);
+    part[(size_t)r] = s;
+  }
+  double s = 0.0;
+  for (double x : part) s += x;
+  return s;
+}
+
+double maxabs_valid(const orc_ctx* c, const Arr& a) {
+  double m = 0.0;
+  for (int k = 0; k < c->nk; ++k)
+    for (int j = 0; j < c->N; ++j)
+      for (int i = 0; i < c->N; ++i) m = std::max(m, std::fabs(a(i, j, k)));
+  return m;
+}
+
+// Solve L phi = f (L = +Laplacian, MLABecLaplacian with a=0, b=-1, B=1,
+// poisson.cpp:128-153) for the singular Neumann/periodic problem. The mean of
+// f is removed first as MLMG does for singular problems; phi has zero mean.
+int poisson_exact(orc_ctx* c, const Arr& fin, Arr& phi, int* iters_out, double* res_out) {
+  const int N = c->N;
+  const long ncell = (long)N * N * (c->D == 3 ? N : 1);
+  MGLevel& F = c->mg[0];
+  Arr b, r, z, p, q, x;
+  define_cell(c, b, 0); define_cell(c, r, 0); define_cell(c, z, 0); define_cell(c, q, 0);
+  define_cell(c, p, 1); define_cell(c, x, 1);
+  // b = -(f - mean f): PCG on the SPD operator -L
+  double fm = 0.0;
+  {
+    std::vector<double> rows((size_t)N * c->nk);
+    for (int k = 0; k < c->nk; ++k)
+      for (int j = 0; j < N; ++j) {
+        double s = 0.0;
+        for (int i = 0; i < N; ++i) s += fin(i, j, k);
+        rows[(size_t)(j + N * k)] = s;
+      }
+    for (double v : rows) fm += v;
+    fm /= (double)ncell;
+  }
+  for (int k = 0; k < c->nk; ++k)
+    for (int j = 0; j < N; ++j)
+      for (int i = 0; i < N; ++i) b(i, j, k) = -(fin(i, j, k) - fm);
+  const double bnorm = maxabs_valid(c, b);
+  phi.setVal(0.0);
+  if (bnorm == 0.0) { *iters_out = 0; *res_out = 0.0; return ORC_OK; }
+  auto applyA = [&](Arr& in, Arr& out) {  // out = -L in
+    for (int k = 0; k < c->nk; ++k)
+      for (int j = 0; j < N; ++j)
+        for (int i = 0; i < N; ++i) F.x(i, j, k) = in(i, j, k);
+    mg_ghost(c, F, F.x);
+    const long rows = (long)N * c->nk;
+#pragma omp parallel for schedule(static)
+    for (long rr = 0; rr < rows; ++rr) {
+      int j = (int)(rr % N), k = (int)(rr / N);
+      for (int i = 0; i < N; ++i) out(i, j, k) = mg_apply_pt(c, F, F.x, i, j, k);
+    }
+  };
+  auto precond = [&](Arr& in, Arr& out) {  // out ~= (-L)^-1 in, mean removed
+    for (int k = 0; k < c->nk; ++k)
+      for (int j = 0; j < N; ++j)
+        for (int i = 0; i < N; ++i) F.f(i, j, k) = in(i, j, k);
+    F.x.setVal(0.0);
+    mg_vcycle(c, 0);
+    double s = 0.0;
+    for (int k = 0; k < c->nk; ++k)
+      for (int j = 0; j < N; ++j)
+        for (int i = 0; i < N; ++i) s += F.x(i, j, k);
+    s /= (double)ncell;
+    for (int k = 0; k < c->nk; ++k)
+      for (int j = 0; j < N; ++j)
+        for (int i = 0; i < N; ++i) out(i, j, k) = F.x(i, j, k) - s;
+  };
+  x.setVal(0.0);
+  r.v = b.v;
+  precond(r, z);
+  for (int k = 0; k < c->nk; ++k)
+    for (int j = 0; j < N; ++j)
+      for (int i = 0; i < N; ++i) p(i, j, k) = z(i, j, k);
+  double rz = dot_valid(c, r, z);
+  const double tol = c->P.poisson_tol > 0 ? c->P.poisson_tol : 1e-13;
+  double best = 1e300;
+  int since_best = 0, it = 0;
+  double rel = 1.0;
+  for (it = 1; it <= 1000; ++it) {
+    applyA(p, q);
+    const double pq = dot_valid(c, p, q);
+    if (pq <= 0.0) break;
+    const double alpha = rz / pq;
+    for (int k = 0; k < c->nk; ++k)
+      for (int j = 0; j < N; ++j)
+        for (int i = 0; i < N; ++i) {
+          x(i, j, k) += alpha * p(i, j, k);
+          r(i, j, k) -= alpha * q(i, j, k);
+        }
+    if (it % 8 == 0) {  // replace the recursive residual by the true one
+      applyA(x, q);
+      for (int k = 0; k < c->nk; ++k)
+        for (int j = 0; j < N; ++j)
+          for (int i = 0; i < N; ++i) r(i, j, k) = b(i, j, k) - q(i, j, k);
+    }
+    rel = maxabs_valid(c, r) / bnorm;
+    if (rel < best * 0.5) { best = rel; since_best = 0; } else { ++since_best; }
+    if (rel <= tol || since_best >= 16) break;
+    precond(r, z);
+    const double rz2 = dot_valid(c, r, z);
+    const double beta = rz2 / rz;
+    rz = rz2;
+    for (int k = 0; k < c->nk; ++k)
+      for (int j = 0; j < N; ++j)
+        for (int i = 0; i < N; ++i) p(i, j, k) = z(i, j, k) + beta * p(i, j, k);
+  }
+  // true residual of the returned solution
+  applyA(x, q);
+  double rmax = 0.0;
+  for (int k = 0; k < c->nk; ++k)
+    for (int j = 0; j < N; ++j)
+      for (int i = 0; i < N; ++i) rmax = std::max(rmax, std::fabs(b(i, j, k) - q(i, j, k)));
+  for (int k = 0; k < c->nk; ++k)
+    for (int j = 0; j < N; ++j)
+      for (int i = 0; i < N; ++i) phi(i, j, k) = x(i, j, k);
+  *iters_out = it;
+  *res_out = rmax / bnorm;
+  return ORC_OK;
+}
+
+// poisson_righthand_side_calc (fn_rhs.cpp:71-125) on a face field
+void poisson_rhs_calc(orc_ctx* c, Arr* vel, double dt, double* norm0, double* sum) {
+  par_cells(c, [&](int i, int j, int k) {
+    double s = (vel[0](i + 1, j, k) - vel[0](i, j, k)) / c->dx[0] + (vel[1](i, j + 1, k) - vel[1](i, j, k)) / c->dx[1];
+    if (c->D == 3) s = s + (vel[2](i, j, k + 1) - vel[2](i, j, k)) / c->dx[2];
+    c->prhs(i, j, k) = s;
+  });
+  *norm0 = maxabs_valid(c, c->prhs);
+  par_cells(c, [&](int i, int j, int k) { c->prhs(i, j, k) = (1.5 / dt) * c->prhs(i, j, k); });
+  const int N = c->N;
+  std::vector<double> rows((size_t)N * c->nk);
+  for (int k = 0; k < c->nk; ++k)
+    for (int j = 0; j < N; ++j) {
+      double s = 0.0;
+      for (int i = 0; i < N; ++i) s += c->prhs(i, j, k);
+      rows[(size_t)(j + N * k)] = s;
+    }
+  double s = 0.0;
+  for (double v : rows) s += v;
+  *sum = s;
+}
+
+void set_threads(const orc_ctx* c) {
+#ifdef _OPENMP
+  if (c->P.nthreads > 0) omp_set_num_threads(c->P.nthreads);
+#else
+  (void)c;
+#endif
+}
+
+}  // namespace
+
+extern "C" {
+
+int orc_create(const orc_params* p, orc_ctx** out) {
+  if (!p || !out) return ORC_ERR_ARG;
+  if (p->dim != 2 && p->dim != 3) return ORC_ERR_ARG;
+  if (p->n_cell < 4) return ORC_ERR_ARG;
+  orc_ctx* c = new orc_ctx();
+  c->P = *p;
+  c->D = p->dim;
+  c->N = p->n_cell;
+  c->nk = (c->D == 3) ? c->N : 1;
+  for (int d = 0; d < 3; ++d) {
+    c->dx[d] = (d < c->D) ? (p->prob_hi[d] - p->prob_lo[d]) / (double)c->N : 1.0;
+    c->periodic[d] = (d < c->D) && p->bc_lo[d] == 111 && p->bc_hi[d] == 111;
+  }
+  for (int d = 0; d < c->D; ++d) {
+    // a periodic code on one side only is left unfilled by the reference
+    if ((p->bc_lo[d] == 111) != (p->bc_hi[d] == 111)) { delete c; return ORC_ERR_BC; }
+  }
+  split_boxes(c);
+  for (int d = 0; d < c->D; ++d) {
+    define_face(c, c->velCont[d], d); define_face(c, c->velContPrev[d], d);
+    define_face(c, c->velContDiff[d], d); define_face(c, c->velStar[d], d);
+    define_face(c, c->velStarDiff[d], d); define_face(c, c->mrhs[d], d);
+    define_face(c, c->gradp[d], d); define_face(c, c->gradphi[d], d);
+    for (int m = 0; m < c->D; ++m) define_face(c, c->half[m][d], d);
+    define_cell(c, c->cart[d], 2);
+    define_cell(c, c->conv[d], 0); define_cell(c, c->visc[d], 0);
+    define_cell(c, c->total[d], 1);
+  }
+  define_cell(c, c->ctx[0], 1); define_cell(c, c->ctx[1], 1);
+  define_cell(c, c->prhs, 1); define_cell(c, c->psol, 1);
+  // RK coefficients (main.cpp:861-870)
+  const double d_tau = 0.4 * p->dt;
+  c->rk[0] = d_tau * 0.25;
+  c->rk[1] = d_tau * (1.0 / 3.0);
+  c->rk[2] = d_tau * 0.5;
+  c->rk[3] = d_tau * 1.0;
+  mg_build(c);
+  // validate BC codes once by a dry ghost fill on zeros
+  if (!cont2cart(c, c->velCont)) { delete c; return ORC_ERR_BC; }
+  *out = c;
+  return ORC_OK;
+}
+
+void orc_destroy(orc_ctx* c) { delete c; }
+
+const char* orc_last_error(const orc_ctx* c) { return c ? c->err.c_str() : ""; }
+
+int orc_init(orc_ctx* c, int init_case) {
+  set_threads(c);
+  const double* lo = c->P.prob_lo;
+  const double* dx = c->dx;
+  c->time = 0.0;
+  const double dt = c->P.dt;
+  // hybrid_grid_init (fn_init.cpp:61-229, kn_init.H:8-37)
+  const double nu_decay = c->P.fix_quirks ? (1.0 / c->P.ren) : 1.0;  // quirk Q6
+  for (int d = 0; d < c->D; ++d)
+    par_faces(c, d, [&](int i, int j, int k) {
+      double u = 0.0, up = 0.0;
+      if (init_case == 1 && d < 2) {
+        const double x = lo[0] + (i + (d == 0 ? 0.0 : 0.5)) * dx[0];
+        const double y = lo[1] + (j + (d == 1 ? 0.0 : 0.5)) * dx[1];
+        if (d == 0) {
+          u = std::sin(x) * std::cos(y);
+          up = std::sin(x) * std::cos(y) * std::exp(-2.0 * nu_decay * (c->time - dt));
+        } else {
+          u = -std::cos(x) * std::sin(y);
+          up = -std::cos(x) * std::sin(y) * std::exp(-2.0 * nu_decay * (c->time - dt));
+        }
+      }
+      c->velCont[d](i, j, k) = u;
+      c->velContPrev[d](i, j, k) = up;
+    });
+  for (int m = 0; m < c->D; ++m) c->cart[m].setVal(0.0);
+  par_cells(c, [&](int i, int j, int k) {
+    if (init_case == 1) {
+      const double x = lo[0] + (i + 0.5) * dx[0];
+      const double y = lo[1] + (j + 0.5) * dx[1];
+      c->cart[0](i, j, k) = std::sin(x) * std::cos(y);
+      c->cart[1](i, j, k) = -std::cos(x) * std::sin(y);
+      c->ctx[0](i, j, k) = 0.25 * (std::cos(2.0 * x) + std::cos(2.0 * y));
+    } else {
+      for (int m = 0; m < c->D; ++m) c->cart[m](i, j, k) = 0.0;
+      c->ctx[0](i, j, k) = 0.0;
+    }
+    c->ctx[1](i, j, k) = 0.0;
+  });
+  for (int m = 0; m < c->D; ++m) fill_periodic(c, c->cart[m], 2);
+  // init ghost fill (fn_init.cpp:240-532) matches cont2cart except that the
+  // east slip wall is tested as -135 there
+  for (int d = 0; d < c->D; ++d)
+    for (int side = 0; side < 2; ++side) {
+      int saved = c->P.fix_quirks;
+      if (d == 0 && side == 1 && c->P.bc_hi[0] == -135) c->P.fix_quirks = 1;
+      bool ok = cart_bc_side(c, d, side);
+      c->P.fix_quirks = saved;
+      if (!ok) return ORC_ERR_BC;
+    }
+  ctx_ghosts(c);
+  return ORC_OK;
+}
+
+static void load_face(orc_ctx* c, Arr& a, int d, const double* src) {
+  const long ni = face_hi(c, d, 0) + 1, nj = face_hi(c, d, 1) + 1;
+  const long nkk = (c->D == 3) ? face_hi(c, d, 2) + 1 : 1;
+  for (long k = 0; k < nkk; ++k)
+    for (long j = 0; j < nj; ++j)
+      for (long i = 0; i < ni; ++i) a((int)i, (int)j, (int)k) = src[i + ni * (j + nj * k)];
+}
+static void store_face(const orc_ctx* c, const Arr& a, int d, double* dst) {
+  const long ni = face_hi(c, d, 0) + 1, nj = face_hi(c, d, 1) + 1;
+  const long nkk = (c->D == 3) ? face_hi(c, d, 2) + 1 : 1;
+  for (long k = 0; k < nkk; ++k)
+    for (long j = 0; j < nj; ++j)
+      for (long i = 0; i < ni; ++i) dst[i + ni * (j + nj * k)] = a((int)i, (int)j, (int)k);
+}
+static void load_cell(orc_ctx* c, Arr& a, const double* src) {
+  const long N = c->N;
+  for (long k = 0; k < c->nk; ++k)
+    for (long j = 0; j < N; ++j)
+      for (long i = 0; i < N; ++i) a((int)i, (int)j, (int)k) = src[i + N * (j + N * k)];
+}
+static void store_cell(const orc_ctx* c, const Arr& a, double* dst) {
+  const long N = c->N;
+  for (long k = 0; k < c->nk; ++k)
+    for (long j = 0; j < N; ++j)
+      for (long i = 0; i < N; ++i) dst[i + N * (j + N * k)] = a((int)i, (int)j, (int)k);
+}
+
+int orc_set_state(orc_ctx* c, const double* const* u, const double* const* u_prev, const double* p, double time) {
+  if (!c || !u || !u_prev || !p) return ORC_ERR_ARG;
+  set_threads(c);
+  for (int d = 0; d < c->D; ++d) {
+    load_face(c, c->velCont[d], d, u[d]);
+    load_face(c, c->velContPrev[d], d, u_prev[d]);
+  }
+  c->ctx[0].setVal(0.0);
+  c->ctx[1].setVal(0.0);
+  load_cell(c, c->ctx[0], p);
+  ctx_ghosts(c);
+  c->time = time;
+  if (!cont2cart(c, c->velCont)) return ORC_ERR_BC;
+  return ORC_OK;
+}
+
+int orc_get_state(const orc_ctx* c, double* const* u, double* const* u_prev, double* p, double* phi) {
+  if (!c) return ORC_ERR_ARG;
+  for (int d = 0; d < c->D; ++d) {
+    if (u) store_face(c, c->velCont[d], d, u[d]);
+    if (u_prev) store_face(c, c->velContPrev[d], d, u_prev[d]);
+  }
+  if (p) store_cell(c, c->ctx[0], p);
+  if (phi) store_cell(c, c->ctx[1], phi);
+  return ORC_OK;
+}
+
+int orc_set_cart(orc_ctx* c, const double* const* cart) {
+  if (!c || !cart) return ORC_ERR_ARG;
+  for (int m = 0; m < c->D; ++m) load_cell(c, c->cart[m], cart[m]);
+  for (int m = 0; m < c->D; ++m) fill_periodic(c, c->cart[m], 2);
+  for (int d = 0; d < c->D; ++d)
+    for (int side = 0; side < 2; ++side)
+      if (!cart_bc_side(c, d, side)) return ORC_ERR_BC;
+  return ORC_OK;
+}
+
+int orc_step_begin(orc_ctx* c) {
+  // main.cpp:879-887
+  for (int d = 0; d < c->D; ++d) {
+    par_faces(c, d, [&](int i, int j, int k) {
+      c->velContDiff[d](i, j, k) = c->velCont[d](i, j, k) - c->velContPrev[d](i, j, k);
+      c->velContPrev[d](i, j, k) = c->velCont[d](i, j, k);
+      c->velStar[d](i, j, k) = c->velCont[d](i, j, k);
+    });
+  }
+  c->time = c->time + c->P.dt;
+  return ORC_OK;
+}
+
+int orc_rk_stage(orc_ctx* c, int sub) {
+  set_threads(c);
+  // main.cpp:931-1017
+  gradient_calc(c);
+  for (int m = 0; m < c->D; ++m) c->total[m].setVal(0.0);
+  convective_flux(c);
+  viscous_flux(c);
+  flux_ghosts(c, true);
+  momentum_rhs(c);
+  // runge_kutta4_pseudo_time_stepping (momentum.cpp:9-94)
+  const double dt = c->P.dt;
+  const double rks = c->rk[sub];
+  for (int d = 0; d < c->D; ++d) {
+    par_faces(c, d, [&](int i, int j, int k) {
+      double r = c->mrhs[d](i, j, k);
+      r = r - (1.5 / dt) * (c->velStar[d](i, j, k) - c->velContPrev[d](i, j, k)) + (0.5 / dt) * c->velContDiff[d](i, j, k);
+      c->mrhs[d](i, j, k) = r;
+      c->velStar[d](i, j, k) = c->velCont[d](i, j, k) + (rks * r);
+    });
+  }
+  if (!cont2cart(c, c->velStar)) return ORC_ERR_BC;
+  return ORC_OK;
+}
+
+// Error_Computation (utilities.cpp:421-493) with StagL2Norm/SumAbsStag
+// (utilities.cpp:669-778): weight 1/2 on the first and last face of every box.
+static double error_computation(orc_ctx* c) {
+  const double npts = (c->D == 3) ? (double)c->N * (double)c->N * (double)c->N : (double)c->N * (double)c->N;
+  double normError = 0.0;
+  for (int d = 0; d < c->D; ++d) {
+    par_faces(c, d, [&](int i, int j, int k) {
+      c->velStarDiff[d](i, j, k) = c->velCont[d](i, j, k) - c->velStar[d](i, j, k);
+    });
+    double total = 0.0;
+    for (const Box& b : c->boxes) {
+      int lo[3] = {b.lo[0], b.lo[1], b.lo[2]}, hi[3] = {b.hi[0], b.hi[1], b.hi[2]};
+      hi[d] += 1;  // nodal in d
+      const int nj = hi[1] - lo[1] + 1, nkk = hi[2] - lo[2] + 1;
+      std::vector<double> rows((size_t)nj * nkk, 0.0);
+#pragma omp parallel for schedule(static)
+      for (long r = 0; r < (long)nj * nkk; ++r) {
+        const int j = lo[1] + (int)(r % nj), k = lo[2] + (int)(r / nj);
+        double s = 0.0;
+        for (int i = lo[0]; i <= hi[0]; ++i) {
+          const int idx[3] = {i, j, k};
+          const double w = (idx[d] > lo[d] && idx[d] < hi[d]) ? 1.0 : 0.5;
+          const double q = c->velStarDiff[d](i, j, k);
+          s += std::fabs((q * q) * w);
+        }
+        rows[(size_t)r] = s;
+      }
+      double bs = 0.0;
+      for (double v : rows) bs += v;
+      total += bs;
+    }
+    const double e = std::sqrt(total) / std::sqrt(npts);
+    normError = (d == 0) ? e : std::max(normError, e);
+  }
+  return normError;
+}
+
+double orc_pseudo_norm(orc_ctx* c) {
+  set_threads(c);
+  const double e = error_computation(c);
+  for (int d = 0; d < c->D; ++d) c->velCont[d].v = c->velStar[d].v;  // main.cpp:1023-1026
+  return e;
+}
+
+int orc_explicit_predictor(orc_ctx* c, double* norm) {
+  set_threads(c);
+  // main.cpp:902-925; no flux reflection in this mode (quirk Q3)
+  gradient_calc(c);
+  for (int m = 0; m < c->D; ++m) c->total[m].setVal(0.0);
+  convective_flux(c);
+  viscous_flux(c);
+  flux_ghosts(c, false);
+  momentum_rhs(c);
+  const double dt = c->P.dt;
+  // explicit_time_marching (momentum.cpp:96-192)
+  for (int d = 0; d < c->D; ++d)
+    par_faces(c, d, [&](int i, int j, int k) {
+      c->mrhs[d](i, j, k) = c->mrhs[d](i, j, k) + (1.0 / (2.0 * dt)) * c->velContDiff[d](i, j, k);
+    });
+  for (int d = 0; d < c->D; ++d)
+    par_faces(c, d, [&](int i, int j, int k) {
+      c->velStar[d](i, j, k) = c->velStar[d](i, j, k) + ((dt / 1.5) * c->mrhs[d](i, j, k));
+    });
+  const double e = error_computation(c);
+  for (int d = 0; d < c->D; ++d) c->velCont[d].v = c->velStar[d].v;
+  if (norm) *norm = e;
+  return ORC_OK;
+}
+
+int orc_poisson_rhs(orc_ctx* c, double* divmax, double* sum) {
+  set_threads(c);
+  double n0, s;
+  poisson_rhs_calc(c, c->velStar, c->P.dt, &n0, &s);
+  if (divmax) *divmax = n0;
+  if (sum) *sum = s;
+  return ORC_OK;
+}
+
+int orc_poisson_solve(orc_ctx* c, int* iters, double* res) {
+  set_threads(c);
+  int it = 0;
+  double r = 0.0;
+  c->psol.setVal(0.0);  // poisson.cpp:63
+  int st = poisson_exact(c, c->prhs, c->psol, &it, &r);
+  if (iters) *iters = it;
+  if (res) *res = r;
+  return st;
+}
+
+int orc_project(orc_ctx* c, double* divmax) {
+  set_threads(c);
+  // copy phi into userCtx comp 1 + ghosts (main.cpp:1078-1158)
+  par_cells(c, [&](int i, int j, int k) { c->ctx[1](i, j, k) = c->psol(i, j, k); });
+  ctx_ghosts(c);
+  // update_solution (poisson.cpp:192-392)
+  gradient_calc(c);
+  const double dt = c->P.dt;
+  for (int d = 0; d < c->D; ++d)
+    par_faces(c, d, [&](int i, int j, int k) {
+      c->velCont[d](i, j, k) = c->velStar[d](i, j, k) - (c->gradphi[d](i, j, k) * dt / 1.5);
+    });
+  if (!cont2cart(c, c->velCont)) return ORC_ERR_BC;
+  par_cells(c, [&](int i, int j, int k) { c->ctx[0](i, j, k) = c->ctx[0](i, j, k) + c->ctx[1](i, j, k); });
+  ctx_ghosts(c);
+  // post-step divergence check (main.cpp:1180 -> fn_rhs.cpp:93-104)
+  double n0, s;
+  poisson_rhs_calc(c, c->velCont, dt, &n0, &s);
+  if (divmax) *divmax = n0;
+  return ORC_OK;
+}
+
+int orc_step(orc_ctx* c, orc_step_stats* st) {
+  if (!c) return ORC_ERR_ARG;
+  set_threads(c);
+  orc_step_stats s;
+  std::memset(&s, 0, sizeof(s));
+  orc_step_begin(c);
+  int countIter = 0;
+  double normError = 1.e9;
+  while (normError > c->P.momentum_tolerance) {
+    if (c->P.pseudo_timestepping == 0) {
+      orc_explicit_predictor(c, &normError);
+      countIter = 1;
+      break;
+    }
+    for (int sub = 0; sub < 4; ++sub) {
+      int r = orc_rk_stage(c, sub);
+      if (r != ORC_OK) return r;
+    }
+    normError = orc_pseudo_norm(c);
+    countIter++;
+    if (countIter > c->P.iter_num) { s.status = 1; break; }
+    if (normError > 1.e2) { s.status = 2; break; }
+  }
+  s.pseudo_iters = countIter;
+  s.norm_error = normError;
+  orc_poisson_rhs(c, &s.div_before, &s.rhs_sum);
+  orc_poisson_solve(c, &s.poisson_iters, &s.poisson_res);
+  int r = orc_project(c, &s.div_after);
+  if (st) *st = s;
+  return r;
+}
+
+int orc_get_field(const orc_ctx* c, int which, int comp, double* out) {
+  if (!c || !out) return ORC_ERR_ARG;
+  if (which <= 4) {
+    if (comp < 0 || comp >= c->D) return ORC_ERR_ARG;
+    const Arr* a = which == 0 ? c->velStar : which == 1 ? c->velCont : which == 2 ? c->velContPrev
+                 : which == 3 ? c->velContDiff : c->mrhs;
+    store_face(c, a[comp], comp, out);
+    return ORC_OK;
+  }
+  if (which == 10) { store_cell(c, c->ctx[0], out); return ORC_OK; }
+  if (which == 11) { store_cell(c, c->ctx[1], out); return ORC_OK; }
+  if (which == 12) { store_cell(c, c->prhs, out); return ORC_OK; }
+  if (which >= 13 && which < 13 + c->D) { store_cell(c, c->cart[which - 13], out); return ORC_OK; }
+  if (which >= 20 && which < 20 + c->D) { store_cell(c, c->total[which - 20], out); return ORC_OK; }
+  return ORC_ERR_ARG;
+}
+
+int orc_put_field(orc_ctx* c, int which, int comp, const double* in) {
+  if (!c || !in) return ORC_ERR_ARG;
+  if (which <= 4) {
+    if (comp < 0 || comp >= c->D) return ORC_ERR_ARG;
+    Arr* a = which == 0 ? c->velStar : which == 1 ? c->velCont : which == 2 ? c->velContPrev
+           : which == 3 ? c->velContDiff : c->mrhs;
+    load_face(c, a[comp], comp, in);
+    return ORC_OK;
+  }
+  if (which == 10) { load_cell(c, c->ctx[0], in); ctx_ghosts(c); return ORC_OK; }
+  if (which == 11) { load_cell(c, c->ctx[1], in); ctx_ghosts(c); return ORC_OK; }
+  if (which == 12) { load_cell(c, c->prhs, in); return ORC_OK; }
+  return ORC_ERR_ARG;
+}
+
+int orc_solve_poisson_array(orc_ctx* c, const double* f, double* phi, int* iters, double* res) {
+  if (!c || !f || !phi) return ORC_ERR_ARG;
+  set_threads(c);
+  Arr fa, pa;
+  define_cell(c, fa, 1);
+  define_cell(c, pa, 1);
+  load_cell(c, fa, f);
+  int it = 0;
+  double r = 0.0;
+  int st = poisson_exact(c, fa, pa, &it, &r);
+  store_cell(c, pa, phi);
+  if (iters) *iters = it;
+  if (res) *res = r;
+  return st;
+}
+
+}  // extern "C"

@@ -1,0 +1,196 @@
+"""Parity of the CUDA path (through the C ABI) with the CPU oracle.
+
+Tolerances: the FP64 exact mode reproduces the oracle's pseudo-stages bit for
+bit (same operation order, no FMA); whole steps differ only through the
+Poisson solve (different solver, both converged to <= 1e-12 relative), so u, v
+and p (modulo its additive constant) must agree to a relative L2 of 1e-10 per
+step, with identical pseudo-iteration counts K.
+"""
+import math
+
+import numpy as np
+import pytest
+
+import amressif_gb300 as ns
+from oracle.orc import FIELD_MRHS, FIELD_STAR, Oracle
+
+pytestmark = pytest.mark.gpu
+
+TOL_STEP = 1e-10
+
+
+def rel(a, b):
+    nb = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / (nb if nb > 0 else 1.0)
+
+
+def relp(a, b):
+    return rel(a - a.mean(), b - b.mean())
+
+
+CASES = {
+    # name: (n, oracle kwargs, gpu kwargs, init case)
+    "cavity32": (32, dict(ren=100.0, dt=1e-3, max_grid_size=(32, 16, 16)), dict(ren=100.0, fixed_dt=1e-3), 0),
+    "cavity40_partial_tiles": (40, dict(ren=100.0, dt=2e-3, max_grid_size=(40, 40, 40)), dict(ren=100.0, fixed_dt=2e-3), 0),
+    "cavity128_cfg1": (128, dict(ren=100.0, dt=0.5 / 128, max_grid_size=(64, 64, 64)),
+                       dict(ren=100.0, fixed_dt=0.5 / 128, max_grid_size=(64, 64, 64)), 0),
+    "tgv64_parity": (64, dict(ren=1000.0, dt=0.5 * 2 * math.pi / 64, prob_hi=(2 * math.pi,) * 3,
+                              bc_lo=(111,) * 3, bc_hi=(111,) * 3),
+                     dict(ren=1000.0, fixed_dt=0.5 * 2 * math.pi / 64, prob_hi=(2 * math.pi,) * 3,
+                          bc_lo=(111,) * 3, bc_hi=(111,) * 3), 1),
+    "tgv64_fixed": (64, dict(ren=1000.0, dt=0.5 * 2 * math.pi / 64, prob_hi=(2 * math.pi,) * 3,
+                             bc_lo=(111,) * 3, bc_hi=(111,) * 3, fix_quirks=1),
+                    dict(ren=1000.0, fixed_dt=0.5 * 2 * math.pi / 64, prob_hi=(2 * math.pi,) * 3,
+                         bc_lo=(111,) * 3, bc_hi=(111,) * 3, fix_quirks=1), 1),
+}
+
+
+def make_pair(name, precision=ns.PREC_FP64_EXACT, tol=1e-12, **extra):
+    n, okw, gkw, case = CASES[name]
+    o = Oracle(n, iter_num=100, poisson_tol=min(tol, 1e-13), **okw)
+    o.init(case)
+    p = ns.default_params(n_cell=n, iter_num=100, precision=precision, poisson_tol_rel=tol, **gkw, **extra)
+    s = ns.Solver(p)
+    s.init(case)
+    return o, s
+
+
+def sync_state(o, s):
+    u, up, p, _ = o.get_state()
+    s.set_state(u, up, p)
+    o.set_state(u, up, p)
+
+
+@pytest.mark.parametrize("name", ["cavity32", "cavity40_partial_tiles", "cavity128_cfg1", "tgv64_parity", "tgv64_fixed"])
+def test_rk_stages_bit_exact(gpu_lib, oracle_lib, name):
+    o, s = make_pair(name)
+    for _ in range(3):
+        o.step()
+    sync_state(o, s)
+    o.step_begin()
+    s.step_begin()
+    for it in range(2):
+        for sub in range(4):
+            o.rk_stage(sub)
+            s.rk_stage(sub)
+            for d in range(2):
+                np.testing.assert_array_equal(s.get_field(ns.FIELD_VEL_STAR, d), o.field(FIELD_STAR, d),
+                                              err_msg="stage %d comp %d" % (sub, d))
+        eo = o.pseudo_norm()
+        eg = s.pseudo_norm()
+        assert abs(eg - eo) <= 1e-13 * abs(eo), (eg, eo)
+
+
+def test_first_stage_uses_analytic_cell_velocity(gpu_lib, oracle_lib):
+    """hybrid_grid_init sets velCart analytically; the first stage must use it."""
+    o, s = make_pair("tgv64_parity")
+    o.step_begin()
+    s.step_begin()
+    o.rk_stage(0)
+    s.rk_stage(0)
+    for d in range(2):
+        np.testing.assert_array_equal(s.get_field(ns.FIELD_VEL_STAR, d), o.field(FIELD_STAR, d))
+
+
+def test_explicit_predictor_bit_exact(gpu_lib, oracle_lib):
+    n, okw, gkw, case = CASES["cavity32"]
+    o = Oracle(n, iter_num=100, pseudo_timestepping=0, **okw)
+    o.init(case)
+    for _ in range(2):
+        o.step()
+    p = ns.default_params(n_cell=n, pseudo_timestepping=0, precision=ns.PREC_FP64_EXACT, **gkw)
+    s = ns.Solver(p)
+    s.init(case)
+    sync_state(o, s)
+    o.step_begin()
+    s.step_begin()
+    eo = o.explicit_predictor()
+    eg = s.explicit_predictor()
+    for d in range(2):
+        np.testing.assert_array_equal(s.get_field(ns.FIELD_VEL_STAR, d), o.field(FIELD_STAR, d))
+    assert abs(eg - eo) <= 1e-13 * abs(eo)
+
+
+@pytest.mark.parametrize("precision", [ns.PREC_FP64, ns.PREC_MIXED])
+@pytest.mark.parametrize("name", ["cavity128_cfg1", "tgv64_fixed"])
+def test_poisson_and_projection(gpu_lib, oracle_lib, name, precision):
+    o, s = make_pair(name, precision=ns.PREC_FP64_EXACT, tol=1e-12)
+    for _ in range(2):
+        o.step()
+    sync_state(o, s)
+    o.step_begin()
+    s.step_begin()
+    for _ in range(200):
+        for sub in range(4):
+            o.rk_stage(sub)
+            s.rk_stage(sub)
+        eo, eg = o.pseudo_norm(), s.pseudo_norm()
+        if eo <= 1e-10:
+            break
+    assert eg <= 1e-10
+    do, so_ = o.poisson_rhs()
+    dg, sg = s.poisson_rhs()
+    assert abs(dg - do) <= 1e-14 * abs(do)
+    np.testing.assert_array_equal(s.get_field(ns.FIELD_POISSON_RHS), o.field(12))
+    o.poisson_solve()
+    cyc, res = s.poisson_solve(precision)
+    assert res <= 1e-12 and cyc >= 1
+    phig, phio = s.get_field(ns.FIELD_PHI), o.field(11)
+    assert relp(phig, phio) <= 1e-10
+    dao = o.project()
+    dag = s.project()
+    assert dag <= 1e-10 * max(1.0, 1.5 / o.params.dt) and dag <= 1e-9
+    u, _, p, _ = s.get_state()
+    uo, _, po, _ = o.get_state()
+    for d in range(2):
+        assert rel(u[d], uo[d]) <= TOL_STEP
+    assert relp(p, po) <= TOL_STEP
+
+
+@pytest.mark.parametrize("name,nsteps", [("cavity32", 11), ("cavity128_cfg1", 6), ("tgv64_parity", 6), ("tgv64_fixed", 6)])
+def test_steps_resynced(gpu_lib, oracle_lib, name, nsteps):
+    """Per-step parity: both sides start every step from the oracle's state."""
+    o, s = make_pair(name)
+    for step in range(nsteps):
+        sync_state(o, s)
+        so = o.step()
+        sg = s.step()
+        assert sg["pseudo_iters"] == so["pseudo_iters"], (step, sg, so)
+        u, _, p, _ = s.get_state()
+        uo, _, po, _ = o.get_state()
+        for d in range(2):
+            assert rel(u[d], uo[d]) <= TOL_STEP, (step, d, rel(u[d], uo[d]))
+        assert relp(p, po) <= TOL_STEP, (step, relp(p, po))
+        assert sg["div_after"] <= 1e-9
+
+
+def test_free_running_matches_golden(gpu_lib):
+    """The shipped inputs physics, 11 free-running steps, against the committed fixture."""
+    import os
+
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "cavity32_exec_inputs.npz"))
+    p = ns.default_params(n_cell=32, precision=ns.PREC_FP64_EXACT, poisson_tol_rel=1e-13)
+    s = ns.Solver(p)
+    s.init(ns.INIT_CAVITY)
+    for step in range(1, 12):
+        st = s.step()
+        assert st["pseudo_iters"] == int(g["K"][step - 1])
+        u, _, pp, _ = s.get_state()
+        assert rel(u[0], g["u_%d" % step]) <= TOL_STEP
+        assert rel(u[1], g["v_%d" % step]) <= TOL_STEP
+        assert relp(pp, g["p_%d" % step]) <= TOL_STEP
+
+
+@pytest.mark.parametrize("precision", [ns.PREC_FP64, ns.PREC_MIXED])
+def test_fast_modes_track_oracle(gpu_lib, oracle_lib, precision):
+    o, s = make_pair("cavity128_cfg1", precision=precision)
+    for step in range(4):
+        sync_state(o, s)
+        so = o.step()
+        sg = s.step()
+        u, _, p, _ = s.get_state()
+        uo, _, po, _ = o.get_state()
+        for d in range(2):
+            assert rel(u[d], uo[d]) <= 1e-9, (step, d)
+        assert relp(p, po) <= 1e-9
+        assert abs(sg["pseudo_iters"] - so["pseudo_iters"]) <= 1

@@ -1,0 +1,187 @@
+"""Checks of the CPU oracle itself (no GPU).
+
+The reference ships no golden vectors, so the oracle is checked against
+(a) an independent numpy restatement of the RK stage (bit-exact),
+(b) a spectral (DCT / FFT) solve of the same discrete Poisson problem,
+(c) the known answers of the reference's own formulas: zero discrete
+divergence after projection, zero wall-normal velocity, the analytic
+Taylor-Green decay u0 exp(-2 nu t) with second-order convergence, and the
+BDF2 fixed point of the converged pseudo-time loop,
+(d) the committed golden fixtures (regression pin across x86 and Arm builds).
+"""
+import math
+import os
+
+import numpy as np
+import pytest
+
+from oracle.orc import FIELD_BASE, FIELD_MRHS, FIELD_STAR, Oracle
+from tests import npstage
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def cavity(n, **kw):
+    args = dict(ren=100.0, dt=1e-3, iter_num=100, max_grid_size=(n, n // 2, 16))
+    args.update(kw)
+    return Oracle(n, **args)
+
+
+def run_steps(o, k):
+    return [o.step() for _ in range(k)]
+
+
+@pytest.mark.parametrize("periodic", [False, True])
+def test_stage_matches_numpy_restatement(oracle_lib, periodic):
+    n = 24
+    if periodic:
+        L = 2 * math.pi
+        o = Oracle(n, prob_hi=(L, L, L), ren=400.0, dt=0.5 * L / n, bc_lo=(111, 111, 111), bc_hi=(111, 111, 111))
+        o.init(1)
+        bc_lo, bc_hi, inflow, per = (111, 111), (111, 111), (1.0, 0.0), (True, True)
+        dx = L / n
+    else:
+        o = cavity(n)
+        o.init(0)
+        bc_lo, bc_hi, inflow, per = (135, 135), (135, 165), (1.0, 0.0), (False, False)
+        dx = 1.0 / n
+    run_steps(o, 3)
+    u, up, p, _ = o.get_state()
+    o.set_state(u, up, p)
+    o.step_begin()
+    un = [o.field(2, d) for d in range(2)]
+    du = [o.field(3, d) for d in range(2)]
+    us = [o.field(FIELD_STAR, d) for d in range(2)]
+    ub = [o.field(FIELD_BASE, d) for d in range(2)]
+    dt = o.params.dt
+    rk = 0.4 * dt * 0.25
+    ref, rhs = npstage.stage(us, ub, un, du, p, n, dx, dx, dt, o.params.ren, rk, bc_lo, bc_hi, inflow, per)
+    o.rk_stage(0)
+    for d in range(2):
+        got = o.field(FIELD_STAR, d)
+        np.testing.assert_array_equal(got, ref[d])
+        np.testing.assert_array_equal(o.field(FIELD_MRHS, d), rhs[d])
+
+
+def _neumann_eigs(n, h):
+    k = np.arange(n)
+    return -(4.0 / h ** 2) * np.sin(np.pi * k / (2 * n)) ** 2
+
+
+def test_poisson_matches_dct_solution(oracle_lib):
+    from scipy.fft import dctn, idctn
+
+    n = 32
+    o = cavity(n)
+    rng = np.random.default_rng(0)
+    f = rng.standard_normal((n, n))
+    phi, it, res = o.solve_poisson(f)
+    assert res <= 1e-12
+    h = 1.0 / n
+    lam = _neumann_eigs(n, h)[None, :] + _neumann_eigs(n, h)[:, None]
+    fh = dctn(f - f.mean(), type=2, norm="ortho")
+    lam[0, 0] = 1.0
+    ph = fh / lam
+    ph[0, 0] = 0.0
+    ref = idctn(ph, type=2, norm="ortho")
+    err = np.abs((phi - phi.mean()) - (ref - ref.mean())).max() / np.abs(ref).max()
+    assert err <= 1e-11
+
+
+def test_poisson_matches_fft_solution_periodic(oracle_lib):
+    n = 32
+    L = 2 * math.pi
+    o = Oracle(n, prob_hi=(L, L, L), ren=100.0, dt=0.01, bc_lo=(111, 111, 111), bc_hi=(111, 111, 111))
+    rng = np.random.default_rng(1)
+    f = rng.standard_normal((n, n))
+    phi, it, res = o.solve_poisson(f)
+    h = L / n
+    k = np.arange(n)
+    e = -(4.0 / h ** 2) * np.sin(np.pi * k / n) ** 2
+    lam = e[None, :] + e[:, None]
+    lam[0, 0] = 1.0
+    fh = np.fft.fft2(f - f.mean())
+    ph = fh / lam
+    ph[0, 0] = 0.0
+    ref = np.real(np.fft.ifft2(ph))
+    err = np.abs((phi - phi.mean()) - (ref - ref.mean())).max() / np.abs(ref).max()
+    assert err <= 1e-11
+
+
+def test_cavity_invariants(oracle_lib):
+    n = 32
+    o = cavity(n)
+    o.init(0)
+    stats = run_steps(o, 5)
+    u, up, p, phi = o.get_state()
+    for s in stats:
+        assert s["div_after"] <= 1e-12
+        assert s["norm_error"] <= 1e-10
+        assert 1 <= s["pseudo_iters"] <= 101
+    # wall-normal velocities stay exactly zero (quirk Q4: R = 0 there)
+    assert np.all(u[0][:, 0] == 0) and np.all(u[0][:, -1] == 0)
+    assert np.all(u[1][0, :] == 0) and np.all(u[1][-1, :] == 0)
+    # the lid drags the top row to the right
+    assert u[0][-1, 1:-1].min() > 0
+
+
+def test_bdf2_fixed_point(oracle_lib):
+    """At pseudo-convergence the BDF2 residual of the predictor vanishes."""
+    n = 24
+    o = cavity(n, momentum_tolerance=1e-13, iter_num=400)
+    o.init(0)
+    run_steps(o, 2)
+    u, up, p, _ = o.get_state()
+    o.set_state(u, up, p)
+    o.step_begin()
+    for _ in range(400):
+        for sub in range(4):
+            o.rk_stage(sub)
+        e = o.pseudo_norm()
+        if e < 1e-13:
+            break
+    # one more stage from the converged state: its residual is the BDF2 equation
+    o.rk_stage(0)
+    r = [o.field(FIELD_MRHS, d) for d in range(2)]
+    scale = max(np.abs(u[0]).max(), 1e-30) * 1.5 / o.params.dt
+    assert max(np.abs(r[0]).max(), np.abs(r[1]).max()) <= 1e-8 * scale
+
+
+def test_taylor_green_decay_second_order(oracle_lib):
+    errs = []
+    for n in (16, 32, 64):
+        L = 2 * math.pi
+        dx = L / n
+        dt = 0.25 * dx
+        o = Oracle(n, prob_hi=(L, L, L), ren=100.0, dt=dt, iter_num=200, bc_lo=(111, 111, 111),
+                   bc_hi=(111, 111, 111), fix_quirks=1)
+        o.init(1)
+        u0, _, _, _ = o.get_state()
+        T = 0.2
+        ns = int(round(T / dt))
+        for _ in range(ns):
+            o.step()
+        u, _, _, _ = o.get_state()
+        ex = u0[0] * math.exp(-2.0 * ns * dt / 100.0)
+        errs.append(np.abs(u[0] - ex).max())
+    rate1 = math.log2(errs[0] / errs[1])
+    rate2 = math.log2(errs[1] / errs[2])
+    assert rate1 > 1.7 and rate2 > 1.7, errs
+
+
+def test_golden_fixtures(oracle_lib):
+    path = os.path.join(GOLDEN, "cavity32_exec_inputs.npz")
+    if not os.path.exists(path):
+        pytest.skip("golden fixture not generated")
+    g = np.load(path)
+    o = Oracle(32, max_grid_size=(32, 16, 16), ren=100.0, dt=1e-3, iter_num=100, poisson_tol=1e-13)
+    o.init(0)
+    for step in range(1, int(g["nsteps"]) + 1):
+        s = o.step()
+        assert s["pseudo_iters"] == int(g["K"][step - 1])
+        if ("u_%d" % step) in g:
+            u, _, p, _ = o.get_state()
+            np.testing.assert_allclose(u[0], g["u_%d" % step], rtol=0, atol=1e-13)
+            np.testing.assert_allclose(u[1], g["v_%d" % step], rtol=0, atol=1e-13)
+            pc = p - p.mean()
+            np.testing.assert_allclose(pc, g["p_%d" % step], rtol=0, atol=1e-11)
