@@ -34,7 +34,12 @@ EXPORTS = [
     "ns_get_dt", "ns_get_time", "ns_init_fields", "ns_put_box", "ns_get_box", "ns_set_state",
     "ns_get_state", "ns_step_begin", "ns_rk_stage", "ns_pseudo_norm", "ns_explicit_predictor",
     "ns_poisson_rhs", "ns_poisson_solve", "ns_project", "ns_step", "ns_step_host", "ns_sync",
+    "ns_profile_enable", "ns_profile_read", "ns_launch_count",
 ]
+
+PROF_KINDS = ["stage_exact", "stage_fast", "anchor", "increment", "explicit", "step_begin", "poisson_rhs",
+              "project", "mg_smooth0", "mg_smooth", "mg_restrict0", "mg_restrict", "mg_bottom", "mg_resnorm",
+              "dc_update", "other"]
 
 
 class NsError(RuntimeError):
@@ -127,6 +132,10 @@ def lib():
         L.ns_step.argtypes = [vp, P(NsStepStats)]
         L.ns_step_host.argtypes = [vp, P(dp), P(dp), dp, P(NsStepStats)]
         L.ns_sync.argtypes = [vp]
+        L.ns_profile_enable.argtypes = [vp, ctypes.c_int]
+        L.ns_profile_read.argtypes = [vp, dp, P(ctypes.c_longlong), ctypes.c_int, ctypes.c_int]
+        L.ns_launch_count.argtypes = [vp]
+        L.ns_launch_count.restype = ctypes.c_longlong
         _lib = L
     return _lib
 
@@ -280,3 +289,17 @@ class Solver:
 
     def sync(self):
         self._check(lib().ns_sync(self.h), "ns_sync")
+
+    def profile(self, on=True):
+        self._check(lib().ns_profile_enable(self.h, 1 if on else 0), "ns_profile_enable")
+
+    def profile_read(self, reset=False):
+        """{kind: (launches, total device ms)} from the per-launch CUDA events."""
+        k = len(PROF_KINDS)
+        ms = (ctypes.c_double * k)()
+        cnt = (ctypes.c_longlong * k)()
+        self._check(lib().ns_profile_read(self.h, ms, cnt, k, 1 if reset else 0), "ns_profile_read")
+        return {PROF_KINDS[i]: (int(cnt[i]), float(ms[i])) for i in range(k)}
+
+    def launch_count(self):
+        return int(lib().ns_launch_count(self.h))

@@ -33,6 +33,11 @@ cudaError_t launch_mg_bottom(const MGLevels<T>& M, int lb, int x_zero, cudaStrea
 template <typename T>
 cudaError_t launch_mg_resnorm(const MGLevels<T>& M, double* part, unsigned* counter, double* out, cudaStream_t s);
 
+// kernels_mixed.cu
+struct IncArgs;
+cudaError_t launch_inc_stage(const IncArgs& a, cudaStream_t s);
+cudaError_t launch_add_inc(const Geom& g, const double* const* base, const float* const* e, double* const* out, cudaStream_t s);
+
 struct DCArgs {
   int n;
   long pitch;

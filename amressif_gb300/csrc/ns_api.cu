@@ -19,6 +19,7 @@
 
 #include "../../include/amressif_gpu.h"
 #include "launch.h"
+#include "stage_inc2d.cuh"
 
 using namespace ns;
 
@@ -62,6 +63,15 @@ struct ns_ctx {
   double* red_h = nullptr;  // pinned mirror
   cudaEvent_t ev[4];
   bool ev_ok = false;
+  // mixed iteration: E[0] holds an increment not yet added to the base
+  bool mix_pending = false;
+  // per-kernel timing (CUDA events around each launch) and launch count
+  bool prof = false;
+  std::vector<cudaEvent_t> evpool;
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pend;
+  double pms[NS_PROF_KINDS] = {0};
+  long long pcnt[NS_PROF_KINDS] = {0};
+  long long launches = 0;
   std::string err;
 };
 
@@ -126,6 +136,8 @@ void free_all(ns_ctx* c) {
   F(c->part); F(c->counter); F(c->red);
   if (c->red_h) cudaFreeHost(c->red_h);
   if (c->ev_ok) for (auto& e : c->ev) cudaEventDestroy(e);
+  for (auto& p : c->pend) { cudaEventDestroy(p.second.first); cudaEventDestroy(p.second.second); }
+  for (auto& e : c->evpool) cudaEventDestroy(e);
   if (c->own_stream && c->st) cudaStreamDestroy(c->st);
 }
 
@@ -169,9 +181,12 @@ int alloc_levels(ns_ctx* c, MGLevels<T>& M, bool own_level0) {
   return NS_OK;
 }
 
+void prof_resolve(ns_ctx* c);
+
 int sync_red(ns_ctx* c, int first, int count) {
   CK(cudaMemcpyAsync(c->red_h + first, c->red + first, count * sizeof(double), cudaMemcpyDeviceToHost, c->st), "readback");
   CK(cudaStreamSynchronize(c->st), "stream sync");
+  if (c->prof) prof_resolve(c);
   return NS_OK;
 }
 
@@ -196,6 +211,60 @@ int pick_out(int base, int in) {
     if (i != base && i != in) return i;
   return -2;
 }
+
+cudaEvent_t pool_get(ns_ctx* c) {
+  if (!c->evpool.empty()) {
+    cudaEvent_t e = c->evpool.back();
+    c->evpool.pop_back();
+    return e;
+  }
+  cudaEvent_t e;
+  if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+  return e;
+}
+
+// Fold completed launch timings into the per-kind totals (stream is idle).
+void prof_resolve(ns_ctx* c) {
+  for (auto& p : c->pend) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, p.second.first, p.second.second) == cudaSuccess) {
+      c->pms[p.first] += ms;
+      c->pcnt[p.first] += 1;
+    }
+    c->evpool.push_back(p.second.first);
+    c->evpool.push_back(p.second.second);
+  }
+  c->pend.clear();
+}
+
+// Launch one kernel (a callable returning cudaError_t), counting it and, when
+// profiling is on, bracketing it with events on the context's stream.
+template <class F>
+int launch(ns_ctx* c, int kind, const char* what, F&& f) {
+  cudaEvent_t a = nullptr, b = nullptr;
+  if (c->prof) {
+    a = pool_get(c);
+    b = pool_get(c);
+    if (a) cudaEventRecord(a, c->st);
+  }
+  const cudaError_t e = f();
+  c->launches++;
+  if (c->prof && a && b) {
+    cudaEventRecord(b, c->st);
+    c->pend.push_back({kind, {a, b}});
+    if (c->pend.size() > 4096) {
+      cudaStreamSynchronize(c->st);
+      prof_resolve(c);
+    }
+  }
+  return cuda_check(c, e, what);
+}
+
+#define LAUNCH(kind, what, expr)                                   \
+  do {                                                             \
+    int _r = launch(c, kind, what, [&]() -> cudaError_t { return (expr); }); \
+    if (_r != NS_OK) return _r;                                    \
+  } while (0)
 
 }  // namespace
 
@@ -546,8 +615,8 @@ int ns_step_begin(ns_ctx* c) {
     a.S[m] = c->S[m];
   }
   a.p = c->Pp;
-  cudaError_t e = (c->P.precision == NS_PREC_FP64_EXACT) ? launch_step_begin_exact(a, c->st) : launch_step_begin_fast(a, c->st);
-  CK(e, "step_begin");
+  LAUNCH(NS_PROF_STEP_BEGIN, "step_begin",
+         (c->P.precision == NS_PREC_FP64_EXACT) ? launch_step_begin_exact(a, c->st) : launch_step_begin_fast(a, c->st));
   // velContPrev <- velCont, velStar <- velCont: the old u^{n-1} buffer becomes
   // the target of the projection
   for (int m = 0; m < 2; ++m) std::swap(c->U[m], c->UP[m]);
@@ -572,8 +641,8 @@ static int launch_rk(ns_ctx* c, int sub, bool use_cart) {
   a.rk = c->rk[sub];
   a.do_norm = (sub == 3);
   const int mode = (c->P.precision == NS_PREC_FP64_EXACT) ? kExactRK : kFastRK;
-  cudaError_t e = (mode == kExactRK) ? launch_stage_exact(mode, a, c->st) : launch_stage_fast(mode, a, c->st);
-  CK(e, "rk stage");
+  LAUNCH(mode == kExactRK ? NS_PROF_STAGE_EXACT : NS_PROF_STAGE_FAST, "rk stage",
+         (mode == kExactRK) ? launch_stage_exact(mode, a, c->st) : launch_stage_fast(mode, a, c->st));
   c->cur = outb;
   return NS_OK;
 }
@@ -612,7 +681,7 @@ int ns_explicit_predictor(ns_ctx* c, double* norm) {
     a.cart[m] = c->cart_pending ? c->CART[m] : nullptr;
   }
   a.do_norm = 1;
-  CK(launch_stage_exact(kExplicit, a, c->st), "explicit stage");
+  LAUNCH(NS_PROF_EXPLICIT, "explicit stage", launch_stage_exact(kExplicit, a, c->st));
   c->cart_pending = false;
   c->cur = outb;
   int r = sync_red(c, kRedNorm, 1);
@@ -631,8 +700,9 @@ static int poisson_rhs_async(ns_ctx* c) {
   a.part = c->part;
   a.counter = c->counter;
   a.red_out = c->red + kRedDivBefore;  // {max|div|, sum}
-  cudaError_t e = (c->P.precision == NS_PREC_FP64_EXACT) ? launch_poisson_rhs_exact(a, c->st) : launch_poisson_rhs_fast(a, c->st);
-  return cuda_check(c, e, "poisson rhs");
+  LAUNCH(NS_PROF_POISSON_RHS, "poisson rhs",
+         (c->P.precision == NS_PREC_FP64_EXACT) ? launch_poisson_rhs_exact(a, c->st) : launch_poisson_rhs_fast(a, c->st));
+  return NS_OK;
 }
 
 int ns_poisson_rhs(ns_ctx* c, double* divmax, double* sum) {
@@ -650,11 +720,12 @@ int ns_poisson_rhs(ns_ctx* c, double* divmax, double* sum) {
 template <typename T>
 static int vcycle(ns_ctx* c, MGLevels<T>& M, int x0_zero) {
   for (int l = 0; l < c->lb; ++l) {
-    CK(launch_mg_smooth<T>(M, l, 0, (l > 0) ? 1 : x0_zero, c->st), "mg smooth");
-    CK(launch_mg_restrict<T>(M, l, c->st), "mg restrict");
+    LAUNCH(l == 0 ? NS_PROF_MG_SMOOTH0 : NS_PROF_MG_SMOOTH, "mg smooth", launch_mg_smooth<T>(M, l, 0, (l > 0) ? 1 : x0_zero, c->st));
+    LAUNCH(l == 0 ? NS_PROF_MG_RESTRICT0 : NS_PROF_MG_RESTRICT, "mg restrict", launch_mg_restrict<T>(M, l, c->st));
   }
-  CK(launch_mg_bottom<T>(M, c->lb, (c->lb > 0) ? 1 : x0_zero, c->st), "mg bottom");
-  for (int l = c->lb - 1; l >= 0; --l) CK(launch_mg_smooth<T>(M, l, 1, 0, c->st), "mg prolong+smooth");
+  LAUNCH(NS_PROF_MG_BOTTOM, "mg bottom", launch_mg_bottom<T>(M, c->lb, (c->lb > 0) ? 1 : x0_zero, c->st));
+  for (int l = c->lb - 1; l >= 0; --l)
+    LAUNCH(l == 0 ? NS_PROF_MG_SMOOTH0 : NS_PROF_MG_SMOOTH, "mg prolong+smooth", launch_mg_smooth<T>(M, l, 1, 0, c->st));
   return NS_OK;
 }
 
@@ -666,8 +737,7 @@ extern "C" {
 int ns_poisson_solve(ns_ctx* c, int precision, int* cycles, double* res) {
   if (!c) return NS_ERR_ARG;
   const double nn = (double)c->N * (double)c->N;
-  k_set_mean<<<1, 1, 0, c->st>>>(c->red, 1.0 / nn);
-  CK(cudaGetLastError(), "set mean");
+  LAUNCH(NS_PROF_OTHER, "set mean", (k_set_mean<<<1, 1, 0, c->st>>>(c->red, 1.0 / nn), cudaGetLastError()));
   const int maxc = std::max(1, c->P.poisson_max_cycles);
   const double div_tol_res = c->P.poisson_tol_div > 0 ? c->P.poisson_tol_div * 1.5 / c->dt : 0.0;
   double rnorm0 = 0.0, rn = 0.0;
@@ -695,7 +765,7 @@ int ns_poisson_solve(ns_ctx* c, int precision, int* cycles, double* res) {
     d.phi_in = c->PHI[pc];
     d.phi_out = c->PHI[pc];
     d.first = 1;
-    CK(launch_dc_update(d, c->st), "dc update");
+    LAUNCH(NS_PROF_DC_UPDATE, "dc update", launch_dc_update(d, c->st));
     int r = sync_red(c, kRedRes, 1);
     if (r != NS_OK) return r;
     rnorm0 = c->red_h[kRedRes];
@@ -711,7 +781,7 @@ int ns_poisson_solve(ns_ctx* c, int precision, int* cycles, double* res) {
       d.first = 0;
       d.phi_in = c->PHI[pc];
       d.phi_out = c->PHI[1 - pc];
-      CK(launch_dc_update(d, c->st), "dc update");
+      LAUNCH(NS_PROF_DC_UPDATE, "dc update", launch_dc_update(d, c->st));
       pc = 1 - pc;
       ++ncyc;
       r2 = sync_red(c, kRedRes, 1);
@@ -724,7 +794,7 @@ int ns_poisson_solve(ns_ctx* c, int precision, int* cycles, double* res) {
     c->phi_cur = 0;
     c->M64.x[0] = c->PHI[0];
     CK(cudaMemsetAsync(c->PHI[0], 0, c->fbytes, c->st), "memset phi");  // poisson.cpp:63
-    CK(launch_mg_resnorm<double>(c->M64, c->part, c->counter, c->red + kRedRes, c->st), "resnorm");
+    LAUNCH(NS_PROF_MG_RESNORM, "resnorm", launch_mg_resnorm<double>(c->M64, c->part, c->counter, c->red + kRedRes, c->st));
     int r = sync_red(c, kRedRes, 1);
     if (r != NS_OK) return r;
     rnorm0 = c->red_h[kRedRes];
@@ -738,7 +808,7 @@ int ns_poisson_solve(ns_ctx* c, int precision, int* cycles, double* res) {
       int r2 = vcycle<double>(c, c->M64, ncyc == 0 ? 1 : 0);
       if (r2 != NS_OK) return r2;
       ++ncyc;
-      CK(launch_mg_resnorm<double>(c->M64, c->part, c->counter, c->red + kRedRes, c->st), "resnorm");
+      LAUNCH(NS_PROF_MG_RESNORM, "resnorm", launch_mg_resnorm<double>(c->M64, c->part, c->counter, c->red + kRedRes, c->st));
       r2 = sync_red(c, kRedRes, 1);
       if (r2 != NS_OK) return r2;
       rn = c->red_h[kRedRes];
@@ -765,8 +835,9 @@ static int project_async(ns_ctx* c) {
   a.part = c->part;
   a.counter = c->counter;
   a.red_out = c->red + kRedDivAfter;
-  cudaError_t e = (c->P.precision == NS_PREC_FP64_EXACT) ? launch_project_exact(a, c->st) : launch_project_fast(a, c->st);
-  return cuda_check(c, e, "project");
+  LAUNCH(NS_PROF_PROJECT, "project",
+         (c->P.precision == NS_PREC_FP64_EXACT) ? launch_project_exact(a, c->st) : launch_project_fast(a, c->st));
+  return NS_OK;
 }
 
 int ns_project(ns_ctx* c, double* divmax) {
@@ -779,8 +850,86 @@ int ns_project(ns_ctx* c, double* divmax) {
   return NS_OK;
 }
 
+// One pseudo-iteration of the mixed-precision predictor: FP64 anchor
+// G(u_base) (after adding the pending increment of the previous iteration),
+// then three FP32 increment stages; the fourth stage's increment e4 stays in
+// E[0] and its norm is the pseudo-increment norm of Error_Computation.
+static int mixed_iteration(ns_ctx* c, double* norm) {
+  const int outb = pick_out(c->base, c->base);
+  StageArgs a = base_stage_args(c);
+  for (int m = 0; m < 2; ++m) {
+    a.us[m] = face_ptr(c, c->base, m);
+    a.e4[m] = c->mix_pending ? c->E[0][m] : nullptr;
+    a.out[m] = c->B[outb][m];
+    a.g0[m] = c->G0[m];
+    a.shadow[m] = c->SH[m];
+  }
+  LAUNCH(NS_PROF_ANCHOR, "anchor stage", launch_stage_fast(kAnchor, a, c->st));
+  c->base = outb;
+  c->cur = outb;
+  IncArgs ia;
+  std::memset(&ia, 0, sizeof(ia));
+  ia.g = c->g;
+  ia.part = c->part;
+  ia.counter = c->counter;
+  ia.norm_out = c->red + kRedNorm;
+  for (int m = 0; m < 2; ++m) {
+    ia.sh[m] = c->SH[m];
+    ia.g0[m] = c->G0[m];
+  }
+  for (int s = 1; s <= 3; ++s) {
+    const int src = (s == 2) ? 0 : 1, dst = (s == 2) ? 1 : 0;
+    for (int m = 0; m < 2; ++m) {
+      ia.ein[m] = (s == 1) ? nullptr : c->E[src][m];
+      ia.eout[m] = c->E[dst][m];
+    }
+    ia.rk_prev = (float)c->rk[s - 1];
+    ia.rk = (float)c->rk[s];
+    ia.do_norm = (s == 3);
+    LAUNCH(NS_PROF_INC, "increment stage", launch_inc_stage(ia, c->st));
+  }
+  c->mix_pending = true;
+  int r = sync_red(c, kRedNorm, 1);
+  if (r != NS_OK) return r;
+  *norm = c->red_h[kRedNorm];
+  return NS_OK;
+}
+
+// u* = u_base + e4 once the mixed iteration stops
+static int mixed_finalize(ns_ctx* c) {
+  if (!c->mix_pending) return NS_OK;
+  const int outb = pick_out(c->base, c->base);
+  const double* base[2] = {face_ptr(c, c->base, 0), face_ptr(c, c->base, 1)};
+  const float* e[2] = {c->E[0][0], c->E[0][1]};
+  double* out[2] = {c->B[outb][0], c->B[outb][1]};
+  LAUNCH(NS_PROF_OTHER, "add increment", launch_add_inc(c->g, base, e, out, c->st));
+  c->base = outb;
+  c->cur = outb;
+  c->mix_pending = false;
+  return NS_OK;
+}
+
+static int alloc_mixed(ns_ctx* c) {
+  if (c->SH[0]) return NS_OK;
+  const size_t fb = (size_t)c->pitch * (c->N + 1) * sizeof(float);
+  for (int m = 0; m < 2; ++m) {
+    float** ps[4] = {&c->SH[m], &c->G0[m], &c->E[0][m], &c->E[1][m]};
+    for (float** p : ps) {
+      if (cudaMalloc(p, fb) != cudaSuccess) return fail(c, NS_ERR_NOMEM, "cudaMalloc (mixed) failed");
+      CK(cudaMemsetAsync(*p, 0, fb, c->st), "memset");
+    }
+  }
+  return NS_OK;
+}
+
 int ns_step(ns_ctx* c, ns_step_stats* stats) {
   if (!c) return NS_ERR_ARG;
+  const bool mixed = (c->P.precision == NS_PREC_MIXED) && c->P.pseudo_timestepping != 0;
+  if (mixed) {
+    int ra = alloc_mixed(c);
+    if (ra != NS_OK) return ra;
+  }
+  c->mix_pending = false;
   ns_step_stats s;
   std::memset(&s, 0, sizeof(s));
   if (c->ev_ok) cudaEventRecord(c->ev[0], c->st);
@@ -795,18 +944,28 @@ int ns_step(ns_ctx* c, ns_step_stats* stats) {
       countIter = 1;
       break;
     }
-    for (int sub = 0; sub < 4; ++sub) {
-      r = ns_rk_stage(c, sub);
+    if (mixed && !c->cart_pending) {
+      // the analytic first-stage cell velocity of an initial condition is
+      // only consumed by the FP64 stages, so the first iteration after
+      // ns_init_fields(TGV) runs in FP64
+      r = mixed_iteration(c, &normError);
+      if (r != NS_OK) return r;
+    } else {
+      for (int sub = 0; sub < 4; ++sub) {
+        r = ns_rk_stage(c, sub);
+        if (r != NS_OK) return r;
+      }
+      r = ns_pseudo_norm(c, &normError);
       if (r != NS_OK) return r;
     }
-    r = ns_pseudo_norm(c, &normError);
-    if (r != NS_OK) return r;
     countIter++;
     if (countIter > c->P.iter_num) { s.status = NS_WARN_PSEUDO_MAXITER; break; }
     if (normError > 1.e2) { s.status = NS_WARN_PSEUDO_DIVERGED; break; }
   }
   s.pseudo_iters = countIter;
   s.norm_error = normError;
+  r = mixed_finalize(c);
+  if (r != NS_OK) return r;
   if (c->ev_ok) cudaEventRecord(c->ev[1], c->st);
   r = ns_poisson_rhs(c, &s.div_before, &s.rhs_sum);
   if (r != NS_OK) return r;
@@ -841,5 +1000,32 @@ int ns_step_host(ns_ctx* c, double* const* u, double* const* u_prev, double* p, 
   r = ns_get_state(c, u, u_prev, p, nullptr);
   return r != NS_OK ? r : st;
 }
+
+}  // extern "C"
+
+extern "C" {
+
+int ns_profile_enable(ns_ctx* c, int on) {
+  if (!c) return NS_ERR_ARG;
+  CK(cudaStreamSynchronize(c->st), "stream sync");
+  prof_resolve(c);
+  c->prof = on != 0;
+  return NS_OK;
+}
+
+int ns_profile_read(ns_ctx* c, double* ms, long long* counts, int nkinds, int reset) {
+  if (!c || nkinds < 0) return NS_ERR_ARG;
+  CK(cudaStreamSynchronize(c->st), "stream sync");
+  prof_resolve(c);
+  for (int k = 0; k < nkinds && k < NS_PROF_KINDS; ++k) {
+    if (ms) ms[k] = c->pms[k];
+    if (counts) counts[k] = c->pcnt[k];
+  }
+  if (reset)
+    for (int k = 0; k < NS_PROF_KINDS; ++k) { c->pms[k] = 0.0; c->pcnt[k] = 0; }
+  return NS_OK;
+}
+
+long long ns_launch_count(const ns_ctx* c) { return c ? c->launches : -1; }
 
 }  // extern "C"

@@ -143,6 +143,31 @@ int ns_step_host(ns_ctx* c, double* const* u, double* const* u_prev, double* p, 
 /* Synchronise the context's stream. */
 int ns_sync(ns_ctx* c);
 
+/* ---- instrumentation (no reference counterpart: replaces TinyProfiler
+ * regions, Exec/GNUmakefile:13, and the per-step timer of main.cpp:1173-1175)
+ * Per-kernel-kind device time from CUDA events around every launch on the
+ * context's stream, and the number of kernels launched. */
+#define NS_PROF_STAGE_EXACT 0
+#define NS_PROF_STAGE_FAST 1
+#define NS_PROF_ANCHOR 2
+#define NS_PROF_INC 3
+#define NS_PROF_EXPLICIT 4
+#define NS_PROF_STEP_BEGIN 5
+#define NS_PROF_POISSON_RHS 6
+#define NS_PROF_PROJECT 7
+#define NS_PROF_MG_SMOOTH0 8   /* finest-level smoothing (+ prolongation) */
+#define NS_PROF_MG_SMOOTH 9
+#define NS_PROF_MG_RESTRICT0 10
+#define NS_PROF_MG_RESTRICT 11
+#define NS_PROF_MG_BOTTOM 12
+#define NS_PROF_MG_RESNORM 13
+#define NS_PROF_DC_UPDATE 14
+#define NS_PROF_OTHER 15
+#define NS_PROF_KINDS 16
+int ns_profile_enable(ns_ctx* c, int on);
+int ns_profile_read(ns_ctx* c, double* ms, long long* counts, int nkinds, int reset);
+long long ns_launch_count(const ns_ctx* c);
+
 #ifdef __cplusplus
 }
 #endif

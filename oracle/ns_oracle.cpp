@@ -356,9 +356,9 @@ void ctx_ghosts(orc_ctx* c) {
 }
 
 // ---------------------------------------------------------------------------
-// Exact discrete Poisson solve: PCG on -L with a symmetric V-cycle
-// preconditioner (red-black Gauss-Seidel, cell averaging, constant
-// prolongation, Galerkin-scaled coarse operators). Replaces AMReX MLMG
+// Exact discrete Poisson solve: PCG on -L with a symmetric V(2,2)
+// preconditioner (red-black Gauss-Seidel, bilinear prolongation, its transpose
+// as restriction, rediscretised coarse operators). Replaces AMReX MLMG
 // (poisson.cpp:41-186), which solves the same problem to rel 1e-10.
 // ---------------------------------------------------------------------------
 
@@ -379,7 +379,6 @@ void mg_build(orc_ctx* c) {
     if (n % 2 != 0 || n <= 4) break;
     n /= 2;
     for (int d = 0; d < 3; ++d) h[d] *= 2;
-    scale *= 2.0;
   }
 }
 
@@ -475,21 +474,66 @@ void mg_vcycle(orc_ctx* c, size_t l) {
   mg_smooth(c, L, 0, 2);
   mg_residual(c, L);
   MGLevel& C = c->mg[l + 1];
+  // restriction = transpose of the bilinear prolongation / 2^dim (gathered per
+  // coarse cell so that rows can run in parallel deterministically)
   const double inv = 1.0 / (c->D == 3 ? 8.0 : 4.0);
-  for (int k = 0; k < C.n[2]; ++k)
-    for (int j = 0; j < C.n[1]; ++j)
-      for (int i = 0; i < C.n[0]; ++i) {
-        double s = 0.0;
-        for (int dk = 0; dk < (c->D == 3 ? 2 : 1); ++dk)
-          for (int dj = 0; dj < 2; ++dj)
-            for (int di = 0; di < 2; ++di) s += L.r(2 * i + di, 2 * j + dj, c->D == 3 ? 2 * k + dk : 0);
-        C.f(i, j, k) = s * inv;
+  const long crows = (long)C.n[1] * C.n[2];
+#pragma omp parallel for schedule(static)
+  for (long r = 0; r < crows; ++r) {
+    const int J = (int)(r % C.n[1]), K = (int)(r / C.n[1]);
+    for (int I = 0; I < C.n[0]; ++I) {
+      const int CI[3] = {I, J, K};
+      int cand[3][4], nc[3];
+      double wt[3][4];
+      for (int d = 0; d < 3; ++d) {
+        nc[d] = 0;
+        if (d >= c->D) { cand[d][0] = 0; wt[d][0] = 1.0; nc[d] = 1; continue; }
+        const int n = L.n[d], ncd = C.n[d];
+        for (int q = -1; q <= 2; ++q) {
+          int i = 2 * CI[d] + q;
+          if (c->periodic[d]) i = (i + n) % n;
+          else if (i < 0 || i >= n) continue;
+          const int par = i / 2;
+          int sec = par + ((i & 1) ? 1 : -1);
+          sec = c->periodic[d] ? (sec + ncd) % ncd : std::min(std::max(sec, 0), ncd - 1);
+          const double w = (par == CI[d] ? 0.75 : 0.0) + (sec == CI[d] ? 0.25 : 0.0);
+          if (w != 0.0) { cand[d][nc[d]] = i; wt[d][nc[d]] = w; nc[d]++; }
+        }
       }
+      double s = 0.0;
+      for (int a = 0; a < nc[2]; ++a)
+        for (int b = 0; b < nc[1]; ++b)
+          for (int e = 0; e < nc[0]; ++e) s += wt[0][e] * wt[1][b] * wt[2][a] * L.r(cand[0][e], cand[1][b], cand[2][a]);
+      C.f(I, J, K) = s * inv;
+    }
+  }
   C.x.setVal(0.0);
   mg_vcycle(c, l + 1);
-  for (int k = 0; k < L.n[2]; ++k)
-    for (int j = 0; j < L.n[1]; ++j)
-      for (int i = 0; i < L.n[0]; ++i) L.x(i, j, k) += C.x(i / 2, j / 2, c->D == 3 ? k / 2 : 0);
+  // bilinear (trilinear) cell-centred prolongation, clamped (Neumann) or wrapped
+  const long rows = (long)L.n[1] * L.n[2];
+#pragma omp parallel for schedule(static)
+  for (long r = 0; r < rows; ++r) {
+    const int j = (int)(r % L.n[1]), k = (int)(r / L.n[1]);
+    for (int i = 0; i < L.n[0]; ++i) {
+      const int fi[3] = {i, j, k};
+      int par[3], sec[3];
+      for (int d = 0; d < 3; ++d) {
+        if (d >= c->D) { par[d] = sec[d] = 0; continue; }
+        const int ncd = C.n[d];
+        par[d] = fi[d] / 2;
+        int s2 = par[d] + ((fi[d] & 1) ? 1 : -1);
+        sec[d] = c->periodic[d] ? (s2 + ncd) % ncd : std::min(std::max(s2, 0), ncd - 1);
+      }
+      double s = 0.0;
+      for (int a = 0; a < (c->D == 3 ? 2 : 1); ++a)
+        for (int b = 0; b < 2; ++b)
+          for (int e = 0; e < 2; ++e) {
+            const double w = (e ? 0.25 : 0.75) * (b ? 0.25 : 0.75) * (c->D == 3 ? (a ? 0.25 : 0.75) : 1.0);
+            s += w * C.x(e ? sec[0] : par[0], b ? sec[1] : par[1], c->D == 3 ? (a ? sec[2] : par[2]) : 0);
+          }
+      L.x(i, j, k) += s;
+    }
+  }
   mg_smooth(c, L, 1, 2);
 }
 
@@ -691,7 +735,13 @@ int orc_create(const orc_params* p, orc_ctx** out) {
   define_cell(c, c->ctx[0], 1); define_cell(c, c->ctx[1], 1);
   define_cell(c, c->prhs, 1); define_cell(c, c->psol, 1);
   // RK coefficients (main.cpp:861-870)
-  const double d_tau = 0.4 * p->dt;
+  double d_tau = 0.4 * p->dt;
+  if (p->dtau_clip) {
+    double coeff = 0.0;
+    for (int d = 0; d < c->D; ++d) coeff += 1.0 / (c->dx[d] * c->dx[d]);
+    const double lam = 4.0 / p->ren * coeff + 1.5 / p->dt;
+    d_tau = std::min(d_tau, 0.9 * 2.785 / lam);
+  }
   c->rk[0] = d_tau * 0.25;
   c->rk[1] = d_tau * (1.0 / 3.0);
   c->rk[2] = d_tau * 0.5;

@@ -45,6 +45,7 @@ typedef struct orc_params {
   int fix_quirks;          /* 0: reproduce reference quirks Q1/Q2/Q5/Q6; 1: physically consistent variant */
   double poisson_tol;      /* relative max-norm residual target of the exact solve (<= 1e-12) */
   int nthreads;            /* OpenMP threads (0 = runtime default) */
+  int dtau_clip;           /* 1: clip dtau to 0.9 x the RK4 stability limit (grids where 0.4 dt is unstable) */
 } orc_params;
 
 typedef struct orc_step_stats {
