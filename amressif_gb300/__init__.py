@@ -34,8 +34,26 @@ EXPORTS = [
     "ns_get_dt", "ns_get_time", "ns_init_fields", "ns_put_box", "ns_get_box", "ns_set_state",
     "ns_get_state", "ns_step_begin", "ns_rk_stage", "ns_pseudo_norm", "ns_explicit_predictor",
     "ns_poisson_rhs", "ns_poisson_solve", "ns_project", "ns_step", "ns_step_host", "ns_sync",
-    "ns_profile_enable", "ns_profile_read", "ns_launch_count",
+    "ns_profile_enable", "ns_profile_read", "ns_launch_count", "ns_host_alloc", "ns_host_free",
 ]
+
+
+class PinnedArray:
+    """numpy float64 array over page-locked host memory (ns_host_alloc)."""
+
+    def __init__(self, shape):
+        n = int(np.prod(shape))
+        self.ptr = lib().ns_host_alloc(n * 8)
+        if not self.ptr:
+            raise MemoryError("ns_host_alloc failed")
+        buf = (ctypes.c_double * n).from_address(self.ptr)
+        self.a = np.frombuffer(buf, dtype=np.float64).reshape(shape)
+
+    def free(self):
+        if self.ptr:
+            self.a = None
+            lib().ns_host_free(self.ptr)
+            self.ptr = None
 
 PROF_KINDS = ["stage_exact", "stage_fast", "anchor", "increment", "explicit", "step_begin", "poisson_rhs",
               "project", "mg_smooth0", "mg_smooth", "mg_restrict0", "mg_restrict", "mg_bottom", "mg_resnorm",
@@ -136,6 +154,10 @@ def lib():
         L.ns_profile_read.argtypes = [vp, dp, P(ctypes.c_longlong), ctypes.c_int, ctypes.c_int]
         L.ns_launch_count.argtypes = [vp]
         L.ns_launch_count.restype = ctypes.c_longlong
+        L.ns_host_alloc.argtypes = [ctypes.c_ulonglong]
+        L.ns_host_alloc.restype = ctypes.c_void_p
+        L.ns_host_free.argtypes = [ctypes.c_void_p]
+        L.ns_host_free.restype = None
         _lib = L
     return _lib
 

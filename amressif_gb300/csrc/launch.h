@@ -35,8 +35,12 @@ cudaError_t launch_mg_resnorm(const MGLevels<T>& M, double* part, unsigned* coun
 
 // kernels_mixed.cu
 struct IncArgs;
+struct AnchorFFArgs;
 cudaError_t launch_inc_stage(const IncArgs& a, cudaStream_t s);
-cudaError_t launch_add_inc(const Geom& g, const double* const* base, const float* const* e, double* const* out, cudaStream_t s);
+cudaError_t launch_anchor_ff(const AnchorFFArgs& a, cudaStream_t s);
+cudaError_t launch_split_ff(const Geom& g, const double* const* x, float* const* h, float* const* l, cudaStream_t s);
+cudaError_t launch_ff_add_inc(const Geom& g, const float* const* h, const float* const* l, const float* const* e,
+                              double* const* out, cudaStream_t s);
 
 struct DCArgs {
   int n;

@@ -27,6 +27,8 @@ struct MGLevels {
   T* x[kMaxLevels];
   T* f[kMaxLevels];
   double invh2[kMaxLevels][2];
+  // 1/diagonal for the (east+west, north+south) neighbour counts: index a + 3 b
+  double invdiag[kMaxLevels][9];
   int periodic[2];
   const double* fmean;            // subtracted from f at level 0 when non-null
 };
@@ -34,10 +36,11 @@ struct MGLevels {
 // Gauss-Seidel update of one cell from its four neighbours; w* = 0 removes an
 // absent (Neumann) neighbour from both the sum and the diagonal.
 template <typename T>
-__device__ __forceinline__ T gs_update(T xe, T xw, T xn, T xs, T we, T ww, T wn, T wsn, T ihx, T ihy, T f) {
+__device__ __forceinline__ T gs_update(T xe, T xw, T xn, T xs, T we, T ww, T wn, T wsn, T ihx, T ihy, T f,
+                                       const double* invdiag) {
   const T sum = (we * xe + ww * xw) * ihx + (wn * xn + wsn * xs) * ihy;
-  const T diag = (we + ww) * ihx + (wn + wsn) * ihy;
-  return (sum - f) / diag;
+  const int k = (int)(we + ww) + 3 * (int)(wn + wsn);
+  return (sum - f) * (T)invdiag[k];
 }
 
 template <typename T>
@@ -105,16 +108,19 @@ __global__ void __launch_bounds__(256) k_mg_smooth(MGLevels<T> M, int l, int mod
     const int color = (cfirst + s) & 1;
     const int r = H - 1 - s;
     const int w = TX + 2 * r, h = TY + 2 * r;
-    for (int t = tid; t < w * h; t += NT) {
-      const int a = x0 - r + t % w, b = y0 - r + t / w;
-      if (((a + b) & 1) != color) continue;
+    const int w2 = (w + 1) / 2;  // cells of one colour per row (at most)
+    for (int t = tid; t < w2 * h; t += NT) {
+      const int b = y0 - r + t / w2;
+      const int a0 = x0 - r;
+      const int a = a0 + 2 * (t % w2) + (((a0 + b) & 1) != color ? 1 : 0);
+      if (a >= a0 + w) continue;
       if (!px && (a < 0 || a >= n)) continue;
       if (!py && (b < 0 || b >= n)) continue;
       const int lx = a - (x0 - H), ly = b - (y0 - H);
       const T we = (px || a + 1 < n) ? (T)1 : (T)0, ww = (px || a > 0) ? (T)1 : (T)0;
       const T wn = (py || b + 1 < n) ? (T)1 : (T)0, wsn = (py || b > 0) ? (T)1 : (T)0;
       sm.x[ly][lx] = gs_update<T>(sm.x[ly][lx + 1], sm.x[ly][lx - 1], sm.x[ly + 1][lx], sm.x[ly - 1][lx],
-                                  we, ww, wn, wsn, ihx, ihy, sm.f[ly][lx]);
+                                  we, ww, wn, wsn, ihx, ihy, sm.f[ly][lx], M.invdiag[l]);
     }
     __syncthreads();
   }
@@ -238,7 +244,7 @@ __global__ void __launch_bounds__(1024) k_mg_bottom(MGLevels<T> M, int lb, int x
         const T wn = (py || b + 1 < n) ? (T)1 : (T)0, wsn = (py || b > 0) ? (T)1 : (T)0;
         const T xe = x[b * n + wrapi(a + 1, n)], xw = x[b * n + wrapi(a - 1, n)];
         const T xn = x[wrapi(b + 1, n) * n + a], xs = x[wrapi(b - 1, n) * n + a];
-        x[t] = gs_update<T>(xe, xw, xn, xs, we, ww, wn, wsn, ihx, ihy, f[t]);
+        x[t] = gs_update<T>(xe, xw, xn, xs, we, ww, wn, wsn, ihx, ihy, f[t], M.invdiag[l]);
       }
       __syncthreads();
     }

@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "../../include/amressif_gpu.h"
+#include "anchor_ff2d.cuh"
 #include "launch.h"
 #include "stage_inc2d.cuh"
 
@@ -65,6 +66,13 @@ struct ns_ctx {
   bool ev_ok = false;
   // mixed iteration: E[0] holds an increment not yet added to the base
   bool mix_pending = false;
+  // float-float pseudo-iterate (hi, lo) ping-pong and the split source S
+  float* BH[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+  float* BL[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+  float* SFh[2] = {nullptr, nullptr};
+  float* SFl[2] = {nullptr, nullptr};
+  int mb = 0;
+  bool base_ff_valid = false, s_ff_valid = false;
   // per-kernel timing (CUDA events around each launch) and launch count
   bool prof = false;
   std::vector<cudaEvent_t> evpool;
@@ -129,6 +137,7 @@ void free_all(ns_ctx* c) {
     F(c->U[m]); F(c->UP[m]); F(c->DU[m]); F(c->S[m]); F(c->CART[m]); F(c->PHI[m]);
     for (int i = 0; i < 3; ++i) F(c->B[i][m]);
     F(c->SH[m]); F(c->G0[m]); F(c->E[0][m]); F(c->E[1][m]);
+    F(c->BH[0][m]); F(c->BH[1][m]); F(c->BL[0][m]); F(c->BL[1][m]); F(c->SFh[m]); F(c->SFl[m]);
   }
   F(c->Pp); F(c->F);
   for (int l = 1; l < c->M64.L; ++l) { F(c->M64.x[l]); F(c->M64.f[l]); }
@@ -163,6 +172,11 @@ int alloc_levels(ns_ctx* c, MGLevels<T>& M, bool own_level0) {
     M.pitch[l] = (l == 0) ? c->pitch : round_up(n, 32);
     M.invh2[l][0] = 1.0 / (hx * hx);
     M.invh2[l][1] = 1.0 / (hy * hy);
+    for (int a = 0; a < 3; ++a)
+      for (int b = 0; b < 3; ++b) {
+        const double diag = a * M.invh2[l][0] + b * M.invh2[l][1];
+        M.invdiag[l][a + 3 * b] = diag > 0 ? 1.0 / diag : 0.0;
+      }
     M.x[l] = nullptr;
     M.f[l] = nullptr;
     if (l > 0 || own_level0) {
@@ -382,6 +396,16 @@ int ns_ctx_create(const ns_params* p, void* stream, ns_ctx** out) {
   c->dt = p->fixed_dt != -1.0 ? p->fixed_dt : p->cfl / (2.0 * coeff);
   g.dt = c->dt;
   g.ren = p->ren;
+  for (int d = 0; d < 3; ++d) {
+    g.inv_dx[d] = 1.0 / g.dx[d];
+    g.dx2[d] = g.dx[d] * g.dx[d];
+    g.inv_dx2[d] = 1.0 / g.dx2[d];
+  }
+  g.inv_ren = 1.0 / p->ren;
+  g.c15 = 1.5 / c->dt;
+  g.c05 = 0.5 / c->dt;
+  g.c2dt = 1.0 / (2.0 * c->dt);
+  g.dt15 = c->dt / 1.5;
   // RK coefficients (main.cpp:861-870), optionally clipped to 0.9 x the RK4
   // real-axis stability limit of the stiffest mode
   double d_tau = 0.4 * c->dt;
@@ -625,6 +649,9 @@ int ns_step_begin(ns_ctx* c) {
   c->time += c->dt;
   c->in_step = true;
   c->norm_ready = false;
+  c->mix_pending = false;
+  c->base_ff_valid = false;
+  c->s_ff_valid = false;
   return NS_OK;
 }
 
@@ -850,23 +877,48 @@ int ns_project(ns_ctx* c, double* divmax) {
   return NS_OK;
 }
 
-// One pseudo-iteration of the mixed-precision predictor: FP64 anchor
-// G(u_base) (after adding the pending increment of the previous iteration),
-// then three FP32 increment stages; the fourth stage's increment e4 stays in
-// E[0] and its norm is the pseudo-increment norm of Error_Computation.
+static void split_const(double x, float* out) {
+  out[0] = (float)x;
+  out[1] = (float)(x - (double)out[0]);
+}
+
+// One pseudo-iteration of the mixed-precision predictor: the anchor stage
+// evaluates G(u_base) in float-float arithmetic (after adding the pending
+// increment of the previous iteration), then three FP32 increment stages; the
+// fourth stage's increment e4 stays in E[0] and its norm is the
+// pseudo-increment norm of Error_Computation.
 static int mixed_iteration(ns_ctx* c, double* norm) {
-  const int outb = pick_out(c->base, c->base);
-  StageArgs a = base_stage_args(c);
-  for (int m = 0; m < 2; ++m) {
-    a.us[m] = face_ptr(c, c->base, m);
-    a.e4[m] = c->mix_pending ? c->E[0][m] : nullptr;
-    a.out[m] = c->B[outb][m];
-    a.g0[m] = c->G0[m];
-    a.shadow[m] = c->SH[m];
+  if (!c->s_ff_valid) {
+    const double* S[2] = {c->S[0], c->S[1]};
+    LAUNCH(NS_PROF_OTHER, "split S", launch_split_ff(c->g, S, c->SFh, c->SFl, c->st));
+    c->s_ff_valid = true;
   }
-  LAUNCH(NS_PROF_ANCHOR, "anchor stage", launch_stage_fast(kAnchor, a, c->st));
-  c->base = outb;
-  c->cur = outb;
+  if (!c->base_ff_valid) {
+    const double* B[2] = {face_ptr(c, c->base, 0), face_ptr(c, c->base, 1)};
+    LAUNCH(NS_PROF_OTHER, "split base", launch_split_ff(c->g, B, c->BH[0], c->BL[0], c->st));
+    c->mb = 0;
+    c->base_ff_valid = true;
+    c->mix_pending = false;
+  }
+  AnchorFFArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.g = c->g;
+  const int mb = c->mb, nb = 1 - c->mb;
+  for (int m = 0; m < 2; ++m) {
+    a.bh[m] = c->BH[mb][m];
+    a.bl[m] = c->BL[mb][m];
+    a.e4[m] = c->mix_pending ? c->E[0][m] : nullptr;
+    a.Sh[m] = c->SFh[m];
+    a.Sl[m] = c->SFl[m];
+    a.obh[m] = c->BH[nb][m];
+    a.obl[m] = c->BL[nb][m];
+    a.g0[m] = c->G0[m];
+    split_const(c->g.inv_dx[m], a.inv_dx[m]);
+    split_const(1.0 / (c->g.ren * c->g.dx2[m]), a.vcoef[m]);
+  }
+  split_const(c->g.c15, a.c15);
+  LAUNCH(NS_PROF_ANCHOR, "anchor stage", launch_anchor_ff(a, c->st));
+  c->mb = nb;
   IncArgs ia;
   std::memset(&ia, 0, sizeof(ia));
   ia.g = c->g;
@@ -874,9 +926,12 @@ static int mixed_iteration(ns_ctx* c, double* norm) {
   ia.counter = c->counter;
   ia.norm_out = c->red + kRedNorm;
   for (int m = 0; m < 2; ++m) {
-    ia.sh[m] = c->SH[m];
+    ia.sh[m] = c->BH[nb][m];  // the hi part is the FP32 copy of u_base
     ia.g0[m] = c->G0[m];
+    ia.inv_dx[m] = (float)c->g.inv_dx[m];
+    ia.vcoef[m] = (float)(1.0 / (c->g.ren * c->g.dx2[m]));
   }
+  ia.c15 = (float)c->g.c15;
   for (int s = 1; s <= 3; ++s) {
     const int src = (s == 2) ? 0 : 1, dst = (s == 2) ? 1 : 0;
     for (int m = 0; m < 2; ++m) {
@@ -897,23 +952,26 @@ static int mixed_iteration(ns_ctx* c, double* norm) {
 
 // u* = u_base + e4 once the mixed iteration stops
 static int mixed_finalize(ns_ctx* c) {
-  if (!c->mix_pending) return NS_OK;
+  if (!c->base_ff_valid) return NS_OK;
   const int outb = pick_out(c->base, c->base);
-  const double* base[2] = {face_ptr(c, c->base, 0), face_ptr(c, c->base, 1)};
-  const float* e[2] = {c->E[0][0], c->E[0][1]};
+  const float* h[2] = {c->BH[c->mb][0], c->BH[c->mb][1]};
+  const float* l[2] = {c->BL[c->mb][0], c->BL[c->mb][1]};
+  const float* e[2] = {c->mix_pending ? c->E[0][0] : nullptr, c->mix_pending ? c->E[0][1] : nullptr};
   double* out[2] = {c->B[outb][0], c->B[outb][1]};
-  LAUNCH(NS_PROF_OTHER, "add increment", launch_add_inc(c->g, base, e, out, c->st));
+  LAUNCH(NS_PROF_OTHER, "add increment", launch_ff_add_inc(c->g, h, l, e, out, c->st));
   c->base = outb;
   c->cur = outb;
   c->mix_pending = false;
+  c->base_ff_valid = false;
   return NS_OK;
 }
 
 static int alloc_mixed(ns_ctx* c) {
-  if (c->SH[0]) return NS_OK;
+  if (c->G0[0]) return NS_OK;
   const size_t fb = (size_t)c->pitch * (c->N + 1) * sizeof(float);
   for (int m = 0; m < 2; ++m) {
-    float** ps[4] = {&c->SH[m], &c->G0[m], &c->E[0][m], &c->E[1][m]};
+    float** ps[9] = {&c->G0[m], &c->E[0][m], &c->E[1][m], &c->BH[0][m], &c->BH[1][m],
+                     &c->BL[0][m], &c->BL[1][m], &c->SFh[m], &c->SFl[m]};
     for (float** p : ps) {
       if (cudaMalloc(p, fb) != cudaSuccess) return fail(c, NS_ERR_NOMEM, "cudaMalloc (mixed) failed");
       CK(cudaMemsetAsync(*p, 0, fb, c->st), "memset");
@@ -1027,5 +1085,15 @@ int ns_profile_read(ns_ctx* c, double* ms, long long* counts, int nkinds, int re
 }
 
 long long ns_launch_count(const ns_ctx* c) { return c ? c->launches : -1; }
+
+void* ns_host_alloc(unsigned long long bytes) {
+  void* p = nullptr;
+  if (cudaMallocHost(&p, (size_t)bytes) != cudaSuccess) return nullptr;
+  return p;
+}
+
+void ns_host_free(void* p) {
+  if (p) cudaFreeHost(p);
+}
 
 }  // extern "C"

@@ -32,6 +32,15 @@ struct Geom {
   long plane;     // plane stride (3D); pitch * (N+1)
   double dx[3];
   double dt, ren;
+  // host-computed constants (the same doubles the reference forms inline)
+  double inv_dx[3];   // 1/dx
+  double dx2[3];      // dx*dx
+  double inv_dx2[3];  // 1/(dx*dx)
+  double inv_ren;     // 1/ren
+  double c15;         // 1.5/dt
+  double c05;         // 0.5/dt
+  double c2dt;        // 1/(2 dt)
+  double dt15;        // dt/1.5
   int periodic[3];
   int flux_ghost[3];  // per direction: kReflect (quirk Q1), kWrap, kZero
   int ctx_mirror[3];  // 1: p/phi ghosts mirrored (quirk Q2), 0: periodic wrap

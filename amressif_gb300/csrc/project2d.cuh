@@ -44,8 +44,8 @@ __global__ void __launch_bounds__(256) k_step_begin2d(ProjArgs A) {
       if (pi < 0) pi = g.ctx_mirror[m] ? 0 : N - 1;
       const double pc = (m == 0) ? A.p[(long)b * P + ci] : A.p[(long)ci * P + a];
       const double pm = (m == 0) ? A.p[(long)b * P + pi] : A.p[(long)pi * P + a];
-      const double gp = AR::div(pc - pm, g.dx[m], 1.0 / g.dx[m]);
-      A.S[m][id] = (-gp + (0.5 / g.dt) * d) + (1.5 / g.dt) * un;
+      const double gp = AR::div(pc - pm, g.dx[m], g.inv_dx[m]);
+      A.S[m][id] = (-gp + g.c05 * d) + g.c15 * un;
     }
   }
 }
@@ -62,10 +62,10 @@ __global__ void __launch_bounds__(256) k_poisson_rhs2d(ProjArgs A) {
   const int j = blockIdx.y * 8 + (threadIdx.x >> 5);
   if (i < N && j < N) {
     const long id = (long)j * P + i;
-    const double div = AR::div(A.u[0][id + 1] - A.u[0][id], g.dx[0], 1.0 / g.dx[0]) +
-                       AR::div(A.u[1][id + P] - A.u[1][id], g.dx[1], 1.0 / g.dx[1]);
+    const double div = AR::div(A.u[0][id + 1] - A.u[0][id], g.dx[0], g.inv_dx[0]) +
+                       AR::div(A.u[1][id + P] - A.u[1][id], g.dx[1], g.inv_dx[1]);
     v[0] = fabs(div);
-    const double f = (1.5 / g.dt) * div;
+    const double f = g.c15 * div;
     A.f[id] = f;
     v[1] = f;
   }
@@ -97,7 +97,7 @@ __global__ void __launch_bounds__(256) k_project2d(ProjArgs A) {
       if (pi < 0) pi = g.ctx_mirror[m] ? 0 : N - 1;
       const double pc = (m == 0) ? A.phi[(long)b * P + ci] : A.phi[(long)ci * P + a];
       const double pm = (m == 0) ? A.phi[(long)b * P + pi] : A.phi[(long)pi * P + a];
-      const double gphi = AR::div(pc - pm, g.dx[m], 1.0 / g.dx[m]);
+      const double gphi = AR::div(pc - pm, g.dx[m], g.inv_dx[m]);
       return A.u[m][(long)b * P + a] - AR::div(gphi * dt, 1.5, 1.0 / 1.5);
     };
     const long id = (long)j * P + i;
@@ -108,7 +108,7 @@ __global__ void __launch_bounds__(256) k_project2d(ProjArgs A) {
     if (i == N - 1) A.uout[0][id + 1] = u1;
     if (j == N - 1) A.uout[1][id + P] = v1;
     A.pw[id] = A.p[id] + A.phi[id];
-    const double div = AR::div(u1 - u0, g.dx[0], 1.0 / g.dx[0]) + AR::div(v1 - v0, g.dx[1], 1.0 / g.dx[1]);
+    const double div = AR::div(u1 - u0, g.dx[0], g.inv_dx[0]) + AR::div(v1 - v0, g.dx[1], g.inv_dx[1]);
     v[0] = fabs(div);
   }
   if (grid_reduce_last<1>(v, A.part, A.counter, 1u) && threadIdx.x == 0) A.red_out[0] = v[0];

@@ -92,7 +92,7 @@ __global__ void __launch_bounds__(256) k_stage2d(StageArgs A) {
   const int tid = threadIdx.x, NT = blockDim.x;
   const bool perx = g.periodic[0], pery = g.periodic[1];
   const double dx = g.dx[0], dy = g.dx[1];
-  const double idx_ = 1.0 / dx, idy_ = 1.0 / dy;
+  const double idx_ = g.inv_dx[0], idy_ = g.inv_dx[1];
 
   // ---- 1. cell-centred velocity of the tile + 3-cell halo -----------------
   for (int t = tid; t < SM::CW * SM::CH; t += NT) {
@@ -191,8 +191,8 @@ __global__ void __launch_bounds__(256) k_stage2d(StageArgs A) {
   __syncthreads();
 
   // ---- 3. total = -conv + visc at cells ----------------------------------
-  const double dx2 = dx * dx, dy2 = dy * dy;
-  const double idx2 = 1.0 / dx2, idy2 = 1.0 / dy2, iren = 1.0 / g.ren;
+  const double dx2 = g.dx2[0], dy2 = g.dx2[1];
+  const double idx2 = g.inv_dx2[0], idy2 = g.inv_dx2[1], iren = g.inv_ren;
   for (int t = tid; t < SM::TW * SM::TH; t += NT) {
     const int tx = t % SM::TW, ty = t / SM::TW;
     const int a = x0 - 1 + tx, b = y0 - 1 + ty;
@@ -237,7 +237,7 @@ __global__ void __launch_bounds__(256) k_stage2d(StageArgs A) {
   __syncthreads();
 
   // ---- 4. face RHS and stage update ----------------------------------------
-  const double c15 = 1.5 / g.dt, c05 = 0.5 / g.dt, rk = A.rk;
+  const double c15 = g.c15, c05 = g.c05, rk = A.rk;
   double nrm[2] = {0.0, 0.0};
   // u faces: a in [x0, x0+TX) (+ a = N on the last tile column), b in [y0, y0+TY)
   const int nfx = (x0 + TX >= N) ? (N - x0 + 1) : TX;
@@ -264,14 +264,14 @@ __global__ void __launch_bounds__(256) k_stage2d(StageArgs A) {
       if (pidx < 0) pidx = g.ctx_mirror[d] ? 0 : nf - 1;
       const double pc = (d == 0) ? A.p[(long)cb * P + cidx] : A.p[(long)cidx * P + ca];
       const double pm = (d == 0) ? A.p[(long)cb * P + pidx] : A.p[(long)pidx * P + ca];
-      const double gp = AR::div(pc - pm, g.dx[d], 1.0 / g.dx[d]);
+      const double gp = AR::div(pc - pm, g.dx[d], g.inv_dx[d]);
       double r = -gp + 0.5 * (tm + tc);
       if (MODE == kExactRK) {
-        r = r - (1.5 / g.dt) * (A.us[m][id] - A.un[m][id]) + (0.5 / g.dt) * A.du[m][id];
+        r = r - c15 * (A.us[m][id] - A.un[m][id]) + c05 * A.du[m][id];
         out = A.ub[m][id] + (rk * r);
       } else {
-        r = r + (1.0 / (2.0 * g.dt)) * A.du[m][id];
-        out = A.us[m][id] + ((g.dt / 1.5) * r);
+        r = r + g.c2dt * A.du[m][id];
+        out = A.us[m][id] + (g.dt15 * r);
       }
       A.out[m][id] = out;
     } else if (MODE == kFastRK) {
@@ -286,7 +286,6 @@ __global__ void __launch_bounds__(256) k_stage2d(StageArgs A) {
       A.shadow[m][id] = (float)ubase;
       out = ubase;
     }
-    (void)c05;
     if (A.do_norm) {
       const double w = (face == 0 || face == nf) ? 0.5 : 1.0;
       const double q = A.ub[m][id] - out;

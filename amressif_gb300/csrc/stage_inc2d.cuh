@@ -27,6 +27,9 @@ struct IncArgs {
   float rk_prev;
   float* eout[2];       // e_{s+1} = rk * (G0 + dG)
   float rk;
+  float inv_dx[2];      // 1/dx, 1/dy
+  float vcoef[2];       // 1/(ren dx^2), 1/(ren dy^2)
+  float c15;            // 1.5/dt
   int do_norm;
   double* part;
   unsigned* counter;
@@ -173,8 +176,8 @@ __global__ void __launch_bounds__(256) k_inc_stage2d(IncArgs A) {
   __syncthreads();
 
   // ---- total-flux difference at cells ----------------------------------------
-  const float idx_ = (float)(1.0 / g.dx[0]), idy_ = (float)(1.0 / g.dx[1]);
-  const float vx = (float)(1.0 / (g.ren * g.dx[0] * g.dx[0])), vy = (float)(1.0 / (g.ren * g.dx[1] * g.dx[1]));
+  const float idx_ = A.inv_dx[0], idy_ = A.inv_dx[1];
+  const float vx = A.vcoef[0], vy = A.vcoef[1];
   for (int t = tid; t < SM::TW * SM::TH; t += NT) {
     const int tx = t % SM::TW, ty = t / SM::TW;
     const int a = x0 - 1 + tx, b = y0 - 1 + ty;
@@ -212,7 +215,7 @@ __global__ void __launch_bounds__(256) k_inc_stage2d(IncArgs A) {
   __syncthreads();
 
   // ---- face update --------------------------------------------------------------
-  const float c15 = (float)(1.5 / g.dt), rk = A.rk;
+  const float c15 = A.c15, rk = A.rk;
   double nrm[2] = {0.0, 0.0};
   const int nfx = (x0 + TX >= N) ? (N - x0 + 1) : TX;
   const int nfy = (y0 + TY >= N) ? (N - y0 + 1) : TY;
@@ -239,23 +242,6 @@ __global__ void __launch_bounds__(256) k_inc_stage2d(IncArgs A) {
       const double npts = (double)N * (double)N;
       *A.norm_out = fmax(sqrt(nrm[0]) / sqrt(npts), sqrt(nrm[1]) / sqrt(npts));
     }
-  }
-}
-
-// u* = u_base + e (FP64), the final pseudo-iterate of the mixed iteration
-static __global__ void __launch_bounds__(256) k_add_inc2d(Geom g, const double* b0, const double* b1, const float* e0, const float* e1,
-                                                   double* o0, double* o1) {
-  const int N = g.N;
-  const long P = g.pitch;
-  const long nu = (long)(N + 1) * N;
-  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < 2 * nu; t += (long)gridDim.x * blockDim.x) {
-    const int m = (t < nu) ? 0 : 1;
-    const long q = (m == 0) ? t : t - nu;
-    const int a = (m == 0) ? (int)(q % (N + 1)) : (int)(q % N);
-    const int b = (m == 0) ? (int)(q / (N + 1)) : (int)(q / N);
-    const long id = (long)b * P + a;
-    if (m == 0) o0[id] = b0[id] + (double)e0[id];
-    else o1[id] = b1[id] + (double)e1[id];
   }
 }
 

@@ -1,0 +1,343 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 fractional-step advance.
+
+Workload: 2D lid-driven cavity on the unit square, 4096^2 MAC grid (16.8 M
+cells), Re = 1000, dt = 0.5 dx (lid speed 1), IterNum 100, momentum tolerance
+1e-10, pseudo-time step clipped to 0.9 x the RK4 stability limit, Poisson
+solved until max|div u| <= 1e-10 (and the reference's relative 1e-10), started
+from rest (a 1000-step run). A "step" is one time step: the dual-time BDF2
+predictor, the pressure Poisson solve and the projection.
+
+Metric: steps/s of the mixed-precision solver (FP64 anchors + FP32 increment
+stages, FP32 V-cycles inside FP64 defect correction), with the plain FP64 GPU
+solver timed on the same steps beside it.
+
+`--impl reference` times the CPU restatement of the reference (oracle/) on all
+host cores on a bounded sample of the same workload.
+
+Output: one JSON line (rank 0).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "steps/s at 4096² (div≤1e-10) mixed vs FP64 MG; adjoint/forward time ratio"
+
+# Algorithmic bytes per cell of each kernel kind (compulsory HBM traffic of
+# one launch over the N^2 grid; faces counted as N^2 per direction).
+ALGO_BYTES_PER_CELL = {
+    "stage_exact": 88.0,   # read u*, u_base, u^n, du^n (2 x 8 B each) + p; write u*
+    "stage_fast": 64.0,    # read u*, u_base, S; write u*
+    "anchor": 72.0,        # read u_base, e4 (f32), S; write u_base, FP32 copy, G0 (f32)
+    "increment": 88.0 / 3, # stage 1: read u_b, G0, write e; stages 2-3 also read e (all FP32)
+    "explicit": 88.0,
+    "step_begin": 56.0,    # read u, u_prev, p; write du, S
+    "poisson_rhs": 24.0,   # read 2 faces, write f
+    "project": 56.0,       # read u*, phi, p; write u, p
+    "mg_smooth0": 12.0,    # FP32: read x, f; write x (level 0)
+    "dc_update": 32.0,     # read phi, e (f32), f; write phi, r (f32)
+}
+
+
+def clocks_sampler(stop, out):
+    fields = "clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown," \
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown," \
+             "clocks_event_reasons.sw_power_cap"
+    try:
+        p = subprocess.Popen(["nvidia-smi", "--query-gpu=" + fields, "--format=csv,noheader,nounits", "-lms", "200",
+                              "-i", os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0]],
+                             stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+    except Exception:
+        return
+    try:
+        while not stop.is_set():
+            line = p.stdout.readline()
+            if not line:
+                break
+            out.append([x.strip() for x in line.split(",")])
+    finally:
+        p.terminate()
+        try:
+            p.wait(timeout=5)
+        except Exception:
+            p.kill()
+
+
+def summarize_clocks(samples):
+    if not samples:
+        return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+    sm, mx, reasons = [], [], set()
+    names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+    for s in samples:
+        try:
+            sm.append(float(s[0]))
+            mx.append(float(s[1]))
+        except (ValueError, IndexError):
+            continue
+        for k, v in zip(names, s[3:7]):
+            if v.lower().startswith("active"):
+                reasons.add(k)
+    return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+            "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak_hbm():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ncu_traffic_per_cell():
+    path = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+def workload_params(ns, n, precision):
+    return ns.default_params(n_cell=n, ren=1000.0, fixed_dt=0.5 / n, iter_num=100, momentum_tolerance=1e-10,
+                             max_grid_size=(n, n, n), bc_lo=(135, 135, 135), bc_hi=(135, 165, 135),
+                             inflow_waveform=(1.0, 0.0, 0.0), precision=precision, poisson_tol_rel=1e-10,
+                             poisson_tol_div=1e-10, poisson_max_cycles=200, dtau_clip=1)
+
+
+def cpu_sample(n, steps, threads):
+    """The oracle (CPU restatement of the reference) on host cores."""
+    from oracle.orc import Oracle
+
+    o = Oracle(n, ren=1000.0, dt=0.5 / n, iter_num=100, dtau_clip=1, poisson_tol=1e-10,
+               max_grid_size=(n, n, n), nthreads=threads)
+    o.init(0)
+    ks = []
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        ks.append(o.step()["pseudo_iters"])
+    dt = time.perf_counter() - t0
+    o.close()
+    return steps / dt, ks, dt
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+        import torch.distributed as dist
+
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo", rank=rank, world_size=world)
+        return world, rank, dist
+    return 1, 0, None
+
+
+def run_steps(s, k):
+    stats = [s.step() for _ in range(k)]
+    return stats
+
+
+def bench_ours(args):
+    world, rank, dist = dist_setup()
+    import amressif_gb300 as ns
+
+    n = args.n
+    K, W = args.steps, args.warmup
+    # ---- mixed precision (headline) ----
+    s = ns.Solver(workload_params(ns, n, ns.PREC_MIXED))
+    s.init(ns.INIT_CAVITY)
+    run_steps(s, W)
+    s.profile(True)
+    s.profile_read(reset=True)
+    s.sync()
+    if dist:
+        dist.barrier()
+    l0 = s.launch_count()
+    stop, samples = threading.Event(), []
+    th = threading.Thread(target=clocks_sampler, args=(stop, samples), daemon=True)
+    th.start()
+    t0 = time.perf_counter()
+    stats = run_steps(s, K)
+    s.sync()
+    wall = time.perf_counter() - t0
+    stop.set()
+    th.join(timeout=10)
+    launches = s.launch_count() - l0
+    prof = s.profile_read()
+    s.profile(False)
+    dev_ms = sum(st["ms_predictor"] + st["ms_poisson"] + st["ms_project"] for st in stats)
+    total_s = dev_ms / 1e3
+    if dist:
+        import torch
+
+        t = torch.tensor([total_s], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_s = float(t.item())
+    value = world * K / total_s
+    ms_per_step = 1e3 * total_s / K
+
+    # ---- plain FP64 GPU solver on the same steps ----
+    fp64 = None
+    if not args.no_fp64:
+        s64 = ns.Solver(workload_params(ns, n, ns.PREC_FP64))
+        s64.init(ns.INIT_CAVITY)
+        run_steps(s64, W)
+        s64.sync()
+        st64 = run_steps(s64, K)
+        ms64 = sum(st["ms_predictor"] + st["ms_poisson"] + st["ms_project"] for st in st64) / K
+        u64, _, p64, _ = s64.get_state()
+        u32, _, p32, _ = s.get_state()
+        import numpy as np
+
+        def rel(a, b):
+            return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+        fp64 = {
+            "steps_per_s": 1e3 / ms64,
+            "ms_per_step": ms64,
+            "mixed_speedup": ms64 / ms_per_step,
+            "poisson_ms_per_step": statistics.mean(st["ms_poisson"] for st in st64),
+            "predictor_ms_per_step": statistics.mean(st["ms_predictor"] for st in st64),
+            "pseudo_iters_mean": statistics.mean(st["pseudo_iters"] for st in st64),
+            "mixed_vs_fp64_rel_l2": {"u": rel(u32[0], u64[0]), "v": rel(u32[1], u64[1]),
+                                     "p": rel(p32 - p32.mean(), p64 - p64.mean())},
+        }
+        s64.close()
+
+    # ---- end to end through the C ABI with host buffers ----
+    e2e = None
+    if not args.no_e2e:
+        E = max(1, min(args.e2e_steps, K))
+        shp = [s.face_shape(0), s.face_shape(1)]
+        bufs = [ns.PinnedArray(shp[0]), ns.PinnedArray(shp[1]), ns.PinnedArray(shp[0]), ns.PinnedArray(shp[1]),
+                ns.PinnedArray((n, n))]
+        u, up, p, _ = s.get_state()
+        for b, a in zip(bufs, [u[0], u[1], up[0], up[1], p]):
+            b.a[...] = a
+        uh, uph, ph = [bufs[0].a, bufs[1].a], [bufs[2].a, bufs[3].a], bufs[4].a
+        s.step_host(uh, uph, ph)  # warm-up of the host path
+        t0 = time.perf_counter()
+        for _ in range(E):
+            s.step_host(uh, uph, ph)
+        te = time.perf_counter() - t0
+        nbytes = 8 * (2 * shp[0][0] * shp[0][1] + 2 * shp[1][0] * shp[1][1] + n * n)
+        e2e = {"value": world * E / te, "unit": "steps/s", "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
+               "steps": E, "path": "ns_step_host (pinned host u, u_prev, p in; u, u_prev, p out)"}
+        for b in bufs:
+            b.free()
+
+    # ---- roofline of the dominant kernel ----
+    peak, peak_kind = measured_peak_hbm()
+    dom = max(prof.items(), key=lambda kv: kv[1][1])
+    kind, (cnt, kms) = dom
+    per_launch_ms = kms / max(cnt, 1)
+    bpc = ALGO_BYTES_PER_CELL.get(kind)
+    roofline = None
+    if bpc is not None and cnt > 0:
+        algo = bpc * n * n
+        achieved = algo / (per_launch_ms * 1e-3) / 1e9
+        tr = ncu_traffic_per_cell().get(kind)
+        roofline = {"kernel": kind, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                    "frac": achieved / peak, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
+                    "traffic": (tr * n * n if tr else None), "algorithmic_bytes": algo,
+                    "ms_per_launch": per_launch_ms, "launches": cnt}
+    kernels = {k: {"launches": c, "ms_total": m, "ms_per_launch": (m / c if c else None),
+                   "share": m / max(dev_ms, 1e-9)} for k, (c, m) in prof.items() if c}
+
+    # ---- CPU restatement timed on the host (rank 0, N=1) ----
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        v, ks, secs = cpu_sample(n, args.cpu_steps, threads)
+        cpu = {"value": v, "unit": "steps/s", "cores": threads, "kind": "port",
+               "sample": "%d step(s) from rest of the same %d^2 cavity (%.1f s, K=%s), oracle/ C++ restatement, "
+                         "OpenMP" % (args.cpu_steps, n, secs, ks)}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": K, "warmup": W,
+            "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "mixed (fp64 anchors, fp32 increments and V-cycles)", "data": "synthetic (cavity from rest)",
+            "config": {"workload": "lid-driven cavity %dx%d, Re=1000, dt=0.5dx, steps %d..%d of a 1000-step run from rest"
+                       % (n, n, W + 1, W + K), "n_cell": n, "precision": "mixed",
+                       "parallelism": "replicas" if world > 1 else "single GPU",
+                       "l2_flush": "inputs larger than L2 (every field is >=67 MB, the step touches >1 GB)"},
+            "pseudo_iters_mean": statistics.mean(st["pseudo_iters"] for st in stats),
+            "poisson_cycles_mean": statistics.mean(st["poisson_cycles"] for st in stats),
+            "div_after_max": max(st["div_after"] for st in stats),
+            "phase_ms_per_step": {"predictor": statistics.mean(st["ms_predictor"] for st in stats),
+                                  "poisson": statistics.mean(st["ms_poisson"] for st in stats),
+                                  "project": statistics.mean(st["ms_project"] for st in stats)},
+            "wall_ms_per_step": 1e3 * wall / K,
+            "fp64_mg": fp64,
+            "adjoint_forward_ratio": None,
+            "e2e": e2e,
+            "gpu_launches": launches,
+            "roofline": roofline,
+            "kernels": kernels,
+            "cpu_baseline": cpu,
+            "clocks": summarize_clocks(samples),
+        }
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def bench_reference(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    steps = max(1, min(args.steps, args.cpu_steps))
+    v, ks, secs = cpu_sample(args.n, steps, threads)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "steps/s", "n_gpus": world, "steps": steps,
+        "warmup": 0, "ms_per_step": 1e3 * secs / steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (cavity from rest)",
+        "config": {"workload": "lid-driven cavity %dx%d, Re=1000, dt=0.5dx, steps 1..%d of a 1000-step run from rest"
+                   % (args.n, args.n, steps), "n_cell": args.n},
+        "cpu_baseline": {"value": v, "unit": "steps/s", "cores": threads, "kind": "port",
+                         "sample": "%d step(s) from rest, K=%s (%.1f s); the AMReX reference does not build here "
+                                   "(AMReX not vendored), so its C++ restatement oracle/ is timed" % (steps, ks, secs)},
+        "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=4096)
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--cpu-steps", type=int, default=1)
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    if args.impl == "reference":
+        bench_reference(args)
+    else:
+        bench_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -164,6 +164,11 @@ int ns_sync(ns_ctx* c);
 #define NS_PROF_DC_UPDATE 14
 #define NS_PROF_OTHER 15
 #define NS_PROF_KINDS 16
+/* Page-locked host memory for the ns_step_host / ns_put_box buffers of a
+ * host that keeps its fields in CPU memory (cudaMallocHost). */
+void* ns_host_alloc(unsigned long long bytes);
+void ns_host_free(void* p);
+
 int ns_profile_enable(ns_ctx* c, int on);
 int ns_profile_read(ns_ctx* c, double* ms, long long* counts, int nkinds, int reset);
 long long ns_launch_count(const ns_ctx* c);

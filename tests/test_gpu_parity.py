@@ -181,6 +181,37 @@ def test_free_running_matches_golden(gpu_lib):
         assert relp(pp, g["p_%d" % step]) <= TOL_STEP
 
 
+@pytest.mark.parametrize("name", ["cavity128_cfg1", "tgv64_parity", "tgv64_fixed", "cavity40_partial_tiles"])
+def test_mixed_predictor_matches_fp64(gpu_lib, name):
+    """Float-float anchor + FP32 increments reproduce the FP64 iterates.
+
+    Both solvers start from the same state; the mixed predictor must take the
+    same number of pseudo-iterations and give u, v, p within 1e-11 (relative
+    L2) of the FP64 predictor (both with the FP64 Poisson solve).
+    """
+    n, okw, gkw, case = CASES[name]
+    sol = {}
+    for prec in (ns.PREC_FP64_EXACT, ns.PREC_MIXED):
+        p = ns.default_params(n_cell=n, iter_num=100, precision=prec, poisson_tol_rel=1e-13, **gkw)
+        s = ns.Solver(p)
+        s.init(case)
+        sol[prec] = s
+    ref = sol[ns.PREC_FP64_EXACT]
+    for _ in range(2):
+        ref.step()
+    u, up, pp, _ = ref.get_state()
+    for s in sol.values():
+        s.set_state(u, up, pp)
+    for step in range(3):
+        st = {k: s.step() for k, s in sol.items()}
+        assert st[ns.PREC_MIXED]["pseudo_iters"] == st[ns.PREC_FP64_EXACT]["pseudo_iters"], st
+        a = sol[ns.PREC_MIXED].get_state()
+        b = ref.get_state()
+        for d in range(2):
+            assert rel(a[0][d], b[0][d]) <= 1e-11, (step, d, rel(a[0][d], b[0][d]))
+        assert relp(a[2], b[2]) <= 1e-11, (step, relp(a[2], b[2]))
+
+
 @pytest.mark.parametrize("precision", [ns.PREC_FP64, ns.PREC_MIXED])
 def test_fast_modes_track_oracle(gpu_lib, oracle_lib, precision):
     o, s = make_pair("cavity128_cfg1", precision=precision)
