@@ -106,6 +106,7 @@ class NsStepStats(ctypes.Structure):
         ("ms_predictor", ctypes.c_double),
         ("ms_poisson", ctypes.c_double),
         ("ms_project", ctypes.c_double),
+        ("poisson_fp64_fallback", ctypes.c_int),
     ]
 
 

@@ -7,7 +7,7 @@
 // that G(u_base) = S - (1.5/dt) u_base + avg(-conv + visc) keeps FP64-class
 // accuracy although its terms cancel to the pseudo-residual. The base itself
 // is stored as two float arrays (hi, lo); hi doubles as the FP32 copy read by
-// the increment stages.
+// the increment stages. Thread mapping as in k_inc_stage2d (flattened rectangles).
 #pragma once
 #include "ff.cuh"
 #include "ns_common.cuh"
@@ -30,14 +30,22 @@ struct AnchorFFArgs {
 
 template <int TX, int TY>
 struct AnchorSmem {
+  static constexpr int UW = TX + 7, UH = TY + 6;
+  static constexpr int VW = TX + 6, VH = TY + 7;
   static constexpr int CW = TX + 6, CH = TY + 6;
   static constexpr int FXW = TX + 3, FXH = TY + 2;
   static constexpr int FYW = TX + 2, FYH = TY + 3;
   static constexpr int TW = TX + 2, TH = TY + 2;
+  union {
+    struct {
+      ff u[UH][UW];
+      ff v[VH][VW];
+    } f;
+    ff t[2][TH][TW];  // totals reuse the face tiles once the fluxes exist
+  };
   ff c[2][CH][CW];
   ff fx[2][FXH][FXW];
   ff fy[2][FYH][FYW];
-  ff t[2][TH][TW];
 };
 
 __device__ __forceinline__ ff anchor_u(const AnchorFFArgs& A, int m, long id) {
@@ -50,10 +58,10 @@ __device__ __forceinline__ ff anchor_u(const AnchorFFArgs& A, int m, long id) {
 // ud = ucon+|ucon| and up = ucon-|ucon| are exactly u or 0.
 __device__ __forceinline__ ff quick_flux_ff(ff u, ff a, ff b, ff c, ff e) {
   if (u.hi > 0.f) {
-    const ff q = (ff_scale2(ff_make(-e.hi, -e.lo) - ff_scale2(c, 2.f) + 3.f * b, 0.125f)) + c;
+    const ff q = (ff_scale2(-e - ff_scale2(c, 2.f) + 3.f * b, 0.125f)) + c;
     return u * q;
   } else if (u.hi < 0.f) {
-    const ff q = (ff_scale2(ff_make(-a.hi, -a.lo) - ff_scale2(b, 2.f) + 3.f * c, 0.125f)) + b;
+    const ff q = (ff_scale2(-a - ff_scale2(b, 2.f) + 3.f * c, 0.125f)) + b;
     return u * q;
   }
   return ff_make(0.f, 0.f);
@@ -65,153 +73,151 @@ __device__ __forceinline__ ff cart_ghost_ff(const CartBC& b, int m, ff q) {
   return r == kNeg ? -q : q;
 }
 
-template <int TX, int TY>
-__global__ void __launch_bounds__(256) k_anchor_ff2d(AnchorFFArgs A) {
+template <int TX, int TY, int NT>
+__global__ void __launch_bounds__(NT) k_anchor_ff2d(AnchorFFArgs A) {
   using SM = AnchorSmem<TX, TY>;
-  __shared__ SM sm;
+  extern __shared__ __align__(16) unsigned char anchor_smem_raw[];
+  SM& sm = *reinterpret_cast<SM*>(anchor_smem_raw);
   const Geom& g = A.g;
   const int N = g.N;
   const long P = g.pitch;
   const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
-  const int tid = threadIdx.x, NT = blockDim.x;
   const bool perx = g.periodic[0], pery = g.periodic[1];
+  const ff zero = ff_make(0.f, 0.f);
 
-  for (int t = tid; t < SM::CW * SM::CH; t += NT) {
-    const int lx = t % SM::CW, ly = t / SM::CW;
-    const int a = x0 - 3 + lx, b = y0 - 3 + ly;
-    const bool inx = (a >= 0 && a < N), iny = (b >= 0 && b < N);
-    ff cu = ff_make(0.f, 0.f), cv = cu;
-    if ((inx || perx) && (iny || pery)) {
-      const long id = (long)wrapi(b, N) * P + wrapi(a, N);
-      cu = ff_scale2(anchor_u(A, 0, id) + anchor_u(A, 0, id + 1), 0.5f);
-      cv = ff_scale2(anchor_u(A, 1, id) + anchor_u(A, 1, id + P), 0.5f);
-    }
-    sm.c[0][ly][lx] = cu;
-    sm.c[1][ly][lx] = cv;
+  // ---- 0. face tiles of u_base = base + e4 ----------------------------------
+  NS_RECT_LOOP(SM::UW, SM::UH, NT, r, c) {
+    int b = y0 - 3 + r;
+    if (b < 0 || b >= N) b = pery ? wrapi(b, N) : -1;
+    int a = x0 - 3 + c;
+    if (a < 0 || a > N) a = perx ? wrapi(a, N) : -1;
+    sm.f.u[r][c] = (b >= 0 && a >= 0) ? anchor_u(A, 0, (long)b * P + a) : zero;
   }
-  __syncthreads();
-  if (!perx) {
-    for (int t = tid; t < SM::CW * SM::CH; t += NT) {
-      const int lx = t % SM::CW, ly = t / SM::CW;
-      const int a = x0 - 3 + lx, b = y0 - 3 + ly;
-      if (!(b >= 0 && b < N) && !pery) continue;
-      if (a >= -3 && a < 0) {
-        const int ml = (-a - 1) - (x0 - 3);
-        for (int m = 0; m < 2; ++m) sm.c[m][ly][lx] = cart_ghost_ff(g.bc[0], m, sm.c[m][ly][ml]);
-      } else if (a >= N && a < N + 3) {
-        const int ml = (2 * N - 1 - a) - (x0 - 3);
-        for (int m = 0; m < 2; ++m) sm.c[m][ly][lx] = cart_ghost_ff(g.bc[1], m, sm.c[m][ly][ml]);
-      }
-    }
-    __syncthreads();
-  }
-  if (!pery) {
-    for (int t = tid; t < SM::CW * SM::CH; t += NT) {
-      const int lx = t % SM::CW, ly = t / SM::CW;
-      const int b = y0 - 3 + ly;
-      if (b >= -3 && b < 0) {
-        const int ml = (-b - 1) - (y0 - 3);
-        for (int m = 0; m < 2; ++m) sm.c[m][ly][lx] = cart_ghost_ff(g.bc[2], m, sm.c[m][ml][lx]);
-      } else if (b >= N && b < N + 3) {
-        const int ml = (2 * N - 1 - b) - (y0 - 3);
-        for (int m = 0; m < 2; ++m) sm.c[m][ly][lx] = cart_ghost_ff(g.bc[3], m, sm.c[m][ml][lx]);
-      }
-    }
-    __syncthreads();
-  }
-  const bool wx = (g.flux_ghost[0] == kWrap), wy = (g.flux_ghost[1] == kWrap);
-
-  for (int t = tid; t < SM::FXW * SM::FXH; t += NT) {
-    const int fx = t % SM::FXW, fyy = t / SM::FXW;
-    const int a = x0 - 1 + fx, b = y0 - 1 + fyy;
-    const bool rowin = (b >= 0 && b < N);
-    const bool facein = (a >= 0 && a <= N);
-    const bool need_u = (fyy >= 1 && fyy <= TY) && rowin && (facein || wx);
-    const bool need_v = (fx >= 1 && fx <= TX + 1) && (rowin || wy) && facein;
-    if (!need_u && !need_v) continue;
-    const int aa = facein ? a : wrapi(a, N);
-    const ff ucf = anchor_u(A, 0, (long)wrapi(b, N) * P + aa);
-    const int ly = b - (y0 - 3), lx = a - (x0 - 3);
-    for (int m = 0; m < 2; ++m) {
-      if (m == 0 ? !need_u : !need_v) continue;
-      sm.fx[m][fyy][fx] = quick_flux_ff(ucf, sm.c[m][ly][lx + 1], sm.c[m][ly][lx], sm.c[m][ly][lx - 1], sm.c[m][ly][lx - 2]);
-    }
-  }
-  for (int t = tid; t < SM::FYW * SM::FYH; t += NT) {
-    const int fx = t % SM::FYW, fyy = t / SM::FYW;
-    const int a = x0 - 1 + fx, b = y0 - 1 + fyy;
-    const bool colin = (a >= 0 && a < N);
-    const bool facein = (b >= 0 && b <= N);
-    const bool need_u = (fyy >= 1 && fyy <= TY + 1) && (colin || wx) && facein;
-    const bool need_v = (fx >= 1 && fx <= TX) && colin && (facein || wy);
-    if (!need_u && !need_v) continue;
-    const int bb = facein ? b : wrapi(b, N);
-    const ff vcf = anchor_u(A, 1, (long)bb * P + wrapi(a, N));
-    const int ly = b - (y0 - 3), lx = a - (x0 - 3);
-    for (int m = 0; m < 2; ++m) {
-      if (m == 0 ? !need_u : !need_v) continue;
-      sm.fy[m][fyy][fx] = quick_flux_ff(vcf, sm.c[m][ly + 1][lx], sm.c[m][ly][lx], sm.c[m][ly - 1][lx], sm.c[m][ly - 2][lx]);
-    }
+  NS_RECT_LOOP(SM::VW, SM::VH, NT, r, c) {
+    int b = y0 - 3 + r;
+    if (b < 0 || b > N) b = pery ? wrapi(b, N) : -1;
+    int a = x0 - 3 + c;
+    if (a < 0 || a >= N) a = perx ? wrapi(a, N) : -1;
+    sm.f.v[r][c] = (b >= 0 && a >= 0) ? anchor_u(A, 1, (long)b * P + a) : zero;
   }
   __syncthreads();
 
+  // ---- 1. cell-centred velocity + wall / lid ghosts ---------------------------
+  NS_RECT_LOOP(SM::CW, SM::CH, NT, r, c) {
+      sm.c[0][r][c] = ff_scale2(sm.f.u[r][c] + sm.f.u[r][c + 1], 0.5f);
+      sm.c[1][r][c] = ff_scale2(sm.f.v[r][c] + sm.f.v[r + 1][c], 0.5f);
+    }
+  __syncthreads();
+  const bool lox = !perx && x0 == 0, hix = !perx && x0 + TX + 3 > N;
+  const bool loy = !pery && y0 == 0, hiy = !pery && y0 + TY + 3 > N;
+  if (lox || hix) {
+    for (int q = threadIdx.x; q < 6 * SM::CH; q += NT) {
+      const int r = q / 6, k = q - 6 * (q / 6);
+      const int b = y0 - 3 + r;
+      if (!pery && (b < 0 || b >= N)) continue;
+      int c, cm, side;
+      if (k < 3) { if (!lox) continue; c = k; cm = 5 - k; side = 0; }
+      else {
+        if (!hix) continue;
+        const int a = N + (k - 3);
+        c = a - (x0 - 3);
+        if (c >= SM::CW) continue;
+        cm = (2 * N - 1 - a) - (x0 - 3);
+        side = 1;
+      }
+      for (int m = 0; m < 2; ++m) sm.c[m][r][c] = cart_ghost_ff(g.bc[side], m, sm.c[m][r][cm]);
+    }
+    __syncthreads();
+  }
+  if (loy || hiy) {
+    for (int q = threadIdx.x; q < 6 * SM::CW; q += NT) {
+      const int k = q / SM::CW, c = q - k * SM::CW;
+      int r, rm, side;
+      if (k < 3) { if (!loy) continue; r = k; rm = 5 - k; side = 2; }
+      else {
+        if (!hiy) continue;
+        const int b = N + (k - 3);
+        r = b - (y0 - 3);
+        if (r >= SM::CH) continue;
+        rm = (2 * N - 1 - b) - (y0 - 3);
+        side = 3;
+      }
+      for (int m = 0; m < 2; ++m) sm.c[m][r][c] = cart_ghost_ff(g.bc[side], m, sm.c[m][rm][c]);
+    }
+    __syncthreads();
+  }
+
+  // ---- 2. QUICK half-node fluxes -------------------------------------------------
+  NS_RECT_LOOP(SM::FXW, SM::FXH, NT, fr, fc) {
+      const ff u = sm.f.u[fr + 2][fc + 2];
+#pragma unroll
+      for (int m = 0; m < 2; ++m)
+        sm.fx[m][fr][fc] = quick_flux_ff(u, sm.c[m][fr + 2][fc + 3], sm.c[m][fr + 2][fc + 2], sm.c[m][fr + 2][fc + 1],
+                                         sm.c[m][fr + 2][fc]);
+    }
+  NS_RECT_LOOP(SM::FYW, SM::FYH, NT, fr, fc) {
+      const ff v = sm.f.v[fr + 2][fc + 2];
+#pragma unroll
+      for (int m = 0; m < 2; ++m)
+        sm.fy[m][fr][fc] = quick_flux_ff(v, sm.c[m][fr + 3][fc + 2], sm.c[m][fr + 2][fc + 2], sm.c[m][fr + 1][fc + 2],
+                                         sm.c[m][fr][fc + 2]);
+    }
+  __syncthreads();
+
+  // ---- 3. total = -conv + visc (the face tiles are dead: t reuses them) ------------
   const ff idx_ = ff_make(A.inv_dx[0][0], A.inv_dx[0][1]), idy_ = ff_make(A.inv_dx[1][0], A.inv_dx[1][1]);
   const ff vx = ff_make(A.vcoef[0][0], A.vcoef[0][1]), vy = ff_make(A.vcoef[1][0], A.vcoef[1][1]);
-  for (int t = tid; t < SM::TW * SM::TH; t += NT) {
-    const int tx = t % SM::TW, ty = t / SM::TW;
-    const int a = x0 - 1 + tx, b = y0 - 1 + ty;
-    const bool need_u = (ty >= 1 && ty <= TY) && (b < N) && ((a >= 0 && a < N) || wx);
-    const bool need_v = (tx >= 1 && tx <= TX) && (a < N) && ((b >= 0 && b < N) || wy);
-    const int ly = b - (y0 - 3), lx = a - (x0 - 3);
+  NS_RECT_LOOP(SM::TW, SM::TH, NT, tr, tc) {
 #pragma unroll
-    for (int m = 0; m < 2; ++m) {
-      if (m == 0 ? !need_u : !need_v) continue;
-      const ff conv = (sm.fx[m][ty][tx + 1] - sm.fx[m][ty][tx]) * idx_ + (sm.fy[m][ty + 1][tx] - sm.fy[m][ty][tx]) * idy_;
-      const ff c2 = ff_scale2(sm.c[m][ly][lx], 2.f);
-      const ff visc = (sm.c[m][ly][lx + 1] - c2 + sm.c[m][ly][lx - 1]) * vx + (sm.c[m][ly + 1][lx] - c2 + sm.c[m][ly - 1][lx]) * vy;
-      sm.t[m][ty][tx] = visc - conv;
+      for (int m = 0; m < 2; ++m) {
+        const ff conv = (sm.fx[m][tr][tc + 1] - sm.fx[m][tr][tc]) * idx_ + (sm.fy[m][tr + 1][tc] - sm.fy[m][tr][tc]) * idy_;
+        const ff c2 = ff_scale2(sm.c[m][tr + 2][tc + 2], 2.f);
+        const ff visc = (sm.c[m][tr + 2][tc + 3] - c2 + sm.c[m][tr + 2][tc + 1]) * vx +
+                        (sm.c[m][tr + 3][tc + 2] - c2 + sm.c[m][tr + 1][tc + 2]) * vy;
+        sm.t[m][tr][tc] = visc - conv;
+      }
+    }
+  __syncthreads();
+  const bool wrapx = g.flux_ghost[0] == kWrap, wrapy = g.flux_ghost[1] == kWrap;
+  if ((x0 == 0 || x0 + TX >= N) && !wrapx) {
+    for (int tr = threadIdx.x; tr < SM::TH; tr += NT) {
+      if (x0 == 0) sm.t[0][tr][0] = (g.flux_ghost[0] == kReflect) ? -sm.t[0][tr][1] : zero;
+      const int tc = N - (x0 - 1);
+      if (x0 + TX >= N && tc < SM::TW) sm.t[0][tr][tc] = (g.flux_ghost[0] == kReflect) ? -sm.t[0][tr][tc - 1] : zero;
     }
   }
-  __syncthreads();
-  if (tid < 2 * (TY + TX)) {
-    if (tid < TY) {
-      const int ty = tid + 1;
-      if (x0 == 0 && !wx) sm.t[0][ty][0] = (g.flux_ghost[0] == kReflect) ? -sm.t[0][ty][1] : ff_make(0.f, 0.f);
-    } else if (tid < 2 * TY) {
-      const int ty = tid - TY + 1;
-      const int tx = N - (x0 - 1);
-      if (tx >= 1 && tx < SM::TW && !wx)
-        sm.t[0][ty][tx] = (g.flux_ghost[0] == kReflect) ? -sm.t[0][ty][tx - 1] : ff_make(0.f, 0.f);
-    } else if (tid < 2 * TY + TX) {
-      const int tx = tid - 2 * TY + 1;
-      if (y0 == 0 && !wy) sm.t[1][0][tx] = (g.flux_ghost[1] == kReflect) ? -sm.t[1][1][tx] : ff_make(0.f, 0.f);
-    } else {
-      const int tx = tid - 2 * TY - TX + 1;
-      const int ty = N - (y0 - 1);
-      if (ty >= 1 && ty < SM::TH && !wy)
-        sm.t[1][ty][tx] = (g.flux_ghost[1] == kReflect) ? -sm.t[1][ty - 1][tx] : ff_make(0.f, 0.f);
+  if ((y0 == 0 || y0 + TY >= N) && !wrapy) {
+    for (int tc = threadIdx.x; tc < SM::TW; tc += NT) {
+      if (y0 == 0) sm.t[1][0][tc] = (g.flux_ghost[1] == kReflect) ? -sm.t[1][1][tc] : zero;
+      const int tr = N - (y0 - 1);
+      if (y0 + TY >= N && tr < SM::TH) sm.t[1][tr][tc] = (g.flux_ghost[1] == kReflect) ? -sm.t[1][tr - 1][tc] : zero;
     }
   }
   __syncthreads();
 
+  // ---- 4. G(u_base) at the faces of the tile -----------------------------------------
   const ff c15 = ff_make(A.c15[0], A.c15[1]);
-  const int nfx = (x0 + TX >= N) ? (N - x0 + 1) : TX;
-  const int nfy = (y0 + TY >= N) ? (N - y0 + 1) : TY;
-  const int ncx = min(TX, N - x0), ncy = min(TY, N - y0);
-  for (int t = tid; t < nfx * ncy + ncx * nfy; t += NT) {
-    int m, a, b;
-    if (t < nfx * ncy) { m = 0; a = x0 + t % nfx; b = y0 + t / nfx; }
-    else { const int q = t - nfx * ncy; m = 1; a = x0 + q % ncx; b = y0 + q / ncx; }
+  auto face = [&](int m, int a, int b) {
+    const int tc = a - (x0 - 1), tr = b - (y0 - 1);
     const long id = (long)b * P + a;
-    const int tx = a - (x0 - 1), ty = b - (y0 - 1);
-    const ff tm = (m == 0) ? sm.t[0][ty][tx - 1] : sm.t[1][ty - 1][tx];
-    const ff tc = sm.t[m][ty][tx];
+    const ff tm = (m == 0) ? sm.t[0][tr][tc - 1] : sm.t[1][tr - 1][tc];
+    const ff tc_ = sm.t[m][tr][tc];
     const ff u = anchor_u(A, m, id);
-    const ff G = (ff_make(A.Sh[m][id], A.Sl[m][id]) - c15 * u) + ff_scale2(tm + tc, 0.5f);
+    const ff G = (ff_make(A.Sh[m][id], A.Sl[m][id]) - c15 * u) + ff_scale2(tm + tc_, 0.5f);
     A.obh[m][id] = u.hi;
     A.obl[m][id] = u.lo;
     A.g0[m][id] = G.hi + G.lo;
+  };
+  NS_RECT_LOOP(TX, TY, NT, k, l) {
+    const int a = x0 + l, b = y0 + k;
+    if (a < N && b < N) { face(0, a, b); face(1, a, b); }
   }
+  if (x0 + TX >= N && N > x0)
+    for (int k = threadIdx.x; k < TY; k += NT)
+      if (y0 + k < N) face(0, N, y0 + k);
+  if (y0 + TY >= N && N > y0)
+    for (int k = threadIdx.x; k < TX; k += NT)
+      if (x0 + k < N) face(1, x0 + k, N);
 }
 
 // FP64 field -> float-float (hi, lo) arrays, integer split (no FP64 pipe)

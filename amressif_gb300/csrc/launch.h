@@ -36,6 +36,10 @@ cudaError_t launch_mg_resnorm(const MGLevels<T>& M, double* part, unsigned* coun
 // kernels_mixed.cu
 struct IncArgs;
 struct AnchorFFArgs;
+struct DCffArgs;
+cudaError_t launch_dc_update_ff(const DCffArgs& a, cudaStream_t s);
+cudaError_t launch_rhs_ff(int n, long pitch, const double* f, const double* mean, float* fh, float* fl, cudaStream_t s);
+cudaError_t launch_ff_to_double(int n, long pitch, const float* h, const float* l, double* out, cudaStream_t s);
 cudaError_t launch_inc_stage(const IncArgs& a, cudaStream_t s);
 cudaError_t launch_anchor_ff(const AnchorFFArgs& a, cudaStream_t s);
 cudaError_t launch_split_ff(const Geom& g, const double* const* x, float* const* h, float* const* l, cudaStream_t s);

@@ -19,6 +19,7 @@
 
 #include "../../include/amressif_gpu.h"
 #include "anchor_ff2d.cuh"
+#include "dc_ff2d.cuh"
 #include "launch.h"
 #include "stage_inc2d.cuh"
 
@@ -73,6 +74,12 @@ struct ns_ctx {
   float* SFl[2] = {nullptr, nullptr};
   int mb = 0;
   bool base_ff_valid = false, s_ff_valid = false;
+  // float-float phi (ping-pong) and RHS of the mixed Poisson solve
+  float* PFh[2] = {nullptr, nullptr};
+  float* PFl[2] = {nullptr, nullptr};
+  float* FFh = nullptr;
+  float* FFl = nullptr;
+  long long dc_fallbacks = 0;
   // per-kernel timing (CUDA events around each launch) and launch count
   bool prof = false;
   std::vector<cudaEvent_t> evpool;
@@ -138,7 +145,9 @@ void free_all(ns_ctx* c) {
     for (int i = 0; i < 3; ++i) F(c->B[i][m]);
     F(c->SH[m]); F(c->G0[m]); F(c->E[0][m]); F(c->E[1][m]);
     F(c->BH[0][m]); F(c->BH[1][m]); F(c->BL[0][m]); F(c->BL[1][m]); F(c->SFh[m]); F(c->SFl[m]);
+    F(c->PFh[m]); F(c->PFl[m]);
   }
+  F(c->FFh); F(c->FFl);
   F(c->Pp); F(c->F);
   for (int l = 1; l < c->M64.L; ++l) { F(c->M64.x[l]); F(c->M64.f[l]); }
   for (int l = 0; l < c->M32.L; ++l) { F(c->M32.x[l]); F(c->M32.f[l]); }
@@ -761,6 +770,9 @@ __global__ void k_set_mean(double* red, double inv_n) { red[kRedMean] = red[kRed
 
 extern "C" {
 
+static int alloc_mixed(ns_ctx* c);
+static void split_const(double x, float* out);
+
 int ns_poisson_solve(ns_ctx* c, int precision, int* cycles, double* res) {
   if (!c) return NS_ERR_ARG;
   const double nn = (double)c->N * (double)c->N;
@@ -787,13 +799,32 @@ int ns_poisson_solve(ns_ctx* c, int precision, int* cycles, double* res) {
     d.red_out = c->red + kRedRes;
     d.e = c->M32.x[0];
     d.r32 = c->M32.f[0];
-    // M32 level 0 uses the FP64 pitch of the context (allocated with round_up(N,32))
-    int pc = c->phi_cur;
-    d.phi_in = c->PHI[pc];
-    d.phi_out = c->PHI[pc];
-    d.first = 1;
-    LAUNCH(NS_PROF_DC_UPDATE, "dc update", launch_dc_update(d, c->st));
-    int r = sync_red(c, kRedRes, 1);
+    // phi is carried in float-float (PFF) while the residual can still fall;
+    // if it stalls above the tolerance the sweeps continue with the FP64
+    // residual kernel.
+    int r = alloc_mixed(c);
+    if (r != NS_OK) return r;
+    DCffArgs q;
+    std::memset(&q, 0, sizeof(q));
+    q.n = c->N;
+    q.pitch = c->pitch;
+    q.periodic[0] = c->g.periodic[0];
+    q.periodic[1] = c->g.periodic[1];
+    for (int d2 = 0; d2 < 2; ++d2) split_const(c->M64.invh2[0][d2], q.ih[d2]);
+    q.e = c->M32.x[0];
+    q.r32 = c->M32.f[0];
+    q.f[0] = c->FFh;
+    q.f[1] = c->FFl;
+    q.part = c->part;
+    q.counter = c->counter;
+    q.red_out = c->red + kRedRes;
+    LAUNCH(NS_PROF_OTHER, "rhs split", launch_rhs_ff(c->N, c->pitch, c->F, c->red + kRedMean, c->FFh, c->FFl, c->st));
+    int pf = 0;
+    q.first = 1;
+    q.phin[0] = c->PFh[0]; q.phin[1] = c->PFl[0];
+    q.phout[0] = c->PFh[0]; q.phout[1] = c->PFl[0];
+    LAUNCH(NS_PROF_DC_UPDATE, "dc update", launch_dc_update_ff(q, c->st));
+    r = sync_red(c, kRedRes, 1);
     if (r != NS_OK) return r;
     rnorm0 = c->red_h[kRedRes];
     rn = rnorm0;
@@ -801,22 +832,45 @@ int ns_poisson_solve(ns_ctx* c, int precision, int* cycles, double* res) {
     auto done = [&](double x) { return x <= tol && (div_tol_res <= 0 || x <= div_tol_res); };
     double best = rn;
     int stall = 0;
+    bool ffmode = true;
+    int pc = 0;
     while (!done(rn) && rnorm0 > 0) {
       if (ncyc >= maxc) { status = NS_ERR_MG_STALL; break; }
       int r2 = vcycle<float>(c, c->M32, 1);
       if (r2 != NS_OK) return r2;
-      d.first = 0;
-      d.phi_in = c->PHI[pc];
-      d.phi_out = c->PHI[1 - pc];
-      LAUNCH(NS_PROF_DC_UPDATE, "dc update", launch_dc_update(d, c->st));
-      pc = 1 - pc;
+      if (ffmode) {
+        q.first = 0;
+        q.phin[0] = c->PFh[pf]; q.phin[1] = c->PFl[pf];
+        q.phout[0] = c->PFh[1 - pf]; q.phout[1] = c->PFl[1 - pf];
+        LAUNCH(NS_PROF_DC_UPDATE, "dc update", launch_dc_update_ff(q, c->st));
+        pf = 1 - pf;
+      } else {
+        d.first = 0;
+        d.phi_in = c->PHI[pc];
+        d.phi_out = c->PHI[1 - pc];
+        LAUNCH(NS_PROF_DC_UPDATE, "dc update", launch_dc_update(d, c->st));
+        pc = 1 - pc;
+      }
       ++ncyc;
       r2 = sync_red(c, kRedRes, 1);
       if (r2 != NS_OK) return r2;
       rn = c->red_h[kRedRes];
-      if (rn < 0.5 * best) { best = rn; stall = 0; } else if (++stall >= 6) { status = NS_ERR_MG_STALL; break; }
+      if (rn < 0.5 * best) {
+        best = rn;
+        stall = 0;
+      } else if (++stall >= (ffmode ? 2 : 6)) {
+        if (!ffmode) { status = NS_ERR_MG_STALL; break; }
+        // float-float floor reached: continue from the FP64 phi
+        LAUNCH(NS_PROF_OTHER, "phi to fp64", launch_ff_to_double(c->N, c->pitch, c->PFh[pf], c->PFl[pf], c->PHI[0], c->st));
+        ffmode = false;
+        pc = 0;
+        stall = 0;
+        c->dc_fallbacks++;
+      }
     }
-    c->phi_cur = pc;
+    if (ffmode)
+      LAUNCH(NS_PROF_OTHER, "phi to fp64", launch_ff_to_double(c->N, c->pitch, c->PFh[pf], c->PFl[pf], c->PHI[0], c->st));
+    c->phi_cur = ffmode ? 0 : pc;
   } else {
     c->phi_cur = 0;
     c->M64.x[0] = c->PHI[0];
@@ -922,7 +976,7 @@ static int mixed_iteration(ns_ctx* c, double* norm) {
   IncArgs ia;
   std::memset(&ia, 0, sizeof(ia));
   ia.g = c->g;
-  ia.part = c->part;
+  ia.part = reinterpret_cast<float2*>(c->part);
   ia.counter = c->counter;
   ia.norm_out = c->red + kRedNorm;
   for (int m = 0; m < 2; ++m) {
@@ -970,8 +1024,8 @@ static int alloc_mixed(ns_ctx* c) {
   if (c->G0[0]) return NS_OK;
   const size_t fb = (size_t)c->pitch * (c->N + 1) * sizeof(float);
   for (int m = 0; m < 2; ++m) {
-    float** ps[9] = {&c->G0[m], &c->E[0][m], &c->E[1][m], &c->BH[0][m], &c->BH[1][m],
-                     &c->BL[0][m], &c->BL[1][m], &c->SFh[m], &c->SFl[m]};
+    float** ps[12] = {&c->G0[m], &c->E[0][m], &c->E[1][m], &c->BH[0][m], &c->BH[1][m], &c->BL[0][m],
+                      &c->BL[1][m], &c->SFh[m], &c->SFl[m], &c->PFh[m], &c->PFl[m], m == 0 ? &c->FFh : &c->FFl};
     for (float** p : ps) {
       if (cudaMalloc(p, fb) != cudaSuccess) return fail(c, NS_ERR_NOMEM, "cudaMalloc (mixed) failed");
       CK(cudaMemsetAsync(*p, 0, fb, c->st), "memset");
@@ -1028,7 +1082,9 @@ int ns_step(ns_ctx* c, ns_step_stats* stats) {
   r = ns_poisson_rhs(c, &s.div_before, &s.rhs_sum);
   if (r != NS_OK) return r;
   const int prec = (c->P.precision == NS_PREC_MIXED) ? NS_PREC_MIXED : NS_PREC_FP64;
+  const long long fb0 = c->dc_fallbacks;
   r = ns_poisson_solve(c, prec, &s.poisson_cycles, &s.poisson_res);
+  s.poisson_fp64_fallback = (int)(c->dc_fallbacks - fb0);
   if (r != NS_OK && r != NS_ERR_MG_STALL) return r;
   const int mg_status = r;
   if (c->ev_ok) cudaEventRecord(c->ev[2], c->st);

@@ -132,4 +132,85 @@ __device__ __forceinline__ bool grid_reduce_last(double (&v)[NV], double* part, 
   return true;
 }
 
+// Flattened walk over a W x H rectangle by all NT threads of the block
+// (W, H compile-time, so the division is a multiply-shift).
+#define NS_RECT_LOOP(W, H, NT, r, c)                                        \
+  for (int _t = threadIdx.x, r = 0, c = 0; _t < (W) * (H) &&               \
+       ((r = _t / (W)), (c = _t - r * (W)), true); _t += (NT))
+
+// Block reduction on the FP32 pipes for the mixed-precision kernels: sums
+// are accumulated as float-float pairs (error-free TwoSum), maxima in float.
+// Each block writes (hi, lo) to part2; the last block reduces the partials in
+// block order and returns the totals in v (as double) on thread 0.
+template <int NV, int NT>
+__device__ __forceinline__ bool grid_reduce_last_f(float (&v)[NV], float2* part2, unsigned* counter, unsigned max_mask,
+                                                   double (&out)[NV]) {
+  __shared__ float2 red[NV][NT / 32];
+  __shared__ bool last;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  constexpr int NW = NT / 32;
+  auto ffadd = [](float2 a, float2 b) {
+    const float s = a.x + b.x;
+    const float bb = s - a.x;
+    const float e = (a.x - (s - bb)) + (b.x - bb) + (a.y + b.y);
+    const float h = s + e;
+    return make_float2(h, e - (h - s));
+  };
+#pragma unroll
+  for (int q = 0; q < NV; ++q) {
+    const bool is_max = (max_mask >> q) & 1u;
+    float2 x = make_float2(v[q], 0.f);
+    for (int o = 16; o > 0; o >>= 1) {
+      float2 y;
+      y.x = __shfl_down_sync(0xffffffffu, x.x, o);
+      y.y = __shfl_down_sync(0xffffffffu, x.y, o);
+      x = is_max ? make_float2(fmaxf(x.x, y.x), 0.f) : ffadd(x, y);
+    }
+    if (lane == 0) red[q][warp] = x;
+  }
+  __syncthreads();
+  const int nb = gridDim.x * gridDim.y * gridDim.z;
+  if (threadIdx.x == 0) {
+    const int bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+    for (int q = 0; q < NV; ++q) {
+      const bool is_max = (max_mask >> q) & 1u;
+      float2 x = red[q][0];
+      for (int w = 1; w < NW; ++w) x = is_max ? make_float2(fmaxf(x.x, red[q][w].x), 0.f) : ffadd(x, red[q][w]);
+      part2[(long)q * nb + bid] = x;
+    }
+    __threadfence();
+    const unsigned done = atomicAdd(counter, 1u);
+    last = (done == (unsigned)(nb - 1));
+  }
+  __syncthreads();
+  if (!last) return false;
+  __threadfence();
+#pragma unroll
+  for (int q = 0; q < NV; ++q) {
+    const bool is_max = (max_mask >> q) & 1u;
+    volatile const float2* pv = part2 + (long)q * nb;
+    float2 x = make_float2(0.f, 0.f);
+    for (int b = threadIdx.x; b < nb; b += NT) {
+      const float2 y = make_float2(pv[b].x, pv[b].y);
+      x = is_max ? make_float2(fmaxf(x.x, y.x), 0.f) : ffadd(x, y);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      float2 y;
+      y.x = __shfl_down_sync(0xffffffffu, x.x, o);
+      y.y = __shfl_down_sync(0xffffffffu, x.y, o);
+      x = is_max ? make_float2(fmaxf(x.x, y.x), 0.f) : ffadd(x, y);
+    }
+    __syncthreads();
+    if (lane == 0) red[q][warp] = x;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      float2 s = red[q][0];
+      for (int w = 1; w < NW; ++w) s = is_max ? make_float2(fmaxf(s.x, red[q][w].x), 0.f) : ffadd(s, red[q][w]);
+      out[q] = (double)s.x + (double)s.y;
+    }
+  }
+  if (threadIdx.x == 0) *counter = 0u;
+  return true;
+}
+
 }  // namespace ns

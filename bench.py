@@ -277,6 +277,8 @@ def bench_ours(args):
             "pseudo_iters_mean": statistics.mean(st["pseudo_iters"] for st in stats),
             "poisson_cycles_mean": statistics.mean(st["poisson_cycles"] for st in stats),
             "div_after_max": max(st["div_after"] for st in stats),
+            "div_before_max": max(st["div_before"] for st in stats),
+            "poisson_fp64_fallbacks": sum(st["poisson_fp64_fallback"] for st in stats),
             "phase_ms_per_step": {"predictor": statistics.mean(st["ms_predictor"] for st in stats),
                                   "poisson": statistics.mean(st["ms_poisson"] for st in stats),
                                   "project": statistics.mean(st["ms_project"] for st in stats)},

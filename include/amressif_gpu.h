@@ -86,6 +86,7 @@ typedef struct ns_step_stats {
   double div_after;   /* post-step max|div u| (main.cpp:1180) */
   int status;         /* NS_OK or NS_WARN_* */
   double ms_predictor, ms_poisson, ms_project; /* device time of the phases */
+  int poisson_fp64_fallback; /* mixed solve: 1 if the float-float residual floor forced FP64 sweeps */
 } ns_step_stats;
 
 typedef struct ns_ctx ns_ctx;
