@@ -35,6 +35,7 @@ EXPORTS = [
     "ns_get_state", "ns_step_begin", "ns_rk_stage", "ns_pseudo_norm", "ns_explicit_predictor",
     "ns_poisson_rhs", "ns_poisson_solve", "ns_project", "ns_step", "ns_step_host", "ns_sync",
     "ns_profile_enable", "ns_profile_read", "ns_launch_count", "ns_host_alloc", "ns_host_free",
+    "ns_poisson_rhs_noalloc",
 ]
 
 
@@ -159,6 +160,8 @@ def lib():
         L.ns_host_alloc.restype = ctypes.c_void_p
         L.ns_host_free.argtypes = [ctypes.c_void_p]
         L.ns_host_free.restype = None
+        L.ns_poisson_rhs_noalloc.argtypes = [vp, vp, vp, ctypes.c_int, ctypes.c_longlong, ctypes.c_double,
+                                             ctypes.c_double, ctypes.c_double, dp, vp]
         _lib = L
     return _lib
 

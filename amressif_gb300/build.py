@@ -24,6 +24,7 @@ UNITS = {
     "kernels_fast.cu": [],
     "kernels_mixed.cu": [],
     "ns_api.cu": [],
+    "noalloc.cu": ["-fmad=false"],
 }
 
 

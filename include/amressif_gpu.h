@@ -165,6 +165,24 @@ int ns_sync(ns_ctx* c);
 #define NS_PROF_DC_UPDATE 14
 #define NS_PROF_OTHER 15
 #define NS_PROF_KINDS 16
+/* Poisson right-hand side without any device allocation. No counterpart in
+ * the reference. For callers that cannot call cudaMalloc: a host whose device
+ * memory all belongs to its own arena allocator (AMReX's), or a job whose
+ * memory budget is fixed once it starts. Computes f = (1.5/dt) div u from
+ * caller-owned device arrays u (x faces), v (y faces) and f (cells), all with
+ * row pitch `pitch` elements (u(i,j) at j*pitch+i, pitch >= n_cell+1), and
+ * returns {max|div u|, sum f} in divmax_sum[2] (host memory) after
+ * synchronising `stream` (a cudaStream_t, NULL = default stream). The
+ * reduction scratch is a fixed 1 MB device array inside the library, held on
+ * every GPU that loads it until the process exits: n_cell above 4096 is
+ * rejected with NS_ERR_UNSUPPORTED. The first call on each device looks up
+ * that array's device address; make it before any stream capture. All calls
+ * share the array, so calls that overlap on the GPU (other streams, other
+ * threads) race and must be serialised by the caller. Results are
+ * bit-identical to ns_poisson_rhs. */
+int ns_poisson_rhs_noalloc(const double* u, const double* v, double* f, int n_cell, long long pitch, double dx, double dy,
+                           double dt, double* divmax_sum, void* stream);
+
 /* Page-locked host memory for the ns_step_host / ns_put_box buffers of a
  * host that keeps its fields in CPU memory (cudaMallocHost). */
 void* ns_host_alloc(unsigned long long bytes);
