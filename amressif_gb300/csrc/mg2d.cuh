@@ -29,6 +29,9 @@ struct MGLevels {
   double invh2[kMaxLevels][2];
   // 1/diagonal for the (east+west, north+south) neighbour counts: index a + 3 b
   double invdiag[kMaxLevels][9];
+  // the same constants in T, so that no conversion runs per update
+  T ih[kMaxLevels][2];
+  T idg[kMaxLevels][9];
   int periodic[2];
   const double* fmean;            // subtracted from f at level 0 when non-null
 };
@@ -36,11 +39,12 @@ struct MGLevels {
 // Gauss-Seidel update of one cell from its four neighbours; w* = 0 removes an
 // absent (Neumann) neighbour from both the sum and the diagonal.
 template <typename T>
-__device__ __forceinline__ T gs_update(T xe, T xw, T xn, T xs, T we, T ww, T wn, T wsn, T ihx, T ihy, T f,
-                                       const double* invdiag) {
-  const T sum = (we * xe + ww * xw) * ihx + (wn * xn + wsn * xs) * ihy;
-  const int k = (int)(we + ww) + 3 * (int)(wn + wsn);
-  return (sum - f) * (T)invdiag[k];
+__device__ __forceinline__ T gs_update(T xe, T xw, T xn, T xs, bool we, bool ww, bool wn, bool wsn, T ihx, T ihy, T f,
+                                       const T* idg) {
+  const T zero = (T)0;
+  const T sum = ((we ? xe : zero) + (ww ? xw : zero)) * ihx + ((wn ? xn : zero) + (wsn ? xs : zero)) * ihy;
+  const int k = (int)we + (int)ww + 3 * ((int)wn + (int)wsn);
+  return (sum - f) * idg[k];
 }
 
 template <typename T>
@@ -74,7 +78,7 @@ __global__ void __launch_bounds__(256) k_mg_smooth(MGLevels<T> M, int l, int mod
   const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
   const int tid = threadIdx.x, NT = blockDim.x;
   const bool px = M.periodic[0], py = M.periodic[1];
-  const T ihx = (T)M.invh2[l][0], ihy = (T)M.invh2[l][1];
+  const T ihx = M.ih[l][0], ihy = M.ih[l][1];
   for (int t = tid; t < SM::W * SM::HH; t += NT) {
     const int lx = t % SM::W, ly = t / SM::W;
     const int a = x0 - H + lx, b = y0 - H + ly;
@@ -117,10 +121,10 @@ __global__ void __launch_bounds__(256) k_mg_smooth(MGLevels<T> M, int l, int mod
       if (!px && (a < 0 || a >= n)) continue;
       if (!py && (b < 0 || b >= n)) continue;
       const int lx = a - (x0 - H), ly = b - (y0 - H);
-      const T we = (px || a + 1 < n) ? (T)1 : (T)0, ww = (px || a > 0) ? (T)1 : (T)0;
-      const T wn = (py || b + 1 < n) ? (T)1 : (T)0, wsn = (py || b > 0) ? (T)1 : (T)0;
+      const bool we = px || a + 1 < n, ww = px || a > 0;
+      const bool wn = py || b + 1 < n, wsn = py || b > 0;
       sm.x[ly][lx] = gs_update<T>(sm.x[ly][lx + 1], sm.x[ly][lx - 1], sm.x[ly + 1][lx], sm.x[ly - 1][lx],
-                                  we, ww, wn, wsn, ihx, ihy, sm.f[ly][lx], M.invdiag[l]);
+                                  we, ww, wn, wsn, ihx, ihy, sm.f[ly][lx], M.idg[l]);
     }
     __syncthreads();
   }
@@ -140,7 +144,7 @@ __global__ void __launch_bounds__(256) k_mg_restrict(MGLevels<T> M, int l) {
   const int n = M.n[l];
   const long P = M.pitch[l];
   const bool px = M.periodic[0], py = M.periodic[1];
-  const T ihx = (T)M.invh2[l][0], ihy = (T)M.invh2[l][1];
+  const T ihx = M.ih[l][0], ihy = M.ih[l][1];
   const T* x = M.x[l];
   T s = (T)0;
 #pragma unroll
@@ -168,7 +172,7 @@ __global__ void __launch_bounds__(256) k_mg_resnorm(MGLevels<T> M, double* part,
   double v[1] = {0.0};
   if (a < n && b < n) {
     const bool px = M.periodic[0], py = M.periodic[1];
-    const T ihx = (T)M.invh2[0][0], ihy = (T)M.invh2[0][1];
+    const T ihx = M.ih[0][0], ihy = M.ih[0][1];
     const T* x = M.x[0];
     const long id = (long)b * P + a;
     const T xc = x[id];
@@ -232,7 +236,7 @@ __global__ void __launch_bounds__(1024) k_mg_bottom(MGLevels<T> M, int lb, int x
   __syncthreads();
   auto smooth = [&](int l, int cfirst) {
     const int n = M.n[l];
-    const T ihx = (T)M.invh2[l][0], ihy = (T)M.invh2[l][1];
+    const T ihx = M.ih[l][0], ihy = M.ih[l][1];
     T* x = sx + off[l];
     const T* f = sf + off[l];
     for (int s = 0; s < 4; ++s) {
@@ -240,18 +244,18 @@ __global__ void __launch_bounds__(1024) k_mg_bottom(MGLevels<T> M, int lb, int x
       for (int t = tid; t < n * n; t += NT) {
         const int a = t % n, b = t / n;
         if (((a + b) & 1) != color) continue;
-        const T we = (px || a + 1 < n) ? (T)1 : (T)0, ww = (px || a > 0) ? (T)1 : (T)0;
-        const T wn = (py || b + 1 < n) ? (T)1 : (T)0, wsn = (py || b > 0) ? (T)1 : (T)0;
+        const bool we = px || a + 1 < n, ww = px || a > 0;
+        const bool wn = py || b + 1 < n, wsn = py || b > 0;
         const T xe = x[b * n + wrapi(a + 1, n)], xw = x[b * n + wrapi(a - 1, n)];
         const T xn = x[wrapi(b + 1, n) * n + a], xs = x[wrapi(b - 1, n) * n + a];
-        x[t] = gs_update<T>(xe, xw, xn, xs, we, ww, wn, wsn, ihx, ihy, f[t], M.invdiag[l]);
+        x[t] = gs_update<T>(xe, xw, xn, xs, we, ww, wn, wsn, ihx, ihy, f[t], M.idg[l]);
       }
       __syncthreads();
     }
   };
   auto apply_negL = [&](int l, const T* in, T* out) {  // out = -L in
     const int n = M.n[l];
-    const T ihx = (T)M.invh2[l][0], ihy = (T)M.invh2[l][1];
+    const T ihx = M.ih[l][0], ihy = M.ih[l][1];
     for (int t = tid; t < n * n; t += NT) {
       const int a = t % n, b = t / n;
       const T c = in[t];

@@ -185,7 +185,10 @@ int alloc_levels(ns_ctx* c, MGLevels<T>& M, bool own_level0) {
       for (int b = 0; b < 3; ++b) {
         const double diag = a * M.invh2[l][0] + b * M.invh2[l][1];
         M.invdiag[l][a + 3 * b] = diag > 0 ? 1.0 / diag : 0.0;
+        M.idg[l][a + 3 * b] = (T)M.invdiag[l][a + 3 * b];
       }
+    M.ih[l][0] = (T)M.invh2[l][0];
+    M.ih[l][1] = (T)M.invh2[l][1];
     M.x[l] = nullptr;
     M.f[l] = nullptr;
     if (l > 0 || own_level0) {
