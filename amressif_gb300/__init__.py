@@ -36,6 +36,8 @@ EXPORTS = [
     "ns_poisson_rhs", "ns_poisson_solve", "ns_project", "ns_step", "ns_step_host", "ns_sync",
     "ns_profile_enable", "ns_profile_read", "ns_launch_count", "ns_host_alloc", "ns_host_free",
     "ns_poisson_rhs_noalloc",
+    "ns_adjoint_opts_default", "ns_set_controls", "ns_step_adjoint_fwd", "ns_step_adjoint_bwd",
+    "ns_adjoint_get_state_grad", "ns_step_jvp", "ns_step_vjp", "ns_adjoint_op",
 ]
 
 
@@ -111,6 +113,33 @@ class NsStepStats(ctypes.Structure):
     ]
 
 
+class NsAdjointOpts(ctypes.Structure):
+    _fields_ = [
+        ("nsteps", ctypes.c_int),
+        ("nsnap", ctypes.c_int),
+        ("lin_tol", ctypes.c_double),
+        ("lin_max_iters", ctypes.c_int),
+    ]
+
+
+class NsAdjointStats(ctypes.Structure):
+    _fields_ = [
+        ("J", ctypes.c_double),
+        ("nsteps", ctypes.c_int),
+        ("nsnap", ctypes.c_int),
+        ("steps_advanced", ctypes.c_longlong),
+        ("predictor_runs", ctypes.c_longlong),
+        ("adjoint_steps", ctypes.c_longlong),
+        ("lin_iters", ctypes.c_longlong),
+        ("lin_max_iters_seen", ctypes.c_int),
+        ("lin_max_res", ctypes.c_double),
+        ("poisson_cycles", ctypes.c_longlong),
+        ("ms_forward", ctypes.c_double),
+        ("ms_backward", ctypes.c_double),
+        ("status", ctypes.c_int),
+    ]
+
+
 _lib = None
 
 
@@ -162,6 +191,15 @@ def lib():
         L.ns_host_free.restype = None
         L.ns_poisson_rhs_noalloc.argtypes = [vp, vp, vp, ctypes.c_int, ctypes.c_longlong, ctypes.c_double,
                                              ctypes.c_double, ctypes.c_double, dp, vp]
+        L.ns_adjoint_opts_default.argtypes = [P(NsAdjointOpts)]
+        L.ns_adjoint_opts_default.restype = None
+        L.ns_set_controls.argtypes = [vp, ctypes.c_int, dp]
+        L.ns_step_adjoint_fwd.argtypes = [vp, P(NsAdjointOpts), ctypes.c_int, dp, dp, P(NsAdjointStats)]
+        L.ns_step_adjoint_bwd.argtypes = [vp, dp, P(NsAdjointStats)]
+        L.ns_adjoint_get_state_grad.argtypes = [vp, P(dp), P(dp), dp]
+        L.ns_step_jvp.argtypes = [vp, P(dp), P(dp), dp, dp, P(dp), P(dp), dp]
+        L.ns_step_vjp.argtypes = [vp, P(dp), P(dp), dp, P(dp), P(dp), dp, dp]
+        L.ns_adjoint_op.argtypes = [vp, ctypes.c_int, P(dp), dp, P(dp), dp]
         _lib = L
     return _lib
 
@@ -184,7 +222,23 @@ def default_params(**kw):
 
 
 def stats_dict(st):
-    return {k: getattr(st, k) for k, _ in NsStepStats._fields_}
+    return {k: getattr(st, k) for k, _ in type(st)._fields_}
+
+
+def adjoint_opts(**kw):
+    o = NsAdjointOpts()
+    lib().ns_adjoint_opts_default(ctypes.byref(o))
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
+
+
+def _pair(arrs):
+    return (ctypes.POINTER(ctypes.c_double) * 2)(*[_dp(a) for a in arrs])
+
+
+def _opt(a):
+    return None if a is None else _dp(a)
 
 
 class Solver:
@@ -329,3 +383,73 @@ class Solver:
 
     def launch_count(self):
         return int(lib().ns_launch_count(self.h))
+
+    # ---- discrete adjoint (ns_step_adjoint_fwd / ns_step_adjoint_bwd pair) ----
+    def set_controls(self, controls):
+        """Piecewise-constant lid profile (len divides n_cell); None: uniform lid."""
+        if controls is None:
+            self._check(lib().ns_set_controls(self.h, 0, None), "ns_set_controls")
+            self.nseg = 0
+            return
+        c = np.ascontiguousarray(controls, dtype=np.float64)
+        self._check(lib().ns_set_controls(self.h, c.size, _dp(c)), "ns_set_controls")
+        self.nseg = c.size
+
+    def adjoint_fwd(self, controls, **opts):
+        """Forward run with binomial snapshots; returns (J, stats dict)."""
+        o = adjoint_opts(**opts)
+        c = np.ascontiguousarray(controls, dtype=np.float64)
+        J = ctypes.c_double()
+        st = NsAdjointStats()
+        self._check(lib().ns_step_adjoint_fwd(self.h, ctypes.byref(o), c.size, _dp(c), ctypes.byref(J), ctypes.byref(st)),
+                    "ns_step_adjoint_fwd", allow_warn=True)
+        self.nseg = c.size
+        return J.value, stats_dict(st)
+
+    def adjoint_bwd(self):
+        """Reverse sweep of the last adjoint_fwd; returns (dJ/dcontrols, stats dict)."""
+        g = np.zeros(max(1, getattr(self, "nseg", 0)))
+        st = NsAdjointStats()
+        self._check(lib().ns_step_adjoint_bwd(self.h, _dp(g), ctypes.byref(st)), "ns_step_adjoint_bwd", allow_warn=True)
+        return g[: getattr(self, "nseg", 0)], stats_dict(st)
+
+    def adjoint_state_grad(self):
+        ub = [np.zeros(self.face_shape(d)) for d in range(2)]
+        upb = [np.zeros(self.face_shape(d)) for d in range(2)]
+        pb = np.zeros((self.n, self.n))
+        self._check(lib().ns_adjoint_get_state_grad(self.h, _pair(ub), _pair(upb), _dp(pb)), "ns_adjoint_get_state_grad")
+        return ub, upb, pb
+
+    def step_jvp(self, du, duprev, dp, dc=None):
+        du = [np.ascontiguousarray(a, dtype=np.float64) for a in du]
+        dup = [np.ascontiguousarray(a, dtype=np.float64) for a in duprev]
+        dp = np.ascontiguousarray(dp, dtype=np.float64)
+        dc = None if dc is None else np.ascontiguousarray(dc, dtype=np.float64)
+        o = [np.zeros(self.face_shape(d)) for d in range(2)]
+        op = [np.zeros(self.face_shape(d)) for d in range(2)]
+        odp = np.zeros((self.n, self.n))
+        self._check(lib().ns_step_jvp(self.h, _pair(du), _pair(dup), _dp(dp), _opt(dc), _pair(o), _pair(op), _dp(odp)),
+                    "ns_step_jvp")
+        return o, op, odp
+
+    def step_vjp(self, ubar, uprevbar, pbar):
+        ub = [np.ascontiguousarray(a, dtype=np.float64) for a in ubar]
+        upb = [np.ascontiguousarray(a, dtype=np.float64) for a in uprevbar]
+        pb = np.ascontiguousarray(pbar, dtype=np.float64)
+        o = [np.zeros(self.face_shape(d)) for d in range(2)]
+        op = [np.zeros(self.face_shape(d)) for d in range(2)]
+        opb = np.zeros((self.n, self.n))
+        cb = np.zeros(max(1, getattr(self, "nseg", 0)))
+        self._check(lib().ns_step_vjp(self.h, _pair(ub), _pair(upb), _dp(pb), _pair(o), _pair(op), _dp(opb), _dp(cb)),
+                    "ns_step_vjp")
+        return o, op, opb, cb[: getattr(self, "nseg", 0)]
+
+    def adjoint_op(self, x, transpose=False, dc=None):
+        """J x (+ dA/dc dc) or (J^T x, dA/dc^T x) at the current state's u*."""
+        x = [np.ascontiguousarray(a, dtype=np.float64) for a in x]
+        y = [np.zeros(self.face_shape(d)) for d in range(2)]
+        cb = np.zeros(max(1, getattr(self, "nseg", 0)))
+        dcv = None if dc is None else np.ascontiguousarray(dc, dtype=np.float64)
+        self._check(lib().ns_adjoint_op(self.h, 1 if transpose else 0, _pair(x), _opt(dcv), _pair(y), _dp(cb)),
+                    "ns_adjoint_op")
+        return (y, cb[: getattr(self, "nseg", 0)]) if transpose else y

@@ -23,7 +23,9 @@ UNITS = {
     "kernels_exact.cu": ["-fmad=false"],
     "kernels_fast.cu": [],
     "kernels_mixed.cu": [],
+    "kernels_adjoint.cu": [],
     "ns_api.cu": [],
+    "adjoint_api.cu": [],
     "noalloc.cu": ["-fmad=false"],
 }
 

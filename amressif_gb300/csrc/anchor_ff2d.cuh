@@ -142,7 +142,15 @@ __global__ void __launch_bounds__(NT) k_anchor_ff2d(AnchorFFArgs A) {
         rm = (2 * N - 1 - b) - (y0 - 3);
         side = 3;
       }
-      for (int m = 0; m < 2; ++m) sm.c[m][r][c] = cart_ghost_ff(g.bc[side], m, sm.c[m][rm][c]);
+      for (int m = 0; m < 2; ++m) {
+        if (side == 3 && m == 0 && g.lid_u != nullptr && g.bc[3].rule[0] == kInlet) {
+          int a = x0 - 3 + c;
+          a = a < 0 ? 0 : (a >= N ? N - 1 : a);
+          sm.c[m][r][c] = ff_from_double(2 * g.lid_u[a]) - sm.c[m][rm][c];
+        } else {
+          sm.c[m][r][c] = cart_ghost_ff(g.bc[side], m, sm.c[m][rm][c]);
+        }
+      }
     }
     __syncthreads();
   }

@@ -1,0 +1,140 @@
+// Private host-side definition of the solver context (ns_ctx) and the helpers
+// shared by the translation units of the C ABI (ns_api.cu: forward advance;
+// adjoint_api.cu: tangent-linear / adjoint of the advance).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "../../include/amressif_gpu.h"
+#include "mg2d.cuh"
+#include "ns_common.cuh"
+
+namespace nsh {
+struct AdjState;  // adjoint workspace (adjoint_api.cu)
+}
+
+struct ns_ctx {
+  ns_params P;
+  ns::Geom g;
+  int N = 0;
+  long pitch = 0;
+  size_t fbytes = 0;  // bytes of one FP64 field
+  cudaStream_t st = nullptr;
+  bool own_stream = false;
+  double dt = 0, time = 0, rk[4] = {0, 0, 0, 0};
+  // FP64 fields
+  double* U[2] = {nullptr, nullptr};
+  double* UP[2] = {nullptr, nullptr};
+  double* DU[2] = {nullptr, nullptr};
+  double* B[3][2] = {{nullptr, nullptr}, {nullptr, nullptr}, {nullptr, nullptr}};
+  double* S[2] = {nullptr, nullptr};
+  double* Pp = nullptr;
+  double* PHI[2] = {nullptr, nullptr};
+  double* F = nullptr;
+  double* CART[2] = {nullptr, nullptr};
+  bool cart_pending = false;
+  // pseudo-iteration state: buffer ids, -1 = UP, 0..2 = B[i]
+  int base = -1, cur = -1;
+  bool in_step = false;
+  bool norm_ready = false;
+  // mixed predictor
+  float* SH[2] = {nullptr, nullptr};
+  float* G0[2] = {nullptr, nullptr};
+  float* E[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+  // multigrid
+  ns::MGLevels<double> M64;
+  ns::MGLevels<float> M32;
+  int lb = 0;
+  int phi_cur = 0;
+  // reductions
+  double* part = nullptr;
+  unsigned* counter = nullptr;
+  double* red = nullptr;    // device scalars
+  double* red_h = nullptr;  // pinned mirror
+  cudaEvent_t ev[4];
+  bool ev_ok = false;
+  // mixed iteration: E[0] holds an increment not yet added to the base
+  bool mix_pending = false;
+  // float-float pseudo-iterate (hi, lo) ping-pong and the split source S
+  float* BH[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+  float* BL[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+  float* SFh[2] = {nullptr, nullptr};
+  float* SFl[2] = {nullptr, nullptr};
+  int mb = 0;
+  bool base_ff_valid = false, s_ff_valid = false;
+  // float-float phi (ping-pong) and RHS of the mixed Poisson solve
+  float* PFh[2] = {nullptr, nullptr};
+  float* PFl[2] = {nullptr, nullptr};
+  float* FFh = nullptr;
+  float* FFl = nullptr;
+  long long dc_fallbacks = 0;
+  // per-kernel timing (CUDA events around each launch) and launch count
+  bool prof = false;
+  std::vector<cudaEvent_t> evpool;
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pend;
+  double pms[NS_PROF_KINDS] = {0};
+  long long pcnt[NS_PROF_KINDS] = {0};
+  long long launches = 0;
+  // lid profile (one value per cell column) when controls are set
+  double* lid_col = nullptr;
+  int nseg = 0;
+  nsh::AdjState* adj = nullptr;
+  std::string err;
+};
+
+namespace nsh {
+
+enum RedSlot { kRedNorm = 0, kRedDivBefore = 1, kRedSum = 2, kRedMean = 3, kRedRes = 4, kRedDivAfter = 5, kRedF = 6, kRedObj = 7 };
+
+int fail(ns_ctx* c, int code, const std::string& msg);
+int cuda_check(ns_ctx* c, cudaError_t e, const char* what);
+int sync_red(ns_ctx* c, int first, int count);
+int alloc_field(ns_ctx* c, double** p);
+void prof_resolve(ns_ctx* c);
+cudaEvent_t pool_get(ns_ctx* c);
+// predictor of one step (ns_step_begin, pseudo-iterations, finalisation); the
+// converged u* is face_ptr(c, c->cur, .)
+int run_predictor(ns_ctx* c, ns_step_stats* s);
+void free_adjoint(ns_ctx* c);
+
+inline double* face_ptr(ns_ctx* c, int id, int m) { return id < 0 ? c->UP[m] : c->B[id][m]; }
+
+// Launch one kernel (a callable returning cudaError_t), counting it and, when
+// profiling is on, bracketing it with events on the context's stream.
+template <class F>
+int launch(ns_ctx* c, int kind, const char* what, F&& f) {
+  cudaEvent_t a = nullptr, b = nullptr;
+  if (c->prof) {
+    a = pool_get(c);
+    b = pool_get(c);
+    if (a) cudaEventRecord(a, c->st);
+  }
+  const cudaError_t e = f();
+  c->launches++;
+  if (c->prof && a && b) {
+    cudaEventRecord(b, c->st);
+    c->pend.push_back({kind, {a, b}});
+    if (c->pend.size() > 4096) {
+      cudaStreamSynchronize(c->st);
+      prof_resolve(c);
+    }
+  }
+  return cuda_check(c, e, what);
+}
+
+}  // namespace nsh
+
+#define CK(expr, what)                                  \
+  do {                                                  \
+    int _r = nsh::cuda_check(c, (expr), what);          \
+    if (_r != NS_OK) return _r;                         \
+  } while (0)
+
+#define LAUNCH(kind, what, expr)                                                    \
+  do {                                                                              \
+    int _r = nsh::launch(c, kind, what, [&]() -> cudaError_t { return (expr); });   \
+    if (_r != NS_OK) return _r;                                                     \
+  } while (0)

@@ -46,6 +46,31 @@ cudaError_t launch_split_ff(const Geom& g, const double* const* x, float* const*
 cudaError_t launch_ff_add_inc(const Geom& g, const float* const* h, const float* const* l, const float* const* e,
                               double* const* out, cudaStream_t s);
 
+// kernels_adjoint.cu
+struct AdjArgs;
+cudaError_t launch_adj_cart(const Geom& g, const double* s0, const double* s1, double* d0, double* d1, const double* lid,
+                            int homogeneous, cudaStream_t s);
+cudaError_t launch_jvp(const AdjArgs& a, cudaStream_t s);
+cudaError_t launch_vjp(const AdjArgs& a, cudaStream_t s);
+cudaError_t launch_adj_div(const Geom& g, const double* u0, const double* u1, const double* pb, double coef, double* f,
+                           double* part, unsigned* counter, double* red_out, cudaStream_t s);
+cudaError_t launch_adj_gradsub(const Geom& g, const double* in0, const double* in1, const double* psi, double coef, double* o0,
+                               double* o1, cudaStream_t s);
+cudaError_t launch_adj_lincomb(const Geom& g, double a, const double* x0, const double* x1, double b, const double* y0,
+                               const double* y1, double* o0, double* o1, cudaStream_t s);
+cudaError_t launch_adj_cells(const Geom& g, double a, const double* x, double b, const double* y, double* o, cudaStream_t s);
+cudaError_t launch_tlm_rhs(const Geom& g, const double* const* jl, const double* dp, const double* const* du,
+                           const double* const* dup, double* const* out, cudaStream_t s);
+struct BcgArgs;
+enum BcgPhase { kBcgInit = 0, kBcgAlpha, kBcgS, kBcgOmega, kBcgXR, kBcgP };
+cudaError_t launch_bcg(int phase, const BcgArgs& a, cudaStream_t s);
+cudaError_t launch_adj_objective(const Geom& g, const double* u0, const double* u1, double* part, unsigned* counter,
+                                 double* red_out, cudaStream_t s);
+cudaError_t launch_adj_objective_grad(const Geom& g, const double* u0, const double* u1, double* o0, double* o1,
+                                      cudaStream_t s);
+cudaError_t launch_lid_expand(int N, int nseg, const double* seg, double* col, cudaStream_t s);
+cudaError_t launch_lid_accum(int N, int nseg, const double* col, double coef, double* seg_acc, cudaStream_t s);
+
 struct DCArgs {
   int n;
   long pitch;

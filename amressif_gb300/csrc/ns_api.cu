@@ -19,80 +19,15 @@
 
 #include "../../include/amressif_gpu.h"
 #include "anchor_ff2d.cuh"
+#include "ctx.h"
 #include "dc_ff2d.cuh"
 #include "launch.h"
 #include "stage_inc2d.cuh"
 
 using namespace ns;
+using namespace nsh;
 
-struct ns_ctx {
-  ns_params P;
-  Geom g;
-  int N = 0;
-  long pitch = 0;
-  size_t fbytes = 0;  // bytes of one FP64 field
-  cudaStream_t st = nullptr;
-  bool own_stream = false;
-  double dt = 0, time = 0, rk[4] = {0, 0, 0, 0};
-  // FP64 fields
-  double* U[2] = {nullptr, nullptr};
-  double* UP[2] = {nullptr, nullptr};
-  double* DU[2] = {nullptr, nullptr};
-  double* B[3][2] = {{nullptr, nullptr}, {nullptr, nullptr}, {nullptr, nullptr}};
-  double* S[2] = {nullptr, nullptr};
-  double* Pp = nullptr;
-  double* PHI[2] = {nullptr, nullptr};
-  double* F = nullptr;
-  double* CART[2] = {nullptr, nullptr};
-  bool cart_pending = false;
-  // pseudo-iteration state: buffer ids, -1 = UP, 0..2 = B[i]
-  int base = -1, cur = -1;
-  bool in_step = false;
-  bool norm_ready = false;
-  // mixed predictor
-  float* SH[2] = {nullptr, nullptr};
-  float* G0[2] = {nullptr, nullptr};
-  float* E[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
-  // multigrid
-  MGLevels<double> M64;
-  MGLevels<float> M32;
-  int lb = 0;
-  int phi_cur = 0;
-  // reductions
-  double* part = nullptr;
-  unsigned* counter = nullptr;
-  double* red = nullptr;    // device scalars
-  double* red_h = nullptr;  // pinned mirror
-  cudaEvent_t ev[4];
-  bool ev_ok = false;
-  // mixed iteration: E[0] holds an increment not yet added to the base
-  bool mix_pending = false;
-  // float-float pseudo-iterate (hi, lo) ping-pong and the split source S
-  float* BH[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
-  float* BL[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
-  float* SFh[2] = {nullptr, nullptr};
-  float* SFl[2] = {nullptr, nullptr};
-  int mb = 0;
-  bool base_ff_valid = false, s_ff_valid = false;
-  // float-float phi (ping-pong) and RHS of the mixed Poisson solve
-  float* PFh[2] = {nullptr, nullptr};
-  float* PFl[2] = {nullptr, nullptr};
-  float* FFh = nullptr;
-  float* FFl = nullptr;
-  long long dc_fallbacks = 0;
-  // per-kernel timing (CUDA events around each launch) and launch count
-  bool prof = false;
-  std::vector<cudaEvent_t> evpool;
-  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pend;
-  double pms[NS_PROF_KINDS] = {0};
-  long long pcnt[NS_PROF_KINDS] = {0};
-  long long launches = 0;
-  std::string err;
-};
-
-namespace {
-
-enum RedSlot { kRedNorm = 0, kRedDivBefore = 1, kRedSum = 2, kRedMean = 3, kRedRes = 4, kRedDivAfter = 5, kRedF = 6 };
+namespace nsh {
 
 int fail(ns_ctx* c, int code, const std::string& msg) {
   if (c) c->err = msg;
@@ -104,13 +39,47 @@ int cuda_check(ns_ctx* c, cudaError_t e, const char* what) {
   return fail(c, NS_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
-#define CK(expr, what)                                  \
-  do {                                                  \
-    int _r = cuda_check(c, (expr), what);               \
-    if (_r != NS_OK) return _r;                         \
-  } while (0)
+int alloc_field(ns_ctx* c, double** p) {
+  if (cudaMalloc(p, c->fbytes) != cudaSuccess) return fail(c, NS_ERR_NOMEM, "cudaMalloc failed");
+  if (cudaMemsetAsync(*p, 0, c->fbytes, c->st) != cudaSuccess) return fail(c, NS_ERR_CUDA, "memset failed");
+  return NS_OK;
+}
 
-double* face_ptr(ns_ctx* c, int id, int m) { return id < 0 ? c->UP[m] : c->B[id][m]; }
+int sync_red(ns_ctx* c, int first, int count) {
+  CK(cudaMemcpyAsync(c->red_h + first, c->red + first, count * sizeof(double), cudaMemcpyDeviceToHost, c->st), "readback");
+  CK(cudaStreamSynchronize(c->st), "stream sync");
+  if (c->prof) prof_resolve(c);
+  return NS_OK;
+}
+
+cudaEvent_t pool_get(ns_ctx* c) {
+  if (!c->evpool.empty()) {
+    cudaEvent_t e = c->evpool.back();
+    c->evpool.pop_back();
+    return e;
+  }
+  cudaEvent_t e;
+  if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+  return e;
+}
+
+// Fold completed launch timings into the per-kind totals (stream is idle).
+void prof_resolve(ns_ctx* c) {
+  for (auto& p : c->pend) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, p.second.first, p.second.second) == cudaSuccess) {
+      c->pms[p.first] += ms;
+      c->pcnt[p.first] += 1;
+    }
+    c->evpool.push_back(p.second.first);
+    c->evpool.push_back(p.second.second);
+  }
+  c->pend.clear();
+}
+
+}  // namespace nsh
+
+namespace {
 
 // ghost rule table of one velCart side (utilities.cpp:62-349)
 int make_cart_bc(const ns_params& P, int d, int side, CartBC& b) {
@@ -149,6 +118,8 @@ void free_all(ns_ctx* c) {
   }
   F(c->FFh); F(c->FFl);
   F(c->Pp); F(c->F);
+  F(c->lid_col);
+  free_adjoint(c);
   for (int l = 1; l < c->M64.L; ++l) { F(c->M64.x[l]); F(c->M64.f[l]); }
   for (int l = 0; l < c->M32.L; ++l) { F(c->M32.x[l]); F(c->M32.f[l]); }
   F(c->part); F(c->counter); F(c->red);
@@ -157,12 +128,6 @@ void free_all(ns_ctx* c) {
   for (auto& p : c->pend) { cudaEventDestroy(p.second.first); cudaEventDestroy(p.second.second); }
   for (auto& e : c->evpool) cudaEventDestroy(e);
   if (c->own_stream && c->st) cudaStreamDestroy(c->st);
-}
-
-int alloc_field(ns_ctx* c, double** p) {
-  if (cudaMalloc(p, c->fbytes) != cudaSuccess) return fail(c, NS_ERR_NOMEM, "cudaMalloc failed");
-  if (cudaMemsetAsync(*p, 0, c->fbytes, c->st) != cudaSuccess) return fail(c, NS_ERR_CUDA, "memset failed");
-  return NS_OK;
 }
 
 template <typename T>
@@ -207,15 +172,6 @@ int alloc_levels(ns_ctx* c, MGLevels<T>& M, bool own_level0) {
   return NS_OK;
 }
 
-void prof_resolve(ns_ctx* c);
-
-int sync_red(ns_ctx* c, int first, int count) {
-  CK(cudaMemcpyAsync(c->red_h + first, c->red + first, count * sizeof(double), cudaMemcpyDeviceToHost, c->st), "readback");
-  CK(cudaStreamSynchronize(c->st), "stream sync");
-  if (c->prof) prof_resolve(c);
-  return NS_OK;
-}
-
 StageArgs base_stage_args(ns_ctx* c) {
   StageArgs a;
   std::memset(&a, 0, sizeof(a));
@@ -237,60 +193,6 @@ int pick_out(int base, int in) {
     if (i != base && i != in) return i;
   return -2;
 }
-
-cudaEvent_t pool_get(ns_ctx* c) {
-  if (!c->evpool.empty()) {
-    cudaEvent_t e = c->evpool.back();
-    c->evpool.pop_back();
-    return e;
-  }
-  cudaEvent_t e;
-  if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
-  return e;
-}
-
-// Fold completed launch timings into the per-kind totals (stream is idle).
-void prof_resolve(ns_ctx* c) {
-  for (auto& p : c->pend) {
-    float ms = 0.f;
-    if (cudaEventElapsedTime(&ms, p.second.first, p.second.second) == cudaSuccess) {
-      c->pms[p.first] += ms;
-      c->pcnt[p.first] += 1;
-    }
-    c->evpool.push_back(p.second.first);
-    c->evpool.push_back(p.second.second);
-  }
-  c->pend.clear();
-}
-
-// Launch one kernel (a callable returning cudaError_t), counting it and, when
-// profiling is on, bracketing it with events on the context's stream.
-template <class F>
-int launch(ns_ctx* c, int kind, const char* what, F&& f) {
-  cudaEvent_t a = nullptr, b = nullptr;
-  if (c->prof) {
-    a = pool_get(c);
-    b = pool_get(c);
-    if (a) cudaEventRecord(a, c->st);
-  }
-  const cudaError_t e = f();
-  c->launches++;
-  if (c->prof && a && b) {
-    cudaEventRecord(b, c->st);
-    c->pend.push_back({kind, {a, b}});
-    if (c->pend.size() > 4096) {
-      cudaStreamSynchronize(c->st);
-      prof_resolve(c);
-    }
-  }
-  return cuda_check(c, e, what);
-}
-
-#define LAUNCH(kind, what, expr)                                   \
-  do {                                                             \
-    int _r = launch(c, kind, what, [&]() -> cudaError_t { return (expr); }); \
-    if (_r != NS_OK) return _r;                                    \
-  } while (0)
 
 }  // namespace
 
@@ -1037,17 +939,16 @@ static int alloc_mixed(ns_ctx* c) {
   return NS_OK;
 }
 
-int ns_step(ns_ctx* c, ns_step_stats* stats) {
-  if (!c) return NS_ERR_ARG;
+}  // extern "C"
+
+int nsh::run_predictor(ns_ctx* c, ns_step_stats* sp) {
+  ns_step_stats& s = *sp;
   const bool mixed = (c->P.precision == NS_PREC_MIXED) && c->P.pseudo_timestepping != 0;
   if (mixed) {
     int ra = alloc_mixed(c);
     if (ra != NS_OK) return ra;
   }
   c->mix_pending = false;
-  ns_step_stats s;
-  std::memset(&s, 0, sizeof(s));
-  if (c->ev_ok) cudaEventRecord(c->ev[0], c->st);
   int r = ns_step_begin(c);
   if (r != NS_OK) return r;
   int countIter = 0;
@@ -1079,7 +980,17 @@ int ns_step(ns_ctx* c, ns_step_stats* stats) {
   }
   s.pseudo_iters = countIter;
   s.norm_error = normError;
-  r = mixed_finalize(c);
+  return mixed_finalize(c);
+}
+
+extern "C" {
+
+int ns_step(ns_ctx* c, ns_step_stats* stats) {
+  if (!c) return NS_ERR_ARG;
+  ns_step_stats s;
+  std::memset(&s, 0, sizeof(s));
+  if (c->ev_ok) cudaEventRecord(c->ev[0], c->st);
+  int r = run_predictor(c, &s);
   if (r != NS_OK) return r;
   if (c->ev_ok) cudaEventRecord(c->ev[1], c->st);
   r = ns_poisson_rhs(c, &s.div_before, &s.rhs_sum);

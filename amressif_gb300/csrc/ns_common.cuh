@@ -45,6 +45,10 @@ struct Geom {
   int flux_ghost[3];  // per direction: kReflect (quirk Q1), kWrap, kZero
   int ctx_mirror[3];  // 1: p/phi ghosts mirrored (quirk Q2), 0: periodic wrap
   CartBC bc[6];       // xlo, xhi, ylo, yhi, zlo, zhi
+  // optional lid profile of the north inlet (u component, one value per cell
+  // column, device memory): the ghost becomes 2*lid_u[i] - q instead of
+  // 2*inflow_waveform[0] - q (the controlled lid of the adjoint problem)
+  const double* lid_u;
 };
 
 // periodic index in [0, n) for any a (tiles of small grids reach past one period)
@@ -57,6 +61,15 @@ __host__ __device__ __forceinline__ int wrapi(int a, int n) {
 __device__ __forceinline__ double cart_ghost(const CartBC& b, int m, double q) {
   const int r = b.rule[m];
   return r == kInlet ? b.add[m] - q : (r == kNeg ? -q : q);
+}
+
+// north ghost of column a: the lid profile replaces the uniform inlet value
+__device__ __forceinline__ double cart_ghost_north(const Geom& g, int m, double q, int a) {
+  if (m == 0 && g.lid_u != nullptr && g.bc[3].rule[0] == kInlet) {
+    const int aa = a < 0 ? 0 : (a >= g.N ? g.N - 1 : a);
+    return 2 * g.lid_u[aa] - q;
+  }
+  return cart_ghost(g.bc[3], m, q);
 }
 
 __device__ __forceinline__ float cart_ghost_f(const CartBC& b, int m, float q, bool homogeneous) {

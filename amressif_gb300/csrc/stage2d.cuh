@@ -139,7 +139,7 @@ __global__ void __launch_bounds__(256) k_stage2d(StageArgs A) {
         for (int m = 0; m < 2; ++m) sm.c[m][ly][lx] = cart_ghost(g.bc[2], m, sm.c[m][ml][lx]);
       } else if (b >= N && b < N + 3) {
         const int ml = (2 * N - 1 - b) - (y0 - 3);
-        for (int m = 0; m < 2; ++m) sm.c[m][ly][lx] = cart_ghost(g.bc[3], m, sm.c[m][ml][lx]);
+        for (int m = 0; m < 2; ++m) sm.c[m][ly][lx] = cart_ghost_north(g, m, sm.c[m][ml][lx], x0 - 3 + lx);
       }
     }
     __syncthreads();

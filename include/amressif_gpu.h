@@ -192,6 +192,83 @@ int ns_profile_enable(ns_ctx* c, int on);
 int ns_profile_read(ns_ctx* c, double* ms, long long* counts, int nkinds, int reset);
 long long ns_launch_count(const ns_ctx* c);
 
+/* ---- Discrete adjoint of the time advance (2D wall / lid boxes) ----------
+ *
+ * The differentiated map is one converged step of main_main's loop
+ * (main.cpp:875-1164): the BDF2 predictor u* solving G(u*) = 0 with the
+ * QUICK upwind switches frozen at u*, the Poisson solve and the projection.
+ * Tangent and adjoint linear solves run in FP64 (BiCGStab on the interior
+ * faces); the Poisson solves reuse the FP64 multigrid (self-adjoint). The
+ * forward steps use the context's precision. Periodic boxes and the explicit
+ * predictor (PSEUDO_TIMESTEPPING = 0) return NS_ERR_UNSUPPORTED.
+ *
+ * Controls: the north inlet's u is a piecewise-constant lid profile of nseg
+ * segments of n_cell / nseg columns; the north ghost becomes 2 c_k - phi
+ * (generalising the uniform inflow_waveform[0] of utilities.cpp:255).
+ *
+ * Objective: J = 1/2 sum over the cells of [lo, lo + L/2]^2 of
+ * (phi_u^2 + phi_v^2) dx dy at the final step (phi: cont2cart cell average). */
+
+typedef struct ns_adjoint_opts {
+  int nsteps;          /* steps of the forward run */
+  int nsnap;           /* device state snapshots incl. the initial state (>= 1); >= nsteps keeps every step */
+  double lin_tol;      /* BiCGStab: ||r|| <= lin_tol ||b|| */
+  int lin_max_iters;   /* BiCGStab iteration cap per solve */
+} ns_adjoint_opts;
+
+typedef struct ns_adjoint_stats {
+  double J;                 /* objective of the forward run */
+  int nsteps, nsnap;
+  long long steps_advanced; /* forward steps, first sweep and recomputation */
+  long long predictor_runs; /* predictor-only recomputations of u* */
+  long long adjoint_steps;
+  long long lin_iters;      /* BiCGStab iterations, all solves */
+  int lin_max_iters_seen;
+  double lin_max_res;       /* largest final ||r|| / ||b|| */
+  long long poisson_cycles; /* adjoint Poisson V-cycles */
+  double ms_forward;        /* wall time of ns_step_adjoint_fwd */
+  double ms_backward;       /* wall time of ns_step_adjoint_bwd */
+  int status;
+} ns_adjoint_stats;
+
+void ns_adjoint_opts_default(ns_adjoint_opts* o);
+
+/* Sets the lid controls (host array of nseg values; nseg divides n_cell). nseg
+ * = 0 restores the uniform inflow_waveform lid. */
+int ns_set_controls(ns_ctx* c, int nseg, const double* controls);
+
+/* Forward half of the pair (the analogue of an autograd Function's forward):
+ * sets the controls, runs opts->nsteps steps from the current state keeping
+ * binomial snapshots (Griewank's revolve schedule with opts->nsnap slots),
+ * and returns J. The context is left at the final state. */
+int ns_step_adjoint_fwd(ns_ctx* c, const ns_adjoint_opts* opts, int nseg, const double* controls, double* J,
+                        ns_adjoint_stats* stats);
+
+/* Backward half: reverse sweep from the snapshots of the last
+ * ns_step_adjoint_fwd, returning dJ/dcontrols (host, nseg values). The
+ * gradient with respect to the initial state is kept and can be read with
+ * ns_adjoint_get_state_grad. The context is left at the final state. */
+int ns_step_adjoint_bwd(ns_ctx* c, double* grad, ns_adjoint_stats* stats);
+
+/* dJ/d(u^0, u^{-1}, p^0) of the last backward sweep (host arrays in the
+ * ns_set_state layout; any pointer may be NULL). */
+int ns_adjoint_get_state_grad(ns_ctx* c, double* const* ubar, double* const* uprevbar, double* pbar);
+
+/* One linearised step at the current state (which is not advanced):
+ * tangent: (du, du_prev, dp, dc) -> (du', du_prev', dp') and
+ * adjoint: (ubar', uprevbar', pbar') -> (ubar, uprevbar, pbar, cbar).
+ * Host arrays in the ns_set_state layout; dc / cbar have nseg values (NULL
+ * when no controls are set). */
+int ns_step_jvp(ns_ctx* c, const double* const* du, const double* const* duprev, const double* dp, const double* dc,
+                double* const* du_out, double* const* duprev_out, double* dp_out);
+int ns_step_vjp(ns_ctx* c, const double* const* ubar_out, const double* const* uprevbar_out, const double* pbar_out,
+                double* const* ubar, double* const* uprevbar, double* pbar, double* cbar);
+
+/* The predictor Jacobian at the current state's u*: y = J x (transpose = 0)
+ * or y = J^T x (transpose = 1), plus the lid term (dc in, cbar out; NULL to
+ * skip). Faces in the ns_set_state layout. */
+int ns_adjoint_op(ns_ctx* c, int transpose, const double* const* x, const double* dc, double* const* y, double* cbar);
+
 #ifdef __cplusplus
 }
 #endif
