@@ -10,6 +10,8 @@ import os
 
 import numpy as np
 
+from . import workloads  # noqa: F401  (host-side inputs of the benchmark configurations)
+
 PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG, "libamressif_gb300.so")
 

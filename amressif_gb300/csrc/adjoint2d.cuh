@@ -327,13 +327,14 @@ __global__ void k_vjp_faces(AdjArgs A) {
 
 // ---- projection pieces ------------------------------------------------------------
 // f = D u + coef * pb over interior faces (boundary faces carry no tangent or
-// adjoint), with sum f reduced into red_out[0]
+// adjoint), with sum f reduced into sum_out and max |f| into max_out (nullable)
 __global__ void __launch_bounds__(256) k_adj_div(Geom g, const double* u0, const double* u1, const double* pb, double coef,
-                                                 double* f, double* part, unsigned* counter, double* red_out) {
+                                                 double* f, double* part, unsigned* counter, double* sum_out,
+                                                 double* max_out) {
   const int N = g.N;
   const long P = g.pitch;
   const int i = blockIdx.x * 32 + (threadIdx.x & 31), j = blockIdx.y * 8 + (threadIdx.x >> 5);
-  double v[1] = {0.0};
+  double v[2] = {0.0, 0.0};
   if (i < N && j < N) {
     const long id = (long)j * P + i;
     const double ul = (i >= 1) ? u0[id] : 0.0, ur = (i + 1 <= N - 1) ? u0[id + 1] : 0.0;
@@ -342,8 +343,12 @@ __global__ void __launch_bounds__(256) k_adj_div(Geom g, const double* u0, const
     if (pb) r += coef * pb[id];
     f[id] = r;
     v[0] = r;
+    v[1] = fabs(r);
   }
-  if (grid_reduce_last<1>(v, part, counter, 0u) && threadIdx.x == 0) red_out[0] = v[0];
+  if (grid_reduce_last<2>(v, part, counter, 2u) && threadIdx.x == 0) {
+    sum_out[0] = v[0];
+    if (max_out) max_out[0] = v[1];
+  }
 }
 
 // out = in - coef * grad(psi) on interior faces (mirror ghosts: zero gradient

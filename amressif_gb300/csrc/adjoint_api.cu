@@ -15,8 +15,11 @@
 //   pbar^n  = pbar' + D mu,           cbar += (dA/dc)^T mu,
 // (G^T = -D on the interior faces; the S coefficients are those of the step
 // source of main.cpp:931-1017). Only u* of step k enters the adjoint of step
-// k, so the reverse sweep recomputes u*_k from a snapshot of the state with
-// the predictor alone.
+// k. A snapshot keeps a time level and the u* of the step that produced it;
+// the reverse sweep follows a checkpoint schedule over the snapshot slots
+// (dynamic programming on the step / predictor costs, Griewank's binomial
+// split for long runs) and recomputes u*_k with the predictor alone only
+// inside segments left without a free slot.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -70,16 +73,23 @@ struct AdjState {
   double* LIDB = nullptr;
   double* DSEG = nullptr;
   double* SEGACC = nullptr;
-  // state snapshots: slot k holds U[2], UP[2], Pp
+  // state snapshots: slot k holds U[2], UP[2], Pp of its time level and u*[2]
+  // of the step that produced that level
   double* snap = nullptr;
   int nslots = 0;
   std::vector<int> slot_step;  // -1: free
   std::vector<double> slot_time;
   int final_slot = -1;
+  double* ORPH[2] = {nullptr, nullptr};  // u* of a released snapshot, not yet consumed
+  // previous adjoint Poisson solution (warm start of the next one)
+  double* PSI_PREV = nullptr;
+  bool psi_valid = false;
+  // schedule: best split of a segment of l steps with s free slots
+  std::vector<int> split_arg;  // (s, l) -> steps to advance before the next snapshot; 0: no split
+  int sched_S = -1, sched_L = -1;
   // last forward run
   bool have_fwd = false;
   int nsteps = 0, nsnap = 0;
-  int ustar_step = -1;  // step whose u* is in US
   ns_adjoint_opts opts;
   ns_adjoint_stats st;
 };
@@ -116,7 +126,7 @@ int ensure_adj(ns_ctx* c) {
   for (int m = 0; m < 2 && r == NS_OK; ++m) {
     double** faces[] = {&A.US[m], &A.CT[m], &A.UADV[m], &A.OUT[m], &A.ZERO[m], &A.X[m], &A.R[m], &A.RH[m],
                         &A.PV[m], &A.V[m], &A.SV[m], &A.T[m], &A.BV[m], &A.UB[m], &A.UPB[m], &A.AUS[m],
-                        &A.TL_DU[m], &A.TL_DUP[m], &A.FL[2 * m], &A.FL[2 * m + 1]};
+                        &A.TL_DU[m], &A.TL_DUP[m], &A.FL[2 * m], &A.FL[2 * m + 1], &A.ORPH[m]};
     for (double** p : faces)
       if (r == NS_OK) r = adj_alloc(c, p, fb);
     if (r == NS_OK) r = adj_alloc(c, &A.PHG[m], gb);
@@ -124,6 +134,7 @@ int ensure_adj(ns_ctx* c) {
   }
   if (r == NS_OK) r = adj_alloc(c, &A.PB, fb);
   if (r == NS_OK) r = adj_alloc(c, &A.TL_DP, fb);
+  if (r == NS_OK) r = adj_alloc(c, &A.PSI_PREV, fb);
   if (r == NS_OK) r = adj_alloc(c, &A.DLIDCOL, (size_t)N * sizeof(double));
   if (r == NS_OK) r = adj_alloc(c, &A.LIDB, (size_t)N * sizeof(double));
   if (r == NS_OK) r = adj_alloc(c, &A.DSEG, (size_t)N * sizeof(double));
@@ -302,18 +313,29 @@ void note_lin(ns_ctx* c, int it, double res) {
   s.lin_max_res = std::max(s.lin_max_res, res);
 }
 
-// L psi = P0 F with the FP64 multigrid (F and its sum in red[kRedSum] are set);
-// psi is left in PHI[phi_cur]
-int adj_poisson(ns_ctx* c, const double** psi) {
+// L psi = P0 F with the FP64 multigrid (F, its sum in red[kRedSum] and max|F|
+// in red[kRedF] are set), to poisson_tol_rel * max|F|; psi is left in
+// PHI[phi_cur]. warm: start from the previous solution of the sweep (the
+// adjoint fields change little from one step to the next).
+int adj_poisson(ns_ctx* c, bool warm, const double** psi) {
+  AdjState& A = *c->adj;
   const double keep = c->P.poisson_tol_div;
   c->P.poisson_tol_div = 0.0;
+  c->phi_guess = (warm && A.psi_valid) ? A.PSI_PREV : nullptr;
+  c->tol_from_f = true;
   int cyc = 0;
   double res = 0.0;
   const int r = ns_poisson_solve(c, NS_PREC_FP64, &cyc, &res);
   c->P.poisson_tol_div = keep;
-  c->adj->st.poisson_cycles += cyc;
+  c->phi_guess = nullptr;
+  c->tol_from_f = false;
+  A.st.poisson_cycles += cyc;
   if (r != NS_OK && !(r == NS_ERR_MG_STALL && res < 1e-9)) return r;
   *psi = c->PHI[c->phi_cur];
+  if (warm) {
+    CK(cudaMemcpyAsync(A.PSI_PREV, *psi, c->fbytes, cudaMemcpyDeviceToDevice, c->st), "keep psi");
+    A.psi_valid = true;
+  }
   return NS_OK;
 }
 
@@ -341,9 +363,10 @@ int adjoint_step(ns_ctx* c) {
   AdjState& A = *c->adj;
   const Geom& g = c->g;
   LAUNCH(NS_PROF_OTHER, "adjoint div",
-         launch_adj_div(g, A.UB[0], A.UB[1], A.PB, g.c15, c->F, c->part, c->counter, c->red + kRedSum, c->st));
+         launch_adj_div(g, A.UB[0], A.UB[1], A.PB, g.c15, c->F, c->part, c->counter, c->red + kRedSum, c->red + kRedF,
+                        c->st));
   const double* psi = nullptr;
-  int r = adj_poisson(c, &psi);
+  int r = adj_poisson(c, true, &psi);
   if (r != NS_OK) return r;
   LAUNCH(NS_PROF_OTHER, "adjoint gradsub", launch_adj_gradsub(g, A.UB[0], A.UB[1], psi, 1.0, A.AUS[0], A.AUS[1], c->st));
   LAUNCH(NS_PROF_OTHER, "adjoint lincomb",
@@ -365,7 +388,7 @@ int adjoint_step(ns_ctx* c) {
   LAUNCH(NS_PROF_OTHER, "adjoint lincomb",
          launch_adj_lincomb(g, -g.c05, A.X[0], A.X[1], 0.0, nullptr, nullptr, A.UPB[0], A.UPB[1], c->st));
   LAUNCH(NS_PROF_OTHER, "adjoint div",
-         launch_adj_div(g, A.X[0], A.X[1], A.PB, 1.0, A.PB, c->part, c->counter, c->red + kRedF, c->st));
+         launch_adj_div(g, A.X[0], A.X[1], A.PB, 1.0, A.PB, c->part, c->counter, c->red + kRedScratch, nullptr, c->st));
   A.st.adjoint_steps++;
   return NS_OK;
 }
@@ -391,26 +414,44 @@ int tangent_step(ns_ctx* c, bool dlid) {
   if (r != NS_OK) return r;
   note_lin(c, it, res);
   LAUNCH(NS_PROF_OTHER, "tangent div",
-         launch_adj_div(g, A.X[0], A.X[1], nullptr, 0.0, c->F, c->part, c->counter, c->red + kRedSum, c->st));
+         launch_adj_div(g, A.X[0], A.X[1], nullptr, 0.0, c->F, c->part, c->counter, c->red + kRedSum, c->red + kRedF,
+                        c->st));
   const double* psi = nullptr;
-  r = adj_poisson(c, &psi);
+  r = adj_poisson(c, false, &psi);
   if (r != NS_OK) return r;
   LAUNCH(NS_PROF_OTHER, "tangent gradsub", launch_adj_gradsub(g, A.X[0], A.X[1], psi, 1.0, A.OUT[0], A.OUT[1], c->st));
   LAUNCH(NS_PROF_OTHER, "tangent p", launch_adj_cells(g, 1.0, A.TL_DP, g.c15, psi, A.TL_DP, c->st));
   return NS_OK;
 }
 
-// ---- snapshots and the binomial (revolve) schedule ----------------------------------
+// ---- snapshots and the checkpoint schedule ------------------------------------------
+// slot k: fields 0-4 = U[2], UP[2], Pp of its time level; 5-6 = u*[2] of the
+// step that produced the level
+constexpr int kSlotFields = 7;
+
 double* slot_field(ns_ctx* c, int slot, int f) {
   const size_t words = c->fbytes / sizeof(double);
-  return c->adj->snap + ((size_t)slot * 5 + f) * words;
+  return c->adj->snap + ((size_t)slot * kSlotFields + f) * words;
 }
 
-int store_state(ns_ctx* c, int slot, int step) {
+int copy_pair(ns_ctx* c, double* const* dst, const double* const* src) {
+  for (int m = 0; m < 2; ++m)
+    CK(cudaMemcpyAsync(dst[m], src[m], c->fbytes, cudaMemcpyDeviceToDevice, c->st), "copy faces");
+  return NS_OK;
+}
+
+// store the current state as time level `step`; ustar: u* of the step that
+// produced it (the predictor buffer after ns_step), nullable
+int store_state(ns_ctx* c, int slot, int step, const double* const* ustar) {
   AdjState& A = *c->adj;
   double* src[5] = {c->U[0], c->U[1], c->UP[0], c->UP[1], c->Pp};
   for (int f = 0; f < 5; ++f)
     CK(cudaMemcpyAsync(slot_field(c, slot, f), src[f], c->fbytes, cudaMemcpyDeviceToDevice, c->st), "snapshot store");
+  if (ustar) {
+    double* d[2] = {slot_field(c, slot, 5), slot_field(c, slot, 6)};
+    int r = copy_pair(c, d, ustar);
+    if (r != NS_OK) return r;
+  }
   A.slot_step[slot] = step;
   A.slot_time[slot] = c->time;
   return NS_OK;
@@ -437,15 +478,54 @@ long long beta(int s, int r) {
   return (long long)(b + 0.5);
 }
 
-// Griewank's revolve split of [a, b) with s free snapshot slots: with r the
-// least repetition number for which beta(s, r) >= b - a, the right part gets
-// min(b - a - 1, beta(s - 1, r)) steps (reversed with s - 1 slots and r
-// repetitions), the left part the rest (s slots, r - 1 repetitions).
-int revolve_split(int a, int b, int s) {
-  const long long L = b - a;
+// Cost model of the reversal of a segment of l steps with s free slots, the
+// u* of its last step at hand: a full step costs 1, a predictor-only run
+// kPredCost. With no free slot the steps l-2 .. 0 are reached from the
+// segment's first state (restore, advance, predictor):
+//   T(l, 0) = (l-1)(l-2)/2 + (l-1) kPredCost,
+//   T(l, s) = min_m  m + T(l-m, s-1) + T(m, s)
+// (advance m steps and keep that level, reverse the right part, release the
+// slot, reverse the left part). Solved by dynamic programming when s L^2 is
+// small, else Griewank's binomial split: with r the least repetition number
+// for which beta(s, r) >= l, the right part gets min(l-1, beta(s-1, r)) steps.
+constexpr double kPredCost = 0.75;
+
+void build_schedule(AdjState& A, int L, int S) {
+  S = std::max(0, std::min(S, L - 1));
+  A.sched_L = L;
+  A.sched_S = S;
+  A.split_arg.clear();
+  if ((double)S * L * L > 3.0e8 || S == 0) return;
+  std::vector<double> T((size_t)(S + 1) * (L + 1), 0.0);
+  A.split_arg.assign((size_t)(S + 1) * (L + 1), 0);
+  auto at = [&](int s, int l) -> double& { return T[(size_t)s * (L + 1) + l]; };
+  for (int l = 1; l <= L; ++l) at(0, l) = 0.5 * (l - 1) * (l - 2) + (l - 1) * kPredCost;
+  for (int s = 1; s <= S; ++s) {
+    at(s, 1) = 0.0;
+    for (int l = 2; l <= L; ++l) {
+      double best = at(0, l);
+      int arg = 0;
+      for (int m = 1; m < l; ++m) {
+        const double v = m + at(s - 1, l - m) + at(s, m);
+        if (v < best) { best = v; arg = m; }
+      }
+      at(s, l) = best;
+      A.split_arg[(size_t)s * (L + 1) + l] = arg;
+    }
+  }
+}
+
+// next snapshot of the segment [a, b) with s free slots; -1: reverse it from a
+int next_split(AdjState& A, int a, int b, int s) {
+  const int l = b - a;
+  if (s <= 0 || l < 2) return -1;
+  if (!A.split_arg.empty() && l <= A.sched_L) {
+    const int m = A.split_arg[(size_t)std::min(s, A.sched_S) * (A.sched_L + 1) + l];
+    return m > 0 ? a + m : -1;
+  }
   int r = 1;
-  while (beta(s, r) < L) ++r;
-  const long long right = std::min(L - 1, beta(s - 1, r));
+  while (beta(s, r) < l) ++r;
+  const long long right = std::min((long long)l - 1, beta(s - 1, r));
   return b - (int)right;
 }
 
@@ -474,51 +554,48 @@ int free_slot(ns_ctx* c) {
   return -1;
 }
 
-// adjoint of step k with the state of step k in slot_k
-int adjoint_at(ns_ctx* c, int k, int slot_k) {
-  AdjState& A = *c->adj;
-  if (A.ustar_step != k) {
-    int r = restore_state(c, slot_k);
-    if (r == NS_OK) r = predictor_ustar(c);
-    if (r != NS_OK) return r;
-    A.ustar_step = k;
-  }
-  return adjoint_step(c);
+// adjoint of one step whose u* is in src
+int adjoint_with(ns_ctx* c, const double* const* src) {
+  int r = copy_pair(c, c->adj->US, src);
+  return r != NS_OK ? r : adjoint_step(c);
 }
 
-// reverse the steps [a, b): the state of step a is in slot_a, s slots free
-int reverse(ns_ctx* c, int a, int b, int s, int slot_a) {
+// reverse the steps [a, b): the state of level a is in slot_a, s slots are
+// free and ul holds u* of step b-1
+int reverse(ns_ctx* c, int a, int b, int s, int slot_a, const double* const* ul) {
   AdjState& A = *c->adj;
   if (b - a <= 0) return NS_OK;
-  if (b - a == 1) return adjoint_at(c, a, slot_a);
-  if (s == 0) {
-    for (int k = b - 1; k >= a; --k) {
-      if (A.ustar_step != k) {
-        int r = restore_state(c, slot_a);
-        if (r == NS_OK) r = advance(c, k - a);
-        if (r == NS_OK) r = predictor_ustar(c);
-        if (r != NS_OK) return r;
-        A.ustar_step = k;
-      }
-      int r = adjoint_step(c);
-      if (r != NS_OK) return r;
+  if (b - a == 1) return adjoint_with(c, ul);
+  const int m = next_split(A, a, b, s);
+  if (m < 0) {
+    int r = adjoint_with(c, ul);
+    for (int k = b - 2; k >= a && r == NS_OK; --k) {
+      r = restore_state(c, slot_a);
+      if (r == NS_OK) r = advance(c, k - a);
+      if (r == NS_OK) r = predictor_ustar(c);
+      if (r == NS_OK) r = adjoint_step(c);
     }
-    return NS_OK;
+    return r;
   }
-  const int m = revolve_split(a, b, s);
   int slot_m = find_slot(c, m);
   if (slot_m < 0) {
     slot_m = free_slot(c);
-    if (slot_m < 0) return fail(c, NS_ERR_STATE, "revolve: no free snapshot slot");
+    if (slot_m < 0) return fail(c, NS_ERR_STATE, "checkpoint schedule: no free snapshot slot");
     int r = restore_state(c, slot_a);
     if (r == NS_OK) r = advance(c, m - a);
-    if (r == NS_OK) r = store_state(c, slot_m, m);
+    const double* us[2] = {face_ptr(c, c->cur, 0), face_ptr(c, c->cur, 1)};
+    if (r == NS_OK) r = store_state(c, slot_m, m, us);
     if (r != NS_OK) return r;
   }
-  int r = reverse(c, m, b, s - 1, slot_m);
+  int r = reverse(c, m, b, s - 1, slot_m, ul);
+  if (r != NS_OK) return r;
+  // the slot's state is no longer needed, its u* (step m-1) is: the left
+  // part reverses step m-1 before it releases any other snapshot
+  const double* um[2] = {slot_field(c, slot_m, 5), slot_field(c, slot_m, 6)};
+  r = copy_pair(c, A.ORPH, um);
   if (r != NS_OK) return r;
   A.slot_step[slot_m] = -1;
-  return reverse(c, a, m, s, slot_a);
+  return reverse(c, a, m, s, slot_a, A.ORPH);
 }
 
 double now_ms() {
@@ -591,44 +668,49 @@ int ns_step_adjoint_fwd(ns_ctx* c, const ns_adjoint_opts* opts, int nseg, const 
     if (A.snap) cudaFree(A.snap);
     A.snap = nullptr;
     A.nslots = 0;
-    if (cudaMalloc(&A.snap, (size_t)nslots * 5 * c->fbytes) != cudaSuccess)
+    if (cudaMalloc(&A.snap, (size_t)nslots * kSlotFields * c->fbytes) != cudaSuccess)
       return fail(c, NS_ERR_NOMEM, "cudaMalloc (snapshots) failed");
     A.nslots = nslots;
   }
   A.slot_step.assign(nslots, -1);
   A.slot_time.assign(nslots, 0.0);
   A.final_slot = nslots - 1;
-  // the first descent of the schedule stores its checkpoints on the way
+  if (A.sched_L != opts->nsteps || A.sched_S != std::max(0, std::min(nsched - 1, opts->nsteps - 1)))
+    build_schedule(A, opts->nsteps, nsched - 1);
+  // the first descent of the schedule stores its snapshots on the way
   std::vector<int> first;
   {
     int a = 0, s = nsched - 1;
-    while (opts->nsteps - a > 1 && s > 0) {
-      a = revolve_split(a, opts->nsteps, s);
-      first.push_back(a);
+    while (true) {
+      const int m = next_split(A, a, opts->nsteps, s);
+      if (m < 0) break;
+      first.push_back(m);
+      a = m;
       --s;
     }
   }
   c->cart_pending = false;
-  r = store_state(c, 0, 0);
+  r = store_state(c, 0, 0, nullptr);
   if (r != NS_OK) return r;
   size_t next = 0;
   for (int k = 0; k < opts->nsteps; ++k) {
     if (next < first.size() && first[next] == k) {
       const int slot = free_slot(c);
-      if (slot < 0) return fail(c, NS_ERR_STATE, "revolve: no free snapshot slot");
-      r = store_state(c, slot, k);
+      if (slot < 0) return fail(c, NS_ERR_STATE, "checkpoint schedule: no free snapshot slot");
+      const double* us[2] = {face_ptr(c, c->cur, 0), face_ptr(c, c->cur, 1)};
+      r = store_state(c, slot, k, us);
       if (r != NS_OK) return r;
       ++next;
     }
     r = advance(c, 1);
     if (r != NS_OK) return r;
   }
-  // u* of the last step is still in the predictor buffer
-  for (int m = 0; m < 2; ++m)
-    CK(cudaMemcpyAsync(A.US[m], face_ptr(c, c->cur, m), c->fbytes, cudaMemcpyDeviceToDevice, c->st), "copy u*");
-  A.ustar_step = opts->nsteps - 1;
-  r = store_state(c, A.final_slot, opts->nsteps);
-  if (r != NS_OK) return r;
+  // the final level, with u* of the last step (still in the predictor buffer)
+  {
+    const double* us[2] = {face_ptr(c, c->cur, 0), face_ptr(c, c->cur, 1)};
+    r = store_state(c, A.final_slot, opts->nsteps, us);
+    if (r != NS_OK) return r;
+  }
   LAUNCH(NS_PROF_OTHER, "objective",
          launch_adj_objective(c->g, c->U[0], c->U[1], c->part, c->counter, c->red + kRedObj, c->st));
   // seed of the reverse sweep: dJ/du^N; zero adjoints of u^{N-1}, p^N, the controls and mu
@@ -658,7 +740,9 @@ int ns_step_adjoint_bwd(ns_ctx* c, double* grad, ns_adjoint_stats* stats) {
   CK(cudaStreamSynchronize(c->st), "stream sync");
   const double t0 = now_ms();
   const int nsched = std::min(A.nsnap, A.nsteps);
-  int r = reverse(c, 0, A.nsteps, nsched - 1, 0);
+  A.psi_valid = false;
+  const double* ul[2] = {slot_field(c, A.final_slot, 5), slot_field(c, A.final_slot, 6)};
+  int r = reverse(c, 0, A.nsteps, nsched - 1, 0, ul);
   if (r != NS_OK) return r;
   if (grad && c->nseg > 0)
     CK(cudaMemcpyAsync(grad, A.SEGACC, (size_t)c->nseg * sizeof(double), cudaMemcpyDeviceToHost, c->st), "gradient");
@@ -666,7 +750,6 @@ int ns_step_adjoint_bwd(ns_ctx* c, double* grad, ns_adjoint_stats* stats) {
   if (r != NS_OK) return r;
   CK(cudaStreamSynchronize(c->st), "stream sync");
   A.have_fwd = false;  // the snapshots of the schedule have been consumed
-  A.ustar_step = -1;
   A.st.ms_backward = now_ms() - t0;
   if (stats) *stats = A.st;
   return A.st.status < 0 ? A.st.status : NS_OK;
@@ -707,7 +790,6 @@ int ns_step_jvp(ns_ctx* c, const double* const* du, const double* const* duprev,
     CK(cudaMemcpyAsync(A.DSEG, dc, (size_t)c->nseg * sizeof(double), cudaMemcpyHostToDevice, c->st), "dc upload");
     LAUNCH(NS_PROF_OTHER, "lid expand", launch_lid_expand(c->N, c->nseg, A.DSEG, A.DLIDCOL, c->st));
   }
-  A.ustar_step = -1;
   r = predictor_ustar(c);
   if (r != NS_OK) return r;
   for (int m = 0; m < 2; ++m) CK(cudaMemsetAsync(A.X[m], 0, c->fbytes, c->st), "memset");
@@ -741,10 +823,10 @@ int ns_step_vjp(ns_ctx* c, const double* const* ubar_out, const double* const* u
   LAUNCH(NS_PROF_OTHER, "mask", launch_adj_lincomb(g, 1.0, A.UB[0], A.UB[1], 0.0, nullptr, nullptr, A.UB[0], A.UB[1], c->st));
   LAUNCH(NS_PROF_OTHER, "mask", launch_adj_lincomb(g, 1.0, A.UPB[0], A.UPB[1], 0.0, nullptr, nullptr, A.UPB[0], A.UPB[1], c->st));
   CK(cudaMemsetAsync(A.SEGACC, 0, (size_t)c->N * sizeof(double), c->st), "memset");
-  A.ustar_step = -1;
   r = predictor_ustar(c);
   if (r != NS_OK) return r;
   for (int m = 0; m < 2; ++m) CK(cudaMemsetAsync(A.X[m], 0, c->fbytes, c->st), "memset");
+  A.psi_valid = false;
   r = adjoint_step(c);
   if (r != NS_OK) return r;
   for (int m = 0; m < 2; ++m) {
@@ -775,7 +857,6 @@ int ns_adjoint_op(ns_ctx* c, int transpose, const double* const* x, const double
     LAUNCH(NS_PROF_OTHER, "lid expand", launch_lid_expand(c->N, c->nseg, A.DSEG, A.DLIDCOL, c->st));
   }
   A.have_fwd = false;
-  A.ustar_step = -1;
   r = predictor_ustar(c);
   if (r == NS_OK) r = base_cells(c);
   if (r != NS_OK) return r;

@@ -78,6 +78,11 @@ struct ns_ctx {
   double pms[NS_PROF_KINDS] = {0};
   long long pcnt[NS_PROF_KINDS] = {0};
   long long launches = 0;
+  // initial guess of the next FP64 Poisson solve (the adjoint's warm starts;
+  // null: start from zero) and whether its tolerance is relative to max|f|
+  // (in red[kRedF], written by the kernel that formed f) instead of r0
+  const double* phi_guess = nullptr;
+  bool tol_from_f = false;
   // lid profile (one value per cell column) when controls are set
   double* lid_col = nullptr;
   int nseg = 0;
@@ -87,7 +92,7 @@ struct ns_ctx {
 
 namespace nsh {
 
-enum RedSlot { kRedNorm = 0, kRedDivBefore = 1, kRedSum = 2, kRedMean = 3, kRedRes = 4, kRedDivAfter = 5, kRedF = 6, kRedObj = 7 };
+enum RedSlot { kRedNorm = 0, kRedDivBefore = 1, kRedSum = 2, kRedMean = 3, kRedRes = 4, kRedDivAfter = 5, kRedF = 6, kRedObj = 7, kRedScratch = 8 };
 
 int fail(ns_ctx* c, int code, const std::string& msg);
 int cuda_check(ns_ctx* c, cudaError_t e, const char* what);

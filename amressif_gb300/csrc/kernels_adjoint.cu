@@ -30,9 +30,9 @@ cudaError_t launch_vjp(const AdjArgs& a, cudaStream_t s) {
 }
 
 cudaError_t launch_adj_div(const Geom& g, const double* u0, const double* u1, const double* pb, double coef, double* f,
-                           double* part, unsigned* counter, double* red_out, cudaStream_t s) {
+                           double* part, unsigned* counter, double* sum_out, double* max_out, cudaStream_t s) {
   dim3 grid((g.N + 31) / 32, (g.N + 7) / 8, 1);
-  k_adj_div<<<grid, 256, 0, s>>>(g, u0, u1, pb, coef, f, part, counter, red_out);
+  k_adj_div<<<grid, 256, 0, s>>>(g, u0, u1, pb, coef, f, part, counter, sum_out, max_out);
   return cudaGetLastError();
 }
 

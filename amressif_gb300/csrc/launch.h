@@ -53,7 +53,7 @@ cudaError_t launch_adj_cart(const Geom& g, const double* s0, const double* s1, d
 cudaError_t launch_jvp(const AdjArgs& a, cudaStream_t s);
 cudaError_t launch_vjp(const AdjArgs& a, cudaStream_t s);
 cudaError_t launch_adj_div(const Geom& g, const double* u0, const double* u1, const double* pb, double coef, double* f,
-                           double* part, unsigned* counter, double* red_out, cudaStream_t s);
+                           double* part, unsigned* counter, double* sum_out, double* max_out, cudaStream_t s);
 cudaError_t launch_adj_gradsub(const Geom& g, const double* in0, const double* in1, const double* psi, double coef, double* o0,
                                double* o1, cudaStream_t s);
 cudaError_t launch_adj_lincomb(const Geom& g, double a, const double* x0, const double* x1, double b, const double* y0,

@@ -779,19 +779,26 @@ int ns_poisson_solve(ns_ctx* c, int precision, int* cycles, double* res) {
   } else {
     c->phi_cur = 0;
     c->M64.x[0] = c->PHI[0];
-    CK(cudaMemsetAsync(c->PHI[0], 0, c->fbytes, c->st), "memset phi");  // poisson.cpp:63
+    // the step's solve starts from zero (poisson.cpp:63); the adjoint's solves
+    // start from the previous step's solution with the tolerance relative to |f|
+    const bool warm = c->phi_guess != nullptr;
+    if (warm)
+      CK(cudaMemcpyAsync(c->PHI[0], c->phi_guess, c->fbytes, cudaMemcpyDeviceToDevice, c->st), "phi guess");
+    else
+      CK(cudaMemsetAsync(c->PHI[0], 0, c->fbytes, c->st), "memset phi");
     LAUNCH(NS_PROF_MG_RESNORM, "resnorm", launch_mg_resnorm<double>(c->M64, c->part, c->counter, c->red + kRedRes, c->st));
-    int r = sync_red(c, kRedRes, 1);
+    int r = sync_red(c, kRedRes, c->tol_from_f ? kRedF - kRedRes + 1 : 1);
     if (r != NS_OK) return r;
     rnorm0 = c->red_h[kRedRes];
     rn = rnorm0;
+    if (c->tol_from_f) rnorm0 = std::max(rnorm0, c->red_h[kRedF]);
     const double tol = c->P.poisson_tol_rel * rnorm0;
     auto done = [&](double x) { return x <= tol && (div_tol_res <= 0 || x <= div_tol_res); };
     double best = rn;
     int stall = 0;
     while (!done(rn) && rnorm0 > 0) {
       if (ncyc >= maxc) { status = NS_ERR_MG_STALL; break; }
-      int r2 = vcycle<double>(c, c->M64, ncyc == 0 ? 1 : 0);
+      int r2 = vcycle<double>(c, c->M64, (ncyc == 0 && !warm) ? 1 : 0);
       if (r2 != NS_OK) return r2;
       ++ncyc;
       LAUNCH(NS_PROF_MG_RESNORM, "resnorm", launch_mg_resnorm<double>(c->M64, c->part, c->counter, c->red + kRedRes, c->st));

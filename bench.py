@@ -149,6 +149,74 @@ def run_steps(s, k):
     return stats
 
 
+def adjoint_section(ns, args):
+    """Discrete adjoint on the 512^2 Re=400 cavity: 400 steps, 256 lid controls
+    c = 1 + N(0, 0.05^2) (numpy PCG64, seed 0), J = kinetic energy of the
+    lower-left quarter at the final step, 20 binomial snapshots. Times the plain
+    forward run (ns_step with the same controls) and the ns_step_adjoint_fwd /
+    ns_step_adjoint_bwd pair (wall clock, synchronised), and checks the gradient
+    against central differences (eps = 1e-6) along seeded unit directions."""
+    import numpy as np
+
+    n, L, nseg = args.adj_n, args.adj_steps, 256
+    rng = np.random.default_rng(0)
+    c = 1.0 + 0.05 * rng.standard_normal(nseg)
+
+    def solver(tol):
+        p = ns.default_params(n_cell=n, ren=400.0, fixed_dt=0.5 / n, iter_num=400, momentum_tolerance=tol,
+                              poisson_tol_rel=1e-12, precision=ns.PREC_FP64, max_grid_size=(n, n, n))
+        s = ns.Solver(p)
+        s.init(ns.INIT_CAVITY)
+        return s
+
+    s = solver(1e-10)
+    s.set_controls(c)
+    s.sync()
+    t0 = time.perf_counter()
+    ks = [s.step()["pseudo_iters"] for _ in range(L)]
+    s.sync()
+    plain_ms = 1e3 * (time.perf_counter() - t0)
+    s.close()
+    out = {"workload": "lid-driven cavity %dx%d, Re=400, dt=0.5/n, %d steps from rest, %d lid controls, "
+                       "J = kinetic energy of [0,1/2]^2 at the final step, FP64" % (n, n, L, nseg),
+           "plain_forward_ms": plain_ms, "pseudo_iters_mean": float(np.mean(ks))}
+    for nsnap in ([args.adj_snap, L] if args.adj_store_all else [args.adj_snap]):
+        s = solver(1e-10)
+        J, f = s.adjoint_fwd(c, nsteps=L, nsnap=nsnap, lin_tol=1e-12)
+        g, b = s.adjoint_bwd()
+        s.close()
+        key = "snapshots_%d" % nsnap if nsnap != L else "store_all"
+        out[key] = {"nsnap": nsnap, "J": J, "fwd_ms": f["ms_forward"], "bwd_ms": b["ms_backward"],
+                    "ratio": (f["ms_forward"] + b["ms_backward"]) / plain_ms,
+                    "steps_advanced": b["steps_advanced"], "predictor_runs": b["predictor_runs"],
+                    "bicgstab_iters_per_solve": b["lin_iters"] / max(1, b["adjoint_steps"]),
+                    "bicgstab_max_rel_res": b["lin_max_res"],
+                    "poisson_cycles_per_solve": b["poisson_cycles"] / max(1, b["adjoint_steps"]),
+                    "grad_norm": float(np.linalg.norm(g))}
+    out["ratio"] = out["snapshots_%d" % args.adj_snap]["ratio"]
+    if args.adj_fd > 0:
+        s = solver(1e-13)
+        J, _ = s.adjoint_fwd(c, nsteps=L, nsnap=args.adj_snap, lin_tol=1e-13)
+        g, _ = s.adjoint_bwd()
+        s.close()
+        errs = []
+        for _ in range(args.adj_fd):
+            d = rng.standard_normal(nseg)
+            d /= np.linalg.norm(d)
+            Js = []
+            for sg in (1.0, -1.0):
+                t = solver(1e-13)
+                Jx, _ = t.adjoint_fwd(c + sg * 1e-6 * d, nsteps=L, nsnap=2, lin_tol=1e-13)
+                t.close()
+                Js.append(Jx)
+            fd = (Js[0] - Js[1]) / 2e-6
+            ad = float(g @ d)
+            errs.append(abs(fd - ad) / abs(ad))
+        out["fd_check"] = {"directions": args.adj_fd, "eps": 1e-6, "max_rel_err": max(errs), "rel_errs": errs,
+                           "forward_tolerance": 1e-13}
+    return out
+
+
 def bench_ours(args):
     world, rank, dist = dist_setup()
     import amressif_gb300 as ns
@@ -265,6 +333,10 @@ def bench_ours(args):
                "sample": "%d step(s) from rest of the same %d^2 cavity (%.1f s, K=%s), oracle/ C++ restatement, "
                          "OpenMP" % (args.cpu_steps, n, secs, ks)}
 
+    adjoint = None
+    if rank == 0 and not args.no_adjoint:
+        adjoint = adjoint_section(ns, args)
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": K, "warmup": W,
@@ -284,7 +356,8 @@ def bench_ours(args):
                                   "project": statistics.mean(st["ms_project"] for st in stats)},
             "wall_ms_per_step": 1e3 * wall / K,
             "fp64_mg": fp64,
-            "adjoint_forward_ratio": None,
+            "adjoint_forward_ratio": adjoint["ratio"] if adjoint else None,
+            "adjoint": adjoint,
             "e2e": e2e,
             "gpu_launches": launches,
             "roofline": roofline,
@@ -332,6 +405,12 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--adj-n", type=int, default=512)
+    ap.add_argument("--adj-steps", type=int, default=400)
+    ap.add_argument("--adj-snap", type=int, default=20)
+    ap.add_argument("--adj-fd", type=int, default=2, help="finite-difference directions of the gradient check")
+    ap.add_argument("--adj-store-all", type=int, default=1, help="also time the store-every-step schedule")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
