@@ -5,34 +5,44 @@
 #include "dc_ff2d.cuh"
 #include "launch.h"
 #include "stage_inc2d.cuh"
+#include "stage_inc_col2d.cuh"
+#include "anchor_col2d.cuh"
 
 namespace ns {
 
-constexpr int kMixTX = 32, kMixTY = 32, kMixNT = 512;
-
-static inline dim3 mix_grid(const Geom& g) { return dim3((g.N + kMixTX - 1) / kMixTX, (g.N + kMixTY - 1) / kMixTY, 1); }
-
+// column-marching increment stage: one warp per 26-column x 64-row strip, a
+// cp.async ring of raw face rows per warp in shared memory
 cudaError_t launch_inc_stage(const IncArgs& a, cudaStream_t s) {
-  constexpr size_t smem = sizeof(IncSmem<kMixTX, kMixTY>);
+  constexpr int NT = 128;
+  const int N = a.g.N;
+  const long warps = (long)((N + 1 + kColOut - 1) / kColOut) * ((N + kColH - 1) / kColH);
+  const unsigned blocks = (unsigned)((warps + NT / 32 - 1) / (NT / 32));
+  constexpr size_t smem = inc_col_smem<NT>();
   static bool attr = false;
   if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(k_inc_stage2d<kMixTX, kMixTY, kMixNT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(k_inc_col2d<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     attr = true;
   }
-  k_inc_stage2d<kMixTX, kMixTY, kMixNT><<<mix_grid(a.g), kMixNT, smem, s>>>(a);
+  k_inc_col2d<NT><<<blocks, NT, smem, s>>>(a);
   return cudaGetLastError();
 }
 
+// column-marching float-float anchor: one warp per 26-column x 64-row strip,
+// a cp.async ring of raw face rows per warp in shared memory
 cudaError_t launch_anchor_ff(const AnchorFFArgs& a, cudaStream_t s) {
-  constexpr size_t smem = sizeof(AnchorSmem<kMixTX, kMixTY>);
+  constexpr int NT = 128;
+  const int N = a.g.N;
+  const long warps = (long)((N + 1 + kColOut - 1) / kColOut) * ((N + kColH - 1) / kColH);
+  const unsigned blocks = (unsigned)((warps + NT / 32 - 1) / (NT / 32));
+  constexpr size_t smem = anchor_col_smem<NT>();
   static bool attr = false;
   if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(k_anchor_ff2d<kMixTX, kMixTY, kMixNT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(k_anchor_col2d<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     attr = true;
   }
-  k_anchor_ff2d<kMixTX, kMixTY, kMixNT><<<mix_grid(a.g), kMixNT, smem, s>>>(a);
+  k_anchor_col2d<NT><<<blocks, NT, smem, s>>>(a);
   return cudaGetLastError();
 }
 
