@@ -36,7 +36,7 @@ METRIC = "steps/s at 4096² (div≤1e-10) mixed vs FP64 MG; adjoint/forward time
 ALGO_BYTES_PER_CELL = {
     "stage_exact": 88.0,   # read u*, u_base, u^n, du^n (2 x 8 B each) + p; write u*
     "stage_fast": 64.0,    # read u*, u_base, S; write u*
-    "anchor": 72.0,        # read u_base, e4 (f32), S; write u_base, FP32 copy, G0 (f32)
+    "anchor": 64.0,        # read base hi/lo, e4, S hi/lo (f32); write base hi/lo, G0 (f32)
     "increment": 88.0 / 3, # stage 1: read u_b, G0, write e; stages 2-3 also read e (all FP32)
     "explicit": 88.0,
     "step_begin": 56.0,    # read u, u_prev, p; write du, S
