@@ -225,3 +225,53 @@ def test_fast_modes_track_oracle(gpu_lib, oracle_lib, precision):
             assert rel(u[d], uo[d]) <= 1e-9, (step, d)
         assert relp(p, po) <= 1e-9
         assert abs(sg["pseudo_iters"] - so["pseudo_iters"]) <= 1
+
+
+BC_CASES = {
+    # name: (bc_lo, bc_hi, fix_quirks)
+    "south_slip": ((135, -135, 135), (135, 165, 135), 0),
+    "west_slip": ((-135, 135, 135), (135, 165, 135), 0),
+    "east_slip_code1": ((135, 135, 135), (1, 165, 135), 0),       # quirk Q5: east slip is tested as == 1
+    "east_slip_fixed": ((135, 135, 135), (-135, 165, 135), 1),
+    "west_inlet_165": ((165, 135, 135), (135, 165, 135), 0),
+    "west_inlet_m165": ((-165, 135, 135), (135, 135, 135), 0),
+    "south_inlet": ((135, 165, 135), (135, 135, 135), 0),
+}
+
+
+@pytest.mark.parametrize("precision", [ns.PREC_FP64_EXACT, ns.PREC_MIXED])
+@pytest.mark.parametrize("name", sorted(BC_CASES))
+def test_bc_codes_resynced(gpu_lib, oracle_lib, name, precision):
+    """Wall, slip and inlet codes of utilities.cpp:62-349 on every side: per-step
+    parity with the oracle (both sides start each step from the oracle's state)."""
+    lo, hi, fq = BC_CASES[name]
+    n = 48
+    o = Oracle(n, ren=100.0, dt=2e-3, iter_num=100, poisson_tol=1e-13, max_grid_size=(n, n, n), bc_lo=lo, bc_hi=hi,
+               fix_quirks=fq)
+    o.init(0)
+    p = ns.default_params(n_cell=n, ren=100.0, fixed_dt=2e-3, iter_num=100, precision=precision, poisson_tol_rel=1e-12,
+                          max_grid_size=(n, n, n), bc_lo=lo, bc_hi=hi, fix_quirks=fq)
+    s = ns.Solver(p)
+    s.init(ns.INIT_CAVITY)
+    tol = TOL_STEP if precision == ns.PREC_FP64_EXACT else 1e-9
+    for step in range(4):
+        if step > 0:
+            sync_state(o, s)
+        so = o.step()
+        sg = s.step()
+        assert sg["pseudo_iters"] == so["pseudo_iters"], (name, step, sg["pseudo_iters"], so["pseudo_iters"])
+        u, _, pg, _ = s.get_state()
+        uo, _, po, _ = o.get_state()
+        for d in range(2):
+            assert rel(u[d], uo[d]) <= tol, (name, step, d, rel(u[d], uo[d]))
+        assert relp(pg, po) <= tol, (name, step, relp(pg, po))
+    o.close()
+    s.close()
+
+
+def test_east_slip_code_m135_unsupported_in_parity_mode(gpu_lib):
+    """The reference leaves stale ghosts for an east -135 wall (it tests slip as
+    == 1, quirk Q5); the parity mode refuses it instead of guessing."""
+    p = ns.default_params(n_cell=32, bc_lo=(135, 135, 135), bc_hi=(-135, 165, 135), fix_quirks=0)
+    with pytest.raises(ns.NsError):
+        ns.Solver(p)
