@@ -40,6 +40,7 @@ EXPORTS = [
     "ns_poisson_rhs_noalloc",
     "ns_adjoint_opts_default", "ns_set_controls", "ns_step_adjoint_fwd", "ns_step_adjoint_bwd",
     "ns_adjoint_get_state_grad", "ns_step_jvp", "ns_step_vjp", "ns_adjoint_op",
+    "ns_checkpoint_get", "ns_checkpoint_put", "ns_get_step",
 ]
 
 
@@ -202,6 +203,10 @@ def lib():
         L.ns_step_jvp.argtypes = [vp, P(dp), P(dp), dp, dp, P(dp), P(dp), dp]
         L.ns_step_vjp.argtypes = [vp, P(dp), P(dp), dp, P(dp), P(dp), dp, dp]
         L.ns_adjoint_op.argtypes = [vp, ctypes.c_int, P(dp), dp, P(dp), dp]
+        L.ns_checkpoint_get.argtypes = [vp, P(dp), P(dp), dp, dp, P(ctypes.c_longlong)]
+        L.ns_checkpoint_put.argtypes = [vp, P(dp), P(dp), dp, ctypes.c_double, ctypes.c_longlong]
+        L.ns_get_step.argtypes = [vp]
+        L.ns_get_step.restype = ctypes.c_longlong
         _lib = L
     return _lib
 
@@ -385,6 +390,26 @@ class Solver:
 
     def launch_count(self):
         return int(lib().ns_launch_count(self.h))
+
+    @property
+    def step_count(self):
+        return int(lib().ns_get_step(self.h))
+
+    def checkpoint_get(self):
+        """(u, u_prev, p, time, step): the restart state of SaveCheckpoint"""
+        u = [np.zeros(self.face_shape(d)) for d in range(2)]
+        up = [np.zeros(self.face_shape(d)) for d in range(2)]
+        p = np.zeros((self.n, self.n))
+        t, k = ctypes.c_double(), ctypes.c_longlong()
+        self._check(lib().ns_checkpoint_get(self.h, _pair(u), _pair(up), _dp(p), ctypes.byref(t), ctypes.byref(k)),
+                    "ns_checkpoint_get")
+        return u, up, p, t.value, k.value
+
+    def checkpoint_put(self, u, u_prev, p, time, step):
+        u = [np.ascontiguousarray(a, dtype=np.float64) for a in u]
+        up = [np.ascontiguousarray(a, dtype=np.float64) for a in u_prev]
+        p = np.ascontiguousarray(p, dtype=np.float64)
+        self._check(lib().ns_checkpoint_put(self.h, _pair(u), _pair(up), _dp(p), time, step), "ns_checkpoint_put")
 
     # ---- discrete adjoint (ns_step_adjoint_fwd / ns_step_adjoint_bwd pair) ----
     def set_controls(self, controls):

@@ -90,6 +90,7 @@ struct AdjState {
   // last forward run
   bool have_fwd = false;
   int nsteps = 0, nsnap = 0;
+  long long step0 = 0;  // step counter of the context at the start of the forward run
   ns_adjoint_opts opts;
   ns_adjoint_stats st;
 };
@@ -463,6 +464,7 @@ int restore_state(ns_ctx* c, int slot) {
   for (int f = 0; f < 5; ++f)
     CK(cudaMemcpyAsync(dst[f], slot_field(c, slot, f), c->fbytes, cudaMemcpyDeviceToDevice, c->st), "snapshot restore");
   c->time = A.slot_time[slot];
+  c->step = A.step0 + A.slot_step[slot];
   c->in_step = false;
   c->cart_pending = false;
   return NS_OK;
@@ -661,6 +663,7 @@ int ns_step_adjoint_fwd(ns_ctx* c, const ns_adjoint_opts* opts, int nseg, const 
   A.have_fwd = false;
   A.nsteps = opts->nsteps;
   A.nsnap = opts->nsnap;
+  A.step0 = c->step;
   // snapshot slots: min(nsnap, nsteps) for the schedule plus one for the final state
   const int nsched = std::min(opts->nsnap, opts->nsteps);
   const int nslots = nsched + 1;

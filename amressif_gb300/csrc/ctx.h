@@ -25,6 +25,7 @@ struct ns_ctx {
   cudaStream_t st = nullptr;
   bool own_stream = false;
   double dt = 0, time = 0, rk[4] = {0, 0, 0, 0};
+  long long step = 0;  // completed ns_step calls since init / checkpoint put
   // FP64 fields
   double* U[2] = {nullptr, nullptr};
   double* UP[2] = {nullptr, nullptr};

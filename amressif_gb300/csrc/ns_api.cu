@@ -532,6 +532,7 @@ int ns_init_fields(ns_ctx* c, int init_case) {
   const double* uup[2] = {up.data(), vp.data()};
   int r = ns_set_state(c, uu, uup, p.data(), 0.0);
   if (r != NS_OK) return r;
+  c->step = 0;
   // the reference sets velCart analytically at init (not by cont2cart)
   const int l0[3] = {0, 0, 0}, h0[3] = {N - 1, N - 1, 0};
   r = ns_put_box(c, NS_FIELD_CART, 0, cu.data(), l0, h0, N, 0, 0);
@@ -1011,6 +1012,7 @@ int ns_step(ns_ctx* c, ns_step_stats* stats) {
   if (c->ev_ok) cudaEventRecord(c->ev[2], c->st);
   r = ns_project(c, &s.div_after);
   if (r != NS_OK) return r;
+  c->step++;
   if (c->ev_ok) {
     cudaEventRecord(c->ev[3], c->st);
     cudaEventSynchronize(c->ev[3]);
@@ -1024,6 +1026,27 @@ int ns_step(ns_ctx* c, ns_step_stats* stats) {
   if (mg_status != NS_OK) return mg_status;
   return s.status;
 }
+
+int ns_checkpoint_get(ns_ctx* c, double* const* u, double* const* u_prev, double* p, double* time, long long* step) {
+  if (!c || !u || !u_prev || !p) return NS_ERR_ARG;
+  if (c->in_step) return fail(c, NS_ERR_STATE, "checkpoint inside a step");
+  const int r = ns_get_state(c, u, u_prev, p, nullptr);
+  if (r != NS_OK) return r;
+  if (time) *time = c->time;
+  if (step) *step = c->step;
+  return NS_OK;
+}
+
+int ns_checkpoint_put(ns_ctx* c, const double* const* u, const double* const* u_prev, const double* p, double time,
+                      long long step) {
+  if (!c || step < 0) return NS_ERR_ARG;
+  const int r = ns_set_state(c, u, u_prev, p, time);
+  if (r != NS_OK) return r;
+  c->step = step;
+  return NS_OK;
+}
+
+long long ns_get_step(const ns_ctx* c) { return c ? c->step : -1; }
 
 int ns_step_host(ns_ctx* c, double* const* u, double* const* u_prev, double* p, ns_step_stats* stats) {
   if (!c || !u || !u_prev || !p) return NS_ERR_ARG;

@@ -125,6 +125,18 @@ int ns_get_box(ns_ctx* c, int field, int comp, double* data, const int lo[3], co
 int ns_set_state(ns_ctx* c, const double* const* u, const double* const* u_prev, const double* p, double time);
 int ns_get_state(ns_ctx* c, double* const* u, double* const* u_prev, double* p, double* phi);
 
+/* Checkpoint / restart state of SaveCheckpoint / LoadCheckpoint
+ * (utilities.cpp:792-1023): u^n, u^{n-1}, p, the time and the number of steps
+ * taken. phi is not part of it (the reference does not save it either; the
+ * advance recomputes it every step). After ns_checkpoint_put the next ns_step
+ * continues the saved run bit for bit: the cell velocity of the first stage
+ * is rebuilt from the faces, as a restart of the reference does
+ * (main.cpp:387-784). Host arrays as in ns_set_state. */
+int ns_checkpoint_get(ns_ctx* c, double* const* u, double* const* u_prev, double* p, double* time, long long* step);
+int ns_checkpoint_put(ns_ctx* c, const double* const* u, const double* const* u_prev, const double* p, double time,
+                      long long step);
+long long ns_get_step(const ns_ctx* c);
+
 /* ---- building blocks, one per reference call site ------------------------ */
 int ns_step_begin(ns_ctx* c);                              /* main.cpp:879-887 */
 int ns_rk_stage(ns_ctx* c, int sub);                       /* main.cpp:931-1017 (fused) */

@@ -1,0 +1,46 @@
+"""Checkpoint directory layout of SaveCheckpoint / LoadCheckpoint (no GPU)."""
+import os
+
+import numpy as np
+
+from amressif_gb300 import checkpoint as ck
+
+
+def state(n, seed=0):
+    r = np.random.default_rng(seed)
+    u = [r.standard_normal((n, n + 1)), r.standard_normal((n + 1, n))]
+    up = [r.standard_normal((n, n + 1)), r.standard_normal((n + 1, n))]
+    return u, up, r.standard_normal((n, n))
+
+
+def test_round_trip_uneven_boxes(tmp_path):
+    n = 10
+    u, up, p = state(n)
+    path = ck.write_checkpoint(str(tmp_path), 7, u, up, p, 0.123456789012345678, (4, 3))
+    assert os.path.basename(path) == "checkpoint00007"
+    u2, up2, p2, t = ck.read_checkpoint(path)
+    assert t == float("%.15g" % 0.123456789012345678)
+    np.testing.assert_array_equal(p2, p)
+    for a, b in zip(u + up, u2 + up2):
+        np.testing.assert_array_equal(a, b)
+
+
+def test_header_and_boxes(tmp_path):
+    n = 8
+    u, up, p = state(n, 1)
+    path = ck.write_checkpoint(str(tmp_path), 0, u, up, p, 2.5, (4, 8))
+    lines = open(os.path.join(path, "Header")).read().splitlines()
+    assert lines[:5] == ["Checkpoint file for AMRESSIF", "2.5", "(2 0", "((0,0) (3,7) (0,0))", "((4,0) (7,7) (0,0))"]
+    h = open(os.path.join(path, "Level_0", "vel_xCont_H")).read()
+    assert "((0,0) (4,7) (1,0))" in h and "((4,0) (8,7) (1,0))" in h  # face boxes share the face between boxes
+    with open(os.path.join(path, "Level_0", "vel_xCont_D_00000"), "rb") as f:
+        head = f.readline().decode()
+    assert head.startswith("FAB ((8, (64 11 52 0 1 12 0 1023)),(8, (8 7 6 5 4 3 2 1)))((0,0) (4,7) (1,0)) 1")
+
+
+def test_chop_covers_domain():
+    boxes = ck.chop(13, (5, 4))
+    cover = np.zeros((13, 13), int)
+    for (x0, y0), (x1, y1) in boxes:
+        cover[y0:y1 + 1, x0:x1 + 1] += 1
+    assert (cover == 1).all()
