@@ -96,6 +96,8 @@ class NsParams(ctypes.Structure):
         ("poisson_tol_div", ctypes.c_double),
         ("poisson_max_cycles", ctypes.c_int),
         ("dtau_clip", ctypes.c_int),
+        ("poisson_solver", ctypes.c_int),
+        ("gmres_restart", ctypes.c_int),
     ]
 
 

@@ -1,5 +1,7 @@
 """Checkpoint files in the directory layout of the reference's SaveCheckpoint /
-LoadCheckpoint (utilities.cpp:792-1023), host side.
+LoadCheckpoint (utilities.cpp:792-1023), and plotfiles in the layout of its
+Export_Flow_Field (utilities.cpp:534-570, AMReX WriteSingleLevelPlotfile), host
+side.
 
 Layout written (2D):
 
@@ -150,3 +152,83 @@ def read_checkpoint(path):
     up = [_read_multifab(os.path.join(lv, "vel_xContPrev"), (n, n + 1)),
           _read_multifab(os.path.join(lv, "vel_yContPrev"), (n + 1, n))]
     return u, up, p, time
+
+
+# ---- plotfiles (Export_Flow_Field) ----------------------------------------------------
+
+PLOT_VARS = ("pressure", "U", "V")
+
+
+def cell_velocity(u):
+    """velCart of cont2cart (utilities.cpp:49-53): face averages at the cells"""
+    return 0.5 * (u[0][:, :-1] + u[0][:, 1:]), 0.5 * (u[1][:-1, :] + u[1][1:, :])
+
+
+def write_plotfile(root, name, step, u, p, time, max_grid_size, prob_lo=(0.0, 0.0), prob_hi=(1.0, 1.0)):
+    """pltfile <name>NNNNN with the components pressure, U, V (cell-centred
+    velocity from the faces), as Export_Flow_Field writes them; returns the path."""
+    n = p.shape[0]
+    path = os.path.join(root, "%s%05d" % (name, step))
+    os.makedirs(os.path.join(path, "Level_0"), exist_ok=True)
+    cells = chop(n, max_grid_size)
+    dx = [(prob_hi[d] - prob_lo[d]) / n for d in range(2)]
+    cu, cv = cell_velocity(u)
+    comps = [p, cu, cv]
+    with open(os.path.join(path, "Header"), "w") as h:
+        h.write("HyperCLaw-V1.1\n%d\n" % len(PLOT_VARS))
+        h.write("".join(v + "\n" for v in PLOT_VARS))
+        h.write("2\n%.17g\n0\n" % time)
+        h.write("%.17g %.17g\n%.17g %.17g\n\n" % (prob_lo[0], prob_lo[1], prob_hi[0], prob_hi[1]))
+        h.write(_box_str((0, 0), (n - 1, n - 1), (0, 0)) + "\n")
+        h.write("%d\n%.17g %.17g\n0\n0\n" % (step, dx[0], dx[1]))
+        h.write("0 %d %.17g\n%d\n" % (len(cells), time, step))
+        for lo, hi in cells:
+            for d in range(2):
+                h.write("%.17g %.17g\n" % (prob_lo[d] + lo[d] * dx[d], prob_lo[d] + (hi[d] + 1) * dx[d]))
+        h.write("Level_0/Cell\n")
+    prefix = os.path.join(path, "Level_0", "Cell")
+    offsets, mins, maxs = [], [], []
+    with open(prefix + "_D_00000", "wb") as f:
+        for lo, hi in cells:
+            offsets.append(f.tell())
+            f.write(("FAB %s%s %d\n" % (REAL_DESCRIPTOR, _box_str(lo, hi, (0, 0)), len(comps))).encode())
+            for c in comps:  # component-major, Fortran order within a component
+                sub = np.ascontiguousarray(c[lo[1]:hi[1] + 1, lo[0]:hi[0] + 1], dtype="<f8")
+                f.write(sub.tobytes())
+            mins.append([float(c[lo[1]:hi[1] + 1, lo[0]:hi[0] + 1].min()) for c in comps])
+            maxs.append([float(c[lo[1]:hi[1] + 1, lo[0]:hi[0] + 1].max()) for c in comps])
+    with open(prefix + "_H", "w") as h:
+        h.write("1\n0\n%d\n0\n" % len(comps))
+        h.write(_boxarray_str(cells, (0, 0)) + "\n")
+        h.write("%d\n" % len(cells))
+        for off in offsets:
+            h.write("FabOnDisk: Cell_D_00000 %d\n" % off)
+        for table in (mins, maxs):
+            h.write("\n%d,%d\n" % (len(cells), len(comps)))
+            h.write("".join("".join("%.17g," % v for v in row) + "\n" for row in table))
+    return path
+
+
+def read_plotfile(path):
+    """{variable: (n, n) array}, time and step of a plotfile written above"""
+    with open(os.path.join(path, "Header")) as h:
+        lines = h.read().splitlines()
+    nv = int(lines[1])
+    names = lines[2:2 + nv]
+    time = float(lines[3 + nv])
+    with open(os.path.join(path, "Level_0", "Cell_H")) as h:
+        text = h.read()
+    boxes = [((int(m[0]), int(m[1])), (int(m[2]), int(m[3]))) for m in _BOX_RE.findall(text)]
+    fods = re.findall(r"FabOnDisk: (\S+) (\d+)", text)
+    n = max(hi[0] for _, hi in boxes) + 1
+    out = {v: np.full((n, n), np.nan) for v in names}
+    for (lo, hi), (fname, off) in zip(boxes, fods):
+        with open(os.path.join(path, "Level_0", fname), "rb") as f:
+            f.seek(int(off))
+            f.readline()
+            nx, ny = hi[0] - lo[0] + 1, hi[1] - lo[1] + 1
+            vals = np.frombuffer(f.read(8 * nx * ny * nv), dtype="<f8").reshape(nv, ny, nx)
+            for k, v in enumerate(names):
+                out[v][lo[1]:hi[1] + 1, lo[0]:hi[0] + 1] = vals[k]
+    step = int(lines[nv + 9])  # after the domain box of level 0
+    return out, time, step

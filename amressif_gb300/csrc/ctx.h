@@ -84,6 +84,14 @@ struct ns_ctx {
   // (in red[kRedF], written by the kernel that formed f) instead of r0
   const double* phi_guess = nullptr;
   bool tol_from_f = false;
+  // GMRES option of the Poisson solve: Krylov basis and scratch (lazily allocated)
+  std::vector<double*> gm_v;
+  double* gm_w = nullptr;
+  double* gm_z = nullptr;
+  double* gm_b = nullptr;
+  double* gm_part = nullptr;
+  double* gm_dev = nullptr;   // device scalars: dot products, coefficients
+  double* gm_host = nullptr;  // pinned mirror
   // lid profile (one value per cell column) when controls are set
   double* lid_col = nullptr;
   int nseg = 0;

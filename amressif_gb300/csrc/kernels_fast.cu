@@ -1,5 +1,6 @@
 // Fast-arithmetic instantiations (FMA contraction allowed): the FP64 fast
 // stage, the mixed-precision anchor, the multigrid and the defect correction.
+#include "gmres2d.cuh"
 #include "launch.h"
 
 namespace ns {
@@ -78,6 +79,34 @@ cudaError_t launch_mg_resnorm(const MGLevels<T>& M, double* part, unsigned* coun
   const int n = M.n[0];
   dim3 grid((n + 31) / 32, (n + 7) / 8, 1);
   k_mg_resnorm<T><<<grid, 256, 0, s>>>(M, part, counter, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gm_lap(int n, long P, int px, int py, double ihx, double ihy, const double* x, double* y, cudaStream_t s) {
+  const dim3 grid((n + 31) / 32, (n + 7) / 8, 1);
+  k_gm_lap<<<grid, 256, 0, s>>>(n, P, px, py, ihx, ihy, x, y);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gm_axpby(int n, long P, double a, const double* x, double b, const double* y, const double* sc, double c,
+                            double* out, cudaStream_t s) {
+  const dim3 grid((n + 31) / 32, (n + 7) / 8, 1);
+  k_gm_axpby<<<grid, 256, 0, s>>>(n, P, a, x, b, y, sc, c, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gm_mdot(int n, long P, int nv, const GmVecs& V, const double* w, double* part, unsigned* counter,
+                           double* out, cudaStream_t s) {
+  if (nv < 1 || nv > kGmMaxV) return cudaErrorInvalidValue;
+  k_gm_mdot<256><<<kGmBlocks, 256, 0, s>>>(n, P, nv, V, w, part, counter, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gm_maxpy(int n, long P, int nv, const GmVecs& V, const double* coef, double s_, double* w,
+                            cudaStream_t s) {
+  if (nv < 1 || nv > kGmMaxV) return cudaErrorInvalidValue;
+  const dim3 grid((n + 31) / 32, (n + 7) / 8, 1);
+  k_gm_maxpy<<<grid, 256, 0, s>>>(n, P, nv, V, coef, s_, w);
   return cudaGetLastError();
 }
 

@@ -71,6 +71,16 @@ cudaError_t launch_adj_objective_grad(const Geom& g, const double* u0, const dou
 cudaError_t launch_lid_expand(int N, int nseg, const double* seg, double* col, cudaStream_t s);
 cudaError_t launch_lid_accum(int N, int nseg, const double* col, double coef, double* seg_acc, cudaStream_t s);
 
+// kernels_fast.cu: GMRES option of the Poisson solve
+struct GmVecs;
+cudaError_t launch_gm_lap(int n, long P, int px, int py, double ihx, double ihy, const double* x, double* y, cudaStream_t s);
+cudaError_t launch_gm_axpby(int n, long P, double a, const double* x, double b, const double* y, const double* sc, double c,
+                            double* out, cudaStream_t s);
+cudaError_t launch_gm_mdot(int n, long P, int nv, const GmVecs& V, const double* w, double* part, unsigned* counter,
+                           double* out, cudaStream_t s);
+cudaError_t launch_gm_maxpy(int n, long P, int nv, const GmVecs& V, const double* coef, double s_, double* w,
+                            cudaStream_t s);
+
 struct DCArgs {
   int n;
   long pitch;

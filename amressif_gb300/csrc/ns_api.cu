@@ -21,6 +21,8 @@
 #include "anchor_ff2d.cuh"
 #include "ctx.h"
 #include "dc_ff2d.cuh"
+#define NS_GMRES_ARGS_ONLY  // structs and constants only: the kernels are compiled in kernels_fast.cu
+#include "gmres2d.cuh"
 #include "launch.h"
 #include "stage_inc2d.cuh"
 
@@ -119,6 +121,9 @@ void free_all(ns_ctx* c) {
   F(c->FFh); F(c->FFl);
   F(c->Pp); F(c->F);
   F(c->lid_col);
+  for (double* v : c->gm_v) F(v);
+  F(c->gm_w); F(c->gm_z); F(c->gm_b); F(c->gm_part); F(c->gm_dev);
+  if (c->gm_host) cudaFreeHost(c->gm_host);
   free_adjoint(c);
   for (int l = 1; l < c->M64.L; ++l) { F(c->M64.x[l]); F(c->M64.f[l]); }
   for (int l = 0; l < c->M32.L; ++l) { F(c->M32.x[l]); F(c->M32.f[l]); }
@@ -221,6 +226,8 @@ void ns_params_default(ns_params* p) {
   p->poisson_tol_div = 0.0;
   p->poisson_max_cycles = 200;
   p->dtau_clip = 0;
+  p->poisson_solver = 0;
+  p->gmres_restart = 30;
 }
 
 int ns_params_parse_file(ns_params* p, const char* path) {
@@ -674,6 +681,164 @@ static int vcycle(ns_ctx* c, MGLevels<T>& M, int x0_zero) {
 // mean of f (singular problem, AMReX makes the RHS solvable) written to red[kRedMean]
 __global__ void k_set_mean(double* red, double inv_n) { red[kRedMean] = red[kRedSum] * inv_n; }
 
+// ---- GMRES option (GMRES_Poisson.cpp:56-131) -----------------------------------
+// Restarted GMRES on L phi = f - mean(f) with one FP64 V-cycle as the right
+// preconditioner (a fixed linear map: the correction is M^-1 (V y), one more
+// V-cycle per restart, so only the basis V is stored). Classical Gram-Schmidt
+// with one re-orthogonalisation pass, Givens rotations on the host. The
+// iteration stops on the same max-norm residual test as the V-cycle solver.
+static int gmres_alloc(ns_ctx* c, int m) {
+  if ((int)c->gm_v.size() >= m + 1) return NS_OK;
+  for (int k = (int)c->gm_v.size(); k < m + 1; ++k) {
+    double* v = nullptr;
+    if (alloc_field(c, &v) != NS_OK) return NS_ERR_NOMEM;
+    c->gm_v.push_back(v);
+  }
+  if (!c->gm_w) {
+    if (alloc_field(c, &c->gm_w) != NS_OK || alloc_field(c, &c->gm_z) != NS_OK || alloc_field(c, &c->gm_b) != NS_OK)
+      return NS_ERR_NOMEM;
+    if (cudaMalloc(&c->gm_part, (size_t)kGmMaxV * kGmBlocks * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&c->gm_dev, 2 * kGmMaxV * sizeof(double)) != cudaSuccess ||
+        cudaMallocHost(&c->gm_host, 2 * kGmMaxV * sizeof(double)) != cudaSuccess)
+      return fail(c, NS_ERR_NOMEM, "cudaMalloc (GMRES) failed");
+  }
+  return NS_OK;
+}
+
+static int gmres_precond(ns_ctx* c, const double* in, double* out) {
+  double* x0 = c->M64.x[0];
+  double* f0 = c->M64.f[0];
+  const double* fm = c->M64.fmean;
+  c->M64.x[0] = out;
+  c->M64.f[0] = const_cast<double*>(in);
+  c->M64.fmean = nullptr;
+  const int r = vcycle<double>(c, c->M64, 1);
+  c->M64.x[0] = x0;
+  c->M64.f[0] = f0;
+  c->M64.fmean = fm;
+  return r;
+}
+
+// out[k] = (w, V[k]) for k < nv, read back to c->gm_host
+static int gmres_dots(ns_ctx* c, const std::vector<double*>& V, int nv, const double* w) {
+  GmVecs vv;
+  std::memset(&vv, 0, sizeof(vv));
+  for (int k = 0; k < nv; ++k) vv.v[k] = V[k];
+  LAUNCH(NS_PROF_OTHER, "gmres dots", launch_gm_mdot(c->N, c->pitch, nv, vv, w, c->gm_part, c->counter, c->gm_dev, c->st));
+  CK(cudaMemcpyAsync(c->gm_host, c->gm_dev, nv * sizeof(double), cudaMemcpyDeviceToHost, c->st), "readback");
+  CK(cudaStreamSynchronize(c->st), "stream sync");
+  if (c->prof) prof_resolve(c);
+  return NS_OK;
+}
+
+// w += s * sum_k coef[k] V[k] (coef from the host)
+static int gmres_update(ns_ctx* c, const std::vector<double*>& V, int nv, const double* coef, double s, double* w) {
+  GmVecs vv;
+  std::memset(&vv, 0, sizeof(vv));
+  for (int k = 0; k < nv; ++k) vv.v[k] = V[k];
+  CK(cudaMemcpyAsync(c->gm_dev + kGmMaxV, coef, nv * sizeof(double), cudaMemcpyHostToDevice, c->st), "coefficients");
+  LAUNCH(NS_PROF_OTHER, "gmres update", launch_gm_maxpy(c->N, c->pitch, nv, vv, c->gm_dev + kGmMaxV, s, w, c->st));
+  // the next host write of the coefficients must wait for this kernel
+  CK(cudaStreamSynchronize(c->st), "stream sync");
+  return NS_OK;
+}
+
+static int poisson_gmres(ns_ctx* c, double tol_rel, double div_tol_res, int maxc, int* cycles, double* rnorm0_out,
+                         double* rn_out) {
+  const int m = std::max(2, std::min(c->P.gmres_restart, kGmMaxV - 1));
+  int r = gmres_alloc(c, m);
+  if (r != NS_OK) return r;
+  const int N = c->N;
+  const long P = c->pitch;
+  const int px = c->g.periodic[0], py = c->g.periodic[1];
+  const double ihx = c->M64.invh2[0][0], ihy = c->M64.invh2[0][1];
+  std::vector<double*>& V = c->gm_v;
+  double* x = c->PHI[0];
+  c->phi_cur = 0;
+  c->M64.x[0] = c->PHI[0];
+  // b = f - mean(f); x = 0 (poisson.cpp:63)
+  LAUNCH(NS_PROF_OTHER, "gmres rhs", launch_gm_axpby(N, P, 1.0, c->F, 0.0, nullptr, c->red + kRedMean, -1.0, c->gm_b, c->st));
+  CK(cudaMemsetAsync(x, 0, c->fbytes, c->st), "memset phi");
+  LAUNCH(NS_PROF_MG_RESNORM, "resnorm", launch_mg_resnorm<double>(c->M64, c->part, c->counter, c->red + kRedRes, c->st));
+  r = sync_red(c, kRedRes, 1);
+  if (r != NS_OK) return r;
+  const double rnorm0 = c->red_h[kRedRes];
+  double rn = rnorm0;
+  *rnorm0_out = rnorm0;
+  const double tol = tol_rel * rnorm0;
+  auto done = [&](double v) { return v <= tol && (div_tol_res <= 0 || v <= div_tol_res); };
+  int its = 0;
+  std::vector<double> H((size_t)(m + 1) * m), cs(m), sn(m), g(m + 1), y(m);
+  auto h = [&](int i, int j) -> double& { return H[(size_t)i * m + j]; };
+  while (!done(rn) && rnorm0 > 0 && its < maxc) {
+    // r0 = b - L x into V[0]; beta = |r0|
+    LAUNCH(NS_PROF_OTHER, "gmres apply", launch_gm_lap(N, P, px, py, ihx, ihy, x, c->gm_w, c->st));
+    LAUNCH(NS_PROF_OTHER, "gmres r0", launch_gm_axpby(N, P, 1.0, c->gm_b, -1.0, c->gm_w, nullptr, 0.0, V[0], c->st));
+    r = gmres_dots(c, V, 1, V[0]);
+    if (r != NS_OK) return r;
+    const double beta = std::sqrt(c->gm_host[0]);
+    if (!(beta > 0)) break;
+    LAUNCH(NS_PROF_OTHER, "gmres scale", launch_gm_axpby(N, P, 1.0 / beta, V[0], 0.0, nullptr, nullptr, 0.0, V[0], c->st));
+    std::fill(g.begin(), g.end(), 0.0);
+    g[0] = beta;
+    int k = 0;
+    for (int j = 0; j < m && its < maxc; ++j) {
+      ++its;
+      r = gmres_precond(c, V[j], c->gm_z);
+      if (r == NS_OK) LAUNCH(NS_PROF_OTHER, "gmres apply", launch_gm_lap(N, P, px, py, ihx, ihy, c->gm_z, c->gm_w, c->st));
+      if (r != NS_OK) return r;
+      for (int i = 0; i <= j; ++i) h(i, j) = 0.0;
+      for (int pass = 0; pass < 2; ++pass) {  // classical Gram-Schmidt, twice
+        r = gmres_dots(c, V, j + 1, c->gm_w);
+        if (r == NS_OK) r = gmres_update(c, V, j + 1, c->gm_host, -1.0, c->gm_w);
+        if (r != NS_OK) return r;
+        for (int i = 0; i <= j; ++i) h(i, j) += c->gm_host[i];
+      }
+      std::vector<double*> wv(1, c->gm_w);
+      r = gmres_dots(c, wv, 1, c->gm_w);
+      if (r != NS_OK) return r;
+      const double hn = std::sqrt(c->gm_host[0]);
+      // Givens rotations of column j
+      for (int i = 0; i < j; ++i) {
+        const double t = cs[i] * h(i, j) + sn[i] * h(i + 1, j);
+        h(i + 1, j) = -sn[i] * h(i, j) + cs[i] * h(i + 1, j);
+        h(i, j) = t;
+      }
+      const double den = std::hypot(h(j, j), hn);
+      cs[j] = den > 0 ? h(j, j) / den : 1.0;
+      sn[j] = den > 0 ? hn / den : 0.0;
+      h(j, j) = den;
+      g[j + 1] = -sn[j] * g[j];
+      g[j] = cs[j] * g[j];
+      k = j + 1;
+      if (hn > 0 && j + 1 < m)
+        LAUNCH(NS_PROF_OTHER, "gmres scale",
+               launch_gm_axpby(N, P, 1.0 / hn, c->gm_w, 0.0, nullptr, nullptr, 0.0, V[j + 1], c->st));
+      // the 2-norm estimate |g[j+1]| against the max-norm target (|r|_inf <= |r|_2)
+      if (std::fabs(g[j + 1]) <= 0.5 * tol || hn == 0) break;
+    }
+    // y = H^-1 g; x += M^-1 (V y)
+    for (int i = k - 1; i >= 0; --i) {
+      double t = g[i];
+      for (int l = i + 1; l < k; ++l) t -= h(i, l) * y[l];
+      y[i] = h(i, i) != 0 ? t / h(i, i) : 0.0;
+    }
+    CK(cudaMemsetAsync(c->gm_w, 0, c->fbytes, c->st), "memset");
+    r = gmres_update(c, V, k, y.data(), 1.0, c->gm_w);
+    if (r == NS_OK) r = gmres_precond(c, c->gm_w, c->gm_z);
+    if (r == NS_OK) LAUNCH(NS_PROF_OTHER, "gmres x", launch_gm_axpby(N, P, 1.0, x, 1.0, c->gm_z, nullptr, 0.0, x, c->st));
+    if (r != NS_OK) return r;
+    // the true max-norm residual of the multigrid test
+    LAUNCH(NS_PROF_MG_RESNORM, "resnorm", launch_mg_resnorm<double>(c->M64, c->part, c->counter, c->red + kRedRes, c->st));
+    r = sync_red(c, kRedRes, 1);
+    if (r != NS_OK) return r;
+    rn = c->red_h[kRedRes];
+  }
+  *cycles = its;
+  *rn_out = rn;
+  return done(rn) || rnorm0 == 0 ? NS_OK : NS_ERR_MG_STALL;
+}
+
 extern "C" {
 
 static int alloc_mixed(ns_ctx* c);
@@ -688,7 +853,10 @@ int ns_poisson_solve(ns_ctx* c, int precision, int* cycles, double* res) {
   double rnorm0 = 0.0, rn = 0.0;
   int ncyc = 0;
   int status = NS_OK;
-  if (precision == NS_PREC_MIXED) {
+  if (c->P.poisson_solver == 1) {
+    status = poisson_gmres(c, c->P.poisson_tol_rel, div_tol_res, maxc, &ncyc, &rnorm0, &rn);
+    if (status != NS_OK && status != NS_ERR_MG_STALL) return status;
+  } else if (precision == NS_PREC_MIXED) {
     // FP32 V-cycles inside an FP64 defect correction
     DCArgs d;
     std::memset(&d, 0, sizeof(d));

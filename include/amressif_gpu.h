@@ -74,6 +74,9 @@ typedef struct ns_params {
   double poisson_tol_div;    /* additionally require max|div u| <= this after projection (0 = off) */
   int poisson_max_cycles;    /* V-cycle / defect-correction cap (MLMG maxiter 2000) */
   int dtau_clip;             /* 0: dtau = 0.4 dt (main.cpp:861); 1: also clip to 0.9 x RK4 stability limit */
+  int poisson_solver;        /* 0: multigrid V-cycles; 1: restarted GMRES with one FP64 V-cycle as right
+                                preconditioner (the GMRES option of GMRES_Poisson.cpp:56-131) */
+  int gmres_restart;         /* Krylov vectors per GMRES cycle (<= 31) */
 } ns_params;
 
 typedef struct ns_step_stats {

@@ -44,3 +44,19 @@ def test_chop_covers_domain():
     for (x0, y0), (x1, y1) in boxes:
         cover[y0:y1 + 1, x0:x1 + 1] += 1
     assert (cover == 1).all()
+
+
+def test_plotfile_round_trip(tmp_path):
+    n = 12
+    u, up, p = state(n, 2)
+    path = ck.write_plotfile(str(tmp_path), "plt", 42, u, p, 0.75, (8, 5))
+    assert os.path.basename(path) == "plt00042"
+    fields, t, step = ck.read_plotfile(path)
+    assert t == 0.75 and step == 42
+    cu, cv = ck.cell_velocity(u)
+    np.testing.assert_array_equal(fields["pressure"], p)
+    np.testing.assert_array_equal(fields["U"], cu)
+    np.testing.assert_array_equal(fields["V"], cv)
+    head = open(os.path.join(path, "Header")).read().splitlines()
+    assert head[:6] == ["HyperCLaw-V1.1", "3", "pressure", "U", "V", "2"]
+    assert head[-1] == "Level_0/Cell"

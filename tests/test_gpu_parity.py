@@ -275,3 +275,41 @@ def test_east_slip_code_m135_unsupported_in_parity_mode(gpu_lib):
     p = ns.default_params(n_cell=32, bc_lo=(135, 135, 135), bc_hi=(-135, 165, 135), fix_quirks=0)
     with pytest.raises(ns.NsError):
         ns.Solver(p)
+
+
+@pytest.mark.parametrize("name", ["cavity32", "cavity128_cfg1", "tgv64_parity", "tgv64_fixed"])
+def test_gmres_option_resynced(gpu_lib, oracle_lib, name):
+    """The GMRES option of the Poisson solve (GMRES_Poisson.cpp:56-131, here
+    with one V-cycle as the right preconditioner) reaches the same discrete
+    solution: per-step parity with the oracle, like the V-cycle solver."""
+    o, s = make_pair(name, poisson_solver=1, gmres_restart=20)
+    for step in range(3):
+        sync_state(o, s)
+        so = o.step()
+        sg = s.step()
+        assert sg["pseudo_iters"] == so["pseudo_iters"]
+        assert sg["poisson_res"] <= 1e-12 and sg["poisson_cycles"] >= 1
+        u, _, p, _ = s.get_state()
+        uo, _, po, _ = o.get_state()
+        for d in range(2):
+            assert rel(u[d], uo[d]) <= TOL_STEP, (step, d, rel(u[d], uo[d]))
+        assert relp(p, po) <= TOL_STEP
+
+
+def test_gmres_matches_vcycles(gpu_lib):
+    sols = {}
+    for solver in (0, 1):
+        p = ns.default_params(n_cell=128, ren=100.0, fixed_dt=0.5 / 128, precision=ns.PREC_FP64, poisson_tol_rel=1e-13,
+                              poisson_solver=solver, gmres_restart=8)
+        s = ns.Solver(p)
+        s.init(ns.INIT_CAVITY)
+        for _ in range(2):
+            st = s.step()
+        sols[solver] = (s.get_state(), st)
+    (ua, _, pa, _), sta = sols[0]
+    (ub, _, pb, _), stb = sols[1]
+    for d in range(2):
+        assert rel(ub[d], ua[d]) <= 1e-11
+    assert relp(pb, pa) <= 1e-11
+    # restarts of 8 vectors: more Krylov iterations than 8 are possible, and fine
+    assert stb["poisson_cycles"] <= 4 * max(sta["poisson_cycles"], 1)
