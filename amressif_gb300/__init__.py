@@ -289,7 +289,13 @@ class Solver:
         return lib().ns_get_time(self.h)
 
     def face_shape(self, d):
-        return (self.n + (1 if d == 1 else 0), self.n + (1 if d == 0 else 0))
+        n = self.n
+        if self.dim == 3:
+            return (n + (d == 2), n + (d == 1), n + (d == 0))
+        return (n + (1 if d == 1 else 0), n + (1 if d == 0 else 0))
+
+    def cell_shape(self):
+        return (self.n,) * self.dim
 
     def init(self, case):
         self._check(lib().ns_init_fields(self.h, case), "ns_init_fields")
@@ -298,17 +304,17 @@ class Solver:
         u = [np.ascontiguousarray(a, dtype=np.float64) for a in u]
         up = [np.ascontiguousarray(a, dtype=np.float64) for a in u_prev]
         p = np.ascontiguousarray(p, dtype=np.float64)
-        au = (ctypes.POINTER(ctypes.c_double) * 2)(*[_dp(a) for a in u])
-        aup = (ctypes.POINTER(ctypes.c_double) * 2)(*[_dp(a) for a in up])
+        au = (ctypes.POINTER(ctypes.c_double) * self.dim)(*[_dp(a) for a in u])
+        aup = (ctypes.POINTER(ctypes.c_double) * self.dim)(*[_dp(a) for a in up])
         self._check(lib().ns_set_state(self.h, au, aup, _dp(p), time), "ns_set_state")
 
     def get_state(self):
-        u = [np.zeros(self.face_shape(d)) for d in range(2)]
-        up = [np.zeros(self.face_shape(d)) for d in range(2)]
-        p = np.zeros((self.n, self.n))
-        phi = np.zeros((self.n, self.n))
-        au = (ctypes.POINTER(ctypes.c_double) * 2)(*[_dp(a) for a in u])
-        aup = (ctypes.POINTER(ctypes.c_double) * 2)(*[_dp(a) for a in up])
+        u = [np.zeros(self.face_shape(d)) for d in range(self.dim)]
+        up = [np.zeros(self.face_shape(d)) for d in range(self.dim)]
+        p = np.zeros(self.cell_shape())
+        phi = np.zeros(self.cell_shape())
+        au = (ctypes.POINTER(ctypes.c_double) * self.dim)(*[_dp(a) for a in u])
+        aup = (ctypes.POINTER(ctypes.c_double) * self.dim)(*[_dp(a) for a in up])
         self._check(lib().ns_get_state(self.h, au, aup, _dp(p), _dp(phi)), "ns_get_state")
         return u, up, p, phi
 

@@ -26,6 +26,8 @@ UNITS = {
     "kernels_adjoint.cu": [],
     "ns_api.cu": [],
     "adjoint_api.cu": [],
+    "kernels3d.cu": [],
+    "ns3d_api.cu": [],
     "noalloc.cu": ["-fmad=false"],
 }
 

@@ -14,6 +14,7 @@
 
 namespace nsh {
 struct AdjState;  // adjoint workspace (adjoint_api.cu)
+struct State3D;   // fields of a dim = 3 context (ns3d_api.cu)
 }
 
 struct ns_ctx {
@@ -96,6 +97,7 @@ struct ns_ctx {
   double* lid_col = nullptr;
   int nseg = 0;
   nsh::AdjState* adj = nullptr;
+  nsh::State3D* s3 = nullptr;
   std::string err;
 };
 
@@ -113,6 +115,12 @@ cudaEvent_t pool_get(ns_ctx* c);
 // converged u* is face_ptr(c, c->cur, .)
 int run_predictor(ns_ctx* c, ns_step_stats* s);
 void free_adjoint(ns_ctx* c);
+// dim = 3 (ns3d_api.cu)
+int create3d(ns_ctx* c);
+void free3d(ns_ctx* c);
+int set_state3d(ns_ctx* c, const double* const* u, const double* const* up, const double* p, double time);
+int get_state3d(ns_ctx* c, double* const* u, double* const* up, double* p, double* phi);
+int step3d(ns_ctx* c, ns_step_stats* s);
 
 inline double* face_ptr(ns_ctx* c, int id, int m) { return id < 0 ? c->UP[m] : c->B[id][m]; }
 

@@ -1,0 +1,96 @@
+// Launchers of the 3D kernels (ns3d.cuh).
+#include "ns3d.cuh"  // kernels (before launch3d.h, which includes the argument structs only)
+#include "launch3d.h"
+
+namespace ns {
+
+static inline dim3 grid3(int nx, int ny, int nz) { return dim3((nx + 31) / 32, (ny + 7) / 8, nz); }
+
+cudaError_t launch3_cart(const Arg3& a, cudaStream_t s) {
+  const int N = a.g.N;
+  k3_cart<<<grid3(N + 4, N + 4, N + 4), 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+cudaError_t launch3_total(const Arg3& a, cudaStream_t s) {
+  const int N = a.g.N;
+  k3_total<<<grid3(N, N, N), 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+cudaError_t launch3_face(const Arg3& a, cudaStream_t s) {
+  const int N = a.g.N;
+  k3_face<<<grid3(N + 1, N + 1, N + 1), 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+cudaError_t launch3_step_begin(const Arg3& a, cudaStream_t s) {
+  const int N = a.g.N;
+  k3_step_begin<<<grid3(N + 1, N + 1, N + 1), 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+cudaError_t launch3_rhs(const Arg3& a, cudaStream_t s) {
+  const int N = a.g.N;
+  k3_rhs<<<grid3(N, N, N), 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+cudaError_t launch3_project(const Arg3& a, cudaStream_t s) {
+  const int N = a.g.N;
+  k3_project<<<grid3(N + 1, N + 1, N + 1), 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+cudaError_t launch3_div(const Arg3& a, cudaStream_t s) {
+  const int N = a.g.N;
+  k3_div<<<grid3(N, N, N), 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+long blocks3_face(int N) { return (long)((N + 1 + 31) / 32) * ((N + 1 + 7) / 8) * (N + 1); }
+
+template <typename T>
+cudaError_t launch3_mg_rb(const MG3<T>& M, int l, int color, cudaStream_t s) {
+  const int n = M.n[l];
+  k3_mg_rb<T><<<grid3(n, n, n), 256, 0, s>>>(M, l, color);
+  return cudaGetLastError();
+}
+template <typename T>
+cudaError_t launch3_mg_restrict(const MG3<T>& M, int l, cudaStream_t s) {
+  const int n = M.n[l + 1];
+  k3_mg_restrict<T><<<grid3(n, n, n), 256, 0, s>>>(M, l);
+  return cudaGetLastError();
+}
+template <typename T>
+cudaError_t launch3_mg_prolong(const MG3<T>& M, int l, cudaStream_t s) {
+  const int n = M.n[l];
+  k3_mg_prolong<T><<<grid3(n, n, n), 256, 0, s>>>(M, l);
+  return cudaGetLastError();
+}
+template <typename T>
+cudaError_t launch3_mg_bottom(const MG3<T>& M, int l, int sweeps, cudaStream_t s) {
+  k3_mg_bottom<T><<<1, 1024, 0, s>>>(M, l, sweeps);
+  return cudaGetLastError();
+}
+template <typename T>
+cudaError_t launch3_mg_resnorm(const MG3<T>& M, double* part, unsigned* counter, double* out, cudaStream_t s) {
+  const int n = M.n[0];
+  k3_mg_resnorm<T><<<grid3(n, n, n), 256, 0, s>>>(M, part, counter, out);
+  return cudaGetLastError();
+}
+cudaError_t launch3_dc_add(const MG3<double>& M, const float* e, cudaStream_t s) {
+  const int n = M.n[0];
+  k3_dc_add<<<grid3(n, n, n), 256, 0, s>>>(M, e);
+  return cudaGetLastError();
+}
+cudaError_t launch3_dc_res(const MG3<double>& M, float* r32, double* part, unsigned* counter, double* out, cudaStream_t s) {
+  const int n = M.n[0];
+  k3_dc_res<<<grid3(n, n, n), 256, 0, s>>>(M, r32, part, counter, out);
+  return cudaGetLastError();
+}
+
+#define NS3_INST(T)                                                                               \
+  template cudaError_t launch3_mg_rb<T>(const MG3<T>&, int, int, cudaStream_t);                   \
+  template cudaError_t launch3_mg_restrict<T>(const MG3<T>&, int, cudaStream_t);                  \
+  template cudaError_t launch3_mg_prolong<T>(const MG3<T>&, int, cudaStream_t);                   \
+  template cudaError_t launch3_mg_bottom<T>(const MG3<T>&, int, int, cudaStream_t);               \
+  template cudaError_t launch3_mg_resnorm<T>(const MG3<T>&, double*, unsigned*, double*, cudaStream_t);
+NS3_INST(double)
+NS3_INST(float)
+#undef NS3_INST
+
+}  // namespace ns

@@ -1,0 +1,33 @@
+// Host-side launchers of the 3D kernels (kernels3d.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#define NS_3D_ARGS_ONLY
+#include "ns3d.cuh"
+#undef NS_3D_ARGS_ONLY
+
+namespace ns {
+
+cudaError_t launch3_cart(const Arg3& a, cudaStream_t s);
+cudaError_t launch3_total(const Arg3& a, cudaStream_t s);
+cudaError_t launch3_face(const Arg3& a, cudaStream_t s);
+cudaError_t launch3_step_begin(const Arg3& a, cudaStream_t s);
+cudaError_t launch3_rhs(const Arg3& a, cudaStream_t s);
+cudaError_t launch3_project(const Arg3& a, cudaStream_t s);
+cudaError_t launch3_div(const Arg3& a, cudaStream_t s);
+long blocks3_face(int N);  // blocks of the largest reducing launch
+
+template <typename T>
+cudaError_t launch3_mg_rb(const MG3<T>& M, int l, int color, cudaStream_t s);
+template <typename T>
+cudaError_t launch3_mg_restrict(const MG3<T>& M, int l, cudaStream_t s);
+template <typename T>
+cudaError_t launch3_mg_prolong(const MG3<T>& M, int l, cudaStream_t s);
+template <typename T>
+cudaError_t launch3_mg_bottom(const MG3<T>& M, int l, int sweeps, cudaStream_t s);
+template <typename T>
+cudaError_t launch3_mg_resnorm(const MG3<T>& M, double* part, unsigned* counter, double* out, cudaStream_t s);
+cudaError_t launch3_dc_add(const MG3<double>& M, const float* e, cudaStream_t s);
+cudaError_t launch3_dc_res(const MG3<double>& M, float* r32, double* part, unsigned* counter, double* out, cudaStream_t s);
+
+}  // namespace ns

@@ -1,0 +1,355 @@
+// Host driver of the 3D advance (dim = 3): the time loop of main_main
+// (main.cpp:875-1180) over the kernels of ns3d.cuh. The 3D context supports
+// the whole-step API (ns_step, ns_set_state / ns_get_state, checkpoints);
+// the per-call-site building blocks and the adjoint are 2D only.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "ctx.h"
+#include "launch3d.h"
+
+using namespace ns;
+using namespace nsh;
+
+namespace nsh {
+
+struct State3D {
+  std::vector<void*> allocs;
+  size_t fb = 0;  // bytes of one level-0 field
+  double* U[3] = {nullptr, nullptr, nullptr};
+  double* UP[3] = {nullptr, nullptr, nullptr};
+  double* DU[3] = {nullptr, nullptr, nullptr};
+  double* S[3] = {nullptr, nullptr, nullptr};
+  double* B[3][3] = {};
+  double* Pp = nullptr;
+  double* PHI = nullptr;
+  double* F = nullptr;
+  double* PH[3] = {nullptr, nullptr, nullptr};  // ghosted cell velocity
+  double* T[3] = {nullptr, nullptr, nullptr};   // cell totals
+  double* part = nullptr;
+  MG3<double> M64;
+  MG3<float> M32;
+  int base = -1, cur = -1;
+};
+
+void free3d(ns_ctx* c) {
+  if (!c->s3) return;
+  for (void* p : c->s3->allocs) cudaFree(p);
+  delete c->s3;
+  c->s3 = nullptr;
+}
+
+}  // namespace nsh
+
+namespace {
+
+long rup(long x, long a) { return (x + a - 1) / a * a; }
+
+template <typename P>
+int alloc3(ns_ctx* c, P** p, size_t bytes) {
+  if (cudaMalloc(p, bytes) != cudaSuccess) return fail(c, NS_ERR_NOMEM, "cudaMalloc (3D) failed");
+  c->s3->allocs.push_back(*p);
+  CK(cudaMemsetAsync(*p, 0, bytes, c->st), "memset");
+  return NS_OK;
+}
+
+template <typename T>
+int levels3(ns_ctx* c, MG3<T>& M, bool own0) {
+  State3D& S = *c->s3;
+  int n = c->N;
+  M.L = 0;
+  for (int d = 0; d < 3; ++d) M.periodic[d] = c->g.periodic[d];
+  M.fmean = nullptr;
+  double h[3] = {c->g.dx[0], c->g.dx[1], c->g.dx[2]};
+  while (true) {
+    const int l = M.L;
+    if (l >= kMaxLevels3) return fail(c, NS_ERR_ARG, "too many multigrid levels");
+    M.n[l] = n;
+    M.pitch[l] = (l == 0) ? c->pitch : rup(n, 32);
+    M.plane[l] = (l == 0) ? c->pitch * (c->N + 1) : M.pitch[l] * n;
+    for (int d = 0; d < 3; ++d) M.ih[l][d] = (T)(1.0 / (h[d] * h[d]));
+    M.x[l] = nullptr;
+    M.f[l] = nullptr;
+    if (l > 0 || own0) {
+      const size_t bytes = (l == 0) ? S.fb / sizeof(double) * sizeof(T) : (size_t)M.plane[l] * n * sizeof(T);
+      int r = alloc3(c, &M.x[l], bytes);
+      if (r == NS_OK) r = alloc3(c, &M.f[l], bytes);
+      if (r != NS_OK) return r;
+    }
+    M.L++;
+    if (!(n % 4 == 0 && n > 4)) break;
+    n /= 2;
+    for (double& x : h) x *= 2;
+  }
+  return NS_OK;
+}
+
+Arg3 args(ns_ctx* c) {
+  State3D& S = *c->s3;
+  Arg3 a;
+  std::memset(&a, 0, sizeof(a));
+  a.g = c->g;
+  for (int m = 0; m < 3; ++m) {
+    a.ph[m] = S.PH[m];
+    a.t[m] = S.T[m];
+  }
+  a.part = S.part;
+  a.counter = c->counter;
+  return a;
+}
+
+double* face3(ns_ctx* c, int id, int m) { return id < 0 ? c->s3->UP[m] : c->s3->B[id][m]; }
+
+int pick3(int base, int in) {
+  for (int i = 0; i < 3; ++i)
+    if (i != base && i != in) return i;
+  return -2;
+}
+
+template <typename T>
+int vcycle3(ns_ctx* c, MG3<T>& M) {
+  for (int l = 0; l + 1 < M.L; ++l) {
+    for (int s = 0; s < 4; ++s) LAUNCH(l == 0 ? NS_PROF_MG_SMOOTH0 : NS_PROF_MG_SMOOTH, "mg3 smooth", launch3_mg_rb<T>(M, l, s & 1, c->st));
+    LAUNCH(l == 0 ? NS_PROF_MG_RESTRICT0 : NS_PROF_MG_RESTRICT, "mg3 restrict", launch3_mg_restrict<T>(M, l, c->st));
+  }
+  LAUNCH(NS_PROF_MG_BOTTOM, "mg3 bottom", launch3_mg_bottom<T>(M, M.L - 1, 50, c->st));
+  for (int l = M.L - 2; l >= 0; --l) {
+    LAUNCH(NS_PROF_MG_SMOOTH, "mg3 prolong", launch3_mg_prolong<T>(M, l, c->st));
+    for (int s = 0; s < 4; ++s) LAUNCH(l == 0 ? NS_PROF_MG_SMOOTH0 : NS_PROF_MG_SMOOTH, "mg3 smooth", launch3_mg_rb<T>(M, l, (s + 1) & 1, c->st));
+  }
+  return NS_OK;
+}
+
+__global__ void k3_set_mean(double* red, double inv_n) { red[kRedMean] = red[kRedSum] * inv_n; }
+
+// phi solves L phi = f - mean(f) to poisson_tol_rel (and the divergence
+// tolerance); FP64 V-cycles, or FP32 V-cycles inside an FP64 defect correction
+int poisson3(ns_ctx* c, int* cycles, double* res, long long* fallbacks) {
+  State3D& S = *c->s3;
+  const double n3 = (double)c->N * c->N * c->N;
+  LAUNCH(NS_PROF_OTHER, "set mean", (k3_set_mean<<<1, 1, 0, c->st>>>(c->red, 1.0 / n3), cudaGetLastError()));
+  S.M64.x[0] = S.PHI;
+  S.M64.f[0] = S.F;
+  S.M64.fmean = c->red + kRedMean;
+  CK(cudaMemsetAsync(S.PHI, 0, S.fb, c->st), "memset phi");
+  const bool mixed = c->P.precision == NS_PREC_MIXED;
+  const int maxc = std::max(1, c->P.poisson_max_cycles);
+  const double div_tol_res = c->P.poisson_tol_div > 0 ? c->P.poisson_tol_div * 1.5 / c->dt : 0.0;
+  auto residual = [&]() -> int {
+    if (mixed) LAUNCH(NS_PROF_DC_UPDATE, "dc residual", launch3_dc_res(S.M64, S.M32.f[0], S.part, c->counter, c->red + kRedRes, c->st));
+    else LAUNCH(NS_PROF_MG_RESNORM, "resnorm", launch3_mg_resnorm<double>(S.M64, S.part, c->counter, c->red + kRedRes, c->st));
+    return sync_red(c, kRedRes, 1);
+  };
+  int r = residual();
+  if (r != NS_OK) return r;
+  const double r0 = c->red_h[kRedRes];
+  double rn = r0, best = r0;
+  const double tol = c->P.poisson_tol_rel * r0;
+  auto done = [&](double x) { return x <= tol && (div_tol_res <= 0 || x <= div_tol_res); };
+  int ncyc = 0, stall = 0, status = NS_OK;
+  while (!done(rn) && r0 > 0) {
+    if (ncyc >= maxc) { status = NS_ERR_MG_STALL; break; }
+    if (mixed) {
+      CK(cudaMemsetAsync(S.M32.x[0], 0, S.fb / 2, c->st), "memset e");  // each correction starts from zero
+      r = vcycle3<float>(c, S.M32);
+      if (r == NS_OK) LAUNCH(NS_PROF_DC_UPDATE, "dc add", launch3_dc_add(S.M64, S.M32.x[0], c->st));
+    } else {
+      r = vcycle3<double>(c, S.M64);
+    }
+    if (r != NS_OK) return r;
+    ++ncyc;
+    r = residual();
+    if (r != NS_OK) return r;
+    rn = c->red_h[kRedRes];
+    if (rn < 0.5 * best) { best = rn; stall = 0; } else if (++stall >= 6) { status = NS_ERR_MG_STALL; break; }
+  }
+  (void)fallbacks;
+  *cycles = ncyc;
+  *res = r0 > 0 ? rn / r0 : 0.0;
+  if (status != NS_OK) c->err = "Poisson residual stalled before the tolerance";
+  return status;
+}
+
+// ns_set_state layout of face d: (N + [d==0]) x (N + [d==1]) x (N + [d==2]), x fastest
+cudaMemcpy3DParms copy_parms(ns_ctx* c, int d, const double* host, double* dev, bool put) {
+  const int N = c->N;
+  const size_t nx = N + (d == 0), ny = N + (d == 1), nz = N + (d == 2);
+  cudaMemcpy3DParms q;
+  std::memset(&q, 0, sizeof(q));
+  cudaPitchedPtr h = make_cudaPitchedPtr(const_cast<double*>(host), nx * sizeof(double), nx, ny);
+  cudaPitchedPtr g = make_cudaPitchedPtr(dev, (size_t)c->pitch * sizeof(double), (size_t)c->pitch, (size_t)N + 1);
+  q.srcPtr = put ? h : g;
+  q.dstPtr = put ? g : h;
+  q.extent = make_cudaExtent(nx * sizeof(double), ny, nz);
+  q.kind = put ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost;
+  return q;
+}
+
+int copy_cells3(ns_ctx* c, const double* host, double* dev, bool put) {
+  const int N = c->N;
+  cudaMemcpy3DParms q;
+  std::memset(&q, 0, sizeof(q));
+  cudaPitchedPtr h = make_cudaPitchedPtr(const_cast<double*>(host), (size_t)N * sizeof(double), N, N);
+  cudaPitchedPtr g = make_cudaPitchedPtr(dev, (size_t)c->pitch * sizeof(double), (size_t)c->pitch, (size_t)N + 1);
+  q.srcPtr = put ? h : g;
+  q.dstPtr = put ? g : h;
+  q.extent = make_cudaExtent((size_t)N * sizeof(double), N, N);
+  q.kind = put ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost;
+  CK(cudaMemcpy3DAsync(&q, c->st), "3D copy");
+  return NS_OK;
+}
+
+}  // namespace
+
+namespace nsh {
+
+int create3d(ns_ctx* c) {
+  const int N = c->N;
+  c->s3 = new State3D();
+  State3D& S = *c->s3;
+  S.fb = (size_t)c->pitch * (N + 1) * (N + 1) * sizeof(double);
+  c->fbytes = S.fb;
+  int r = NS_OK;
+  for (int m = 0; m < 3 && r == NS_OK; ++m) {
+    double** fs[] = {&S.U[m], &S.UP[m], &S.DU[m], &S.S[m], &S.B[0][m], &S.B[1][m], &S.B[2][m], &S.T[m]};
+    for (double** p : fs)
+      if (r == NS_OK) r = alloc3(c, p, S.fb);
+    if (r == NS_OK) r = alloc3(c, &S.PH[m], (size_t)(N + 4) * (N + 4) * (N + 4) * sizeof(double));
+  }
+  if (r == NS_OK) r = alloc3(c, &S.Pp, S.fb);
+  if (r == NS_OK) r = alloc3(c, &S.PHI, S.fb);
+  if (r == NS_OK) r = alloc3(c, &S.F, S.fb);
+  if (r == NS_OK) r = alloc3(c, &S.part, (size_t)4 * (blocks3_face(N) + 1024) * sizeof(double));
+  if (r == NS_OK) r = levels3<double>(c, S.M64, false);
+  if (r == NS_OK && c->P.precision == NS_PREC_MIXED) r = levels3<float>(c, S.M32, true);
+  return r;
+}
+
+int set_state3d(ns_ctx* c, const double* const* u, const double* const* up, const double* p, double time) {
+  State3D& S = *c->s3;
+  for (int d = 0; d < 3; ++d) {
+    cudaMemcpy3DParms q = copy_parms(c, d, u[d], S.U[d], true);
+    CK(cudaMemcpy3DAsync(&q, c->st), "3D copy");
+    q = copy_parms(c, d, up[d], S.UP[d], true);
+    CK(cudaMemcpy3DAsync(&q, c->st), "3D copy");
+  }
+  int r = copy_cells3(c, p, S.Pp, true);
+  if (r != NS_OK) return r;
+  CK(cudaMemsetAsync(S.PHI, 0, S.fb, c->st), "memset phi");
+  c->time = time;
+  c->in_step = false;
+  return ns_sync(c);
+}
+
+int get_state3d(ns_ctx* c, double* const* u, double* const* up, double* p, double* phi) {
+  State3D& S = *c->s3;
+  for (int d = 0; d < 3; ++d) {
+    if (u && u[d]) {
+      cudaMemcpy3DParms q = copy_parms(c, d, u[d], S.U[d], false);
+      CK(cudaMemcpy3DAsync(&q, c->st), "3D copy");
+    }
+    if (up && up[d]) {
+      cudaMemcpy3DParms q = copy_parms(c, d, up[d], S.UP[d], false);
+      CK(cudaMemcpy3DAsync(&q, c->st), "3D copy");
+    }
+  }
+  if (p) { int r = copy_cells3(c, p, S.Pp, false); if (r) return r; }
+  if (phi) { int r = copy_cells3(c, phi, S.PHI, false); if (r) return r; }
+  return ns_sync(c);
+}
+
+int step3d(ns_ctx* c, ns_step_stats* stats) {
+  State3D& S = *c->s3;
+  if (c->P.pseudo_timestepping == 0) return fail(c, NS_ERR_UNSUPPORTED, "3D: the explicit predictor is not built");
+  ns_step_stats s;
+  std::memset(&s, 0, sizeof(s));
+  if (c->ev_ok) cudaEventRecord(c->ev[0], c->st);
+  // ---- step begin: du, S from (u^n, u^{n-1}, p); u^{n-1} buffer becomes the target
+  Arg3 a = args(c);
+  for (int m = 0; m < 3; ++m) {
+    a.un[m] = S.U[m];
+    a.uprev[m] = S.UP[m];
+    a.du[m] = S.DU[m];
+    a.S[m] = S.S[m];
+  }
+  a.p = S.Pp;
+  LAUNCH(NS_PROF_STEP_BEGIN, "step begin 3d", launch3_step_begin(a, c->st));
+  for (int m = 0; m < 3; ++m) std::swap(S.U[m], S.UP[m]);
+  c->time += c->dt;
+  S.base = S.cur = -1;
+  // ---- dual-time pseudo-iterations (main.cpp:898-1040)
+  int count = 0;
+  double norm = 1.e9;
+  while (norm > c->P.momentum_tolerance) {
+    for (int sub = 0; sub < 4; ++sub) {
+      const int outb = pick3(S.base, S.cur);
+      Arg3 b = args(c);
+      for (int m = 0; m < 3; ++m) {
+        b.u[m] = face3(c, S.cur, m);
+        b.ub[m] = face3(c, S.base, m);
+        b.S[m] = S.S[m];
+        b.out[m] = S.B[outb][m];
+      }
+      b.rk = c->rk[sub];
+      b.do_norm = (sub == 3);
+      b.red_out = c->red + kRedNorm;
+      LAUNCH(NS_PROF_STAGE_FAST, "cart 3d", launch3_cart(b, c->st));
+      LAUNCH(NS_PROF_STAGE_FAST, "total 3d", launch3_total(b, c->st));
+      LAUNCH(NS_PROF_STAGE_FAST, "face 3d", launch3_face(b, c->st));
+      S.cur = outb;
+    }
+    int r = sync_red(c, kRedNorm, 1);
+    if (r != NS_OK) return r;
+    norm = c->red_h[kRedNorm];
+    S.base = S.cur;
+    count++;
+    if (count > c->P.iter_num) { s.status = NS_WARN_PSEUDO_MAXITER; break; }
+    if (norm > 1.e2) { s.status = NS_WARN_PSEUDO_DIVERGED; break; }
+  }
+  s.pseudo_iters = count;
+  s.norm_error = norm;
+  if (c->ev_ok) cudaEventRecord(c->ev[1], c->st);
+  // ---- Poisson right-hand side, solve, projection
+  Arg3 p = args(c);
+  for (int m = 0; m < 3; ++m) p.u[m] = face3(c, S.cur, m);
+  p.f = S.F;
+  p.red_out = c->red + kRedDivBefore;
+  LAUNCH(NS_PROF_POISSON_RHS, "rhs 3d", launch3_rhs(p, c->st));
+  int r = sync_red(c, kRedDivBefore, 2);
+  if (r != NS_OK) return r;
+  s.div_before = c->red_h[kRedDivBefore];
+  s.rhs_sum = c->red_h[kRedSum];
+  long long fb = 0;
+  const int mg = poisson3(c, &s.poisson_cycles, &s.poisson_res, &fb);
+  if (mg != NS_OK && mg != NS_ERR_MG_STALL) return mg;
+  if (c->ev_ok) cudaEventRecord(c->ev[2], c->st);
+  for (int m = 0; m < 3; ++m) p.out[m] = S.U[m];
+  p.p = S.Pp;
+  p.pw = S.Pp;
+  p.phi = S.PHI;
+  p.red_out = c->red + kRedDivAfter;
+  LAUNCH(NS_PROF_PROJECT, "project 3d", launch3_project(p, c->st));
+  LAUNCH(NS_PROF_PROJECT, "div 3d", launch3_div(p, c->st));
+  r = sync_red(c, kRedDivAfter, 1);
+  if (r != NS_OK) return r;
+  s.div_after = c->red_h[kRedDivAfter];
+  c->step++;
+  if (c->ev_ok) {
+    cudaEventRecord(c->ev[3], c->st);
+    cudaEventSynchronize(c->ev[3]);
+    float t0 = 0, t1 = 0, t2 = 0;
+    cudaEventElapsedTime(&t0, c->ev[0], c->ev[1]);
+    cudaEventElapsedTime(&t1, c->ev[1], c->ev[2]);
+    cudaEventElapsedTime(&t2, c->ev[2], c->ev[3]);
+    s.ms_predictor = t0; s.ms_poisson = t1; s.ms_project = t2;
+  }
+  if (stats) *stats = s;
+  if (mg != NS_OK) return mg;
+  return s.status;
+}
+
+}  // namespace nsh

@@ -121,6 +121,7 @@ void free_all(ns_ctx* c) {
   F(c->FFh); F(c->FFl);
   F(c->Pp); F(c->F);
   F(c->lid_col);
+  free3d(c);
   for (double* v : c->gm_v) F(v);
   F(c->gm_w); F(c->gm_z); F(c->gm_b); F(c->gm_part); F(c->gm_dev);
   if (c->gm_host) cudaFreeHost(c->gm_host);
@@ -279,8 +280,9 @@ int ns_params_parse_file(ns_params* p, const char* path) {
 int ns_ctx_create(const ns_params* p, void* stream, ns_ctx** out) {
   if (!p || !out) return NS_ERR_ARG;
   *out = nullptr;
-  if (p->dim != 2) return NS_ERR_UNSUPPORTED;
+  if (p->dim != 2 && p->dim != 3) return NS_ERR_UNSUPPORTED;
   if (p->n_cell < 8 || p->n_cell % 8 != 0) return NS_ERR_ARG;
+  const int D = p->dim;
   if (p->ren <= 0) return NS_ERR_ARG;
   ns_ctx* c = new ns_ctx();
   c->P = *p;
@@ -295,7 +297,7 @@ int ns_ctx_create(const ns_params* p, void* stream, ns_ctx** out) {
   g.pitch = c->pitch;
   g.plane = c->pitch * (N + 1);
   for (int d = 0; d < 3; ++d) g.dx[d] = (p->prob_hi[d] - p->prob_lo[d]) / (double)N;
-  for (int d = 0; d < 2; ++d) {
+  for (int d = 0; d < D; ++d) {
     const bool lo111 = p->bc_lo[d] == 111, hi111 = p->bc_hi[d] == 111;
     if (lo111 != hi111) { delete c; return NS_ERR_BC; }
     g.periodic[d] = lo111 && hi111;
@@ -313,7 +315,8 @@ int ns_ctx_create(const ns_params* p, void* stream, ns_ctx** out) {
     }
   }
   // dt rule of main.cpp:285-294
-  const double coeff = 1.0 / (g.dx[0] * g.dx[0]) + 1.0 / (g.dx[1] * g.dx[1]);
+  double coeff = 1.0 / (g.dx[0] * g.dx[0]) + 1.0 / (g.dx[1] * g.dx[1]);
+  if (D == 3) coeff += 1.0 / (g.dx[2] * g.dx[2]);
   c->dt = p->fixed_dt != -1.0 ? p->fixed_dt : p->cfl / (2.0 * coeff);
   g.dt = c->dt;
   g.ren = p->ren;
@@ -346,7 +349,9 @@ int ns_ctx_create(const ns_params* p, void* stream, ns_ctx** out) {
     c->own_stream = true;
   }
   int r = NS_OK;
-  for (int m = 0; m < 2 && r == NS_OK; ++m) {
+  g.dim = D;
+  if (D == 3) r = create3d(c);
+  for (int m = 0; m < 2 && r == NS_OK && D == 2; ++m) {
     r = alloc_field(c, &c->U[m]);
     if (r == NS_OK) r = alloc_field(c, &c->UP[m]);
     if (r == NS_OK) r = alloc_field(c, &c->DU[m]);
@@ -354,10 +359,10 @@ int ns_ctx_create(const ns_params* p, void* stream, ns_ctx** out) {
     if (r == NS_OK) r = alloc_field(c, &c->PHI[m]);
     for (int i = 0; i < 3 && r == NS_OK; ++i) r = alloc_field(c, &c->B[i][m]);
   }
-  if (r == NS_OK) r = alloc_field(c, &c->Pp);
-  if (r == NS_OK) r = alloc_field(c, &c->F);
-  if (r == NS_OK) r = alloc_levels<double>(c, c->M64, false);
-  if (r == NS_OK) r = alloc_levels<float>(c, c->M32, true);
+  if (r == NS_OK && D == 2) r = alloc_field(c, &c->Pp);
+  if (r == NS_OK && D == 2) r = alloc_field(c, &c->F);
+  if (r == NS_OK && D == 2) r = alloc_levels<double>(c, c->M64, false);
+  if (r == NS_OK && D == 2) r = alloc_levels<float>(c, c->M32, true);
   if (r == NS_OK) {
     // reduction scratch: 2 partials per block of the largest launch
     const size_t nb = (size_t)((N + 31) / 32) * ((N + 7) / 8) + 1024;
@@ -428,6 +433,7 @@ static int box_copy(ns_ctx* c, int field, int comp, double* data, const int lo[3
                     long long kstride, int where_device, bool put) {
   (void)kstride;
   if (!c || !data || !lo || !hi || comp < 0 || comp > 1) return NS_ERR_ARG;
+  if (c->P.dim == 3) return fail(c, NS_ERR_UNSUPPORTED, "3D boxes: use ns_set_state / ns_get_state");
   if (field == NS_FIELD_CART) {
     if (!put) return NS_ERR_ARG;
     for (int m = 0; m < 2; ++m)
@@ -468,6 +474,7 @@ int ns_get_box(ns_ctx* c, int field, int comp, double* data, const int lo[3], co
 
 int ns_set_state(ns_ctx* c, const double* const* u, const double* const* u_prev, const double* p, double time) {
   if (!c || !u || !u_prev || !p) return NS_ERR_ARG;
+  if (c->P.dim == 3) return set_state3d(c, u, u_prev, p, time);
   const int N = c->N;
   for (int m = 0; m < 2; ++m) {
     const int lo[3] = {0, 0, 0};
@@ -489,6 +496,7 @@ int ns_set_state(ns_ctx* c, const double* const* u, const double* const* u_prev,
 
 int ns_get_state(ns_ctx* c, double* const* u, double* const* u_prev, double* p, double* phi) {
   if (!c) return NS_ERR_ARG;
+  if (c->P.dim == 3) return get_state3d(c, u, u_prev, p, phi);
   const int N = c->N;
   for (int m = 0; m < 2; ++m) {
     const int lo[3] = {0, 0, 0};
@@ -505,6 +513,16 @@ int ns_get_state(ns_ctx* c, double* const* u, double* const* u_prev, double* p, 
 
 int ns_init_fields(ns_ctx* c, int init_case) {
   if (!c || (init_case != NS_INIT_CAVITY && init_case != NS_INIT_TGV)) return NS_ERR_ARG;
+  if (c->P.dim == 3) {
+    // from rest; other 3D initial fields go through ns_set_state
+    if (init_case != NS_INIT_CAVITY) return fail(c, NS_ERR_UNSUPPORTED, "3D: set the initial field with ns_set_state");
+    const size_t N = c->N, nf = (N + 1) * N * N;
+    std::vector<double> z(nf, 0.0), zc(N * N * N, 0.0);
+    const double* u3[3] = {z.data(), z.data(), z.data()};
+    const int r = ns_set_state(c, u3, u3, zc.data(), 0.0);
+    if (r == NS_OK) c->step = 0;
+    return r;
+  }
   // hybrid_grid_init (fn_init.cpp:61-229, kn_init.H:8-37), evaluated on the
   // host with the C library's sin/cos/exp and uploaded.
   const int N = c->N;
@@ -551,6 +569,7 @@ int ns_init_fields(ns_ctx* c, int init_case) {
 
 int ns_step_begin(ns_ctx* c) {
   if (!c) return NS_ERR_ARG;
+  if (c->P.dim == 3) return fail(c, NS_ERR_UNSUPPORTED, "building blocks are 2D only: use ns_step in 3D");
   ProjArgs a;
   std::memset(&a, 0, sizeof(a));
   a.g = c->g;
@@ -598,6 +617,7 @@ static int launch_rk(ns_ctx* c, int sub, bool use_cart) {
 
 int ns_rk_stage(ns_ctx* c, int sub) {
   if (!c || sub < 0 || sub > 3) return NS_ERR_ARG;
+  if (c->P.dim == 3) return fail(c, NS_ERR_UNSUPPORTED, "building blocks are 2D only: use ns_step in 3D");
   if (!c->in_step) return fail(c, NS_ERR_STATE, "ns_rk_stage before ns_step_begin");
   const bool use_cart = c->cart_pending;
   int r = launch_rk(c, sub, use_cart);
@@ -608,6 +628,7 @@ int ns_rk_stage(ns_ctx* c, int sub) {
 
 int ns_pseudo_norm(ns_ctx* c, double* norm) {
   if (!c) return NS_ERR_ARG;
+  if (c->P.dim == 3) return fail(c, NS_ERR_UNSUPPORTED, "building blocks are 2D only: use ns_step in 3D");
   if (!c->norm_ready) return fail(c, NS_ERR_STATE, "ns_pseudo_norm needs stage 3 first");
   int r = sync_red(c, kRedNorm, 1);
   if (r != NS_OK) return r;
@@ -619,6 +640,7 @@ int ns_pseudo_norm(ns_ctx* c, double* norm) {
 
 int ns_explicit_predictor(ns_ctx* c, double* norm) {
   if (!c) return NS_ERR_ARG;
+  if (c->P.dim == 3) return fail(c, NS_ERR_UNSUPPORTED, "building blocks are 2D only: use ns_step in 3D");
   if (!c->in_step) return fail(c, NS_ERR_STATE, "explicit predictor before ns_step_begin");
   const int in = c->cur;
   const int outb = pick_out(c->base, in);
@@ -656,6 +678,7 @@ static int poisson_rhs_async(ns_ctx* c) {
 
 int ns_poisson_rhs(ns_ctx* c, double* divmax, double* sum) {
   if (!c) return NS_ERR_ARG;
+  if (c->P.dim == 3) return fail(c, NS_ERR_UNSUPPORTED, "building blocks are 2D only: use ns_step in 3D");
   int r = poisson_rhs_async(c);
   if (r == NS_OK) r = sync_red(c, kRedDivBefore, 2);
   if (r != NS_OK) return r;
@@ -846,6 +869,7 @@ static void split_const(double x, float* out);
 
 int ns_poisson_solve(ns_ctx* c, int precision, int* cycles, double* res) {
   if (!c) return NS_ERR_ARG;
+  if (c->P.dim == 3) return fail(c, NS_ERR_UNSUPPORTED, "building blocks are 2D only: use ns_step in 3D");
   const double nn = (double)c->N * (double)c->N;
   LAUNCH(NS_PROF_OTHER, "set mean", (k_set_mean<<<1, 1, 0, c->st>>>(c->red, 1.0 / nn), cudaGetLastError()));
   const int maxc = std::max(1, c->P.poisson_max_cycles);
@@ -1004,6 +1028,7 @@ static int project_async(ns_ctx* c) {
 
 int ns_project(ns_ctx* c, double* divmax) {
   if (!c) return NS_ERR_ARG;
+  if (c->P.dim == 3) return fail(c, NS_ERR_UNSUPPORTED, "building blocks are 2D only: use ns_step in 3D");
   int r = project_async(c);
   if (r == NS_OK) r = sync_red(c, kRedDivAfter, 1);
   if (r != NS_OK) return r;
@@ -1163,6 +1188,7 @@ extern "C" {
 
 int ns_step(ns_ctx* c, ns_step_stats* stats) {
   if (!c) return NS_ERR_ARG;
+  if (c->P.dim == 3) return step3d(c, stats);
   ns_step_stats s;
   std::memset(&s, 0, sizeof(s));
   if (c->ev_ok) cudaEventRecord(c->ev[0], c->st);

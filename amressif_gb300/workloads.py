@@ -68,3 +68,53 @@ def tgv_amplitude(u, v, length=2.0 * math.pi):
 def lid_controls(nseg=256, sigma=0.05, seed=0):
     """Lid velocities 1 + N(0, sigma^2) (numpy PCG64, the given seed)."""
     return 1.0 + sigma * np.random.default_rng(seed).standard_normal(nseg)
+
+
+# ---- 3D (arrays indexed [k, j, i]) -------------------------------------------------
+
+def tgv3d_fields(n, length=2.0 * math.pi):
+    """u = sin x cos y cos z, v = -cos x sin y cos z, w = 0 on the faces; p =
+    (cos 2x + cos 2y)(cos 2z + 2) / 16 at the cell centres."""
+    h = length / n
+    xf = np.arange(n + 1) * h
+    xc = (np.arange(n) + 0.5) * h
+    u = np.sin(xf)[None, None, :] * np.cos(xc)[None, :, None] * np.cos(xc)[:, None, None]
+    v = -np.cos(xc)[None, None, :] * np.sin(xf)[None, :, None] * np.cos(xc)[:, None, None]
+    w = np.zeros((n + 1, n, n))
+    p = (np.cos(2 * xc)[None, None, :] + np.cos(2 * xc)[None, :, None]) * (np.cos(2 * xc)[:, None, None] + 2.0) / 16.0
+    return [u, v, w], p
+
+
+def divfree_perturbation3d(n, amp=1e-3, seed=0, length=2.0 * math.pi):
+    """Periodic, discretely divergence-free 3D perturbation: the MAC curl of a
+    vector potential on the cell edges drawn from the standard normal
+    distribution (numpy PCG64, the given seed), scaled to max |du| = amp."""
+    h = length / n
+    r = np.random.default_rng(seed)
+    ax, ay, az = (r.standard_normal((n, n, n)) for _ in range(3))  # [k, j, i]
+
+    def d(a, axis):  # forward difference a(index + 1) - a(index), periodic
+        return (np.roll(a, -1, axis=axis) - a) / h
+
+    du = d(az, 1) - d(ay, 0)  # x face (i, j+1/2, k+1/2)
+    dv = d(ax, 0) - d(az, 2)  # y face
+    dw = d(ay, 2) - d(ax, 1)  # z face
+    s = amp / max(np.abs(du).max(), np.abs(dv).max(), np.abs(dw).max())
+    u = np.empty((n, n, n + 1)); u[:, :, :n] = s * du; u[:, :, n] = u[:, :, 0]
+    v = np.empty((n, n + 1, n)); v[:, :n, :] = s * dv; v[:, n, :] = v[:, 0, :]
+    w = np.empty((n + 1, n, n)); w[:n, :, :] = s * dw; w[n, :, :] = w[0, :, :]
+    return [u, v, w]
+
+
+def tgv3d_perturbed_state(n, amp=1e-3, seed=0, length=2.0 * math.pi):
+    """(u, u_prev, p) of the perturbed 3D Taylor-Green run: u^{-1} = u^0."""
+    u, p = tgv3d_fields(n, length)
+    du = divfree_perturbation3d(n, amp, seed, length)
+    u0 = [u[m] + du[m] for m in range(3)]
+    return u0, [a.copy() for a in u0], p
+
+
+def mac_divergence3d(u, length=2.0 * math.pi):
+    n = u[0].shape[0]
+    h = length / n
+    return ((u[0][:, :, 1:] - u[0][:, :, :-1]) + (u[1][:, 1:, :] - u[1][:, :-1, :]) + (u[2][1:, :, :] - u[2][:-1, :, :])) / h

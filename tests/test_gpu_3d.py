@@ -1,0 +1,102 @@
+"""The 3D advance (dim = 3): per-step parity with the oracle's 3D restatement
+(lid cavity with walls on every side; perturbed periodic Taylor-Green in the
+reference's parity mode and in the physical mode), the mixed-precision
+Poisson solve (FP32 V-cycles inside FP64 defect correction) against the FP64
+one, and the discrete divergence after every step.
+
+Tolerances: relative L2 <= 1e-10 per step in u, v, w and p (p modulo its
+constant), identical pseudo-iteration counts; mixed vs FP64 <= 1e-10."""
+import math
+
+import numpy as np
+import pytest
+
+import amressif_gb300 as ns
+from amressif_gb300 import workloads as wl
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    nb = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / (nb if nb > 0 else 1.0)
+
+
+def relp(a, b):
+    return rel(a - a.mean(), b - b.mean())
+
+
+L2PI = 2 * math.pi
+CASES3 = {
+    # name: (n, kwargs shared by the oracle and the GPU, periodic TGV input)
+    "cavity16": (16, dict(ren=100.0, bc_lo=(135, 135, 135), bc_hi=(135, 165, 135)), False),
+    "tgv16_parity": (16, dict(ren=1600.0, prob_hi=(L2PI,) * 3, bc_lo=(111,) * 3, bc_hi=(111,) * 3), True),
+    "tgv24_fixed": (24, dict(ren=1600.0, prob_hi=(L2PI,) * 3, bc_lo=(111,) * 3, bc_hi=(111,) * 3, fix_quirks=1), True),
+}
+
+
+def state3(n, tgv):
+    if tgv:
+        return wl.tgv3d_perturbed_state(n, amp=1e-3, seed=0)
+    z = [np.zeros((n, n, n + 1)), np.zeros((n, n + 1, n)), np.zeros((n + 1, n, n))]
+    return z, [a.copy() for a in z], np.zeros((n, n, n))
+
+
+def dt_of(n, kw):
+    h = kw.get("prob_hi", (1.0,))[0] / n
+    return 0.4 * h
+
+
+@pytest.mark.parametrize("name", sorted(CASES3))
+def test_3d_steps_resynced(gpu_lib, oracle_lib, name):
+    from oracle.orc import Oracle
+
+    n, kw, tgv = CASES3[name]
+    dt = dt_of(n, kw)
+    o = Oracle(n, dim=3, dt=dt, iter_num=100, poisson_tol=1e-13, max_grid_size=(n, n, n), **kw)
+    p = ns.default_params(dim=3, n_cell=n, fixed_dt=dt, iter_num=100, precision=ns.PREC_FP64, poisson_tol_rel=1e-12,
+                          max_grid_size=(n, n, n), **kw)
+    s = ns.Solver(p)
+    u, up, pp = state3(n, tgv)
+    o.set_state(u, up, pp)
+    for step in range(3):
+        uo, upo, po, _ = o.get_state()
+        s.set_state(uo, upo, po)
+        so = o.step()
+        sg = s.step()
+        assert sg["pseudo_iters"] == so["pseudo_iters"], (step, sg["pseudo_iters"], so["pseudo_iters"])
+        ug, _, pg, _ = s.get_state()
+        uo, _, po, _ = o.get_state()
+        for d in range(3):
+            assert rel(ug[d], uo[d]) <= 1e-10, (step, d, rel(ug[d], uo[d]))
+        assert relp(pg, po) <= 1e-10, (step, relp(pg, po))
+        if kw.get("fix_quirks") or not tgv:
+            assert sg["div_after"] <= 1e-10
+    o.close()
+
+
+def test_3d_mixed_poisson_matches_fp64(gpu_lib):
+    n = 32
+    kw = dict(ren=1600.0, prob_hi=(L2PI,) * 3, bc_lo=(111,) * 3, bc_hi=(111,) * 3, fix_quirks=1)
+    dt = dt_of(n, kw)
+    out = {}
+    for prec in (ns.PREC_FP64, ns.PREC_MIXED):
+        p = ns.default_params(dim=3, n_cell=n, fixed_dt=dt, iter_num=100, precision=prec, poisson_tol_rel=1e-12,
+                              poisson_tol_div=1e-10, max_grid_size=(n, n, n), **kw)
+        s = ns.Solver(p)
+        s.set_state(*wl.tgv3d_perturbed_state(n, amp=1e-3, seed=0))
+        ks = [s.step()["pseudo_iters"] for _ in range(3)]
+        out[prec] = (ks, s.get_state())
+    assert out[ns.PREC_FP64][0] == out[ns.PREC_MIXED][0]
+    (ua, _, pa, _), (ub, _, pb, _) = out[ns.PREC_FP64][1], out[ns.PREC_MIXED][1]
+    for d in range(3):
+        assert rel(ub[d], ua[d]) <= 1e-10
+    assert relp(pb, pa) <= 1e-10
+
+
+def test_3d_building_blocks_are_2d_only(gpu_lib):
+    p = ns.default_params(dim=3, n_cell=16, fixed_dt=1e-3)
+    s = ns.Solver(p)
+    s.init(ns.INIT_CAVITY)
+    with pytest.raises(ns.NsError):
+        s.step_begin()

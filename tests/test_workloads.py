@@ -39,3 +39,13 @@ def test_lid_controls():
     c = wl.lid_controls(256, seed=0)
     assert c.shape == (256,)
     assert abs(c.mean() - 1.0) < 0.02 and 0.03 < c.std() < 0.07
+
+
+def test_3d_perturbation_is_divergence_free():
+    n = 16
+    du = wl.divfree_perturbation3d(n, amp=1e-3, seed=0)
+    assert [a.shape for a in du] == [(n, n, n + 1), (n, n + 1, n), (n + 1, n, n)]
+    assert math.isclose(max(np.abs(a).max() for a in du), 1e-3, rel_tol=1e-14)
+    assert np.abs(wl.mac_divergence3d(du)).max() <= 1e-14 * n
+    u, p = wl.tgv3d_fields(n)
+    assert np.abs(wl.mac_divergence3d(u)).max() <= 1e-12
