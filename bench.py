@@ -217,6 +217,44 @@ def adjoint_section(ns, args):
     return out
 
 
+def cfg5_section(ns, args):
+    """3D periodic Taylor-Green vortex on [0, 2 pi]^3, 256^3, Re = 1600, dt = 0.4 h
+    (CFL 0.4 for unit velocity), with the seeded 1e-3 divergence-free
+    perturbation; one warm-up step, then timed steps with the mixed-precision
+    Poisson solve (FP32 V-cycles inside FP64 defect correction) and with the
+    FP64 one. The 3D predictor is FP64."""
+    import math
+
+    import numpy as np
+    from amressif_gb300 import workloads as wl
+
+    n, k = args.cfg5_n, args.cfg5_steps
+    h = 2 * math.pi / n
+    out = {"workload": "3D periodic Taylor-Green %d^3, Re=1600, dt=0.4h, seeded 1e-3 perturbation, steps 2..%d"
+                       % (n, k + 1)}
+    state = wl.tgv3d_perturbed_state(n, amp=1e-3, seed=0)
+    for name, prec in (("mixed_poisson", ns.PREC_MIXED), ("fp64", ns.PREC_FP64)):
+        p = ns.default_params(dim=3, n_cell=n, ren=1600.0, fixed_dt=0.4 * h, iter_num=100, precision=prec,
+                              prob_hi=(2 * math.pi,) * 3, bc_lo=(111,) * 3, bc_hi=(111,) * 3, fix_quirks=1,
+                              poisson_tol_rel=1e-10, poisson_tol_div=1e-10, max_grid_size=(n, n, n))
+        s = ns.Solver(p)
+        s.set_state(*state)
+        s.step()
+        s.sync()
+        t0 = time.perf_counter()
+        st = [s.step() for _ in range(k)]
+        s.sync()
+        wall = time.perf_counter() - t0
+        out[name] = {"steps_per_s": k / wall, "ms_per_step": 1e3 * wall / k,
+                     "pseudo_iters": [x["pseudo_iters"] for x in st], "poisson_cycles": [x["poisson_cycles"] for x in st],
+                     "ms_poisson": float(np.mean([x["ms_poisson"] for x in st])),
+                     "ms_predictor": float(np.mean([x["ms_predictor"] for x in st])),
+                     "div_after_max": max(x["div_after"] for x in st)}
+        s.close()
+    out["poisson_speedup_mixed"] = out["fp64"]["ms_poisson"] / out["mixed_poisson"]["ms_poisson"]
+    return out
+
+
 def bench_ours(args):
     world, rank, dist = dist_setup()
     import amressif_gb300 as ns
@@ -336,6 +374,9 @@ def bench_ours(args):
     adjoint = None
     if rank == 0 and not args.no_adjoint:
         adjoint = adjoint_section(ns, args)
+    cfg5 = None
+    if rank == 0 and not args.no_cfg5:
+        cfg5 = cfg5_section(ns, args)
 
     if rank == 0:
         line = {
@@ -358,6 +399,7 @@ def bench_ours(args):
             "fp64_mg": fp64,
             "adjoint_forward_ratio": adjoint["ratio"] if adjoint else None,
             "adjoint": adjoint,
+            "taylor_green_3d": cfg5,
             "e2e": e2e,
             "gpu_launches": launches,
             "roofline": roofline,
@@ -406,6 +448,9 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-cfg5", action="store_true")
+    ap.add_argument("--cfg5-n", type=int, default=256)
+    ap.add_argument("--cfg5-steps", type=int, default=2)
     ap.add_argument("--adj-n", type=int, default=512)
     ap.add_argument("--adj-steps", type=int, default=400)
     ap.add_argument("--adj-snap", type=int, default=20)
