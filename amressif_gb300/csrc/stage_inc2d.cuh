@@ -39,13 +39,16 @@ struct IncArgs {
 
 // QUICK flux difference F(ub + e, phi + eps) - F(ub, phi) (fn_flux_calc.cpp:66-76)
 // a, b, c, e: phi at i+1, i, i-1, i-2; pa..pe the same for eps. Branch-free.
+// udn = max(un, 0) and upn = min(un, 0) are the upwind parts of the new
+// velocity; dud = udn - max(ub, 0) is formed without a subtraction (eb when
+// both signs are positive), and dup = eb - dud (exact except after a sign
+// change from negative to positive, where it differs from -ub by one rounding).
 __device__ __forceinline__ float quick_dflux(float ub, float eb, float a, float b, float c, float e, float pa, float pb_,
                                              float pc, float pe) {
   const float un = ub + eb;
-  const bool sb = ub > 0.f, sn = un > 0.f;
-  const float dud = sn ? (sb ? eb : un) : (sb ? -ub : 0.f);
-  const float dup = sn ? (sb ? 0.f : -ub) : (sb ? un : eb);
-  const float udn = sn ? un : 0.f, upn = sn ? 0.f : un;
+  const float udn = fmaxf(un, 0.f), upn = fminf(un, 0.f);
+  const float dud = (ub > 0.f) ? ((un > 0.f) ? eb : -ub) : udn;
+  const float dup = eb - dud;
   const float qr_phi = fmaf(0.125f, (-a - 2.f * b) + 3.f * c, b);
   const float ql_phi = fmaf(0.125f, (-e - 2.f * c) + 3.f * b, c);
   const float qr_eps = fmaf(0.125f, (-pa - 2.f * pb_) + 3.f * pc, pb_);

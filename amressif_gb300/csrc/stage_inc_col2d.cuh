@@ -192,6 +192,11 @@ __global__ void __launch_bounds__(NT) k_inc_col2d(IncArgs A) {
     const float c15 = A.c15, rk = A.rk;
     const int fgx = g.flux_ghost[0], fgy = g.flux_ghost[1];
     const bool out_lane = lane >= 3 && lane < 3 + kColOut;
+    // per-lane output predicates (loop invariant)
+    const bool out_u = out_lane && i >= 0 && i <= N, out_v = out_lane && i >= 0 && i < N;
+    const bool edge_u = (i == 0 || i == N);
+    const bool rule_u = fgx != kWrap && edge_u;
+    const float wgt_u = edge_u ? 0.5f : 1.f;
     float fyp0 = 0.f, fyp1 = 0.f;  // y flux at face r
     float t1p = 0.f;               // v total of row r-1
     for (int r = r_first; r <= r_last; ++r) {
@@ -226,26 +231,27 @@ __global__ void __launch_bounds__(NT) k_inc_col2d(IncArgs A) {
         const float visc1 = (e1r - 2.f * c.e1 + e1l) * vx + (w[3].e1 - 2.f * c.e1 + w[1].e1) * vy;
         const float t0 = visc0 - conv0, t1 = visc1 - conv1;
         const float t0l = __shfl_up_sync(FULL, t0, 1);
-        if (r >= ys && out_lane) {
-          if (r < N && i >= 0 && i <= N) {  // u face (i, r)
+        if (r >= ys) {  // warp-uniform
+          const long id = (long)r * P + i;
+          if (out_u && r < N) {  // u face (i, r)
             float avg = 0.5f * (t0l + t0);
-            if (fgx != kWrap && (i == 0 || i == N)) avg = (fgx == kReflect) ? 0.f : 0.5f * (i == 0 ? t0 : t0l);
-            const long id = (long)r * P + i;
+            if (rule_u) avg = (fgx == kReflect) ? 0.f : 0.5f * (i == 0 ? t0 : t0l);
             const float e = rk * (gqu[0] + (avg - c15 * ufe[0]));
             A.eout[0][id] = e;
-            const float wgt = (i == 0 || i == N) ? 0.5f : 1.f;
-            n0 = fmaf(wgt * e, e, n0);
+            n0 = fmaf(wgt_u * e, e, n0);
           }
-          if (i >= 0 && i < N) {  // v face (i, r), r <= N
+          if (out_v) {  // v face (i, r), r <= N
+            const bool edge_v = (r == 0 || r == N);
             float avg = 0.5f * (t1p + t1);
-            if (fgy != kWrap && (r == 0 || r == N)) avg = (fgy == kReflect) ? 0.f : 0.5f * (r == 0 ? t1 : t1p);
-            const long id = (long)r * P + i;
-            const float ecur = (r == N) ? es * ev[id] : vle[0];  // face row N as stored
-            const float gcur = (r == N) ? A.g0[1][id] : gqv[0];
+            if (fgy != kWrap && edge_v) avg = (fgy == kReflect) ? 0.f : 0.5f * (r == 0 ? t1 : t1p);
+            float ecur = vle[0], gcur = gqv[0];
+            if (r == N) {  // face row N as stored
+              ecur = es * ev[id];
+              gcur = A.g0[1][id];
+            }
             const float e = rk * (gcur + (avg - c15 * ecur));
             A.eout[1][id] = e;
-            const float wgt = (r == 0 || r == N) ? 0.5f : 1.f;
-            n1 = fmaf(wgt * e, e, n1);
+            n1 = fmaf(edge_v ? 0.5f * e : e, e, n1);
           }
         }
         t1p = t1;
