@@ -2,11 +2,12 @@
 //
 // Layout: every level-0 field is (N+1) planes x (N+1) rows x pitch P, element
 // (i, j, k) at (k (N+1) + j) P + i; x faces u(i, j, k), i in [0, N], and so
-// on. The predictor runs as three gather passes per RK stage (FP64):
+// on. The predictor runs as four gather passes per RK stage (FP64):
 //   k3_cart   ghosted cell velocity phi_m (cont2cart + wall / lid / periodic
 //             ghosts, utilities.cpp:16-350) on [-2, N+1]^3,
-//   k3_total  t_m = visc - conv at the cells (QUICK face fluxes along the
-//             three directions, fn_flux_calc.cpp:66-76, central viscous term),
+//   k3_flux   QUICK fluxes of the three components at every face along the
+//             three directions, each face once (fn_flux_calc.cpp:66-76),
+//   k3_total  t_m = visc - conv at the cells (central viscous term),
 //   k3_face   G = S - (1.5/dt) u* + avg(t) with the flux-ghost rule of the
 //             normal component (main.cpp:945-1014), the RK update and the
 //             pseudo-norm of Error_Computation (utilities.cpp:421-493);
@@ -34,6 +35,7 @@ struct Arg3 {
   const double* phi;     // Poisson solution (cells)
   double* f;             // Poisson right-hand side (cells)
   double* ph[3];         // ghosted cell velocity, (N+4)^3
+  double* fl[3][3];      // face fluxes: fl[d][m] at the faces along d, component m
   double* t[3];          // cell totals
   double rk;
   int do_norm;
@@ -95,6 +97,32 @@ __global__ void __launch_bounds__(256) k3_cart(Arg3 A) {
   }
 }
 
+// QUICK fluxes of the three components at every face along the three
+// directions, each face once: face (i, j, k) along d lies between the cells
+// c - e_d and c
+__global__ void __launch_bounds__(256) k3_flux(Arg3 A) {
+  const Geom& g = A.g;
+  const int N = g.N;
+  NS3_IJK(0, 0, 0)
+  if (i > N || j > N || k > N) return;
+  const long G1[3] = {1, N + 4, (long)(N + 4) * (N + 4)};
+  const long gc = gid3(N, i, j, k);
+  const long fc = id3(g, i, j, k);
+  const int c[3] = {i, j, k};
+  for (int d = 0; d < 3; ++d) {
+    bool ok = true;
+    for (int e = 0; e < 3; ++e)
+      if (e != d && c[e] >= N) ok = false;
+    if (!ok) continue;
+    const long s = G1[d];
+    const double ud = A.u[d][fc];
+    for (int m = 0; m < 3; ++m) {
+      const double* ph = A.ph[m];
+      A.fl[d][m][fc] = quick_flux(ud, ph[gc + s], ph[gc], ph[gc - s], ph[gc - 2 * s]);
+    }
+  }
+}
+
 __global__ void __launch_bounds__(256) k3_total(Arg3 A) {
   const Geom& g = A.g;
   const int N = g.N;
@@ -107,14 +135,12 @@ __global__ void __launch_bounds__(256) k3_total(Arg3 A) {
   for (int m = 0; m < 3; ++m) {
     const double* ph = A.ph[m];
     double conv = 0.0, visc = 0.0;
+    const double p0 = ph[gc];
     for (int d = 0; d < 3; ++d) {
       const long s = G1[d];
-      const double pmm = ph[gc - 2 * s], pm = ph[gc - s], p0 = ph[gc], pp = ph[gc + s], ppp = ph[gc + 2 * s];
-      const double ulo = A.u[d][fc], uhi = A.u[d][fc + fstride[d]];
-      const double flo = quick_flux(ulo, pp, p0, pm, pmm);
-      const double fhi = quick_flux(uhi, ppp, pp, p0, pm);
-      conv += (fhi - flo) * g.inv_dx[d];
-      visc += (pp - 2.0 * p0 + pm) * g.inv_dx2[d];
+      const double* F = A.fl[d][m];
+      conv += (F[fc + fstride[d]] - F[fc]) * g.inv_dx[d];
+      visc += (ph[gc + s] - 2.0 * p0 + ph[gc - s]) * g.inv_dx2[d];
     }
     A.t[m][fc] = visc * g.inv_ren - conv;
   }
@@ -122,11 +148,9 @@ __global__ void __launch_bounds__(256) k3_total(Arg3 A) {
 
 // total of component m at cell index a along m (other indices b, c in
 // [0, N)), with the flux-ghost rule at a = -1 and a = N
-__device__ __forceinline__ double t_along(const Arg3& A, int m, int a, long base, long st, double tin_lo, double tin_hi) {
+__device__ __forceinline__ double t_along(const Arg3& A, int m, int a, long base, long st) {
   const Geom& g = A.g;
   const int N = g.N;
-  (void)tin_lo;
-  (void)tin_hi;
   if (a >= 0 && a < N) return A.t[m][base + a * st];
   const int fg = g.flux_ghost[m];
   if (fg == kWrap) return A.t[m][base + (long)wrapi(a, N) * st];
@@ -151,7 +175,7 @@ __global__ void __launch_bounds__(256) k3_face(Arg3 A) {
     const long id = id3(g, i, j, k);
     const long st = fstride[m];
     const long base = id - (long)a * st;
-    const double tl = t_along(A, m, a - 1, base, st, 0.0, 0.0), tr = t_along(A, m, a, base, st, 0.0, 0.0);
+    const double tl = t_along(A, m, a - 1, base, st), tr = t_along(A, m, a, base, st);
     const double G = (A.S[m][id] - g.c15 * A.u[m][id]) + 0.5 * (tl + tr);
     const double o = A.ub[m][id] + A.rk * G;
     A.out[m][id] = o;

@@ -30,6 +30,7 @@ struct State3D {
   double* F = nullptr;
   double* PH[3] = {nullptr, nullptr, nullptr};  // ghosted cell velocity
   double* T[3] = {nullptr, nullptr, nullptr};   // cell totals
+  double* FL[3][3] = {};                         // face fluxes
   double* part = nullptr;
   MG3<double> M64;
   MG3<float> M32;
@@ -96,6 +97,7 @@ Arg3 args(ns_ctx* c) {
   for (int m = 0; m < 3; ++m) {
     a.ph[m] = S.PH[m];
     a.t[m] = S.T[m];
+    for (int d = 0; d < 3; ++d) a.fl[d][m] = S.FL[d][m];
   }
   a.part = S.part;
   a.counter = c->counter;
@@ -215,7 +217,8 @@ int create3d(ns_ctx* c) {
   c->fbytes = S.fb;
   int r = NS_OK;
   for (int m = 0; m < 3 && r == NS_OK; ++m) {
-    double** fs[] = {&S.U[m], &S.UP[m], &S.DU[m], &S.S[m], &S.B[0][m], &S.B[1][m], &S.B[2][m], &S.T[m]};
+    double** fs[] = {&S.U[m], &S.UP[m], &S.DU[m], &S.S[m], &S.B[0][m], &S.B[1][m], &S.B[2][m], &S.T[m],
+                     &S.FL[0][m], &S.FL[1][m], &S.FL[2][m]};
     for (double** p : fs)
       if (r == NS_OK) r = alloc3(c, p, S.fb);
     if (r == NS_OK) r = alloc3(c, &S.PH[m], (size_t)(N + 4) * (N + 4) * (N + 4) * sizeof(double));
