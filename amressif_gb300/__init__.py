@@ -405,11 +405,11 @@ class Solver:
 
     def checkpoint_get(self):
         """(u, u_prev, p, time, step): the restart state of SaveCheckpoint"""
-        u = [np.zeros(self.face_shape(d)) for d in range(2)]
-        up = [np.zeros(self.face_shape(d)) for d in range(2)]
-        p = np.zeros((self.n, self.n))
+        u = [np.zeros(self.face_shape(d)) for d in range(self.dim)]
+        up = [np.zeros(self.face_shape(d)) for d in range(self.dim)]
+        p = np.zeros(self.cell_shape())
         t, k = ctypes.c_double(), ctypes.c_longlong()
-        self._check(lib().ns_checkpoint_get(self.h, _pair(u), _pair(up), _dp(p), ctypes.byref(t), ctypes.byref(k)),
+        self._check(lib().ns_checkpoint_get(self.h, self._vec(u), self._vec(up), _dp(p), ctypes.byref(t), ctypes.byref(k)),
                     "ns_checkpoint_get")
         return u, up, p, t.value, k.value
 
@@ -417,9 +417,12 @@ class Solver:
         u = [np.ascontiguousarray(a, dtype=np.float64) for a in u]
         up = [np.ascontiguousarray(a, dtype=np.float64) for a in u_prev]
         p = np.ascontiguousarray(p, dtype=np.float64)
-        self._check(lib().ns_checkpoint_put(self.h, _pair(u), _pair(up), _dp(p), time, step), "ns_checkpoint_put")
+        self._check(lib().ns_checkpoint_put(self.h, self._vec(u), self._vec(up), _dp(p), time, step), "ns_checkpoint_put")
 
     # ---- discrete adjoint (ns_step_adjoint_fwd / ns_step_adjoint_bwd pair) ----
+    def _vec(self, arrs):
+        return (ctypes.POINTER(ctypes.c_double) * self.dim)(*[_dp(a) for a in arrs])
+
     def set_controls(self, controls):
         """Piecewise-constant lid profile (len divides n_cell); None: uniform lid."""
         if controls is None:
@@ -449,10 +452,10 @@ class Solver:
         return g[: getattr(self, "nseg", 0)], stats_dict(st)
 
     def adjoint_state_grad(self):
-        ub = [np.zeros(self.face_shape(d)) for d in range(2)]
-        upb = [np.zeros(self.face_shape(d)) for d in range(2)]
-        pb = np.zeros((self.n, self.n))
-        self._check(lib().ns_adjoint_get_state_grad(self.h, _pair(ub), _pair(upb), _dp(pb)), "ns_adjoint_get_state_grad")
+        ub = [np.zeros(self.face_shape(d)) for d in range(self.dim)]
+        upb = [np.zeros(self.face_shape(d)) for d in range(self.dim)]
+        pb = np.zeros(self.cell_shape())
+        self._check(lib().ns_adjoint_get_state_grad(self.h, self._vec(ub), self._vec(upb), _dp(pb)), "ns_adjoint_get_state_grad")
         return ub, upb, pb
 
     def step_jvp(self, du, duprev, dp, dc=None):
@@ -460,10 +463,10 @@ class Solver:
         dup = [np.ascontiguousarray(a, dtype=np.float64) for a in duprev]
         dp = np.ascontiguousarray(dp, dtype=np.float64)
         dc = None if dc is None else np.ascontiguousarray(dc, dtype=np.float64)
-        o = [np.zeros(self.face_shape(d)) for d in range(2)]
-        op = [np.zeros(self.face_shape(d)) for d in range(2)]
-        odp = np.zeros((self.n, self.n))
-        self._check(lib().ns_step_jvp(self.h, _pair(du), _pair(dup), _dp(dp), _opt(dc), _pair(o), _pair(op), _dp(odp)),
+        o = [np.zeros(self.face_shape(d)) for d in range(self.dim)]
+        op = [np.zeros(self.face_shape(d)) for d in range(self.dim)]
+        odp = np.zeros(self.cell_shape())
+        self._check(lib().ns_step_jvp(self.h, self._vec(du), self._vec(dup), _dp(dp), _opt(dc), self._vec(o), self._vec(op), _dp(odp)),
                     "ns_step_jvp")
         return o, op, odp
 
@@ -471,20 +474,20 @@ class Solver:
         ub = [np.ascontiguousarray(a, dtype=np.float64) for a in ubar]
         upb = [np.ascontiguousarray(a, dtype=np.float64) for a in uprevbar]
         pb = np.ascontiguousarray(pbar, dtype=np.float64)
-        o = [np.zeros(self.face_shape(d)) for d in range(2)]
-        op = [np.zeros(self.face_shape(d)) for d in range(2)]
-        opb = np.zeros((self.n, self.n))
+        o = [np.zeros(self.face_shape(d)) for d in range(self.dim)]
+        op = [np.zeros(self.face_shape(d)) for d in range(self.dim)]
+        opb = np.zeros(self.cell_shape())
         cb = np.zeros(max(1, getattr(self, "nseg", 0)))
-        self._check(lib().ns_step_vjp(self.h, _pair(ub), _pair(upb), _dp(pb), _pair(o), _pair(op), _dp(opb), _dp(cb)),
+        self._check(lib().ns_step_vjp(self.h, self._vec(ub), self._vec(upb), _dp(pb), self._vec(o), self._vec(op), _dp(opb), _dp(cb)),
                     "ns_step_vjp")
         return o, op, opb, cb[: getattr(self, "nseg", 0)]
 
     def adjoint_op(self, x, transpose=False, dc=None):
         """J x (+ dA/dc dc) or (J^T x, dA/dc^T x) at the current state's u*."""
         x = [np.ascontiguousarray(a, dtype=np.float64) for a in x]
-        y = [np.zeros(self.face_shape(d)) for d in range(2)]
+        y = [np.zeros(self.face_shape(d)) for d in range(self.dim)]
         cb = np.zeros(max(1, getattr(self, "nseg", 0)))
         dcv = None if dc is None else np.ascontiguousarray(dc, dtype=np.float64)
-        self._check(lib().ns_adjoint_op(self.h, 1 if transpose else 0, _pair(x), _opt(dcv), _pair(y), _dp(cb)),
+        self._check(lib().ns_adjoint_op(self.h, 1 if transpose else 0, self._vec(x), _opt(dcv), self._vec(y), _dp(cb)),
                     "ns_adjoint_op")
         return (y, cb[: getattr(self, "nseg", 0)]) if transpose else y

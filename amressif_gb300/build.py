@@ -28,6 +28,7 @@ UNITS = {
     "adjoint_api.cu": [],
     "kernels3d.cu": [],
     "ns3d_api.cu": [],
+    "adjoint3d_api.cu": [],
     "noalloc.cu": ["-fmad=false"],
 }
 

@@ -33,6 +33,8 @@
 #include "adjoint2d.cuh"
 #include "ctx.h"
 #include "launch.h"
+#include "schedule.h"
+#include "state3d.h"
 
 using namespace ns;
 using namespace nsh;
@@ -84,9 +86,7 @@ struct AdjState {
   // previous adjoint Poisson solution (warm start of the next one)
   double* PSI_PREV = nullptr;
   bool psi_valid = false;
-  // schedule: best split of a segment of l steps with s free slots
-  std::vector<int> split_arg;  // (s, l) -> steps to advance before the next snapshot; 0: no split
-  int sched_S = -1, sched_L = -1;
+  Schedule sched;  // checkpoint schedule of the last forward run
   // last forward run
   bool have_fwd = false;
   int nsteps = 0, nsnap = 0;
@@ -471,67 +471,6 @@ int restore_state(ns_ctx* c, int slot) {
   return NS_OK;
 }
 
-// binomial coefficient C(s + r, s), saturated
-long long beta(int s, int r) {
-  double b = 1.0;
-  for (int k = 1; k <= s; ++k) {
-    b = b * (double)(r + k) / (double)k;
-    if (b > 4.0e18) return (long long)4.0e18;
-  }
-  return (long long)(b + 0.5);
-}
-
-// Cost model of the reversal of a segment of l steps with s free slots, the
-// u* of its last step at hand: a full step costs 1, a predictor-only run
-// kPredCost. With no free slot the steps l-2 .. 0 are reached from the
-// segment's first state (restore, advance, predictor):
-//   T(l, 0) = (l-1)(l-2)/2 + (l-1) kPredCost,
-//   T(l, s) = min_m  m + T(l-m, s-1) + T(m, s)
-// (advance m steps and keep that level, reverse the right part, release the
-// slot, reverse the left part). Solved by dynamic programming when s L^2 is
-// small, else Griewank's binomial split: with r the least repetition number
-// for which beta(s, r) >= l, the right part gets min(l-1, beta(s-1, r)) steps.
-constexpr double kPredCost = 0.75;
-
-void build_schedule(AdjState& A, int L, int S) {
-  S = std::max(0, std::min(S, L - 1));
-  A.sched_L = L;
-  A.sched_S = S;
-  A.split_arg.clear();
-  if ((double)S * L * L > 3.0e8 || S == 0) return;
-  std::vector<double> T((size_t)(S + 1) * (L + 1), 0.0);
-  A.split_arg.assign((size_t)(S + 1) * (L + 1), 0);
-  auto at = [&](int s, int l) -> double& { return T[(size_t)s * (L + 1) + l]; };
-  for (int l = 1; l <= L; ++l) at(0, l) = 0.5 * (l - 1) * (l - 2) + (l - 1) * kPredCost;
-  for (int s = 1; s <= S; ++s) {
-    at(s, 1) = 0.0;
-    for (int l = 2; l <= L; ++l) {
-      double best = at(0, l);
-      int arg = 0;
-      for (int m = 1; m < l; ++m) {
-        const double v = m + at(s - 1, l - m) + at(s, m);
-        if (v < best) { best = v; arg = m; }
-      }
-      at(s, l) = best;
-      A.split_arg[(size_t)s * (L + 1) + l] = arg;
-    }
-  }
-}
-
-// next snapshot of the segment [a, b) with s free slots; -1: reverse it from a
-int next_split(AdjState& A, int a, int b, int s) {
-  const int l = b - a;
-  if (s <= 0 || l < 2) return -1;
-  if (!A.split_arg.empty() && l <= A.sched_L) {
-    const int m = A.split_arg[(size_t)std::min(s, A.sched_S) * (A.sched_L + 1) + l];
-    return m > 0 ? a + m : -1;
-  }
-  int r = 1;
-  while (beta(s, r) < l) ++r;
-  const long long right = std::min((long long)l - 1, beta(s - 1, r));
-  return b - (int)right;
-}
-
 int advance(ns_ctx* c, int nsteps) {
   for (int k = 0; k < nsteps; ++k) {
     ns_step_stats s;
@@ -569,7 +508,7 @@ int reverse(ns_ctx* c, int a, int b, int s, int slot_a, const double* const* ul)
   AdjState& A = *c->adj;
   if (b - a <= 0) return NS_OK;
   if (b - a == 1) return adjoint_with(c, ul);
-  const int m = next_split(A, a, b, s);
+  const int m = A.sched.next(a, b, s);
   if (m < 0) {
     int r = adjoint_with(c, ul);
     for (int k = b - 2; k >= a && r == NS_OK; --k) {
@@ -644,6 +583,7 @@ void ns_adjoint_opts_default(ns_adjoint_opts* o) {
 
 int ns_set_controls(ns_ctx* c, int nseg, const double* controls) {
   if (!c) return NS_ERR_ARG;
+  if (c->P.dim == 3) return fail(c, NS_ERR_UNSUPPORTED, "lid controls: 2D cavity only");
   return set_controls_impl(c, nseg, controls);
 }
 
@@ -651,6 +591,10 @@ int ns_step_adjoint_fwd(ns_ctx* c, const ns_adjoint_opts* opts, int nseg, const 
                         ns_adjoint_stats* stats) {
   if (!c || !opts || opts->nsteps < 1 || opts->nsnap < 1 || opts->lin_max_iters < 1 || !(opts->lin_tol > 0))
     return NS_ERR_ARG;
+  if (c->P.dim == 3) {
+    if (nseg != 0) return fail(c, NS_ERR_ARG, "3D adjoint: no lid controls (the control is the initial state)");
+    return adjoint_fwd3(c, opts, J, stats);
+  }
   int r = check_supported(c);
   if (r != NS_OK) return r;
   CK(cudaStreamSynchronize(c->st), "stream sync");
@@ -679,14 +623,13 @@ int ns_step_adjoint_fwd(ns_ctx* c, const ns_adjoint_opts* opts, int nseg, const 
   A.slot_step.assign(nslots, -1);
   A.slot_time.assign(nslots, 0.0);
   A.final_slot = nslots - 1;
-  if (A.sched_L != opts->nsteps || A.sched_S != std::max(0, std::min(nsched - 1, opts->nsteps - 1)))
-    build_schedule(A, opts->nsteps, nsched - 1);
+  A.sched.build(opts->nsteps, nsched - 1);
   // the first descent of the schedule stores its snapshots on the way
   std::vector<int> first;
   {
     int a = 0, s = nsched - 1;
     while (true) {
-      const int m = next_split(A, a, opts->nsteps, s);
+      const int m = A.sched.next(a, opts->nsteps, s);
       if (m < 0) break;
       first.push_back(m);
       a = m;
@@ -739,6 +682,7 @@ int ns_step_adjoint_fwd(ns_ctx* c, const ns_adjoint_opts* opts, int nseg, const 
 
 int ns_step_adjoint_bwd(ns_ctx* c, double* grad, ns_adjoint_stats* stats) {
   if (!c) return NS_ERR_ARG;
+  if (c->P.dim == 3) return adjoint_bwd3(c, stats);
   if (!c->adj || !c->adj->have_fwd) return fail(c, NS_ERR_STATE, "ns_step_adjoint_bwd needs ns_step_adjoint_fwd first");
   AdjState& A = *c->adj;
   CK(cudaStreamSynchronize(c->st), "stream sync");
@@ -760,6 +704,7 @@ int ns_step_adjoint_bwd(ns_ctx* c, double* grad, ns_adjoint_stats* stats) {
 }
 
 int ns_adjoint_get_state_grad(ns_ctx* c, double* const* ubar, double* const* uprevbar, double* pbar) {
+  if (c && c->P.dim == 3) return adjoint_state_grad3(c, ubar, uprevbar, pbar);
   if (!c || !c->adj) return NS_ERR_ARG;
   AdjState& A = *c->adj;
   for (int m = 0; m < 2; ++m) {
@@ -773,6 +718,7 @@ int ns_adjoint_get_state_grad(ns_ctx* c, double* const* ubar, double* const* upr
 int ns_step_jvp(ns_ctx* c, const double* const* du, const double* const* duprev, const double* dp, const double* dc,
                 double* const* du_out, double* const* duprev_out, double* dp_out) {
   if (!c || !du || !duprev || !dp) return NS_ERR_ARG;
+  if (c->P.dim == 3) return step_jvp3(c, du, duprev, dp, du_out, duprev_out, dp_out);
   int r = check_supported(c);
   if (r == NS_OK) r = ensure_adj(c);
   if (r != NS_OK) return r;
@@ -810,6 +756,7 @@ int ns_step_jvp(ns_ctx* c, const double* const* du, const double* const* duprev,
 int ns_step_vjp(ns_ctx* c, const double* const* ubar_out, const double* const* uprevbar_out, const double* pbar_out,
                 double* const* ubar, double* const* uprevbar, double* pbar, double* cbar) {
   if (!c || !ubar_out || !uprevbar_out || !pbar_out) return NS_ERR_ARG;
+  if (c->P.dim == 3) return step_vjp3(c, ubar_out, uprevbar_out, pbar_out, ubar, uprevbar, pbar);
   int r = check_supported(c);
   if (r == NS_OK) r = ensure_adj(c);
   if (r != NS_OK) return r;
@@ -845,6 +792,7 @@ int ns_step_vjp(ns_ctx* c, const double* const* ubar_out, const double* const* u
 
 int ns_adjoint_op(ns_ctx* c, int transpose, const double* const* x, const double* dc, double* const* y, double* cbar) {
   if (!c || !x || !y) return NS_ERR_ARG;
+  if (c->P.dim == 3) return adjoint_op3(c, transpose, x, y);
   int r = check_supported(c);
   if (r == NS_OK) r = ensure_adj(c);
   if (r != NS_OK) return r;

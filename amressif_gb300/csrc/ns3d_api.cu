@@ -11,34 +11,16 @@
 
 #include "ctx.h"
 #include "launch3d.h"
+#include "state3d.h"
 
 using namespace ns;
 using namespace nsh;
 
 namespace nsh {
 
-struct State3D {
-  std::vector<void*> allocs;
-  size_t fb = 0;  // bytes of one level-0 field
-  double* U[3] = {nullptr, nullptr, nullptr};
-  double* UP[3] = {nullptr, nullptr, nullptr};
-  double* DU[3] = {nullptr, nullptr, nullptr};
-  double* S[3] = {nullptr, nullptr, nullptr};
-  double* B[3][3] = {};
-  double* Pp = nullptr;
-  double* PHI = nullptr;
-  double* F = nullptr;
-  double* PH[3] = {nullptr, nullptr, nullptr};  // ghosted cell velocity
-  double* T[3] = {nullptr, nullptr, nullptr};   // cell totals
-  double* FL[3][3] = {};                         // face fluxes
-  double* part = nullptr;
-  MG3<double> M64;
-  MG3<float> M32;
-  int base = -1, cur = -1;
-};
-
 void free3d(ns_ctx* c) {
   if (!c->s3) return;
+  free_adj3(c);
   for (void* p : c->s3->allocs) cudaFree(p);
   delete c->s3;
   c->s3 = nullptr;
@@ -176,6 +158,10 @@ int poisson3(ns_ctx* c, int* cycles, double* res, long long* fallbacks) {
   return status;
 }
 
+}  // namespace
+
+namespace nsh {
+
 // ns_set_state layout of face d: (N + [d==0]) x (N + [d==1]) x (N + [d==2]), x fastest
 cudaMemcpy3DParms copy_parms(ns_ctx* c, int d, const double* host, double* dev, bool put) {
   const int N = c->N;
@@ -205,9 +191,11 @@ int copy_cells3(ns_ctx* c, const double* host, double* dev, bool put) {
   return NS_OK;
 }
 
-}  // namespace
-
-namespace nsh {
+int copy_faces3(ns_ctx* c, int d, const double* host, double* dev, bool put) {
+  cudaMemcpy3DParms q = copy_parms(c, d, host, dev, put);
+  CK(cudaMemcpy3DAsync(&q, c->st), "3D copy");
+  return NS_OK;
+}
 
 int create3d(ns_ctx* c) {
   const int N = c->N;
@@ -265,12 +253,18 @@ int get_state3d(ns_ctx* c, double* const* u, double* const* up, double* p, doubl
   return ns_sync(c);
 }
 
-int step3d(ns_ctx* c, ns_step_stats* stats) {
+double* face3_ptr(ns_ctx* c, int id, int m) { return face3(c, id, m); }
+
+int poisson3d(ns_ctx* c, int* cycles, double* res) {
+  long long fb = 0;
+  return poisson3(c, cycles, res, &fb);
+}
+
+// step begin and the dual-time pseudo-iterations: u* in face3(c, S.cur); the
+// state (U, UP, time) is rotated as in ns_step_begin
+int predictor3d(ns_ctx* c, ns_step_stats* sp) {
   State3D& S = *c->s3;
-  if (c->P.pseudo_timestepping == 0) return fail(c, NS_ERR_UNSUPPORTED, "3D: the explicit predictor is not built");
-  ns_step_stats s;
-  std::memset(&s, 0, sizeof(s));
-  if (c->ev_ok) cudaEventRecord(c->ev[0], c->st);
+  ns_step_stats& s = *sp;
   // ---- step begin: du, S from (u^n, u^{n-1}, p); u^{n-1} buffer becomes the target
   Arg3 a = args(c);
   for (int m = 0; m < 3; ++m) {
@@ -315,6 +309,17 @@ int step3d(ns_ctx* c, ns_step_stats* stats) {
   }
   s.pseudo_iters = count;
   s.norm_error = norm;
+  return NS_OK;
+}
+
+int step3d(ns_ctx* c, ns_step_stats* stats) {
+  State3D& S = *c->s3;
+  if (c->P.pseudo_timestepping == 0) return fail(c, NS_ERR_UNSUPPORTED, "3D: the explicit predictor is not built");
+  ns_step_stats s;
+  std::memset(&s, 0, sizeof(s));
+  if (c->ev_ok) cudaEventRecord(c->ev[0], c->st);
+  int r = predictor3d(c, &s);
+  if (r != NS_OK) return r;
   if (c->ev_ok) cudaEventRecord(c->ev[1], c->st);
   // ---- Poisson right-hand side, solve, projection
   Arg3 p = args(c);
@@ -322,7 +327,7 @@ int step3d(ns_ctx* c, ns_step_stats* stats) {
   p.f = S.F;
   p.red_out = c->red + kRedDivBefore;
   LAUNCH(NS_PROF_POISSON_RHS, "rhs 3d", launch3_rhs(p, c->st));
-  int r = sync_red(c, kRedDivBefore, 2);
+  r = sync_red(c, kRedDivBefore, 2);
   if (r != NS_OK) return r;
   s.div_before = c->red_h[kRedDivBefore];
   s.rhs_sum = c->red_h[kRedSum];
