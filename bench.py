@@ -255,6 +255,56 @@ def cfg5_section(ns, args):
     return out
 
 
+def cfg5_adjoint_section(ns, args):
+    """Adjoint of the final enstrophy E = 1/2 sum |curl u|^2 dV of the 3D
+    Taylor-Green run with respect to the initial velocity (u^{-1} = u^0):
+    Re = 1600, dt = 0.4 h, the seeded 1e-3 perturbation, mixed-precision
+    Poisson solves, binomial checkpointing with 16 snapshots. Times the plain
+    forward run (ns_step) and the ns_step_adjoint_fwd / ns_step_adjoint_bwd
+    pair (wall clock, synchronised); the grid defaults to 128^3 so that the
+    section takes about a minute (--cfg5-adj-n 256 for the full grid)."""
+    import math
+
+    import numpy as np
+    from amressif_gb300 import workloads as wl
+
+    n, L, nsnap = args.cfg5_adj_n, args.cfg5_adj_steps, args.cfg5_adj_snap
+    h = 2 * math.pi / n
+    state = wl.tgv3d_perturbed_state(n, amp=1e-3, seed=0)
+
+    def solver():
+        p = ns.default_params(dim=3, n_cell=n, ren=1600.0, fixed_dt=0.4 * h, iter_num=100, precision=ns.PREC_MIXED,
+                              prob_hi=(2 * math.pi,) * 3, bc_lo=(111,) * 3, bc_hi=(111,) * 3, fix_quirks=1,
+                              poisson_tol_rel=1e-10, poisson_tol_div=1e-10, max_grid_size=(n, n, n))
+        s = ns.Solver(p)
+        s.set_state(*state)
+        return s
+
+    s = solver()
+    s.sync()
+    t0 = time.perf_counter()
+    ks = [s.step()["pseudo_iters"] for _ in range(L)]
+    s.sync()
+    plain_ms = 1e3 * (time.perf_counter() - t0)
+    s.close()
+    s = solver()
+    J, f = s.adjoint_fwd(np.zeros(0), nsteps=L, nsnap=nsnap, lin_tol=1e-12)
+    _, b = s.adjoint_bwd()
+    ub, upb, _ = s.adjoint_state_grad()
+    s.close()
+    g2 = sum(float(np.sum((a + c) ** 2)) for a, c in zip(ub, upb))
+    return {"workload": "3D periodic Taylor-Green %d^3, Re=1600, dt=0.4h, seeded 1e-3 perturbation, %d steps, "
+                        "dE/du^0 of the final enstrophy, %d snapshots, mixed-precision Poisson" % (n, L, nsnap),
+            "plain_forward_ms": plain_ms, "pseudo_iters_mean": float(np.mean(ks)), "J": J,
+            "fwd_ms": f["ms_forward"], "bwd_ms": b["ms_backward"],
+            "ratio": (f["ms_forward"] + b["ms_backward"]) / plain_ms,
+            "steps_advanced": b["steps_advanced"], "predictor_runs": b["predictor_runs"],
+            "bicgstab_iters_per_solve": b["lin_iters"] / max(1, b["adjoint_steps"]),
+            "bicgstab_max_rel_res": b["lin_max_res"],
+            "poisson_cycles_per_solve": b["poisson_cycles"] / max(1, b["adjoint_steps"]),
+            "grad_norm": math.sqrt(g2)}
+
+
 def bench_ours(args):
     world, rank, dist = dist_setup()
     import amressif_gb300 as ns
@@ -377,6 +427,8 @@ def bench_ours(args):
     cfg5 = None
     if rank == 0 and not args.no_cfg5:
         cfg5 = cfg5_section(ns, args)
+        if not args.no_cfg5_adjoint:
+            cfg5["adjoint"] = cfg5_adjoint_section(ns, args)
 
     if rank == 0:
         line = {
@@ -451,6 +503,10 @@ def main():
     ap.add_argument("--no-cfg5", action="store_true")
     ap.add_argument("--cfg5-n", type=int, default=256)
     ap.add_argument("--cfg5-steps", type=int, default=2)
+    ap.add_argument("--no-cfg5-adjoint", action="store_true")
+    ap.add_argument("--cfg5-adj-n", type=int, default=128)
+    ap.add_argument("--cfg5-adj-steps", type=int, default=200)
+    ap.add_argument("--cfg5-adj-snap", type=int, default=16)
     ap.add_argument("--adj-n", type=int, default=512)
     ap.add_argument("--adj-steps", type=int, default=400)
     ap.add_argument("--adj-snap", type=int, default=20)
