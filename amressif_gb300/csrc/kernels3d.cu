@@ -1,5 +1,6 @@
 // Launchers of the 3D kernels (ns3d.cuh).
 #include "ns3d.cuh"  // kernels (before launch3d.h, which includes the argument structs only)
+#include "ns3d_mixed.cuh"
 #include "launch3d.h"
 
 namespace ns {
@@ -40,6 +41,27 @@ cudaError_t launch3_project(const Arg3& a, cudaStream_t s) {
 cudaError_t launch3_div(const Arg3& a, cudaStream_t s) {
   const int N = a.g.N;
   k3_div<<<grid3(N, N, N), 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+cudaError_t launch3_anchor_face(const Arg3& a, const Anc3& o, cudaStream_t s) {
+  const int N = a.g.N;
+  k3_anchor_face<<<grid3(N + 1, N + 1, N + 1), 256, 0, s>>>(a, o);
+  return cudaGetLastError();
+}
+cudaError_t launch3i_cart(const Inc3& a, cudaStream_t s) {
+  const int N = a.g.N;
+  k3i_cart<<<grid3(N + 4, N + 4, N + 4), 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+cudaError_t launch3i_total(const Inc3& a, cudaStream_t s) {
+  const int N = a.g.N;
+  k3i_flux<<<grid3(N + 1, N + 1, N + 1), 256, 0, s>>>(a);
+  k3i_total<<<grid3(N, N, N), 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+cudaError_t launch3i_face(const Inc3& a, cudaStream_t s) {
+  const int N = a.g.N;
+  k3i_face<<<grid3(N + 1, N + 1, N + 1), 256, 0, s>>>(a);
   return cudaGetLastError();
 }
 long blocks3_face(int N) { return (long)((N + 1 + 31) / 32) * ((N + 1 + 7) / 8) * (N + 1); }

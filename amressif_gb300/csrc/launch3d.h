@@ -4,6 +4,7 @@
 
 #define NS_3D_ARGS_ONLY
 #include "ns3d.cuh"
+#include "ns3d_mixed.cuh"
 #undef NS_3D_ARGS_ONLY
 
 namespace ns {
@@ -16,6 +17,11 @@ cudaError_t launch3_rhs(const Arg3& a, cudaStream_t s);
 cudaError_t launch3_project(const Arg3& a, cudaStream_t s);
 cudaError_t launch3_div(const Arg3& a, cudaStream_t s);
 long blocks3_face(int N);  // blocks of the largest reducing launch
+// mixed-precision predictor (ns3d_mixed.cuh)
+cudaError_t launch3_anchor_face(const Arg3& a, const Anc3& o, cudaStream_t s);
+cudaError_t launch3i_cart(const Inc3& a, cudaStream_t s);
+cudaError_t launch3i_total(const Inc3& a, cudaStream_t s);  // flux increments, then cell totals
+cudaError_t launch3i_face(const Inc3& a, cudaStream_t s);
 
 template <typename T>
 cudaError_t launch3_mg_rb(const MG3<T>& M, int l, int color, cudaStream_t s);

@@ -1,7 +1,8 @@
 // Host driver of the 3D advance (dim = 3): the time loop of main_main
-// (main.cpp:875-1180) over the kernels of ns3d.cuh. The 3D context supports
-// the whole-step API (ns_step, ns_set_state / ns_get_state, checkpoints);
-// the per-call-site building blocks and the adjoint are 2D only.
+// (main.cpp:875-1180) over the kernels of ns3d.cuh (FP64 predictor) and
+// ns3d_mixed.cuh (mixed-precision predictor). The 3D context supports the
+// whole-step API (ns_step, ns_set_state / ns_get_state, checkpoints) and the
+// adjoint (adjoint3d_api.cu); the per-call-site building blocks are 2D only.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -216,7 +217,16 @@ int create3d(ns_ctx* c) {
   if (r == NS_OK) r = alloc3(c, &S.F, S.fb);
   if (r == NS_OK) r = alloc3(c, &S.part, (size_t)4 * (blocks3_face(N) + 1024) * sizeof(double));
   if (r == NS_OK) r = levels3<double>(c, S.M64, false);
-  if (r == NS_OK && c->P.precision == NS_PREC_MIXED) r = levels3<float>(c, S.M32, true);
+  if (r == NS_OK && c->P.precision == NS_PREC_MIXED) {
+    r = levels3<float>(c, S.M32, true);
+    const size_t f32 = S.fb / 2, g32 = (size_t)(N + 4) * (N + 4) * (N + 4) * sizeof(float);
+    for (int m = 0; m < 3 && r == NS_OK; ++m) {
+      float** fs[] = {&S.UB32[m], &S.G0[m], &S.E[0][m], &S.E[1][m]};
+      for (float** p : fs)
+        if (r == NS_OK) r = alloc3(c, p, f32);
+      if (r == NS_OK) r = alloc3(c, &S.PHB32[m], g32);
+    }
+  }
   return r;
 }
 
@@ -260,6 +270,70 @@ int poisson3d(ns_ctx* c, int* cycles, double* res) {
   return poisson3(c, cycles, res, &fb);
 }
 
+}  // namespace nsh
+
+namespace {
+
+// One pseudo-iteration of the mixed-precision predictor (ns3d_mixed.cuh):
+// the FP64 anchor G0 = G(u_b), three FP32 increment stages, u_b + e4 (FP64)
+// into a free buffer, the pseudo-norm of e4 into red[kRedNorm]
+int mixed_iteration3(ns_ctx* c) {
+  State3D& S = *c->s3;
+  Arg3 b = args(c);
+  for (int m = 0; m < 3; ++m) {
+    b.u[m] = face3(c, S.base, m);
+    b.ub[m] = face3(c, S.base, m);
+    b.S[m] = S.S[m];
+  }
+  LAUNCH(NS_PROF_ANCHOR, "anchor cart 3d", launch3_cart(b, c->st));
+  LAUNCH(NS_PROF_ANCHOR, "anchor total 3d", launch3_total(b, c->st));
+  Anc3 o;
+  for (int m = 0; m < 3; ++m) {
+    o.g0[m] = S.G0[m];
+    o.ub[m] = S.UB32[m];
+  }
+  LAUNCH(NS_PROF_ANCHOR, "anchor face 3d", launch3_anchor_face(b, o, c->st));
+  Inc3 q;
+  std::memset(&q, 0, sizeof(q));
+  q.g = c->g;
+  const int outb = pick3(S.base, S.base);
+  for (int m = 0; m < 3; ++m) {
+    q.ub[m] = S.UB32[m];
+    q.g0[m] = S.G0[m];
+    q.phb[m] = S.PHB32[m];
+    q.phe[m] = reinterpret_cast<float*>(S.PH[m]);
+    q.dt[m] = reinterpret_cast<float*>(S.T[m]);
+    for (int d = 0; d < 3; ++d) q.dfl[d][m] = reinterpret_cast<float*>(S.FL[d][m]);
+    q.base64[m] = face3(c, S.base, m);
+    q.out64[m] = S.B[outb][m];
+    q.inv_dx[m] = (float)c->g.inv_dx[m];
+    q.vcoef[m] = (float)(c->g.inv_dx2[m] * c->g.inv_ren);
+  }
+  q.c15 = (float)c->g.c15;
+  q.part = S.part;
+  q.counter = c->counter;
+  q.norm_out = c->red + kRedNorm;
+  for (int s = 1; s <= 3; ++s) {
+    for (int m = 0; m < 3; ++m) {
+      q.ein[m] = s == 1 ? nullptr : S.E[s == 2 ? 0 : 1][m];
+      q.eout[m] = S.E[s == 1 ? 0 : 1][m];
+    }
+    q.rk_prev = (float)c->rk[s - 1];
+    q.rk = (float)c->rk[s];
+    q.first = s == 1;
+    q.last = s == 3;
+    LAUNCH(NS_PROF_INC, "increment cart 3d", launch3i_cart(q, c->st));
+    LAUNCH(NS_PROF_INC, "increment total 3d", launch3i_total(q, c->st));
+    LAUNCH(NS_PROF_INC, "increment face 3d", launch3i_face(q, c->st));
+  }
+  S.cur = outb;
+  return NS_OK;
+}
+
+}  // namespace
+
+namespace nsh {
+
 // step begin and the dual-time pseudo-iterations: u* in face3(c, S.cur); the
 // state (U, UP, time) is rotated as in ns_step_begin
 int predictor3d(ns_ctx* c, ns_step_stats* sp) {
@@ -279,10 +353,14 @@ int predictor3d(ns_ctx* c, ns_step_stats* sp) {
   c->time += c->dt;
   S.base = S.cur = -1;
   // ---- dual-time pseudo-iterations (main.cpp:898-1040)
+  const bool mixed = c->P.precision == NS_PREC_MIXED;
   int count = 0;
   double norm = 1.e9;
   while (norm > c->P.momentum_tolerance) {
-    for (int sub = 0; sub < 4; ++sub) {
+    if (mixed) {
+      int r = mixed_iteration3(c);
+      if (r != NS_OK) return r;
+    } else for (int sub = 0; sub < 4; ++sub) {
       const int outb = pick3(S.base, S.cur);
       Arg3 b = args(c);
       for (int m = 0; m < 3; ++m) {

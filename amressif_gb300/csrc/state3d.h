@@ -25,6 +25,12 @@ struct State3D {
   double* T[3] = {nullptr, nullptr, nullptr};   // cell totals
   double* FL[3][3] = {};                         // face fluxes
   double* part = nullptr;
+  // mixed-precision predictor (FP32): u_b copy, anchor G0, increments, base
+  // cell velocity; the flux / total / cell-velocity increments reuse FL, T, PH
+  float* UB32[3] = {nullptr, nullptr, nullptr};
+  float* G0[3] = {nullptr, nullptr, nullptr};
+  float* E[2][3] = {};
+  float* PHB32[3] = {nullptr, nullptr, nullptr};
   ns::MG3<double> M64;
   ns::MG3<float> M32;
   int base = -1, cur = -1;

@@ -1,8 +1,9 @@
 """The 3D advance (dim = 3): per-step parity with the oracle's 3D restatement
 (lid cavity with walls on every side; perturbed periodic Taylor-Green in the
 reference's parity mode and in the physical mode), the mixed-precision
-Poisson solve (FP32 V-cycles inside FP64 defect correction) against the FP64
-one, and the discrete divergence after every step.
+predictor (FP64 anchor, FP32 increment stages) and Poisson solve (FP32
+V-cycles inside FP64 defect correction) against the FP64 ones, and the
+discrete divergence after every step.
 
 Tolerances: relative L2 <= 1e-10 per step in u, v, w and p (p modulo its
 constant), identical pseudo-iteration counts; mixed vs FP64 <= 1e-10."""
@@ -92,6 +93,29 @@ def test_3d_mixed_poisson_matches_fp64(gpu_lib):
     for d in range(3):
         assert rel(ub[d], ua[d]) <= 1e-10
     assert relp(pb, pa) <= 1e-10
+
+
+@pytest.mark.parametrize("name", sorted(CASES3))
+def test_3d_mixed_predictor_matches_fp64(gpu_lib, name):
+    """FP64 anchor + FP32 increment stages against the FP64 predictor on the
+    same steps (both with FP64-accurate Poisson solves): identical
+    pseudo-iteration counts and u, p within 1e-11 (relative L2)."""
+    n, kw, tgv = CASES3[name]
+    dt = dt_of(n, kw)
+    out = {}
+    for prec in (ns.PREC_FP64, ns.PREC_MIXED):
+        p = ns.default_params(dim=3, n_cell=n, fixed_dt=dt, iter_num=100, precision=prec, poisson_tol_rel=1e-13,
+                              max_grid_size=(n, n, n), **kw)
+        s = ns.Solver(p)
+        s.set_state(*state3(n, tgv))
+        ks = [s.step()["pseudo_iters"] for _ in range(4)]
+        out[prec] = (ks, s.get_state())
+        s.close()
+    assert out[ns.PREC_FP64][0] == out[ns.PREC_MIXED][0]
+    (ua, _, pa, _), (ub, _, pb, _) = out[ns.PREC_FP64][1], out[ns.PREC_MIXED][1]
+    for d in range(3):
+        assert rel(ub[d], ua[d]) <= 1e-11, (d, rel(ub[d], ua[d]))
+    assert relp(pb, pa) <= 1e-11, relp(pb, pa)
 
 
 def test_3d_building_blocks_are_2d_only(gpu_lib):
