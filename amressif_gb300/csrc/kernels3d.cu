@@ -43,9 +43,20 @@ cudaError_t launch3_div(const Arg3& a, cudaStream_t s) {
   k3_div<<<grid3(N, N, N), 256, 0, s>>>(a);
   return cudaGetLastError();
 }
-cudaError_t launch3_anchor_face(const Arg3& a, const Anc3& o, cudaStream_t s) {
+cudaError_t launch3f_cart(const AncFF& a, cudaStream_t s) {
   const int N = a.g.N;
-  k3_anchor_face<<<grid3(N + 1, N + 1, N + 1), 256, 0, s>>>(a, o);
+  k3f_cart<<<grid3(N + 4, N + 4, N + 4), 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+cudaError_t launch3f_total(const AncFF& a, cudaStream_t s) {
+  const int N = a.g.N;
+  k3f_flux<<<grid3(N + 1, N + 1, N + 1), 256, 0, s>>>(a);
+  k3f_total<<<grid3(N, N, N), 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+cudaError_t launch3f_face(const AncFF& a, cudaStream_t s) {
+  const int N = a.g.N;
+  k3f_face<<<grid3(N + 1, N + 1, N + 1), 256, 0, s>>>(a);
   return cudaGetLastError();
 }
 cudaError_t launch3i_cart(const Inc3& a, cudaStream_t s) {

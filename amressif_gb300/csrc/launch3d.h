@@ -18,7 +18,9 @@ cudaError_t launch3_project(const Arg3& a, cudaStream_t s);
 cudaError_t launch3_div(const Arg3& a, cudaStream_t s);
 long blocks3_face(int N);  // blocks of the largest reducing launch
 // mixed-precision predictor (ns3d_mixed.cuh)
-cudaError_t launch3_anchor_face(const Arg3& a, const Anc3& o, cudaStream_t s);
+cudaError_t launch3f_cart(const AncFF& a, cudaStream_t s);
+cudaError_t launch3f_total(const AncFF& a, cudaStream_t s);  // fluxes, then cell totals
+cudaError_t launch3f_face(const AncFF& a, cudaStream_t s);
 cudaError_t launch3i_cart(const Inc3& a, cudaStream_t s);
 cudaError_t launch3i_total(const Inc3& a, cudaStream_t s);  // flux increments, then cell totals
 cudaError_t launch3i_face(const Inc3& a, cudaStream_t s);

@@ -274,25 +274,36 @@ int poisson3d(ns_ctx* c, int* cycles, double* res) {
 
 namespace {
 
+// (hi, lo) float pair of an FP64 constant
+void split2(double x, float* out) {
+  out[0] = (float)x;
+  out[1] = (float)(x - (double)out[0]);
+}
+
 // One pseudo-iteration of the mixed-precision predictor (ns3d_mixed.cuh):
-// the FP64 anchor G0 = G(u_b), three FP32 increment stages, u_b + e4 (FP64)
-// into a free buffer, the pseudo-norm of e4 into red[kRedNorm]
+// the float-float anchor G0 = G(u_b), three FP32 increment stages, u_b + e4
+// (FP64) into a free buffer, the pseudo-norm of e4 into red[kRedNorm]
 int mixed_iteration3(ns_ctx* c) {
   State3D& S = *c->s3;
-  Arg3 b = args(c);
+  AncFF f;
+  std::memset(&f, 0, sizeof(f));
+  f.g = c->g;
   for (int m = 0; m < 3; ++m) {
-    b.u[m] = face3(c, S.base, m);
-    b.ub[m] = face3(c, S.base, m);
-    b.S[m] = S.S[m];
+    f.u[m] = face3(c, S.base, m);
+    f.S[m] = S.S[m];
+    f.ph[m] = reinterpret_cast<float2*>(S.PH[m]);
+    f.ph32[m] = S.PHB32[m];
+    f.t[m] = reinterpret_cast<float2*>(S.T[m]);
+    for (int d = 0; d < 3; ++d) f.fl[d][m] = reinterpret_cast<float2*>(S.FL[d][m]);
+    f.g0[m] = S.G0[m];
+    f.ub[m] = S.UB32[m];
+    split2(c->g.inv_dx[m], f.inv_dx[m]);
+    split2(c->g.inv_dx2[m] * c->g.inv_ren, f.vcoef[m]);
   }
-  LAUNCH(NS_PROF_ANCHOR, "anchor cart 3d", launch3_cart(b, c->st));
-  LAUNCH(NS_PROF_ANCHOR, "anchor total 3d", launch3_total(b, c->st));
-  Anc3 o;
-  for (int m = 0; m < 3; ++m) {
-    o.g0[m] = S.G0[m];
-    o.ub[m] = S.UB32[m];
-  }
-  LAUNCH(NS_PROF_ANCHOR, "anchor face 3d", launch3_anchor_face(b, o, c->st));
+  split2(c->g.c15, f.c15);
+  LAUNCH(NS_PROF_ANCHOR, "anchor cart 3d", launch3f_cart(f, c->st));
+  LAUNCH(NS_PROF_ANCHOR, "anchor total 3d", launch3f_total(f, c->st));
+  LAUNCH(NS_PROF_ANCHOR, "anchor face 3d", launch3f_face(f, c->st));
   Inc3 q;
   std::memset(&q, 0, sizeof(q));
   q.g = c->g;
@@ -320,7 +331,6 @@ int mixed_iteration3(ns_ctx* c) {
     }
     q.rk_prev = (float)c->rk[s - 1];
     q.rk = (float)c->rk[s];
-    q.first = s == 1;
     q.last = s == 3;
     LAUNCH(NS_PROF_INC, "increment cart 3d", launch3i_cart(q, c->st));
     LAUNCH(NS_PROF_INC, "increment total 3d", launch3i_total(q, c->st));

@@ -1,19 +1,23 @@
 // Mixed-precision 3D predictor (NS_PREC_MIXED): each pseudo-iteration
 // evaluates the BDF2 residual G at u_b, u_b + e1, u_b + e2, u_b + e3
-// (main.cpp:945-1014). The anchor G0 = G(u_b) is computed in FP64 by the
-// cart / flux / total passes of ns3d.cuh and k3_anchor_face below, which
-// rounds G0 and u_b to FP32. The three other stages evaluate only the
-// increment dG(u_b; e) = G(u_b + e) - G0 in FP32:
+// (main.cpp:945-1014). The anchor G0 = G(u_b) is computed in float-float
+// arithmetic (ff.cuh, about 48 bits, on the FP32 pipes) by four passes that
+// mirror the FP64 ones of ns3d.cuh: cell velocity with ghosts, QUICK fluxes,
+// cell totals, face residual; it rounds G0 and u_b to FP32. The three other
+// stages evaluate only the increment dG(u_b; e) = G(u_b + e) - G0 in FP32:
 //   dF = (un+ - ub+) Q+(phi_b) + (un- - ub-) Q-(phi_b) + un Q_sign(un)(phi_e)
 // for the QUICK flux F = u+ Q+(phi) + u- Q-(phi) (fn_flux_calc.cpp:66-76),
 // with un = ub + e and the positive-part difference un+ - ub+ taken from the
 // signs (e, -ub or max(un, 0)), so no term subtracts nearly equal FP32
 // numbers; the viscous term, the ghost rules (homogeneous for the increment)
 // and the flux-ghost rule of the faces are linear. Every FP32 rounding error
-// is proportional to the increment, so the fixed point is the FP64 one. The
-// last stage writes u_b + e4 in FP64 and the pseudo-norm of e4 (the
-// Error_Computation norm, utilities.cpp:421-493).
+// is proportional to the increment, so the fixed point is the float-float
+// one, within a few units of 1e-15 of the FP64 one. The last stage writes
+// u_b + e4 in FP64 and the pseudo-norm of e4 (the Error_Computation norm,
+// utilities.cpp:421-493); no other pass issues an FP64 arithmetic
+// instruction.
 #pragma once
+#include "ff.cuh"
 #include "ns3d.cuh"
 
 namespace ns {
@@ -24,34 +28,152 @@ struct Inc3 {
   const float* g0[3];      // G(u_b) rounded to FP32 (faces)
   const float* ein[3];     // stage input increment; nullptr: rk_prev * g0
   float* eout[3];          // stage output increment (not written by the last stage)
-  float* phb[3];           // ghosted FP32 cell velocity of u_b, (N+4)^3
-  float* phe[3];           // ghosted cell velocity of the increment
+  const float* phb[3];     // ghosted FP32 cell velocity of u_b, (N+4)^3
+  float* phe[3];           // ghosted cell velocity of the increment, (N+4)^3
   float* dfl[3][3];        // flux increments dfl[d][m] at the faces along d
   float* dt[3];            // cell total increments
   const double* base64[3]; // u_b (last stage)
   double* out64[3];        // u_b + e4 (last stage)
   float rk_prev, rk, c15;
   float inv_dx[3], vcoef[3];  // 1/dx, 1/(Re dx^2)
-  int first, last;
+  int last;
   double* part;
   unsigned* counter;
   double* norm_out;
 };
 
-struct Anc3 {
-  float* g0[3];
-  float* ub[3];
+// float-float anchor: values are (hi, lo) float pairs
+struct AncFF {
+  Geom g;
+  const double* u[3];  // u_b (faces)
+  const double* S[3];  // step source (faces)
+  float2* ph[3];       // ghosted cell velocity, (N+4)^3
+  float* ph32[3];      // the same rounded to FP32: the base cell velocity of the increments
+  float2* fl[3][3];    // fluxes fl[d][m] at the faces along d
+  float2* t[3];        // cell totals
+  float* g0[3];        // G(u_b) rounded to FP32
+  float* ub[3];        // u_b rounded to FP32
+  float inv_dx[3][2], vcoef[3][2], c15[2];  // constants as (hi, lo)
 };
 
 #ifndef NS_3D_ARGS_ONLY
 
-__device__ __forceinline__ float inc_e(const Inc3& A, int m, long id) {
-  return A.ein[m] ? A.ein[m][id] : A.rk_prev * A.g0[m][id];
+__device__ __forceinline__ ff ld_ff(const double* p, long i) { return ff_from_double(p[i]); }
+__device__ __forceinline__ ff ld2(const float2* p, long i) {
+  const float2 v = p[i];
+  return ff_make(v.x, v.y);
+}
+__device__ __forceinline__ void st2(float2* p, long i, ff v) { p[i] = make_float2(v.hi, v.lo); }
+__device__ __forceinline__ ff ffc(const float (&c)[2]) { return ff_make(c[0], c[1]); }
+__device__ __forceinline__ float ff_round(ff v) { return v.hi + v.lo; }
+
+// ---- float-float anchor ----------------------------------------------------------------
+// ghosted cell velocity of u_b (the rules of k3_cart)
+__global__ void __launch_bounds__(256) k3f_cart(AncFF A) {
+  const Geom& g = A.g;
+  const int N = g.N;
+  NS3_IJK(2, 2, 2)
+  if (i > N + 1 || j > N + 1 || k > N + 1) return;
+  const int c[3] = {i, j, k};
+  int out_d = -1, nout = 0;
+  for (int d = 0; d < 3; ++d)
+    if (c[d] < 0 || c[d] >= N) { out_d = d; ++nout; }
+  int cm[3] = {i, j, k};
+  int side = 0;
+  if (nout == 1) {
+    const int d = out_d;
+    side = c[d] < 0 ? 0 : 1;
+    cm[d] = g.periodic[d] ? wrapi(c[d], N) : (c[d] < 0 ? -c[d] - 1 : 2 * N - 1 - c[d]);
+  }
+  const bool mirror = nout == 1 && !g.periodic[out_d];
+  const long gi = gid3(N, i, j, k);
+  for (int m = 0; m < 3; ++m) {
+    ff v = ff_make(0.f, 0.f);
+    if (nout <= 1) {
+      const long a = id3(g, cm[0], cm[1], cm[2]);
+      const long b = a + (m == 0 ? 1 : (m == 1 ? g.pitch : g.plane));
+      v = ff_scale2(ld_ff(A.u[m], a) + ld_ff(A.u[m], b), 0.5f);
+      if (mirror) {
+        const CartBC& bc = g.bc[2 * out_d + side];
+        const int r = bc.rule[m];
+        if (r == kInlet) v = ff_from_double(bc.add[m]) - v;
+        else if (r == kNeg) v = -v;
+      }
+    }
+    st2(A.ph[m], gi, v);
+    A.ph32[m][gi] = ff_round(v);
+  }
 }
 
-// G0 = S - (1.5/dt) u_b + avg(t) (FP64, as k3_face with u = u_b), rounded to
-// FP32 together with u_b
-__global__ void __launch_bounds__(256) k3_anchor_face(Arg3 A, Anc3 O) {
+// u > 0: 3/4 x(-1) + 3/8 x(0) - 1/8 x(-2); u <= 0: 3/8 x(-1) + 3/4 x(0) - 1/8 x(+1)
+__device__ __forceinline__ ff q3p_ff(ff x2, ff x1, ff x0) { return (0.75f * x1 + 0.375f * x0) + ff_scale2(x2, -0.125f); }
+__device__ __forceinline__ ff q3m_ff(ff x1, ff x0, ff xa) { return (0.375f * x1 + 0.75f * x0) + ff_scale2(xa, -0.125f); }
+
+// QUICK fluxes of the three components at every face along the three
+// directions, each face once (the faces of k3_flux)
+__global__ void __launch_bounds__(256) k3f_flux(AncFF A) {
+  const Geom& g = A.g;
+  const int N = g.N;
+  NS3_IJK(0, 0, 0)
+  if (i > N || j > N || k > N) return;
+  const long G1[3] = {1, N + 4, (long)(N + 4) * (N + 4)};
+  const long gc = gid3(N, i, j, k);
+  const long fc = id3(g, i, j, k);
+  const int c[3] = {i, j, k};
+  for (int d = 0; d < 3; ++d) {
+    bool ok = true;
+    for (int e = 0; e < 3; ++e)
+      if (e != d && c[e] >= N) ok = false;
+    if (!ok) continue;
+    const long s = G1[d];
+    const ff ud = ld_ff(A.u[d], fc);
+    for (int m = 0; m < 3; ++m) {
+      const float2* ph = A.ph[m];
+      ff F = ff_make(0.f, 0.f);
+      if (ud.hi > 0.f) F = ud * q3p_ff(ld2(ph, gc - 2 * s), ld2(ph, gc - s), ld2(ph, gc));
+      else if (ud.hi < 0.f) F = ud * q3m_ff(ld2(ph, gc - s), ld2(ph, gc), ld2(ph, gc + s));
+      st2(A.fl[d][m], fc, F);
+    }
+  }
+}
+
+// t_m = nu lap(phi_m) - div F_m at the cells
+__global__ void __launch_bounds__(256) k3f_total(AncFF A) {
+  const Geom& g = A.g;
+  const int N = g.N;
+  NS3_IJK(0, 0, 0)
+  if (i >= N || j >= N || k >= N) return;
+  const long G1[3] = {1, N + 4, (long)(N + 4) * (N + 4)};
+  const long gc = gid3(N, i, j, k);
+  const long fc = id3(g, i, j, k);
+  const long fstride[3] = {1, g.pitch, g.plane};
+  for (int m = 0; m < 3; ++m) {
+    const float2* ph = A.ph[m];
+    const ff p2 = ff_scale2(ld2(ph, gc), 2.f);
+    ff acc = ff_make(0.f, 0.f);
+    for (int d = 0; d < 3; ++d) {
+      const long s = G1[d];
+      const float2* F = A.fl[d][m];
+      const ff lap = (ld2(ph, gc + s) + ld2(ph, gc - s)) - p2;
+      acc = acc + (ffc(A.vcoef[d]) * lap - ffc(A.inv_dx[d]) * (ld2(F, fc + fstride[d]) - ld2(F, fc)));
+    }
+    st2(A.t[m], fc, acc);
+  }
+}
+
+__device__ __forceinline__ ff t_along_ff(const AncFF& A, int m, int a, long base, long st) {
+  const int N = A.g.N;
+  if (a >= 0 && a < N) return ld2(A.t[m], base + a * st);
+  const int fg = A.g.flux_ghost[m];
+  if (fg == kWrap) return ld2(A.t[m], base + (long)wrapi(a, N) * st);
+  if (fg == kZero) return ff_make(0.f, 0.f);
+  const int am = a < 0 ? 0 : N - 1;
+  return -ld2(A.t[m], base + (long)am * st);
+}
+
+// G0 = S - (1.5/dt) u_b + avg(t) with the flux-ghost rule (k3_face with
+// u = u_b), rounded to FP32 together with u_b
+__global__ void __launch_bounds__(256) k3f_face(AncFF A) {
   const Geom& g = A.g;
   const int N = g.N;
   NS3_IJK(0, 0, 0)
@@ -64,16 +186,21 @@ __global__ void __launch_bounds__(256) k3_anchor_face(Arg3 A, Anc3 O) {
     const long id = id3(g, i, j, k);
     const long st = fstride[m];
     const long base = id - (long)a * st;
-    const double tl = t_along(A, m, a - 1, base, st), tr = t_along(A, m, a, base, st);
-    const double u = A.u[m][id];
-    const double G = (A.S[m][id] - g.c15 * u) + 0.5 * (tl + tr);
-    O.g0[m][id] = (float)G;
-    O.ub[m][id] = (float)u;
+    const ff tl = t_along_ff(A, m, a - 1, base, st), tr = t_along_ff(A, m, a, base, st);
+    const ff u = ld_ff(A.u[m], id);
+    const ff G = (ld_ff(A.S[m], id) - ffc(A.c15) * u) + ff_scale2(tl + tr, 0.5f);
+    A.g0[m][id] = ff_round(G);
+    A.ub[m][id] = ff_round(u);
   }
 }
 
-// ghosted cell velocity of the increment (homogeneous ghosts) and, in the
-// first stage, of u_b; cells with more than one index outside [0, N) are 0
+// ---- FP32 increment stages ----------------------------------------------------------------
+__device__ __forceinline__ float inc_e(const Inc3& A, int m, long id) {
+  return A.ein[m] ? A.ein[m][id] : A.rk_prev * A.g0[m][id];
+}
+
+// ghosted cell velocity of the increment (homogeneous ghosts); cells with
+// more than one index outside [0, N) are 0
 __global__ void __launch_bounds__(256) k3i_cart(Inc3 A) {
   const Geom& g = A.g;
   const int N = g.N;
@@ -93,20 +220,14 @@ __global__ void __launch_bounds__(256) k3i_cart(Inc3 A) {
   const bool mirror = nout == 1 && !g.periodic[out_d];
   const long gi = gid3(N, i, j, k);
   for (int m = 0; m < 3; ++m) {
-    float ve = 0.f, vb = 0.f;
+    float ve = 0.f;
     if (nout <= 1) {
       const long a = id3(g, cm[0], cm[1], cm[2]);
       const long b = a + (m == 0 ? 1 : (m == 1 ? g.pitch : g.plane));
       ve = 0.5f * (inc_e(A, m, a) + inc_e(A, m, b));
-      if (A.first) vb = 0.5f * (A.ub[m][a] + A.ub[m][b]);
-      if (mirror) {
-        const CartBC& bc = g.bc[2 * out_d + side];
-        ve = cart_ghost_f(bc, m, ve, true);
-        if (A.first) vb = cart_ghost_f(bc, m, vb, false);
-      }
+      if (mirror) ve = cart_ghost_f(g.bc[2 * out_d + side], m, ve, true);
     }
     A.phe[m][gi] = ve;
-    if (A.first) A.phb[m][gi] = vb;
   }
 }
 
