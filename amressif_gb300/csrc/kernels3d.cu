@@ -59,6 +59,23 @@ cudaError_t launch3f_face(const AncFF& a, cudaStream_t s) {
   k3f_face<<<grid3(N + 1, N + 1, N + 1), 256, 0, s>>>(a);
   return cudaGetLastError();
 }
+cudaError_t launch3f_store(const Geom& g, const float2* const* in, double* const* out, cudaStream_t s) {
+  const int N = g.N;
+  k3f_store<<<grid3(N + 1, N + 1, N + 1), 256, 0, s>>>(g, in[0], in[1], in[2], out[0], out[1], out[2]);
+  return cudaGetLastError();
+}
+cudaError_t launch3_dcff(const DCff3& a, cudaStream_t s) {
+  k3_dcff<<<grid3(a.n, a.n, a.n), 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+cudaError_t launch3_rhs_ff(int n, long pitch, long plane, const double* f, const double* mean, float2* out, cudaStream_t s) {
+  k3_rhs_ff<<<grid3(n, n, n), 256, 0, s>>>(n, pitch, plane, f, mean, out);
+  return cudaGetLastError();
+}
+cudaError_t launch3_ff_cells(int n, long pitch, long plane, const float2* in, double* out, cudaStream_t s) {
+  k3_ff_cells<<<grid3(n, n, n), 256, 0, s>>>(n, pitch, plane, in, out);
+  return cudaGetLastError();
+}
 cudaError_t launch3i_cart(const Inc3& a, cudaStream_t s) {
   const int N = a.g.N;
   k3i_cart<<<grid3(N + 4, N + 4, N + 4), 256, 0, s>>>(a);
@@ -104,16 +121,6 @@ template <typename T>
 cudaError_t launch3_mg_resnorm(const MG3<T>& M, double* part, unsigned* counter, double* out, cudaStream_t s) {
   const int n = M.n[0];
   k3_mg_resnorm<T><<<grid3(n, n, n), 256, 0, s>>>(M, part, counter, out);
-  return cudaGetLastError();
-}
-cudaError_t launch3_dc_add(const MG3<double>& M, const float* e, cudaStream_t s) {
-  const int n = M.n[0];
-  k3_dc_add<<<grid3(n, n, n), 256, 0, s>>>(M, e);
-  return cudaGetLastError();
-}
-cudaError_t launch3_dc_res(const MG3<double>& M, float* r32, double* part, unsigned* counter, double* out, cudaStream_t s) {
-  const int n = M.n[0];
-  k3_dc_res<<<grid3(n, n, n), 256, 0, s>>>(M, r32, part, counter, out);
   return cudaGetLastError();
 }
 

@@ -21,6 +21,10 @@ long blocks3_face(int N);  // blocks of the largest reducing launch
 cudaError_t launch3f_cart(const AncFF& a, cudaStream_t s);
 cudaError_t launch3f_total(const AncFF& a, cudaStream_t s);  // fluxes, then cell totals
 cudaError_t launch3f_face(const AncFF& a, cudaStream_t s);
+cudaError_t launch3f_store(const Geom& g, const float2* const* in, double* const* out, cudaStream_t s);
+cudaError_t launch3_dcff(const DCff3& a, cudaStream_t s);
+cudaError_t launch3_rhs_ff(int n, long pitch, long plane, const double* f, const double* mean, float2* out, cudaStream_t s);
+cudaError_t launch3_ff_cells(int n, long pitch, long plane, const float2* in, double* out, cudaStream_t s);
 cudaError_t launch3i_cart(const Inc3& a, cudaStream_t s);
 cudaError_t launch3i_total(const Inc3& a, cudaStream_t s);  // flux increments, then cell totals
 cudaError_t launch3i_face(const Inc3& a, cudaStream_t s);
@@ -35,7 +39,5 @@ template <typename T>
 cudaError_t launch3_mg_bottom(const MG3<T>& M, int l, int sweeps, cudaStream_t s);
 template <typename T>
 cudaError_t launch3_mg_resnorm(const MG3<T>& M, double* part, unsigned* counter, double* out, cudaStream_t s);
-cudaError_t launch3_dc_add(const MG3<double>& M, const float* e, cudaStream_t s);
-cudaError_t launch3_dc_res(const MG3<double>& M, float* r32, double* part, unsigned* counter, double* out, cudaStream_t s);
 
 }  // namespace ns

@@ -435,33 +435,6 @@ __global__ void __launch_bounds__(256) k3_mg_resnorm(MG3<T> M, double* part, uns
   if (grid_reduce_last<1>(v, part, counter, 1u) && threadIdx.x == 0) red_out[0] = v[0];
 }
 
-// defect correction of the mixed solve: phi += e (FP32); then r = f - mean -
-// L phi in FP64 into r32 (the FP32 hierarchy's level-0 f), max |r| reduced
-__global__ void __launch_bounds__(256) k3_dc_add(MG3<double> M, const float* e) {
-  const int n = M.n[0];
-  const int i = blockIdx.x * 32 + (threadIdx.x & 31), j = blockIdx.y * 8 + (threadIdx.x >> 5), k = blockIdx.z;
-  if (i >= n || j >= n || k >= n) return;
-  const long id = (long)k * M.plane[0] + (long)j * M.pitch[0] + i;
-  M.x[0][id] += (double)e[id];
-}
-
-__global__ void __launch_bounds__(256) k3_dc_res(MG3<double> M, float* r32, double* part, unsigned* counter,
-                                                 double* red_out) {
-  const int n = M.n[0];
-  const int i = blockIdx.x * 32 + (threadIdx.x & 31), j = blockIdx.y * 8 + (threadIdx.x >> 5), k = blockIdx.z;
-  double v[1] = {0.0};
-  if (i < n && j < n && k < n) {
-    const long id = (long)k * M.plane[0] + (long)j * M.pitch[0] + i;
-    const double xc = M.x[0][id];
-    double dg;
-    const double s = mg3_lap_terms(M, 0, i, j, k, xc, &dg);
-    const double r = mg3_f(M, 0, id) - (s - dg * xc);
-    r32[id] = (float)r;
-    v[0] = fabs(r);
-  }
-  if (grid_reduce_last<1>(v, part, counter, 1u) && threadIdx.x == 0) red_out[0] = v[0];
-}
-
 #endif  // NS_3D_ARGS_ONLY
 
 }  // namespace ns

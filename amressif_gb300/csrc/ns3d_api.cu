@@ -124,12 +124,41 @@ int poisson3(ns_ctx* c, int* cycles, double* res, long long* fallbacks) {
   const bool mixed = c->P.precision == NS_PREC_MIXED;
   const int maxc = std::max(1, c->P.poisson_max_cycles);
   const double div_tol_res = c->P.poisson_tol_div > 0 ? c->P.poisson_tol_div * 1.5 / c->dt : 0.0;
-  auto residual = [&]() -> int {
-    if (mixed) LAUNCH(NS_PROF_DC_UPDATE, "dc residual", launch3_dc_res(S.M64, S.M32.f[0], S.part, c->counter, c->red + kRedRes, c->st));
-    else LAUNCH(NS_PROF_MG_RESNORM, "resnorm", launch3_mg_resnorm<double>(S.M64, S.part, c->counter, c->red + kRedRes, c->st));
+  // mixed: phi as float-float pairs in PHF[pf]; each sweep adds the FP32
+  // correction and recomputes the residual (k3_dcff), phi goes to FP64 at the end
+  DCff3 dc;
+  std::memset(&dc, 0, sizeof(dc));
+  int pf = 0;
+  if (mixed) {
+    dc.n = c->N;
+    dc.pitch = c->pitch;
+    dc.plane = (long)c->pitch * (c->N + 1);
+    for (int d = 0; d < 3; ++d) {
+      dc.periodic[d] = c->g.periodic[d];
+      dc.ih[d][0] = (float)(1.0 / (c->g.dx[d] * c->g.dx[d]));
+      dc.ih[d][1] = (float)(1.0 / (c->g.dx[d] * c->g.dx[d]) - (double)dc.ih[d][0]);
+    }
+    dc.r32 = S.M32.f[0];
+    dc.f = S.FF;
+    dc.part = S.part;
+    dc.counter = c->counter;
+    dc.red_out = c->red + kRedRes;
+    LAUNCH(NS_PROF_DC_UPDATE, "f - mean (ff)", launch3_rhs_ff(c->N, dc.pitch, dc.plane, S.F, c->red + kRedMean, S.FF, c->st));
+  }
+  auto residual = [&](bool first) -> int {
+    if (mixed) {
+      dc.first = first;
+      dc.phin = S.PHF[pf];
+      dc.phout = S.PHF[first ? pf : 1 - pf];
+      dc.e = first ? nullptr : S.M32.x[0];
+      LAUNCH(NS_PROF_DC_UPDATE, "dc update", launch3_dcff(dc, c->st));
+      if (!first) pf = 1 - pf;
+    } else {
+      LAUNCH(NS_PROF_MG_RESNORM, "resnorm", launch3_mg_resnorm<double>(S.M64, S.part, c->counter, c->red + kRedRes, c->st));
+    }
     return sync_red(c, kRedRes, 1);
   };
-  int r = residual();
+  int r = residual(true);
   if (r != NS_OK) return r;
   const double r0 = c->red_h[kRedRes];
   double rn = r0, best = r0;
@@ -141,17 +170,17 @@ int poisson3(ns_ctx* c, int* cycles, double* res, long long* fallbacks) {
     if (mixed) {
       CK(cudaMemsetAsync(S.M32.x[0], 0, S.fb / 2, c->st), "memset e");  // each correction starts from zero
       r = vcycle3<float>(c, S.M32);
-      if (r == NS_OK) LAUNCH(NS_PROF_DC_UPDATE, "dc add", launch3_dc_add(S.M64, S.M32.x[0], c->st));
     } else {
       r = vcycle3<double>(c, S.M64);
     }
     if (r != NS_OK) return r;
     ++ncyc;
-    r = residual();
+    r = residual(false);
     if (r != NS_OK) return r;
     rn = c->red_h[kRedRes];
     if (rn < 0.5 * best) { best = rn; stall = 0; } else if (++stall >= 6) { status = NS_ERR_MG_STALL; break; }
   }
+  if (mixed) LAUNCH(NS_PROF_DC_UPDATE, "phi to FP64", launch3_ff_cells(c->N, dc.pitch, dc.plane, S.PHF[pf], S.PHI, c->st));
   (void)fallbacks;
   *cycles = ncyc;
   *res = r0 > 0 ? rn / r0 : 0.0;
@@ -225,7 +254,10 @@ int create3d(ns_ctx* c) {
       for (float** p : fs)
         if (r == NS_OK) r = alloc3(c, p, f32);
       if (r == NS_OK) r = alloc3(c, &S.PHB32[m], g32);
+      for (int b = 0; b < 2 && r == NS_OK; ++b) r = alloc3(c, &S.BF[b][m], S.fb);
     }
+    for (int b = 0; b < 2 && r == NS_OK; ++b) r = alloc3(c, &S.PHF[b], S.fb);
+    if (r == NS_OK) r = alloc3(c, &S.FF, S.fb);
   }
   return r;
 }
@@ -288,8 +320,10 @@ int mixed_iteration3(ns_ctx* c) {
   AncFF f;
   std::memset(&f, 0, sizeof(f));
   f.g = c->g;
+  const int nb = S.bf < 0 ? 0 : 1 - S.bf;
   for (int m = 0; m < 3; ++m) {
     f.u[m] = face3(c, S.base, m);
+    f.uff[m] = S.bf < 0 ? nullptr : S.BF[S.bf][m];
     f.S[m] = S.S[m];
     f.ph[m] = reinterpret_cast<float2*>(S.PH[m]);
     f.ph32[m] = S.PHB32[m];
@@ -307,7 +341,6 @@ int mixed_iteration3(ns_ctx* c) {
   Inc3 q;
   std::memset(&q, 0, sizeof(q));
   q.g = c->g;
-  const int outb = pick3(S.base, S.base);
   for (int m = 0; m < 3; ++m) {
     q.ub[m] = S.UB32[m];
     q.g0[m] = S.G0[m];
@@ -316,7 +349,8 @@ int mixed_iteration3(ns_ctx* c) {
     q.dt[m] = reinterpret_cast<float*>(S.T[m]);
     for (int d = 0; d < 3; ++d) q.dfl[d][m] = reinterpret_cast<float*>(S.FL[d][m]);
     q.base64[m] = face3(c, S.base, m);
-    q.out64[m] = S.B[outb][m];
+    q.baseff[m] = S.bf < 0 ? nullptr : S.BF[S.bf][m];
+    q.outff[m] = S.BF[nb][m];
     q.inv_dx[m] = (float)c->g.inv_dx[m];
     q.vcoef[m] = (float)(c->g.inv_dx2[m] * c->g.inv_ren);
   }
@@ -336,7 +370,20 @@ int mixed_iteration3(ns_ctx* c) {
     LAUNCH(NS_PROF_INC, "increment total 3d", launch3i_total(q, c->st));
     LAUNCH(NS_PROF_INC, "increment face 3d", launch3i_face(q, c->st));
   }
-  S.cur = outb;
+  S.bf = nb;
+  return NS_OK;
+}
+
+// u* (float-float) to FP64 in a free buffer, once the iteration stops
+int mixed_finalize3(ns_ctx* c) {
+  State3D& S = *c->s3;
+  if (S.bf < 0) return NS_OK;
+  const int outb = pick3(S.base, S.base);
+  const float2* in[3] = {S.BF[S.bf][0], S.BF[S.bf][1], S.BF[S.bf][2]};
+  double* out[3] = {S.B[outb][0], S.B[outb][1], S.B[outb][2]};
+  LAUNCH(NS_PROF_OTHER, "store u* 3d", launch3f_store(c->g, in, out, c->st));
+  S.base = S.cur = outb;
+  S.bf = -1;
   return NS_OK;
 }
 
@@ -364,6 +411,7 @@ int predictor3d(ns_ctx* c, ns_step_stats* sp) {
   S.base = S.cur = -1;
   // ---- dual-time pseudo-iterations (main.cpp:898-1040)
   const bool mixed = c->P.precision == NS_PREC_MIXED;
+  S.bf = -1;
   int count = 0;
   double norm = 1.e9;
   while (norm > c->P.momentum_tolerance) {
@@ -397,7 +445,7 @@ int predictor3d(ns_ctx* c, ns_step_stats* sp) {
   }
   s.pseudo_iters = count;
   s.norm_error = norm;
-  return NS_OK;
+  return mixed ? mixed_finalize3(c) : NS_OK;
 }
 
 int step3d(ns_ctx* c, ns_step_stats* stats) {

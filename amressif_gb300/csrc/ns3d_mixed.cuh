@@ -13,9 +13,12 @@
 // and the flux-ghost rule of the faces are linear. Every FP32 rounding error
 // is proportional to the increment, so the fixed point is the float-float
 // one, within a few units of 1e-15 of the FP64 one. The last stage writes
-// u_b + e4 in FP64 and the pseudo-norm of e4 (the Error_Computation norm,
-// utilities.cpp:421-493); no other pass issues an FP64 arithmetic
-// instruction.
+// u_b + e4 and the pseudo-norm of e4 (the Error_Computation norm,
+// utilities.cpp:421-493, reduced in float-float). Between pseudo-iterations
+// u_b is carried as float-float pairs; it is read from the FP64 u^n in the
+// first iteration and stored to FP64 once, when the iteration stops, so no
+// pass but that store issues an FP64 arithmetic instruction (GB300 runs FP64
+// at 1/73 of the FP32 rate).
 #pragma once
 #include "ff.cuh"
 #include "ns3d.cuh"
@@ -32,8 +35,9 @@ struct Inc3 {
   float* phe[3];           // ghosted cell velocity of the increment, (N+4)^3
   float* dfl[3][3];        // flux increments dfl[d][m] at the faces along d
   float* dt[3];            // cell total increments
-  const double* base64[3]; // u_b (last stage)
-  double* out64[3];        // u_b + e4 (last stage)
+  const double* base64[3]; // u_b in FP64 (last stage of the first iteration) ...
+  const float2* baseff[3]; // ... or as float-float pairs (later iterations)
+  float2* outff[3];        // u_b + e4 (last stage)
   float rk_prev, rk, c15;
   float inv_dx[3], vcoef[3];  // 1/dx, 1/(Re dx^2)
   int last;
@@ -45,7 +49,8 @@ struct Inc3 {
 // float-float anchor: values are (hi, lo) float pairs
 struct AncFF {
   Geom g;
-  const double* u[3];  // u_b (faces)
+  const double* u[3];  // u_b in FP64 (first iteration) ...
+  const float2* uff[3];  // ... or as float-float pairs (faces)
   const double* S[3];  // step source (faces)
   float2* ph[3];       // ghosted cell velocity, (N+4)^3
   float* ph32[3];      // the same rounded to FP32: the base cell velocity of the increments
@@ -54,6 +59,26 @@ struct AncFF {
   float* g0[3];        // G(u_b) rounded to FP32
   float* ub[3];        // u_b rounded to FP32
   float inv_dx[3][2], vcoef[3][2], c15[2];  // constants as (hi, lo)
+};
+
+// float-float defect correction of the mixed-precision 3D Poisson solve:
+// phi is carried as (hi, lo) pairs; each sweep adds the FP32 V-cycle
+// correction e and recomputes r = (f - mean f) - L phi (the 7-point operator
+// of mg3_lap_terms) in float-float, with max |r| reduced on the FP32 pipes
+struct DCff3 {
+  int n;
+  long pitch, plane;
+  int periodic[3];
+  float ih[3][2];      // 1/h^2 per direction as (hi, lo)
+  const float2* phin;  // phi (input; ignored when first)
+  float2* phout;       // phi + e (output)
+  const float* e;      // FP32 correction (nullable)
+  float* r32;          // FP32 residual: the right-hand side of the next V-cycle
+  const float2* f;     // f - mean f
+  int first;           // phi = 0
+  double* part;
+  unsigned* counter;
+  double* red_out;     // max |r|
 };
 
 #ifndef NS_3D_ARGS_ONLY
@@ -66,6 +91,7 @@ __device__ __forceinline__ ff ld2(const float2* p, long i) {
 __device__ __forceinline__ void st2(float2* p, long i, ff v) { p[i] = make_float2(v.hi, v.lo); }
 __device__ __forceinline__ ff ffc(const float (&c)[2]) { return ff_make(c[0], c[1]); }
 __device__ __forceinline__ float ff_round(ff v) { return v.hi + v.lo; }
+__device__ __forceinline__ ff ld_base(const AncFF& A, int m, long i) { return A.uff[m] ? ld2(A.uff[m], i) : ld_ff(A.u[m], i); }
 
 // ---- float-float anchor ----------------------------------------------------------------
 // ghosted cell velocity of u_b (the rules of k3_cart)
@@ -92,7 +118,7 @@ __global__ void __launch_bounds__(256) k3f_cart(AncFF A) {
     if (nout <= 1) {
       const long a = id3(g, cm[0], cm[1], cm[2]);
       const long b = a + (m == 0 ? 1 : (m == 1 ? g.pitch : g.plane));
-      v = ff_scale2(ld_ff(A.u[m], a) + ld_ff(A.u[m], b), 0.5f);
+      v = ff_scale2(ld_base(A, m, a) + ld_base(A, m, b), 0.5f);
       if (mirror) {
         const CartBC& bc = g.bc[2 * out_d + side];
         const int r = bc.rule[m];
@@ -126,7 +152,7 @@ __global__ void __launch_bounds__(256) k3f_flux(AncFF A) {
       if (e != d && c[e] >= N) ok = false;
     if (!ok) continue;
     const long s = G1[d];
-    const ff ud = ld_ff(A.u[d], fc);
+    const ff ud = ld_base(A, d, fc);
     for (int m = 0; m < 3; ++m) {
       const float2* ph = A.ph[m];
       ff F = ff_make(0.f, 0.f);
@@ -187,7 +213,7 @@ __global__ void __launch_bounds__(256) k3f_face(AncFF A) {
     const long st = fstride[m];
     const long base = id - (long)a * st;
     const ff tl = t_along_ff(A, m, a - 1, base, st), tr = t_along_ff(A, m, a, base, st);
-    const ff u = ld_ff(A.u[m], id);
+    const ff u = ld_base(A, m, id);
     const ff G = (ld_ff(A.S[m], id) - ffc(A.c15) * u) + ff_scale2(tl + tr, 0.5f);
     A.g0[m][id] = ff_round(G);
     A.ub[m][id] = ff_round(u);
@@ -304,12 +330,12 @@ __device__ __forceinline__ float t_along_inc(const Inc3& A, int m, int a, long b
 }
 
 // e_out = rk (G0 - (1.5/dt) e_in + avg(dt)); the last stage writes
-// u_b + e_out in FP64 and the pseudo-norm of e_out
+// u_b + e_out (float-float) and the pseudo-norm of e_out
 __global__ void __launch_bounds__(256) k3i_face(Inc3 A) {
   const Geom& g = A.g;
   const int N = g.N;
   NS3_IJK(0, 0, 0)
-  double nrm[3] = {0.0, 0.0, 0.0};
+  float nrm[3] = {0.f, 0.f, 0.f};
   const long fstride[3] = {1, g.pitch, g.plane};
   for (int m = 0; m < 3; ++m) {
     const int lim[3] = {N + (m == 0), N + (m == 1), N + (m == 2)};
@@ -323,18 +349,89 @@ __global__ void __launch_bounds__(256) k3i_face(Inc3 A) {
     const float G = (A.g0[m][id] - A.c15 * inc_e(A, m, id)) + 0.5f * (tl + tr);
     const float eo = A.rk * G;
     if (A.last) {
-      A.out64[m][id] = A.base64[m][id] + (double)eo;
+      const ff b = A.baseff[m] ? ld2(A.baseff[m], id) : ld_ff(A.base64[m], id);
+      st2(A.outff[m], id, ff_add_f(b, eo));
       const float w = (a == 0 || a == N) ? 0.5f : 1.f;
-      nrm[m] = (double)(eo * eo * w);
+      nrm[m] = eo * eo * w;
     } else {
       A.eout[m][id] = eo;
     }
   }
-  if (A.last && grid_reduce_last<3>(nrm, A.part, A.counter, 0u) && threadIdx.x == 0) {
+  double tot[3];
+  if (A.last && grid_reduce_last_f<3, 256>(nrm, reinterpret_cast<float2*>(A.part), A.counter, 0u, tot) &&
+      threadIdx.x == 0) {
     const double npts = (double)N * N * N;
     double e = 0.0;
-    for (int m = 0; m < 3; ++m) e = fmax(e, sqrt(nrm[m]) / sqrt(npts));
+    for (int m = 0; m < 3; ++m) e = fmax(e, sqrt(tot[m]) / sqrt(npts));
     *A.norm_out = e;
+  }
+}
+
+// ---- float-float defect correction (Poisson) ------------------------------------------------
+__device__ __forceinline__ ff dc3_val(const DCff3& A, long id) {
+  if (A.first) return ff_make(0.f, 0.f);
+  const ff v = ld2(A.phin, id);
+  return A.e ? ff_add_f(v, A.e[id]) : v;
+}
+
+__global__ void __launch_bounds__(256) k3_dcff(DCff3 A) {
+  const int n = A.n;
+  const int i = blockIdx.x * 32 + (threadIdx.x & 31), j = blockIdx.y * 8 + (threadIdx.x >> 5), k = blockIdx.z;
+  float v[1] = {0.f};
+  if (i < n && j < n && k < n) {
+    const long id = (long)k * A.plane + (long)j * A.pitch + i;
+    const int c[3] = {i, j, k};
+    const long st[3] = {1, A.pitch, A.plane};
+    const ff xc = dc3_val(A, id);
+    ff lap = ff_make(0.f, 0.f);
+    for (int d = 0; d < 3; ++d) {
+      ff s = ff_make(0.f, 0.f);
+      if (A.periodic[d] || c[d] + 1 < n) s = s + (dc3_val(A, id + ((c[d] + 1 < n) ? st[d] : -(long)(n - 1) * st[d])) - xc);
+      if (A.periodic[d] || c[d] > 0) s = s + (dc3_val(A, id + ((c[d] > 0) ? -st[d] : (long)(n - 1) * st[d])) - xc);
+      lap = lap + ffc(A.ih[d]) * s;
+    }
+    const ff r = ld2(A.f, id) - lap;
+    st2(A.phout, id, xc);
+    const float r1 = ff_round(r);
+    A.r32[id] = r1;
+    v[0] = fabsf(r1);
+  }
+  double out[1];
+  if (grid_reduce_last_f<1, 256>(v, reinterpret_cast<float2*>(A.part), A.counter, 1u, out) && threadIdx.x == 0)
+    A.red_out[0] = out[0];
+}
+
+// f - mean f as (hi, lo) pairs (integer split, no FP64 instruction)
+__global__ void __launch_bounds__(256) k3_rhs_ff(int n, long pitch, long plane, const double* f, const double* mean,
+                                                 float2* out) {
+  const int i = blockIdx.x * 32 + (threadIdx.x & 31), j = blockIdx.y * 8 + (threadIdx.x >> 5), k = blockIdx.z;
+  if (i >= n || j >= n || k >= n) return;
+  const long id = (long)k * plane + (long)j * pitch + i;
+  st2(out, id, ld_ff(f, id) - ff_from_double(*mean));
+}
+
+// phi (FP64) = hi + lo
+__global__ void __launch_bounds__(256) k3_ff_cells(int n, long pitch, long plane, const float2* in, double* out) {
+  const int i = blockIdx.x * 32 + (threadIdx.x & 31), j = blockIdx.y * 8 + (threadIdx.x >> 5), k = blockIdx.z;
+  if (i >= n || j >= n || k >= n) return;
+  const long id = (long)k * plane + (long)j * pitch + i;
+  const float2 v = in[id];
+  out[id] = (double)v.x + (double)v.y;
+}
+
+// u* = hi + lo in FP64 on every face, once the pseudo-iterations stop
+__global__ void __launch_bounds__(256) k3f_store(Geom g, const float2* in0, const float2* in1, const float2* in2,
+                                                 double* o0, double* o1, double* o2) {
+  const int N = g.N;
+  NS3_IJK(0, 0, 0)
+  const float2* in[3] = {in0, in1, in2};
+  double* out[3] = {o0, o1, o2};
+  for (int m = 0; m < 3; ++m) {
+    const int lim[3] = {N + (m == 0), N + (m == 1), N + (m == 2)};
+    if (i >= lim[0] || j >= lim[1] || k >= lim[2]) continue;
+    const long id = id3(g, i, j, k);
+    const float2 v = in[m][id];
+    out[m][id] = (double)v.x + (double)v.y;
   }
 }
 

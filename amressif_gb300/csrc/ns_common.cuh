@@ -115,16 +115,31 @@ __device__ __forceinline__ bool grid_reduce_last(double (&v)[NV], double* part, 
   if (!last) return false;
   // The whole last block reduces the partials: thread t takes blocks
   // t, t+blockDim, ... in order, then a fixed shuffle/shared-memory tree.
+  // The partials are read from L2 (__ldcg: other blocks' fenced stores are
+  // visible there) eight at a time, so the loads overlap; they are combined
+  // in the same order as one at a time.
   __threadfence();
   const int nb = gridDim.x * gridDim.y * gridDim.z;
+  const int stride = blockDim.x;
 #pragma unroll
   for (int q = 0; q < NV; ++q) {
     const bool is_max = (max_mask >> q) & 1u;
-    volatile const double* pv = part + (long)q * nb;
+    const double* pv = part + (long)q * nb;
     double x = 0.0;
     bool first = true;
-    for (int b = threadIdx.x; b < nb; b += blockDim.x) {
-      const double y = pv[b];
+    int b = threadIdx.x;
+    for (; b + 7 * stride < nb; b += 8 * stride) {
+      double y[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) y[u] = __ldcg(pv + b + u * stride);
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        x = first ? y[u] : (is_max ? fmax(x, y[u]) : x + y[u]);
+        first = false;
+      }
+    }
+    for (; b < nb; b += stride) {
+      const double y = __ldcg(pv + b);
       x = first ? y : (is_max ? fmax(x, y) : x + y);
       first = false;
     }
@@ -201,10 +216,18 @@ __device__ __forceinline__ bool grid_reduce_last_f(float (&v)[NV], float2* part2
 #pragma unroll
   for (int q = 0; q < NV; ++q) {
     const bool is_max = (max_mask >> q) & 1u;
-    volatile const float2* pv = part2 + (long)q * nb;
+    const float2* pv = part2 + (long)q * nb;
     float2 x = make_float2(0.f, 0.f);
-    for (int b = threadIdx.x; b < nb; b += NT) {
-      const float2 y = make_float2(pv[b].x, pv[b].y);
+    int b = threadIdx.x;
+    for (; b + 7 * NT < nb; b += 8 * NT) {  // L2 loads, eight in flight, combined in order
+      float2 y[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) y[u] = __ldcg(pv + b + u * NT);
+#pragma unroll
+      for (int u = 0; u < 8; ++u) x = is_max ? make_float2(fmaxf(x.x, y[u].x), 0.f) : ffadd(x, y[u]);
+    }
+    for (; b < nb; b += NT) {
+      const float2 y = __ldcg(pv + b);
       x = is_max ? make_float2(fmaxf(x.x, y.x), 0.f) : ffadd(x, y);
     }
     for (int o = 16; o > 0; o >>= 1) {

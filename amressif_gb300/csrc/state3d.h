@@ -31,6 +31,10 @@ struct State3D {
   float* G0[3] = {nullptr, nullptr, nullptr};
   float* E[2][3] = {};
   float* PHB32[3] = {nullptr, nullptr, nullptr};
+  float2* BF[2][3] = {};  // u_b as float-float pairs between pseudo-iterations
+  float2* PHF[2] = {};    // Poisson phi as float-float pairs (mixed defect correction)
+  float2* FF = nullptr;   // f - mean f as float-float pairs
+  int bf = -1;            // BF slot holding u_b; -1: u_b is the FP64 u^n
   ns::MG3<double> M64;
   ns::MG3<float> M32;
   int base = -1, cur = -1;

@@ -234,7 +234,8 @@ def cfg5_section(ns, args):
     out = {"workload": "3D periodic Taylor-Green %d^3, Re=1600, dt=0.4h, seeded 1e-3 perturbation, steps 2..%d"
                        % (n, k + 1)}
     state = wl.tgv3d_perturbed_state(n, amp=1e-3, seed=0)
-    for name, prec in (("mixed", ns.PREC_MIXED), ("fp64", ns.PREC_FP64)):
+    precs = [("mixed", ns.PREC_MIXED)] + ([] if args.no_cfg5_fp64 else [("fp64", ns.PREC_FP64)])
+    for name, prec in precs:
         p = ns.default_params(dim=3, n_cell=n, ren=1600.0, fixed_dt=0.4 * h, iter_num=100, precision=prec,
                               prob_hi=(2 * math.pi,) * 3, bc_lo=(111,) * 3, bc_hi=(111,) * 3, fix_quirks=1,
                               poisson_tol_rel=1e-10, poisson_tol_div=1e-10, max_grid_size=(n, n, n))
@@ -252,9 +253,10 @@ def cfg5_section(ns, args):
                      "ms_predictor": float(np.mean([x["ms_predictor"] for x in st])),
                      "div_after_max": max(x["div_after"] for x in st)}
         s.close()
-    out["poisson_speedup_mixed"] = out["fp64"]["ms_poisson"] / out["mixed"]["ms_poisson"]
-    out["predictor_speedup_mixed"] = out["fp64"]["ms_predictor"] / out["mixed"]["ms_predictor"]
-    out["step_speedup_mixed"] = out["fp64"]["ms_per_step"] / out["mixed"]["ms_per_step"]
+    if "fp64" in out:
+        out["poisson_speedup_mixed"] = out["fp64"]["ms_poisson"] / out["mixed"]["ms_poisson"]
+        out["predictor_speedup_mixed"] = out["fp64"]["ms_predictor"] / out["mixed"]["ms_predictor"]
+        out["step_speedup_mixed"] = out["fp64"]["ms_per_step"] / out["mixed"]["ms_per_step"]
     return out
 
 
@@ -507,6 +509,9 @@ def main():
     ap.add_argument("--cfg5-n", type=int, default=256)
     ap.add_argument("--cfg5-steps", type=int, default=2)
     ap.add_argument("--no-cfg5-adjoint", action="store_true")
+    ap.add_argument("--no-cfg5-fp64", action="store_true")
+    ap.add_argument("--section", default="all", choices=["all", "cfg5"],
+                    help="cfg5: run only the 3D Taylor-Green section and print it (profiling runs)")
     ap.add_argument("--cfg5-adj-n", type=int, default=128)
     ap.add_argument("--cfg5-adj-steps", type=int, default=200)
     ap.add_argument("--cfg5-adj-snap", type=int, default=16)
@@ -518,7 +523,14 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
-    if args.impl == "reference":
+    if args.section == "cfg5":
+        import amressif_gb300 as ns
+
+        out = cfg5_section(ns, args)
+        if not args.no_cfg5_adjoint:
+            out["adjoint"] = cfg5_adjoint_section(ns, args)
+        print(json.dumps({"taylor_green_3d": out}))
+    elif args.impl == "reference":
         bench_reference(args)
     else:
         bench_ours(args)
