@@ -1,5 +1,8 @@
 // Tangent-linear and adjoint operators of one 3D step, periodic boxes in the
-// physical mode (flux ghosts wrapped, p / phi ghosts wrapped), FP64.
+// physical mode (flux ghosts wrapped, p / phi ghosts wrapped). The operators
+// are FP64; in the mixed-precision mode the linear solves refine an FP64
+// residual with inner FP32 BiCGStab solves (the operator kernels are
+// templates on the element type).
 //
 // In a periodic direction face N is the image of face 0 (the step updates
 // both identically), so the degrees of freedom are the faces 0 .. N-1 of
@@ -17,18 +20,23 @@
 
 namespace ns {
 
-struct A3Args {
+// operands of the predictor Jacobian in element type T (double: the FP64
+// operator; float: the inner solves of the mixed-precision refinement)
+template <typename T>
+struct A3T {
   Geom g;
-  const double* us[3];  // base u* (faces)
-  double* phb[3];       // base cell velocity
-  double* q[3][3];      // base QUICK interpolant of component m at the faces along d
-  const double* v[3];   // tangent direction / adjoint input
-  double* dph[3];       // cell velocity tangent / adjoint
-  double* fl[3][3];     // face flux tangents / adjoints
-  double* ct[3];        // cell totals (tangent) / tbar (adjoint)
-  double* uadv[3];      // advecting-velocity adjoint
-  double* out[3];
+  const T* us[3];  // base u* (faces)
+  T* phb[3];       // base cell velocity
+  T* q[3][3];      // base QUICK interpolant of component m at the faces along d
+  const T* v[3];   // tangent direction / adjoint input
+  T* dph[3];       // cell velocity tangent / adjoint
+  T* fl[3][3];     // face flux tangents / adjoints
+  T* ct[3];        // cell totals (tangent) / tbar (adjoint)
+  T* uadv[3];      // advecting-velocity adjoint
+  T* out[3];
+  T ix[3], vc[3], c15;  // 1/dx, 1/(Re dx^2), 1.5/dt in T
 };
+using A3Args = A3T<double>;
 
 struct Bcg3 {
   Geom g;
@@ -40,6 +48,37 @@ struct Bcg3 {
   double* s[3];
   double* t[3];
   const double* b[3];
+  double* sc;
+  double* part;
+  unsigned* counter;
+};
+
+// mixed-precision refinement of a Jacobian solve op(J) x = b: the FP64
+// residual r = b - op(J) x (op in FP64) rounded to FP32, an inner FP32
+// BiCGStab for op(J) d = r, x += d
+struct Ref3 {
+  Geom g;
+  const double* b[3];
+  const double* v[3];  // op(J) x
+  float* r32[3];
+  double* x[3];
+  const float* d[3];
+  double* sc;          // sc[kRfRR] = max |r|, sc[kRfBB] = max |b|
+  double* part;
+  unsigned* counter;
+};
+enum RefScalar { kRfRR = kBcN, kRfBB = kBcN + 1, kRfN = kBcN + 2 };
+
+struct Bcg3f {
+  Geom g;
+  float* x[3];
+  float* r[3];
+  float* rh[3];
+  float* p[3];
+  float* v[3];
+  float* s[3];
+  float* t[3];
+  const float* b[3];
   double* sc;
   double* part;
   unsigned* counter;
@@ -63,75 +102,86 @@ __device__ __forceinline__ long wid(const Geom& g, int i, int j, int k, int d, i
   if (i >= N || j >= N || k >= N) return;                        \
   const long id = id3(A.g, i, j, k);
 
-__device__ __forceinline__ double qleft3(double e, double c, double b) { return -0.125 * e + 0.75 * c + 0.375 * b; }
-__device__ __forceinline__ double qright3(double c, double b, double a) { return 0.375 * c + 0.75 * b - 0.125 * a; }
+template <typename T>
+__device__ __forceinline__ T qleft3(T e, T c, T b) { return (T)-0.125 * e + (T)0.75 * c + (T)0.375 * b; }
+template <typename T>
+__device__ __forceinline__ T qright3(T c, T b, T a) { return (T)0.375 * c + (T)0.75 * b - (T)0.125 * a; }
 
 // QUICK interpolant at face f along d of a cell field x, switch from u
-__device__ __forceinline__ double quick_at(const Geom& g, const double* x, int i, int j, int k, int d, double u) {
-  if (u > 0) return qleft3(x[wid(g, i, j, k, d, -2)], x[wid(g, i, j, k, d, -1)], x[id3(g, i, j, k)]);
+template <typename T>
+__device__ __forceinline__ T quick_at(const Geom& g, const T* x, int i, int j, int k, int d, T u) {
+  if (u > (T)0) return qleft3(x[wid(g, i, j, k, d, -2)], x[wid(g, i, j, k, d, -1)], x[id3(g, i, j, k)]);
   return qright3(x[wid(g, i, j, k, d, -1)], x[id3(g, i, j, k)], x[wid(g, i, j, k, d, 1)]);
 }
 
-__global__ void __launch_bounds__(256) k3a_base_cells(A3Args A) {
+template <typename T>
+__global__ void __launch_bounds__(256) k3a_base_cells(A3T<T> A) {
   NS3A_IJK
-  for (int m = 0; m < 3; ++m) A.phb[m][id] = 0.5 * (A.us[m][id] + A.us[m][wid(A.g, i, j, k, m, 1)]);
+  for (int m = 0; m < 3; ++m) A.phb[m][id] = (T)0.5 * (A.us[m][id] + A.us[m][wid(A.g, i, j, k, m, 1)]);
 }
 
-__global__ void __launch_bounds__(256) k3a_base_q(A3Args A) {
+template <typename T>
+__global__ void __launch_bounds__(256) k3a_base_q(A3T<T> A) {
   NS3A_IJK
   for (int d = 0; d < 3; ++d) {
-    const double u = A.us[d][id];
-    for (int m = 0; m < 3; ++m) A.q[d][m][id] = quick_at(A.g, A.phb[m], i, j, k, d, u);
+    const T u = A.us[d][id];
+    for (int m = 0; m < 3; ++m) A.q[d][m][id] = quick_at(A.g, (const T*)A.phb[m], i, j, k, d, u);
   }
 }
 
 // ---- tangent ------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k3a_jv_cells(A3Args A) {
+template <typename T>
+__global__ void __launch_bounds__(256) k3a_jv_cells(A3T<T> A) {
   NS3A_IJK
-  for (int m = 0; m < 3; ++m) A.dph[m][id] = 0.5 * (A.v[m][id] + A.v[m][wid(A.g, i, j, k, m, 1)]);
+  for (int m = 0; m < 3; ++m) A.dph[m][id] = (T)0.5 * (A.v[m][id] + A.v[m][wid(A.g, i, j, k, m, 1)]);
 }
 
-__global__ void __launch_bounds__(256) k3a_jv_flux(A3Args A) {
+template <typename T>
+__global__ void __launch_bounds__(256) k3a_jv_flux(A3T<T> A) {
   NS3A_IJK
   for (int d = 0; d < 3; ++d) {
-    const double u = A.us[d][id], du = A.v[d][id];
-    for (int m = 0; m < 3; ++m) A.fl[d][m][id] = du * A.q[d][m][id] + u * quick_at(A.g, A.dph[m], i, j, k, d, u);
+    const T u = A.us[d][id], du = A.v[d][id];
+    for (int m = 0; m < 3; ++m) A.fl[d][m][id] = du * A.q[d][m][id] + u * quick_at(A.g, (const T*)A.dph[m], i, j, k, d, u);
   }
 }
 
-__global__ void __launch_bounds__(256) k3a_jv_total(A3Args A) {
+template <typename T>
+__global__ void __launch_bounds__(256) k3a_jv_total(A3T<T> A) {
   NS3A_IJK
   const Geom& g = A.g;
   for (int m = 0; m < 3; ++m) {
-    const double* x = A.dph[m];
-    const double c = x[id];
-    double visc = 0.0, conv = 0.0;
+    const T* x = A.dph[m];
+    const T c = x[id];
+    T visc = (T)0, conv = (T)0;
     for (int d = 0; d < 3; ++d) {
-      visc += (x[wid(g, i, j, k, d, 1)] - 2.0 * c + x[wid(g, i, j, k, d, -1)]) * g.inv_dx2[d];
-      conv += (A.fl[d][m][wid(g, i, j, k, d, 1)] - A.fl[d][m][id]) * g.inv_dx[d];
+      visc += (x[wid(g, i, j, k, d, 1)] - (T)2 * c + x[wid(g, i, j, k, d, -1)]) * A.vc[d];
+      conv += (A.fl[d][m][wid(g, i, j, k, d, 1)] - A.fl[d][m][id]) * A.ix[d];
     }
-    A.ct[m][id] = visc * g.inv_ren - conv;
+    A.ct[m][id] = visc - conv;
   }
 }
 
-__global__ void __launch_bounds__(256) k3a_jv_faces(A3Args A) {
+template <typename T>
+__global__ void __launch_bounds__(256) k3a_jv_faces(A3T<T> A) {
   NS3A_IJK
   for (int m = 0; m < 3; ++m)
-    A.out[m][id] = 0.5 * (A.ct[m][wid(A.g, i, j, k, m, -1)] + A.ct[m][id]) - A.g.c15 * A.v[m][id];
+    A.out[m][id] = (T)0.5 * (A.ct[m][wid(A.g, i, j, k, m, -1)] + A.ct[m][id]) - A.c15 * A.v[m][id];
 }
 
 // ---- adjoint ------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k3a_vj_tbar(A3Args A) {
+template <typename T>
+__global__ void __launch_bounds__(256) k3a_vj_tbar(A3T<T> A) {
   NS3A_IJK
-  for (int m = 0; m < 3; ++m) A.ct[m][id] = 0.5 * (A.v[m][id] + A.v[m][wid(A.g, i, j, k, m, 1)]);
+  for (int m = 0; m < 3; ++m) A.ct[m][id] = (T)0.5 * (A.v[m][id] + A.v[m][wid(A.g, i, j, k, m, 1)]);
 }
 
-__global__ void __launch_bounds__(256) k3a_vj_flux(A3Args A) {
+template <typename T>
+__global__ void __launch_bounds__(256) k3a_vj_flux(A3T<T> A) {
   NS3A_IJK
   for (int d = 0; d < 3; ++d) {
-    double ua = 0.0;
+    T ua = (T)0;
     for (int m = 0; m < 3; ++m) {
-      const double fb = (A.ct[m][id] - A.ct[m][wid(A.g, i, j, k, d, -1)]) * A.g.inv_dx[d];
+      const T fb = (A.ct[m][id] - A.ct[m][wid(A.g, i, j, k, d, -1)]) * A.ix[d];
       A.fl[d][m][id] = fb;
       ua += fb * A.q[d][m][id];
     }
@@ -140,34 +190,37 @@ __global__ void __launch_bounds__(256) k3a_vj_flux(A3Args A) {
 }
 
 // weight of cell offset o (cell - face) in the face's QUICK interpolant
-__device__ __forceinline__ double quick_w3(bool pos, int o) {
-  if (pos) return o == -2 ? -0.125 : (o == -1 ? 0.75 : (o == 0 ? 0.375 : 0.0));
-  return o == -1 ? 0.375 : (o == 0 ? 0.75 : (o == 1 ? -0.125 : 0.0));
+template <typename T>
+__device__ __forceinline__ T quick_w3(bool pos, int o) {
+  if (pos) return o == -2 ? (T)-0.125 : (o == -1 ? (T)0.75 : (o == 0 ? (T)0.375 : (T)0));
+  return o == -1 ? (T)0.375 : (o == 0 ? (T)0.75 : (o == 1 ? (T)-0.125 : (T)0));
 }
 
-__global__ void __launch_bounds__(256) k3a_vj_cells(A3Args A) {
+template <typename T>
+__global__ void __launch_bounds__(256) k3a_vj_cells(A3T<T> A) {
   NS3A_IJK
   const Geom& g = A.g;
   for (int m = 0; m < 3; ++m) {
-    const double* tb = A.ct[m];
-    const double c = tb[id];
-    double s = 0.0;
+    const T* tb = A.ct[m];
+    const T c = tb[id];
+    T s = (T)0;
     for (int d = 0; d < 3; ++d) {
-      s += (tb[wid(g, i, j, k, d, 1)] - 2.0 * c + tb[wid(g, i, j, k, d, -1)]) * g.inv_dx2[d] * g.inv_ren;
+      s += (tb[wid(g, i, j, k, d, 1)] - (T)2 * c + tb[wid(g, i, j, k, d, -1)]) * A.vc[d];
       for (int f = -1; f <= 2; ++f) {  // faces (along d) whose stencil holds this cell
         const long fid = wid(g, i, j, k, d, f);
-        const double u = A.us[d][fid];
-        s += A.fl[d][m][fid] * u * quick_w3(u > 0, -f);
+        const T u = A.us[d][fid];
+        s += A.fl[d][m][fid] * u * quick_w3<T>(u > (T)0, -f);
       }
     }
     A.dph[m][id] = s;
   }
 }
 
-__global__ void __launch_bounds__(256) k3a_vj_faces(A3Args A) {
+template <typename T>
+__global__ void __launch_bounds__(256) k3a_vj_faces(A3T<T> A) {
   NS3A_IJK
   for (int m = 0; m < 3; ++m)
-    A.out[m][id] = A.uadv[m][id] + 0.5 * (A.dph[m][wid(A.g, i, j, k, m, -1)] + A.dph[m][id]) - A.g.c15 * A.v[m][id];
+    A.out[m][id] = A.uadv[m][id] + (T)0.5 * (A.dph[m][wid(A.g, i, j, k, m, -1)] + A.dph[m][id]) - A.c15 * A.v[m][id];
 }
 
 // ---- projection pieces (wrapped) --------------------------------------------------------
@@ -328,6 +381,155 @@ __global__ void __launch_bounds__(256) k3b_p(Bcg3 A) {
   for (int m = 0; m < 3; ++m) A.p[m][id] = A.r[m][id] + be * (A.p[m][id] - om * A.v[m][id]);
 }
 #undef BCG3_PROLOGUE
+
+// ---- mixed-precision refinement -------------------------------------------------------------
+#define REF3_PROLOGUE                                                                                          \
+  const int i = blockIdx.x * 32 + (threadIdx.x & 31), j = blockIdx.y * 8 + (threadIdx.x >> 5), k = blockIdx.z; \
+  const bool in = i < A.g.N && j < A.g.N && k < A.g.N;                                                         \
+  const long id = in ? id3(A.g, i, j, k) : 0;
+
+__global__ void __launch_bounds__(256) k3r_to_f32(Geom g, const double* x0, const double* x1, const double* x2, float* y0,
+                                                  float* y1, float* y2) {
+  const int i = blockIdx.x * 32 + (threadIdx.x & 31), j = blockIdx.y * 8 + (threadIdx.x >> 5), k = blockIdx.z;
+  if (i >= g.N || j >= g.N || k >= g.N) return;
+  const long id = id3(g, i, j, k);
+  y0[id] = (float)x0[id];
+  y1[id] = (float)x1[id];
+  y2[id] = (float)x2[id];
+}
+
+// max |b - op(J) x| and max |b| (max norms: no squares to underflow in FP32)
+__global__ void __launch_bounds__(256) k3r_resmax(Ref3 A) {
+  REF3_PROLOGUE
+  float red[2] = {0.f, 0.f};
+  if (in)
+    for (int m = 0; m < 3; ++m) {
+      const double b = A.b[m][id];
+      red[0] = fmaxf(red[0], (float)fabs(b - A.v[m][id]));
+      red[1] = fmaxf(red[1], (float)fabs(b));
+    }
+  double out[2];
+  if (grid_reduce_last_f<2, 256>(red, reinterpret_cast<float2*>(A.part), A.counter, 3u, out) && threadIdx.x == 0) {
+    A.sc[kRfRR] = out[0];
+    A.sc[kRfBB] = out[1];
+  }
+}
+
+// r32 = (b - op(J) x) / max |r|: the right-hand side of the inner solve, O(1)
+__global__ void __launch_bounds__(256) k3r_scaled(Ref3 A, double inv) {
+  REF3_PROLOGUE
+  if (!in) return;
+  for (int m = 0; m < 3; ++m) A.r32[m][id] = (float)((A.b[m][id] - A.v[m][id]) * inv);
+}
+
+// x += max |r| d
+__global__ void __launch_bounds__(256) k3r_update(Ref3 A, double scale) {
+  REF3_PROLOGUE
+  if (!in) return;
+  for (int m = 0; m < 3; ++m) A.x[m][id] += scale * (double)A.d[m][id];
+}
+#undef REF3_PROLOGUE
+
+// ---- BiCGStab in FP32 (the inner solves), from x = 0 ------------------------------------------
+#define BCGF_PROLOGUE                                                                                          \
+  const int i = blockIdx.x * 32 + (threadIdx.x & 31), j = blockIdx.y * 8 + (threadIdx.x >> 5), k = blockIdx.z; \
+  const bool in = i < A.g.N && j < A.g.N && k < A.g.N;                                                         \
+  const long id = in ? id3(A.g, i, j, k) : 0;
+
+__global__ void __launch_bounds__(256) k3c_init(Bcg3f A) {
+  BCGF_PROLOGUE
+  float red[1] = {0.f};
+  if (in)
+    for (int m = 0; m < 3; ++m) {
+      const float r = A.b[m][id];
+      A.x[m][id] = 0.f;
+      A.r[m][id] = r;
+      A.rh[m][id] = r;
+      A.p[m][id] = r;
+      red[0] += r * r;
+    }
+  double out[1];
+  if (grid_reduce_last_f<1, 256>(red, reinterpret_cast<float2*>(A.part), A.counter, 0u, out) && threadIdx.x == 0) {
+    double* sc = A.sc;
+    sc[kBcRho] = out[0];
+    sc[kBcAlpha] = 1.0;
+    sc[kBcOmega] = 1.0;
+    sc[kBcBeta] = 0.0;
+    sc[kBcRR] = out[0];
+    sc[kBcRR0] = out[0];
+    sc[kBcBB] = out[0];
+    sc[kBcBreak] = 0.0;
+  }
+}
+
+__global__ void __launch_bounds__(256) k3c_alpha(Bcg3f A) {
+  BCGF_PROLOGUE
+  float red[1] = {0.f};
+  if (in)
+    for (int m = 0; m < 3; ++m) red[0] += A.rh[m][id] * A.v[m][id];
+  double out[1];
+  if (grid_reduce_last_f<1, 256>(red, reinterpret_cast<float2*>(A.part), A.counter, 0u, out) && threadIdx.x == 0) {
+    double* sc = A.sc;
+    if (out[0] != 0.0 && isfinite(out[0])) sc[kBcAlpha] = sc[kBcRho] / out[0];
+    else { sc[kBcAlpha] = 0.0; sc[kBcBreak] = 1.0; }
+  }
+}
+
+__global__ void __launch_bounds__(256) k3c_s(Bcg3f A) {
+  BCGF_PROLOGUE
+  if (!in) return;
+  const float al = (float)A.sc[kBcAlpha];
+  for (int m = 0; m < 3; ++m) A.s[m][id] = A.r[m][id] - al * A.v[m][id];
+}
+
+__global__ void __launch_bounds__(256) k3c_omega(Bcg3f A) {
+  BCGF_PROLOGUE
+  float red[2] = {0.f, 0.f};
+  if (in)
+    for (int m = 0; m < 3; ++m) {
+      const float t = A.t[m][id];
+      red[0] += t * A.s[m][id];
+      red[1] += t * t;
+    }
+  double out[2];
+  if (grid_reduce_last_f<2, 256>(red, reinterpret_cast<float2*>(A.part), A.counter, 0u, out) && threadIdx.x == 0) {
+    double* sc = A.sc;
+    sc[kBcOmega] = out[1] > 0.0 ? out[0] / out[1] : 0.0;
+    if (sc[kBcOmega] == 0.0) sc[kBcBreak] = 2.0;
+  }
+}
+
+__global__ void __launch_bounds__(256) k3c_xr(Bcg3f A) {
+  BCGF_PROLOGUE
+  const float al = (float)A.sc[kBcAlpha], om = (float)A.sc[kBcOmega];
+  float red[2] = {0.f, 0.f};
+  if (in)
+    for (int m = 0; m < 3; ++m) {
+      const float s = A.s[m][id];
+      A.x[m][id] += al * A.p[m][id] + om * s;
+      const float r = s - om * A.t[m][id];
+      A.r[m][id] = r;
+      red[0] += A.rh[m][id] * r;
+      red[1] += r * r;
+    }
+  double out[2];
+  if (grid_reduce_last_f<2, 256>(red, reinterpret_cast<float2*>(A.part), A.counter, 0u, out) && threadIdx.x == 0) {
+    double* sc = A.sc;
+    const double rho = sc[kBcRho], al64 = sc[kBcAlpha], om64 = sc[kBcOmega];
+    sc[kBcBeta] = (rho != 0.0 && om64 != 0.0) ? (out[0] / rho) * (al64 / om64) : 0.0;
+    if (rho == 0.0) sc[kBcBreak] = 3.0;
+    sc[kBcRho] = out[0];
+    sc[kBcRR] = out[1];
+  }
+}
+
+__global__ void __launch_bounds__(256) k3c_p(Bcg3f A) {
+  BCGF_PROLOGUE
+  if (!in) return;
+  const float be = (float)A.sc[kBcBeta], om = (float)A.sc[kBcOmega];
+  for (int m = 0; m < 3; ++m) A.p[m][id] = A.r[m][id] + be * (A.p[m][id] - om * A.v[m][id]);
+}
+#undef BCGF_PROLOGUE
 
 // ---- enstrophy: E = 1/2 sum over the edges of |curl u|^2 dV ----------------------------------
 // omega_x at the x edge (i+1/2, j, k) = dw/dy - dv/dz, and cyclically

@@ -47,6 +47,18 @@ struct Adj3 {
   double* TL_DUP[3] = {};
   double* OM[3] = {};
   double* ORPH[3] = {};
+  // mixed-precision refinement: FP32 base operands and inner BiCGStab vectors
+  bool mixed = false;
+  float* US32[3] = {};
+  float* PHB32[3] = {};
+  float* Q32[3][3] = {};
+  float* XF[3] = {};
+  float* RF[3] = {};
+  float* RHF[3] = {};
+  float* PF[3] = {};
+  float* VF[3] = {};
+  float* SF[3] = {};
+  float* TF[3] = {};
   double* PB = nullptr;
   double* TL_DP = nullptr;
   double* sc = nullptr;
@@ -114,9 +126,16 @@ int ensure3(ns_ctx* c) {
   }
   if (r == NS_OK) r = al(&A.PB, S.fb);
   if (r == NS_OK) r = al(&A.TL_DP, S.fb);
-  if (r == NS_OK) r = al(&A.sc, kBcN * sizeof(double));
-  if (r == NS_OK && cudaMallocHost(&A.sc_h, kBcN * sizeof(double)) != cudaSuccess)
+  if (r == NS_OK) r = al(&A.sc, kRfN * sizeof(double));
+  if (r == NS_OK && cudaMallocHost(&A.sc_h, kRfN * sizeof(double)) != cudaSuccess)
     r = fail(c, NS_ERR_NOMEM, "cudaMallocHost (3D adjoint) failed");
+  A.mixed = c->P.precision == NS_PREC_MIXED;
+  for (int m = 0; m < 3 && r == NS_OK && A.mixed; ++m) {
+    float** fs[] = {&A.US32[m], &A.PHB32[m], &A.Q32[0][m], &A.Q32[1][m], &A.Q32[2][m], &A.XF[m], &A.RF[m],
+                    &A.RHF[m], &A.PF[m], &A.VF[m], &A.SF[m], &A.TF[m]};
+    for (float** p : fs)
+      if (r == NS_OK) r = al(reinterpret_cast<double**>(p), S.fb / 2);
+  }
   if (r != NS_OK) free_adj3(c);
   return r;
 }
@@ -126,7 +145,10 @@ A3Args a3(ns_ctx* c) {
   A3Args a;
   std::memset(&a, 0, sizeof(a));
   a.g = c->g;
+  a.c15 = c->g.c15;
   for (int m = 0; m < 3; ++m) {
+    a.ix[m] = c->g.inv_dx[m];
+    a.vc[m] = c->g.inv_dx2[m] * c->g.inv_ren;
     a.us[m] = A.US[m];
     a.phb[m] = A.PHB[m];
     a.dph[m] = A.DPH[m];
@@ -140,14 +162,61 @@ A3Args a3(ns_ctx* c) {
   return a;
 }
 
+// FP32 operands: base in US32 / PHB32 / Q32, work arrays as float views of
+// the FP64 ones (the FP64 and FP32 operators never run concurrently)
+A3T<float> a3f(ns_ctx* c) {
+  Adj3& A = *c->s3->adj;
+  A3T<float> a;
+  std::memset(&a, 0, sizeof(a));
+  a.g = c->g;
+  a.c15 = (float)c->g.c15;
+  for (int m = 0; m < 3; ++m) {
+    a.ix[m] = (float)c->g.inv_dx[m];
+    a.vc[m] = (float)(c->g.inv_dx2[m] * c->g.inv_ren);
+    a.us[m] = A.US32[m];
+    a.phb[m] = A.PHB32[m];
+    a.dph[m] = reinterpret_cast<float*>(A.DPH[m]);
+    a.ct[m] = reinterpret_cast<float*>(A.CT[m]);
+    a.uadv[m] = reinterpret_cast<float*>(A.UADV[m]);
+    for (int d = 0; d < 3; ++d) {
+      a.q[d][m] = A.Q32[d][m];
+      a.fl[d][m] = reinterpret_cast<float*>(A.FL[d][m]);
+    }
+  }
+  return a;
+}
+
 #define L3(what, kernel, args)                                                                    \
   LAUNCH(NS_PROF_OTHER, what, (kernel<<<cells_grid(c->N), 256, 0, c->st>>> args, cudaGetLastError()))
 
 // linearisation point: cell velocity and QUICK interpolants of u* (US)
 int base3(ns_ctx* c) {
   const A3Args a = a3(c);
-  L3("adjoint3 base cells", k3a_base_cells, (a));
-  L3("adjoint3 base q", k3a_base_q, (a));
+  L3("adjoint3 base cells", k3a_base_cells<double>, (a));
+  L3("adjoint3 base q", k3a_base_q<double>, (a));
+  if (c->s3->adj->mixed) {
+    Adj3& A = *c->s3->adj;
+    L3("adjoint3 base f32", k3r_to_f32, (c->g, A.US[0], A.US[1], A.US[2], A.US32[0], A.US32[1], A.US32[2]));
+    const A3T<float> f = a3f(c);
+    L3("adjoint3 base cells f32", k3a_base_cells<float>, (f));
+    L3("adjoint3 base q f32", k3a_base_q<float>, (f));
+  }
+  return NS_OK;
+}
+
+template <typename T>
+int apply_t(ns_ctx* c, int transpose, const A3T<T>& a) {
+  if (!transpose) {
+    L3("jvp3 cells", k3a_jv_cells<T>, (a));
+    L3("jvp3 flux", k3a_jv_flux<T>, (a));
+    L3("jvp3 total", k3a_jv_total<T>, (a));
+    L3("jvp3 faces", k3a_jv_faces<T>, (a));
+  } else {
+    L3("vjp3 tbar", k3a_vj_tbar<T>, (a));
+    L3("vjp3 flux", k3a_vj_flux<T>, (a));
+    L3("vjp3 cells", k3a_vj_cells<T>, (a));
+    L3("vjp3 faces", k3a_vj_faces<T>, (a));
+  }
   return NS_OK;
 }
 
@@ -158,23 +227,22 @@ int apply3(ns_ctx* c, int transpose, double* const* x, double* const* y) {
     a.v[m] = x[m];
     a.out[m] = y[m];
   }
-  if (!transpose) {
-    L3("jvp3 cells", k3a_jv_cells, (a));
-    L3("jvp3 flux", k3a_jv_flux, (a));
-    L3("jvp3 total", k3a_jv_total, (a));
-    L3("jvp3 faces", k3a_jv_faces, (a));
-  } else {
-    L3("vjp3 tbar", k3a_vj_tbar, (a));
-    L3("vjp3 flux", k3a_vj_flux, (a));
-    L3("vjp3 cells", k3a_vj_cells, (a));
-    L3("vjp3 faces", k3a_vj_faces, (a));
+  return apply_t(c, transpose, a);
+}
+
+// the same in FP32 on the FP32 base
+int apply3f(ns_ctx* c, int transpose, float* const* x, float* const* y) {
+  A3T<float> a = a3f(c);
+  for (int m = 0; m < 3; ++m) {
+    a.v[m] = x[m];
+    a.out[m] = y[m];
   }
-  return NS_OK;
+  return apply_t(c, transpose, a);
 }
 
 int scalars3(ns_ctx* c) {
   Adj3& A = *c->s3->adj;
-  CK(cudaMemcpyAsync(A.sc_h, A.sc, kBcN * sizeof(double), cudaMemcpyDeviceToHost, c->st), "readback");
+  CK(cudaMemcpyAsync(A.sc_h, A.sc, kRfN * sizeof(double), cudaMemcpyDeviceToHost, c->st), "readback");
   CK(cudaStreamSynchronize(c->st), "stream sync");
   if (c->prof) prof_resolve(c);
   return NS_OK;
@@ -241,6 +309,98 @@ int bicg3(ns_ctx* c, int transpose, int* iters, double* res) {
   return NS_OK;
 }
 
+// inner FP32 BiCGStab of the refinement: op(J) XF = RF from XF = 0 until the
+// residual falls by rel_tol, a breakdown, or max_it iterations
+int bicg3f(ns_ctx* c, int transpose, double rel_tol, int max_it, int* iters) {
+  Adj3& A = *c->s3->adj;
+  Bcg3f b;
+  std::memset(&b, 0, sizeof(b));
+  b.g = c->g;
+  for (int m = 0; m < 3; ++m) {
+    b.x[m] = A.XF[m]; b.r[m] = A.RF[m]; b.rh[m] = A.RHF[m]; b.p[m] = A.PF[m];
+    b.v[m] = A.VF[m]; b.s[m] = A.SF[m]; b.t[m] = A.TF[m]; b.b[m] = A.RF[m];  // r starts as b, in place
+  }
+  b.sc = A.sc;
+  b.part = c->s3->part;
+  b.counter = c->counter;
+  L3("bicgstab3 f32 init", k3c_init, (b));
+  int r = scalars3(c);
+  if (r != NS_OK) return r;
+  const double rr0 = A.sc_h[kBcRR];
+  int it = 0;
+  double rel = rr0 > 0.0 ? 1.0 : 0.0;
+  while (rel > rel_tol && it < max_it) {
+    r = apply3f(c, transpose, A.PF, A.VF);
+    if (r != NS_OK) return r;
+    L3("bicgstab3 f32 alpha", k3c_alpha, (b));
+    L3("bicgstab3 f32 s", k3c_s, (b));
+    r = apply3f(c, transpose, A.SF, A.TF);
+    if (r != NS_OK) return r;
+    L3("bicgstab3 f32 omega", k3c_omega, (b));
+    L3("bicgstab3 f32 x r", k3c_xr, (b));
+    L3("bicgstab3 f32 p", k3c_p, (b));
+    ++it;
+    r = scalars3(c);
+    if (r != NS_OK) return r;
+    rel = std::sqrt(A.sc_h[kBcRR] / rr0);
+    if (!std::isfinite(rel)) return fail(c, NS_ERR_CUDA, "BiCGStab (FP32): non-finite residual");
+    if (A.sc_h[kBcBreak] != 0.0) break;
+  }
+  *iters = it;
+  return NS_OK;
+}
+
+constexpr double kInnerTol = 1e-5;  // residual reduction of one inner FP32 solve
+constexpr int kMaxRefine = 8;
+
+// op(J) X = BV from the guess in X: FP64 BiCGStab, or (mixed precision) FP64
+// residuals refined by inner FP32 solves; the relative residual of the
+// refinement is max |r| / max |b|
+int solve3(ns_ctx* c, int transpose, int* iters, double* res) {
+  Adj3& A = *c->s3->adj;
+  if (!A.mixed) return bicg3(c, transpose, iters, res);
+  Ref3 f;
+  std::memset(&f, 0, sizeof(f));
+  f.g = c->g;
+  for (int m = 0; m < 3; ++m) {
+    f.b[m] = A.BV[m]; f.v[m] = A.V[m]; f.r32[m] = A.RF[m]; f.x[m] = A.X[m]; f.d[m] = A.XF[m];
+  }
+  f.sc = A.sc;
+  f.part = c->s3->part;
+  f.counter = c->counter;
+  const double tol = A.opts.lin_tol;
+  int inner = 0;
+  double rel = 0.0;
+  for (int outer = 0;; ++outer) {
+    int r = apply3(c, transpose, A.X, A.V);
+    if (r != NS_OK) return r;
+    L3("refine residual max", k3r_resmax, (f));
+    r = scalars3(c);
+    if (r != NS_OK) return r;
+    const double rmax = A.sc_h[kRfRR], bmax = A.sc_h[kRfBB];
+    if (!(bmax > 0.0)) {
+      for (int m = 0; m < 3; ++m) CK(cudaMemsetAsync(A.X[m], 0, c->s3->fb, c->st), "memset");
+      rel = 0.0;
+      break;
+    }
+    rel = rmax / bmax;
+    if (!std::isfinite(rel)) return fail(c, NS_ERR_CUDA, "refinement: non-finite residual");
+    if (rel <= tol || outer >= kMaxRefine || inner >= A.opts.lin_max_iters) break;
+    L3("refine residual f32", k3r_scaled, (f, 1.0 / rmax));
+    int it = 0;
+    r = bicg3f(c, transpose, kInnerTol, A.opts.lin_max_iters, &it);
+    if (r != NS_OK) return r;
+    inner += it;
+    L3("refine update", k3r_update, (f, rmax));
+  }
+  *iters = inner;
+  *res = rel;
+  A.st.lin_iters += inner;
+  A.st.lin_max_iters_seen = std::max(A.st.lin_max_iters_seen, inner);
+  A.st.lin_max_res = std::max(A.st.lin_max_res, rel);
+  return NS_OK;
+}
+
 // F = D u + coef pb (sum into red[kRedSum]); psi = L^-1 P0 F in PHI
 int poisson_adj3(ns_ctx* c, double* const* u, const double* pb, double coef, const double** psi) {
   State3D& S = *c->s3;
@@ -291,7 +451,7 @@ int adj_step3(ns_ctx* c) {
   if (r != NS_OK) return r;
   int it = 0;
   double res = 0.0;
-  r = bicg3(c, 1, &it, &res);
+  r = solve3(c, 1, &it, &res);
   if (r != NS_OK) return r;
   L3("adjoint3 ubar", k3a_lincomb, (g, 1.0, A.UPB[0], A.UPB[1], A.UPB[2], g.c15 + g.c05, A.X[0], A.X[1], A.X[2], A.UB[0], A.UB[1], A.UB[2]));
   L3("adjoint3 uprevbar", k3a_lincomb, (g, -g.c05, A.X[0], A.X[1], A.X[2], 0.0, nullptr, nullptr, nullptr, A.UPB[0], A.UPB[1], A.UPB[2]));
@@ -314,7 +474,7 @@ int tan_step3(ns_ctx* c) {
   L3("tangent3 rhs", k3a_tlm_rhs, (ta, A.TL_DP, A.TL_DUP[0], A.TL_DUP[1], A.TL_DUP[2]));
   int it = 0;
   double res = 0.0;
-  r = bicg3(c, 0, &it, &res);
+  r = solve3(c, 0, &it, &res);
   if (r != NS_OK) return r;
   const double* psi = nullptr;
   r = poisson_adj3(c, A.X, nullptr, 0.0, &psi);

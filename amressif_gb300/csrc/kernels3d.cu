@@ -89,7 +89,7 @@ cudaError_t launch3i_total(const Inc3& a, cudaStream_t s) {
 }
 cudaError_t launch3i_face(const Inc3& a, cudaStream_t s) {
   const int N = a.g.N;
-  k3i_face<<<grid3(N + 1, N + 1, N + 1), 256, 0, s>>>(a);
+  k3i_face<<<grid3(N + 1, N + 1, (N + kIncFaceKZ) / kIncFaceKZ), 256, 0, s>>>(a);
   return cudaGetLastError();
 }
 long blocks3_face(int N) { return (long)((N + 1 + 31) / 32) * ((N + 1 + 7) / 8) * (N + 1); }

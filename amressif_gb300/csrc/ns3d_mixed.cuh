@@ -330,31 +330,40 @@ __device__ __forceinline__ float t_along_inc(const Inc3& A, int m, int a, long b
 }
 
 // e_out = rk (G0 - (1.5/dt) e_in + avg(dt)); the last stage writes
-// u_b + e_out (float-float) and the pseudo-norm of e_out
+// u_b + e_out (float-float) and the pseudo-norm of e_out. Each block walks
+// kIncFaceKZ planes, so the reducing launch has few blocks (one partial and
+// one counter update per block).
+constexpr int kIncFaceKZ = 8;
+
 __global__ void __launch_bounds__(256) k3i_face(Inc3 A) {
   const Geom& g = A.g;
   const int N = g.N;
-  NS3_IJK(0, 0, 0)
+  const int i = (int)(blockIdx.x * 32 + (threadIdx.x & 31));
+  const int j = (int)(blockIdx.y * 8 + (threadIdx.x >> 5));
   float nrm[3] = {0.f, 0.f, 0.f};
   const long fstride[3] = {1, g.pitch, g.plane};
-  for (int m = 0; m < 3; ++m) {
-    const int lim[3] = {N + (m == 0), N + (m == 1), N + (m == 2)};
-    if (i >= lim[0] || j >= lim[1] || k >= lim[2]) continue;
-    const int c[3] = {i, j, k};
-    const int a = c[m];
-    const long id = id3(g, i, j, k);
-    const long st = fstride[m];
-    const long base = id - (long)a * st;
-    const float tl = t_along_inc(A, m, a - 1, base, st), tr = t_along_inc(A, m, a, base, st);
-    const float G = (A.g0[m][id] - A.c15 * inc_e(A, m, id)) + 0.5f * (tl + tr);
-    const float eo = A.rk * G;
-    if (A.last) {
-      const ff b = A.baseff[m] ? ld2(A.baseff[m], id) : ld_ff(A.base64[m], id);
-      st2(A.outff[m], id, ff_add_f(b, eo));
-      const float w = (a == 0 || a == N) ? 0.5f : 1.f;
-      nrm[m] = eo * eo * w;
-    } else {
-      A.eout[m][id] = eo;
+  for (int kk = 0; kk < kIncFaceKZ; ++kk) {
+    const int k = (int)blockIdx.z * kIncFaceKZ + kk;
+    if (k > N) break;
+    for (int m = 0; m < 3; ++m) {
+      const int lim[3] = {N + (m == 0), N + (m == 1), N + (m == 2)};
+      if (i >= lim[0] || j >= lim[1] || k >= lim[2]) continue;
+      const int c[3] = {i, j, k};
+      const int a = c[m];
+      const long id = id3(g, i, j, k);
+      const long st = fstride[m];
+      const long base = id - (long)a * st;
+      const float tl = t_along_inc(A, m, a - 1, base, st), tr = t_along_inc(A, m, a, base, st);
+      const float G = (A.g0[m][id] - A.c15 * inc_e(A, m, id)) + 0.5f * (tl + tr);
+      const float eo = A.rk * G;
+      if (A.last) {
+        const ff b = A.baseff[m] ? ld2(A.baseff[m], id) : ld_ff(A.base64[m], id);
+        st2(A.outff[m], id, ff_add_f(b, eo));
+        const float w = (a == 0 || a == N) ? 0.5f : 1.f;
+        nrm[m] += eo * eo * w;
+      } else {
+        A.eout[m][id] = eo;
+      }
     }
   }
   double tot[3];
