@@ -83,9 +83,13 @@ struct DCff3 {
 
 #ifndef NS_3D_ARGS_ONLY
 
-__device__ __forceinline__ ff ld_ff(const double* p, long i) { return ff_from_double(p[i]); }
+// Every input of these kernels is read-only for the launch (outputs go to other
+// buffers), so loads use the non-coherent path: the compiler may then issue
+// them ahead of the stores, which keeps many loads in flight per thread.
+__device__ __forceinline__ float ldf(const float* p, long i) { return __ldg(p + i); }
+__device__ __forceinline__ ff ld_ff(const double* p, long i) { return ff_from_double(__ldg(p + i)); }
 __device__ __forceinline__ ff ld2(const float2* p, long i) {
-  const float2 v = p[i];
+  const float2 v = __ldg(p + i);
   return ff_make(v.x, v.y);
 }
 __device__ __forceinline__ void st2(float2* p, long i, ff v) { p[i] = make_float2(v.hi, v.lo); }
@@ -146,19 +150,22 @@ __global__ void __launch_bounds__(256) k3f_flux(AncFF A) {
   const long gc = gid3(N, i, j, k);
   const long fc = id3(g, i, j, k);
   const int c[3] = {i, j, k};
+  // every face thread loads all its stencils (indices stay inside the ghosted
+  // array), selects the upwind one and stores only the faces that exist, so
+  // the loads of the three directions are independent of any branch
+#pragma unroll
   for (int d = 0; d < 3; ++d) {
-    bool ok = true;
-    for (int e = 0; e < 3; ++e)
-      if (e != d && c[e] >= N) ok = false;
-    if (!ok) continue;
+    const bool ok = (d == 0 || c[0] < N) && (d == 1 || c[1] < N) && (d == 2 || c[2] < N);
     const long s = G1[d];
     const ff ud = ld_base(A, d, fc);
+    const bool pos = ud.hi > 0.f;
+#pragma unroll
     for (int m = 0; m < 3; ++m) {
       const float2* ph = A.ph[m];
-      ff F = ff_make(0.f, 0.f);
-      if (ud.hi > 0.f) F = ud * q3p_ff(ld2(ph, gc - 2 * s), ld2(ph, gc - s), ld2(ph, gc));
-      else if (ud.hi < 0.f) F = ud * q3m_ff(ld2(ph, gc - s), ld2(ph, gc), ld2(ph, gc + s));
-      st2(A.fl[d][m], fc, F);
+      const ff x2 = ld2(ph, gc - 2 * s), x1 = ld2(ph, gc - s), x0 = ld2(ph, gc), xa = ld2(ph, gc + s);
+      const ff q = pos ? q3p_ff(x2, x1, x0) : q3m_ff(x1, x0, xa);
+      const ff F = ud.hi != 0.f ? ud * q : ff_make(0.f, 0.f);
+      if (ok) st2(A.fl[d][m], fc, F);
     }
   }
 }
@@ -222,7 +229,7 @@ __global__ void __launch_bounds__(256) k3f_face(AncFF A) {
 
 // ---- FP32 increment stages ----------------------------------------------------------------
 __device__ __forceinline__ float inc_e(const Inc3& A, int m, long id) {
-  return A.ein[m] ? A.ein[m][id] : A.rk_prev * A.g0[m][id];
+  return A.ein[m] ? ldf(A.ein[m], id) : A.rk_prev * ldf(A.g0[m], id);
 }
 
 // ghosted cell velocity of the increment (homogeneous ghosts); cells with
@@ -278,7 +285,7 @@ __global__ void __launch_bounds__(256) k3i_flux(Inc3 A) {
       if (e != d && c[e] >= N) ok = false;
     if (!ok) continue;
     const long s = G1[d];
-    const float ub = A.ub[d][fc];
+    const float ub = ldf(A.ub[d], fc);
     const float e = inc_e(A, d, fc);
     const float un = ub + e;
     const float dpos = ub > 0.f ? (un > 0.f ? e : -ub) : fmaxf(un, 0.f);  // un+ - ub+
@@ -287,9 +294,9 @@ __global__ void __launch_bounds__(256) k3i_flux(Inc3 A) {
     for (int m = 0; m < 3; ++m) {
       const float* pb = A.phb[m];
       const float* pe = A.phe[m];
-      const float b2 = pb[gc - 2 * s], b1 = pb[gc - s], b0 = pb[gc], ba = pb[gc + s];
-      const float e1 = pe[gc - s], e0 = pe[gc];
-      const float qe = pos ? q3p(pe[gc - 2 * s], e1, e0) : q3m(e1, e0, pe[gc + s]);
+      const float b2 = ldf(pb, gc - 2 * s), b1 = ldf(pb, gc - s), b0 = ldf(pb, gc), ba = ldf(pb, gc + s);
+      const float e1 = ldf(pe, gc - s), e0 = ldf(pe, gc);
+      const float qe = pos ? q3p(ldf(pe, gc - 2 * s), e1, e0) : q3m(e1, e0, ldf(pe, gc + s));
       A.dfl[d][m][fc] = dpos * q3p(b2, b1, b0) + dneg * q3m(b1, b0, ba) + un * qe;
     }
   }
@@ -307,13 +314,13 @@ __global__ void __launch_bounds__(256) k3i_total(Inc3 A) {
   const long fstride[3] = {1, g.pitch, g.plane};
   for (int m = 0; m < 3; ++m) {
     const float* ph = A.phe[m];
-    const float p0 = ph[gc];
+    const float p0 = ldf(ph, gc);
     float conv = 0.f, visc = 0.f;
     for (int d = 0; d < 3; ++d) {
       const long s = G1[d];
       const float* F = A.dfl[d][m];
-      conv += (F[fc + fstride[d]] - F[fc]) * A.inv_dx[d];
-      visc += (ph[gc + s] - 2.f * p0 + ph[gc - s]) * A.vcoef[d];
+      conv += (ldf(F, fc + fstride[d]) - ldf(F, fc)) * A.inv_dx[d];
+      visc += (ldf(ph, gc + s) - 2.f * p0 + ldf(ph, gc - s)) * A.vcoef[d];
     }
     A.dt[m][fc] = visc - conv;
   }
@@ -321,12 +328,12 @@ __global__ void __launch_bounds__(256) k3i_total(Inc3 A) {
 
 __device__ __forceinline__ float t_along_inc(const Inc3& A, int m, int a, long base, long st) {
   const int N = A.g.N;
-  if (a >= 0 && a < N) return A.dt[m][base + a * st];
+  if (a >= 0 && a < N) return ldf(A.dt[m], base + a * st);
   const int fg = A.g.flux_ghost[m];
-  if (fg == kWrap) return A.dt[m][base + (long)wrapi(a, N) * st];
+  if (fg == kWrap) return ldf(A.dt[m], base + (long)wrapi(a, N) * st);
   if (fg == kZero) return 0.f;
   const int am = a < 0 ? 0 : N - 1;
-  return -A.dt[m][base + (long)am * st];
+  return -ldf(A.dt[m], base + (long)am * st);
 }
 
 // e_out = rk (G0 - (1.5/dt) e_in + avg(dt)); the last stage writes
@@ -354,7 +361,7 @@ __global__ void __launch_bounds__(256) k3i_face(Inc3 A) {
       const long st = fstride[m];
       const long base = id - (long)a * st;
       const float tl = t_along_inc(A, m, a - 1, base, st), tr = t_along_inc(A, m, a, base, st);
-      const float G = (A.g0[m][id] - A.c15 * inc_e(A, m, id)) + 0.5f * (tl + tr);
+      const float G = (ldf(A.g0[m], id) - A.c15 * inc_e(A, m, id)) + 0.5f * (tl + tr);
       const float eo = A.rk * G;
       if (A.last) {
         const ff b = A.baseff[m] ? ld2(A.baseff[m], id) : ld_ff(A.base64[m], id);
@@ -380,7 +387,7 @@ __global__ void __launch_bounds__(256) k3i_face(Inc3 A) {
 __device__ __forceinline__ ff dc3_val(const DCff3& A, long id) {
   if (A.first) return ff_make(0.f, 0.f);
   const ff v = ld2(A.phin, id);
-  return A.e ? ff_add_f(v, A.e[id]) : v;
+  return A.e ? ff_add_f(v, ldf(A.e, id)) : v;
 }
 
 __global__ void __launch_bounds__(256) k3_dcff(DCff3 A) {
