@@ -26,14 +26,18 @@ struct DCffArgs {
   double* red_out;       // {max |r|}
 };
 
+// Tile of 32 x kDcTY cells per block of 256 threads (each thread updates
+// kDcTY / 8 rows), with a one-cell halo of phi + e in shared memory.
+constexpr int kDcTY = 32;
+
 static __global__ void __launch_bounds__(256) k_dc_update_ff2d(DCffArgs A) {
-  __shared__ ff sp[10][34];
+  __shared__ ff sp[kDcTY + 2][34];
   const int n = A.n;
   const long P = A.pitch;
-  const int x0 = blockIdx.x * 32, y0 = blockIdx.y * 8;
+  const int x0 = blockIdx.x * 32, y0 = blockIdx.y * kDcTY;
   const bool px = A.periodic[0], py = A.periodic[1];
   const int lane = threadIdx.x & 31, wy = threadIdx.x >> 5;
-  for (int ly = wy; ly < 10; ly += 8)
+  for (int ly = wy; ly < kDcTY + 2; ly += 8)
     for (int lx = lane; lx < 34; lx += 32) {
       int a = x0 - 1 + lx, b = y0 - 1 + ly;
       ff v = ff_make(0.f, 0.f);
@@ -44,25 +48,28 @@ static __global__ void __launch_bounds__(256) k_dc_update_ff2d(DCffArgs A) {
       sp[ly][lx] = v;
     }
   __syncthreads();
-  const int a = x0 + lane, b = y0 + wy;
+  const ff ihx = ff_make(A.ih[0][0], A.ih[0][1]), ihy = ff_make(A.ih[1][0], A.ih[1][1]);
   float v[1] = {0.f};
-  if (a < n && b < n) {
-    const int lx = lane + 1, ly = wy + 1;
-    const ff c = sp[ly][lx];
-    const ff ihx = ff_make(A.ih[0][0], A.ih[0][1]), ihy = ff_make(A.ih[1][0], A.ih[1][1]);
-    ff sx = ff_make(0.f, 0.f), sy = sx;
-    if (px || a + 1 < n) sx = sx + (sp[ly][lx + 1] - c);
-    if (px || a > 0) sx = sx + (sp[ly][lx - 1] - c);
-    if (py || b + 1 < n) sy = sy + (sp[ly + 1][lx] - c);
-    if (py || b > 0) sy = sy + (sp[ly - 1][lx] - c);
-    const ff lap = sx * ihx + sy * ihy;
-    const long id = (long)b * P + a;
-    const ff r = ff_make(A.f[0][id], A.f[1][id]) - lap;
-    A.phout[0][id] = c.hi;
-    A.phout[1][id] = c.lo;
-    const float r1 = r.hi + r.lo;
-    A.r32[id] = r1;
-    v[0] = fabsf(r1);
+#pragma unroll
+  for (int rr = 0; rr < kDcTY / 8; ++rr) {
+    const int a = x0 + lane, b = y0 + wy + 8 * rr;
+    if (a < n && b < n) {
+      const int lx = lane + 1, ly = wy + 8 * rr + 1;
+      const ff c = sp[ly][lx];
+      ff sx = ff_make(0.f, 0.f), sy = sx;
+      if (px || a + 1 < n) sx = sx + (sp[ly][lx + 1] - c);
+      if (px || a > 0) sx = sx + (sp[ly][lx - 1] - c);
+      if (py || b + 1 < n) sy = sy + (sp[ly + 1][lx] - c);
+      if (py || b > 0) sy = sy + (sp[ly - 1][lx] - c);
+      const ff lap = sx * ihx + sy * ihy;
+      const long id = (long)b * P + a;
+      const ff r = ff_make(A.f[0][id], A.f[1][id]) - lap;
+      A.phout[0][id] = c.hi;
+      A.phout[1][id] = c.lo;
+      const float r1 = r.hi + r.lo;
+      A.r32[id] = r1;
+      v[0] = fmaxf(v[0], fabsf(r1));
+    }
   }
   double out[1];
   if (grid_reduce_last_f<1, 256>(v, reinterpret_cast<float2*>(A.part), A.counter, 1u, out) && threadIdx.x == 0)

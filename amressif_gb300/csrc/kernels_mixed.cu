@@ -52,7 +52,7 @@ cudaError_t launch_split_ff(const Geom& g, const double* const* x, float* const*
 }
 
 cudaError_t launch_dc_update_ff(const DCffArgs& a, cudaStream_t s) {
-  dim3 grid((a.n + 31) / 32, (a.n + 7) / 8, 1);
+  dim3 grid((a.n + 31) / 32, (a.n + kDcTY - 1) / kDcTY, 1);
   k_dc_update_ff2d<<<grid, 256, 0, s>>>(a);
   return cudaGetLastError();
 }

@@ -108,6 +108,7 @@ __global__ void __launch_bounds__(256) k_mg_smooth(MGLevels<T> M, int l, int mod
   }
   __syncthreads();
   const int cfirst = (mode == 1) ? 1 : 0;
+#pragma unroll  // r, w, h, w2 become constants: no runtime integer division per cell
   for (int s = 0; s < 4; ++s) {
     const int color = (cfirst + s) & 1;
     const int r = H - 1 - s;

@@ -144,6 +144,51 @@ def dist_setup():
     return 1, 0, None
 
 
+def vcycle_bytes(n):
+    """Algorithmic bytes of one FP32 V-cycle of the 2D hierarchy: per tiled
+    level (n_l >= 64) the pre-smoothing reads f and writes x (8 B/cell, x
+    starts at 0), the restriction reads x and f and writes the coarse f (9),
+    the prolongation + post-smoothing reads x, f and the coarse x and writes x
+    (13); the levels of 32^2 and below run in one CTA and are left out."""
+    b, m = 0, n
+    while True:
+        if m >= 64:
+            b += 30 * m * m
+        if not (m % 4 == 0 and m > 4):
+            break
+        m //= 2
+    return b
+
+
+def throughput_block(n, K, total_s, stats, prof, peak):
+    """cell-updates/s, whole-step algorithmic GB/s and V-cycle GB/s, each with
+    its fraction of the measured HBM peak"""
+    steps_per_s = K / total_s
+    kmean = statistics.mean(st["pseudo_iters"] for st in stats)
+    cycles = sum(st["poisson_cycles"] for st in stats)
+    algo = sum(ALGO_BYTES_PER_CELL[k] * n * n * c for k, (c, _) in prof.items() if k in ALGO_BYTES_PER_CELL)
+    mg_kinds = ("mg_smooth0", "mg_smooth", "mg_restrict0", "mg_restrict", "mg_bottom")
+    mg_ms = sum(prof[k][1] for k in mg_kinds if k in prof)
+    dc_c, dc_ms = prof.get("dc_update", (0, 0.0))
+    out = {"cell_updates_per_s": steps_per_s * n * n,
+           "rk_stage_cell_updates_per_s": steps_per_s * n * n * kmean * 4,
+           "step_algorithmic_gbs": algo / total_s / 1e9,
+           "step_algorithmic_frac": algo / total_s / 1e9 / peak,
+           "note": "algorithmic bytes of the kinds with a per-cell figure (ALGO_BYTES_PER_CELL) over the device "
+                   "time of the timed steps; the predictor kernels are issue-bound, not HBM-bound"}
+    if cycles > 0 and mg_ms > 0:
+        vb = vcycle_bytes(n)
+        t = mg_ms / cycles * 1e-3
+        out["vcycle"] = {"cycles": cycles, "ms": 1e3 * t, "algorithmic_bytes": vb, "gbs": vb / t / 1e9,
+                         "frac": vb / t / 1e9 / peak}
+        if dc_c:
+            td = dc_ms / dc_c * 1e-3
+            db = ALGO_BYTES_PER_CELL["dc_update"] * n * n
+            out["dc_update"] = {"ms": 1e3 * td, "algorithmic_bytes": db, "gbs": db / td / 1e9,
+                                "frac": db / td / 1e9 / peak}
+    return out
+
+
 def run_steps(s, k):
     stats = [s.step() for _ in range(k)]
     return stats
@@ -416,6 +461,7 @@ def bench_ours(args):
                     "ms_per_launch": per_launch_ms, "launches": cnt}
     kernels = {k: {"launches": c, "ms_total": m, "ms_per_launch": (m / c if c else None),
                    "share": m / max(dev_ms, 1e-9)} for k, (c, m) in prof.items() if c}
+    throughput = throughput_block(n, K, total_s, stats, prof, peak)
 
     # ---- CPU restatement timed on the host (rank 0, N=1) ----
     cpu = None
@@ -460,6 +506,7 @@ def bench_ours(args):
             "e2e": e2e,
             "gpu_launches": launches,
             "roofline": roofline,
+            "throughput": throughput,
             "kernels": kernels,
             "cpu_baseline": cpu,
             "clocks": summarize_clocks(samples),
