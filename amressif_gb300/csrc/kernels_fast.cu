@@ -41,10 +41,10 @@ constexpr int kMgTX = 64, kMgTY = 16;
 template <typename T>
 cudaError_t launch_mg_smooth(const MGLevels<T>& M, int l, int mode, int x_zero, cudaStream_t s) {
   const int n = M.n[l];
-  if constexpr (sizeof(T) == 4) {  // FP32 fine levels: 128 x 32 tiles (43.5 KB), less halo per cell
-    if (n >= 2048) {  // at least 1024 blocks
-      dim3 grid((n + 127) / 128, (n + 31) / 32, 1);
-      k_mg_smooth<T, 128, 32><<<grid, 256, 0, s>>>(M, l, mode, x_zero);
+  if constexpr (sizeof(T) == 4) {  // FP32 finest levels: the warp-marching smoother (>= 4736 warps)
+    if (n >= 4096) {
+      const long warps = (long)((n + kColSmOut - 1) / kColSmOut) * ((n + kColSmH - 1) / kColSmH);
+      k_mg_smooth_col<T><<<(unsigned)((warps + 3) / 4), 128, 0, s>>>(M, l, mode, x_zero);
       return cudaGetLastError();
     }
   }

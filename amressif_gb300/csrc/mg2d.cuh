@@ -25,6 +25,9 @@ struct MGLevels {
   int n[kMaxLevels];
   long pitch[kMaxLevels];
   T* x[kMaxLevels];
+  T* x2[kMaxLevels];              // smoother output: the smoothers read x and write x2 (the
+                                  // caller swaps them), so no block reads a halo another block
+                                  // has already overwritten
   T* f[kMaxLevels];
   double invh2[kMaxLevels][2];
   // 1/diagonal for the (east+west, north+south) neighbour counts: index a + 3 b
@@ -38,13 +41,28 @@ struct MGLevels {
 
 // Gauss-Seidel update of one cell from its four neighbours; w* = 0 removes an
 // absent (Neumann) neighbour from both the sum and the diagonal.
+// explicitly rounded operations: every smoother kernel (tiled, warp-marching)
+// forms exactly the same value, whatever the compiler contracts elsewhere
+__device__ __forceinline__ float rn_add(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float rn_mul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double rn_add(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double rn_mul(double a, double b) { return __dmul_rn(a, b); }
+
+// bilinear cell-centred prolongation weights 9/16, 3/16, 3/16, 1/16 (explicitly rounded)
+template <typename T>
+__device__ __forceinline__ T prolong_add(T x, T c00, T c10, T c01, T c11) {
+  const T a = rn_mul((T)0.5625, c00), b = rn_mul((T)0.1875, rn_add(c10, c01)), d = rn_mul((T)0.0625, c11);
+  return rn_add(x, rn_add(rn_add(a, b), d));
+}
+
 template <typename T>
 __device__ __forceinline__ T gs_update(T xe, T xw, T xn, T xs, bool we, bool ww, bool wn, bool wsn, T ihx, T ihy, T f,
                                        const T* idg) {
   const T zero = (T)0;
-  const T sum = ((we ? xe : zero) + (ww ? xw : zero)) * ihx + ((wn ? xn : zero) + (wsn ? xs : zero)) * ihy;
+  const T sx = rn_mul(rn_add(we ? xe : zero, ww ? xw : zero), ihx);
+  const T sy = rn_mul(rn_add(wn ? xn : zero, wsn ? xs : zero), ihy);
   const int k = (int)we + (int)ww + 3 * ((int)wn + (int)wsn);
-  return (sum - f) * idg[k];
+  return rn_mul(rn_add(rn_add(sx, sy), -f), idg[k]);
 }
 
 template <typename T>
@@ -100,7 +118,7 @@ __global__ void __launch_bounds__(256) k_mg_smooth(MGLevels<T> M, int l, int mod
         const T* xc = M.x[l + 1];
         const T c00 = xc[(long)J * Pc + I], c10 = xc[(long)J * Pc + I2];
         const T c01 = xc[(long)J2 * Pc + I], c11 = xc[(long)J2 * Pc + I2];
-        xv = xv + ((T)0.5625 * c00 + (T)0.1875 * (c10 + c01) + (T)0.0625 * c11);
+        xv = prolong_add(xv, c00, c10, c01, c11);
       }
     }
     sm.x[ly][lx] = xv;
@@ -131,7 +149,128 @@ __global__ void __launch_bounds__(256) k_mg_smooth(MGLevels<T> M, int l, int mod
   }
   for (int t = tid; t < TX * TY; t += NT) {
     const int a = x0 + t % TX, b = y0 + t / TX;
-    if (a < n && b < n) M.x[l][(long)b * P + a] = sm.x[b - (y0 - H)][a - (x0 - H)];
+    if (a < n && b < n) M.x2[l][(long)b * P + a] = sm.x[b - (y0 - H)][a - (x0 - H)];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Warp-marching smoother for the fine levels: the two red-black sweeps of
+// k_mg_smooth (same colours, same update arithmetic, same prolongation), laid
+// out for the GPU's issue rate instead of block barriers. One warp owns a
+// strip of 64 columns, two per lane (kColSmOut = 56 output columns between
+// four halo columns on each side), and a chunk of kColSmH rows, and climbs it
+// with the four half-sweeps as a skewed wavefront: at step t half-sweep s
+// works on row t - s, over the rows the tiled kernel gives it, so a row is
+// final once half-sweep 3 has passed it. y neighbours sit in a six-row
+// register window, x neighbours come by warp shuffle, the next row is loaded
+// one step ahead. Halo columns may take wrong values from the strip edge; an
+// error moves one column per half-sweep, so four halo columns keep the output
+// columns exact.
+// ---------------------------------------------------------------------------
+constexpr int kColSmOut = 56, kColSmH = 64;
+
+template <typename T>
+struct SmRow {
+  T x0, x1, f0, f1;
+};
+
+template <typename T>
+__device__ __forceinline__ SmRow<T> sm_load_row(const MGLevels<T>& M, int l, int mode, int x_zero, int r, int c0, bool cin) {
+  SmRow<T> o;
+  o.x0 = o.x1 = o.f0 = o.f1 = (T)0;
+  const int n = M.n[l];
+  const bool px = M.periodic[0], py = M.periodic[1];
+  if (!cin || !(py || (r >= 0 && r < n))) return o;
+  const int rr = wrapi(r, n), w0 = wrapi(c0, n);  // w0 even, w0 + 1 < n
+  const long id = (long)rr * M.pitch[l] + w0;
+  if (!x_zero) { o.x0 = M.x[l][id]; o.x1 = M.x[l][id + 1]; }
+  o.f0 = level_f(M, l, id);
+  o.f1 = level_f(M, l, id + 1);
+  if (mode == 1) {  // bilinear prolongation of the coarse correction (as k_mg_smooth)
+    const int nc = M.n[l + 1];
+    const long Pc = M.pitch[l + 1];
+    const int I = w0 >> 1, J = rr >> 1;
+    int Im = I - 1, Ip = I + 1, J2 = J + ((rr & 1) ? 1 : -1);
+    Im = px ? wrapi(Im, nc) : max(Im, 0);
+    Ip = px ? wrapi(Ip, nc) : min(Ip, nc - 1);
+    J2 = py ? wrapi(J2, nc) : min(max(J2, 0), nc - 1);
+    const T* xc = M.x[l + 1];
+    const T c00 = xc[(long)J * Pc + I], c01 = xc[(long)J2 * Pc + I];
+    const T cm0 = xc[(long)J * Pc + Im], cm1 = xc[(long)J2 * Pc + Im];  // column w0 - 1 side (w0 even)
+    const T cp0 = xc[(long)J * Pc + Ip], cp1 = xc[(long)J2 * Pc + Ip];  // column w0 + 2 side (w0 + 1 odd)
+    o.x0 = prolong_add(o.x0, c00, cm0, c01, cm1);
+    o.x1 = prolong_add(o.x1, c00, cp0, c01, cp1);
+  }
+  return o;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128) k_mg_smooth_col(MGLevels<T> M, int l, int mode, int x_zero) {
+  constexpr unsigned FULL = 0xffffffffu;
+  const int n = M.n[l];
+  const long P = M.pitch[l];
+  const int lane = threadIdx.x & 31;
+  const int nsx = (n + kColSmOut - 1) / kColSmOut, nsy = (n + kColSmH - 1) / kColSmH;
+  const int gw = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (gw >= nsx * nsy) return;  // warp-uniform; the kernel has no block barrier
+  const int xs = (gw % nsx) * kColSmOut, y0 = (gw / nsx) * kColSmH;
+  const bool px = M.periodic[0], py = M.periodic[1];
+  const T ihx = M.ih[l][0], ihy = M.ih[l][1];
+  const int cfirst = (mode == 1) ? 1 : 0;
+  const int c0 = xs - 4 + 2 * lane, c1 = c0 + 1;   // c0 even; both columns in or both out (n even)
+  const bool cin = px || (c0 >= 0 && c1 < n);
+  const bool we0 = true, ww0 = px || c0 > 0;     // neighbours of c0 (its east neighbour is c1)
+  const bool we1 = px || c1 + 1 < n, ww1 = true; // neighbours of c1
+  const bool out_lane = lane >= 2 && lane <= 29; // columns xs .. xs + 55
+  // window: xw[k] = row t - 4 + k (k = 0..5), fw[k] = f of row t - 3 + k (k = 0..3)
+  T xw[6][2], fw[4][2];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) xw[k][0] = xw[k][1] = (T)0;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) fw[k][0] = fw[k][1] = (T)0;
+  const int t0 = y0 - 3, t1 = y0 + kColSmH + 2;  // rows of half-sweep 0
+  {
+    const SmRow<T> a = sm_load_row(M, l, mode, x_zero, t0 - 1, c0, cin);
+    const SmRow<T> b = sm_load_row(M, l, mode, x_zero, t0, c0, cin);
+    xw[3][0] = a.x0; xw[3][1] = a.x1;
+    xw[4][0] = b.x0; xw[4][1] = b.x1;
+    fw[3][0] = b.f0; fw[3][1] = b.f1;
+  }
+  SmRow<T> nxt = sm_load_row(M, l, mode, x_zero, t0 + 1, c0, cin);
+  for (int t = t0; t <= t1; ++t) {
+    const SmRow<T> cur = nxt;  // row t + 1
+    nxt = sm_load_row(M, l, mode, x_zero, t + 2, c0, cin);
+    xw[5][0] = cur.x0;
+    xw[5][1] = cur.x1;
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+      const int r = t - s, k = 4 - s;
+      const int color = (cfirst + s) & 1;
+      const bool upd1 = ((r & 1) != color);  // c0 has the colour r & 1, c1 the other
+      const T e_of_0 = __shfl_down_sync(FULL, xw[k][0], 1);  // column c1 + 1 (lane + 1's c0)
+      const T w_of_1 = __shfl_up_sync(FULL, xw[k][1], 1);    // column c0 - 1 (lane - 1's c1)
+      const bool rok = r >= y0 - 3 + s && r <= y0 + kColSmH + 2 - s && (py || (r >= 0 && r < n)) && cin;
+      const bool wn = py || r + 1 < n, wsn = py || r > 0;
+      if (rok) {
+        if (!upd1) {
+          xw[k][0] = gs_update<T>(xw[k][1], w_of_1, xw[k + 1][0], xw[k - 1][0], we0, ww0, wn, wsn, ihx, ihy, fw[3 - s][0], M.idg[l]);
+        } else {
+          xw[k][1] = gs_update<T>(e_of_0, xw[k][0], xw[k + 1][1], xw[k - 1][1], we1, ww1, wn, wsn, ihx, ihy, fw[3 - s][1], M.idg[l]);
+        }
+      }
+    }
+    const int ro = t - 3;
+    if (out_lane && c0 >= 0 && c1 < n && ro >= y0 && ro < y0 + kColSmH && ro < n) {  // real cells only
+      const long id = (long)ro * P + c0;
+      M.x2[l][id] = xw[1][0];
+      M.x2[l][id + 1] = xw[1][1];
+    }
+#pragma unroll
+    for (int k = 0; k < 5; ++k) { xw[k][0] = xw[k + 1][0]; xw[k][1] = xw[k + 1][1]; }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) { fw[k][0] = fw[k + 1][0]; fw[k][1] = fw[k + 1][1]; }
+    fw[3][0] = cur.f0;
+    fw[3][1] = cur.f1;
   }
 }
 

@@ -127,7 +127,8 @@ void free_all(ns_ctx* c) {
   if (c->gm_host) cudaFreeHost(c->gm_host);
   free_adjoint(c);
   for (int l = 1; l < c->M64.L; ++l) { F(c->M64.x[l]); F(c->M64.f[l]); }
-  for (int l = 0; l < c->M32.L; ++l) { F(c->M32.x[l]); F(c->M32.f[l]); }
+  for (int l = 0; l < c->M64.L; ++l) F(c->M64.x2[l]);
+  for (int l = 0; l < c->M32.L; ++l) { F(c->M32.x[l]); F(c->M32.f[l]); F(c->M32.x2[l]); }
   F(c->part); F(c->counter); F(c->red);
   if (c->red_h) cudaFreeHost(c->red_h);
   if (c->ev_ok) for (auto& e : c->ev) cudaEventDestroy(e);
@@ -161,14 +162,17 @@ int alloc_levels(ns_ctx* c, MGLevels<T>& M, bool own_level0) {
     M.ih[l][0] = (T)M.invh2[l][0];
     M.ih[l][1] = (T)M.invh2[l][1];
     M.x[l] = nullptr;
+    M.x2[l] = nullptr;
     M.f[l] = nullptr;
+    const size_t bytes = (size_t)M.pitch[l] * (n + 1) * sizeof(T);
     if (l > 0 || own_level0) {
-      const size_t bytes = (size_t)M.pitch[l] * (n + 1) * sizeof(T);
       if (cudaMalloc(&M.x[l], bytes) != cudaSuccess || cudaMalloc(&M.f[l], bytes) != cudaSuccess)
         return fail(c, NS_ERR_NOMEM, "cudaMalloc (multigrid) failed");
       cudaMemsetAsync(M.x[l], 0, bytes, c->st);
       cudaMemsetAsync(M.f[l], 0, bytes, c->st);
     }
+    if (cudaMalloc(&M.x2[l], bytes) != cudaSuccess) return fail(c, NS_ERR_NOMEM, "cudaMalloc (multigrid) failed");
+    cudaMemsetAsync(M.x2[l], 0, bytes, c->st);
     M.L++;
     if (!(n % 4 == 0 && n > 4)) break;
     n /= 2;
@@ -691,13 +695,19 @@ int ns_poisson_rhs(ns_ctx* c, double* divmax, double* sum) {
 
 template <typename T>
 static int vcycle(ns_ctx* c, MGLevels<T>& M, int x0_zero) {
+  // each smoother launch reads x[l] and writes x2[l]; the swap after it makes
+  // the result x[l] again. Two launches per level: the buffers are back in
+  // place when the cycle ends.
   for (int l = 0; l < c->lb; ++l) {
     LAUNCH(l == 0 ? NS_PROF_MG_SMOOTH0 : NS_PROF_MG_SMOOTH, "mg smooth", launch_mg_smooth<T>(M, l, 0, (l > 0) ? 1 : x0_zero, c->st));
+    std::swap(M.x[l], M.x2[l]);
     LAUNCH(l == 0 ? NS_PROF_MG_RESTRICT0 : NS_PROF_MG_RESTRICT, "mg restrict", launch_mg_restrict<T>(M, l, c->st));
   }
   LAUNCH(NS_PROF_MG_BOTTOM, "mg bottom", launch_mg_bottom<T>(M, c->lb, (c->lb > 0) ? 1 : x0_zero, c->st));
-  for (int l = c->lb - 1; l >= 0; --l)
+  for (int l = c->lb - 1; l >= 0; --l) {
     LAUNCH(l == 0 ? NS_PROF_MG_SMOOTH0 : NS_PROF_MG_SMOOTH, "mg prolong+smooth", launch_mg_smooth<T>(M, l, 1, 0, c->st));
+    std::swap(M.x[l], M.x2[l]);
+  }
   return NS_OK;
 }
 
