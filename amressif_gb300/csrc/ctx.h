@@ -45,6 +45,7 @@ struct ns_ctx {
   // mixed predictor
   float* SH[2] = {nullptr, nullptr};
   float* G0[2] = {nullptr, nullptr};
+  float* G0b[2] = {nullptr, nullptr};  // the other anchor buffer (incremental anchor updates)
   float* E[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
   // multigrid
   ns::MGLevels<double> M64;
@@ -60,6 +61,7 @@ struct ns_ctx {
   bool ev_ok = false;
   // mixed iteration: E[0] holds an increment not yet added to the base
   bool mix_pending = false;
+  int mix_it = 0;  // mixed pseudo-iterations of this step (every kAnchorEvery-th anchor is exact)
   // float-float pseudo-iterate (hi, lo) ping-pong and the split source S
   float* BH[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
   float* BL[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};

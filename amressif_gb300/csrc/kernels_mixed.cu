@@ -67,6 +67,13 @@ cudaError_t launch_ff_to_double(int n, long pitch, const float* h, const float* 
   return cudaGetLastError();
 }
 
+cudaError_t launch_ff_base_add(const Geom& g, const float* const* h, const float* const* l, const float* const* e,
+                               float* const* oh, float* const* ol, cudaStream_t s) {
+  const dim3 grid((g.N + 1 + 255) / 256, g.N + 1, 1);
+  k_ff_base_add2d<<<grid, 256, 0, s>>>(g, h[0], l[0], h[1], l[1], e[0], e[1], oh[0], ol[0], oh[1], ol[1]);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_ff_add_inc(const Geom& g, const float* const* h, const float* const* l, const float* const* e,
                               double* const* out, cudaStream_t s) {
   k_ff_add_inc2d<<<1024, 256, 0, s>>>(g, h[0], l[0], h[1], l[1], e[0], e[1], out[0], out[1]);

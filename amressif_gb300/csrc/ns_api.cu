@@ -114,7 +114,7 @@ void free_all(ns_ctx* c) {
   for (int m = 0; m < 2; ++m) {
     F(c->U[m]); F(c->UP[m]); F(c->DU[m]); F(c->S[m]); F(c->CART[m]); F(c->PHI[m]);
     for (int i = 0; i < 3; ++i) F(c->B[i][m]);
-    F(c->SH[m]); F(c->G0[m]); F(c->E[0][m]); F(c->E[1][m]);
+    F(c->SH[m]); F(c->G0[m]); F(c->G0b[m]); F(c->E[0][m]); F(c->E[1][m]);
     F(c->BH[0][m]); F(c->BH[1][m]); F(c->BL[0][m]); F(c->BL[1][m]); F(c->SFh[m]); F(c->SFl[m]);
     F(c->PFh[m]); F(c->PFl[m]);
   }
@@ -1057,6 +1057,10 @@ static void split_const(double x, float* out) {
 // increment of the previous iteration), then three FP32 increment stages; the
 // fourth stage's increment e4 stays in E[0] and its norm is the
 // pseudo-increment norm of Error_Computation.
+// every kAnchorEvery-th pseudo-iteration evaluates the anchor exactly (float-float);
+// the others update it by an FP32 increment evaluation
+constexpr int kAnchorEvery = 8;
+
 static int mixed_iteration(ns_ctx* c, double* norm) {
   if (!c->s_ff_valid) {
     const double* S[2] = {c->S[0], c->S[1]};
@@ -1070,25 +1074,63 @@ static int mixed_iteration(ns_ctx* c, double* norm) {
     c->base_ff_valid = true;
     c->mix_pending = false;
   }
-  AnchorFFArgs a;
-  std::memset(&a, 0, sizeof(a));
-  a.g = c->g;
-  const int mb = c->mb, nb = 1 - c->mb;
-  for (int m = 0; m < 2; ++m) {
-    a.bh[m] = c->BH[mb][m];
-    a.bl[m] = c->BL[mb][m];
-    a.e4[m] = c->mix_pending ? c->E[0][m] : nullptr;
-    a.Sh[m] = c->SFh[m];
-    a.Sl[m] = c->SFl[m];
-    a.obh[m] = c->BH[nb][m];
-    a.obl[m] = c->BL[nb][m];
-    a.g0[m] = c->G0[m];
-    split_const(c->g.inv_dx[m], a.inv_dx[m]);
-    split_const(1.0 / (c->g.ren * c->g.dx2[m]), a.vcoef[m]);
+  const bool exact = !c->mix_pending || (c->mix_it % kAnchorEvery) == 0;
+  ++c->mix_it;
+  if (exact) {
+    AnchorFFArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.g = c->g;
+    const int mb = c->mb, nb = 1 - c->mb;
+    for (int m = 0; m < 2; ++m) {
+      a.bh[m] = c->BH[mb][m];
+      a.bl[m] = c->BL[mb][m];
+      a.e4[m] = c->mix_pending ? c->E[0][m] : nullptr;
+      a.Sh[m] = c->SFh[m];
+      a.Sl[m] = c->SFl[m];
+      a.obh[m] = c->BH[nb][m];
+      a.obl[m] = c->BL[nb][m];
+      a.g0[m] = c->G0[m];
+      split_const(c->g.inv_dx[m], a.inv_dx[m]);
+      split_const(1.0 / (c->g.ren * c->g.dx2[m]), a.vcoef[m]);
+    }
+    split_const(c->g.c15, a.c15);
+    LAUNCH(NS_PROF_ANCHOR, "anchor stage", launch_anchor_ff(a, c->st));
+    c->mb = nb;
+  } else {
+    // incremental anchor: G0 + dG(u_b; e4) by the FP32 increment kernel with
+    // rk = 1 (its rounding error is relative to e4), then u_b + e4 in
+    // float-float; the exact float-float anchor of the next kAnchorEvery-th
+    // iteration removes whatever these updates accumulated
+    const int mb = c->mb, nb = 1 - c->mb;
+    IncArgs u;
+    std::memset(&u, 0, sizeof(u));
+    u.g = c->g;
+    u.part = reinterpret_cast<float2*>(c->part);
+    u.counter = c->counter;
+    u.norm_out = c->red + kRedNorm;
+    for (int m = 0; m < 2; ++m) {
+      u.sh[m] = c->BH[mb][m];
+      u.g0[m] = c->G0[m];
+      u.ein[m] = c->E[0][m];
+      u.eout[m] = c->G0b[m];
+      u.inv_dx[m] = (float)c->g.inv_dx[m];
+      u.vcoef[m] = (float)(1.0 / (c->g.ren * c->g.dx2[m]));
+    }
+    u.c15 = (float)c->g.c15;
+    u.rk_prev = 1.f;
+    u.rk = 1.f;
+    u.do_norm = 0;
+    LAUNCH(NS_PROF_INC, "anchor update", launch_inc_stage(u, c->st));
+    const float* h[2] = {c->BH[mb][0], c->BH[mb][1]};
+    const float* l[2] = {c->BL[mb][0], c->BL[mb][1]};
+    const float* e[2] = {c->E[0][0], c->E[0][1]};
+    float* oh[2] = {c->BH[nb][0], c->BH[nb][1]};
+    float* ol[2] = {c->BL[nb][0], c->BL[nb][1]};
+    LAUNCH(NS_PROF_OTHER, "base update", launch_ff_base_add(c->g, h, l, e, oh, ol, c->st));
+    for (int m = 0; m < 2; ++m) std::swap(c->G0[m], c->G0b[m]);
+    c->mb = nb;
   }
-  split_const(c->g.c15, a.c15);
-  LAUNCH(NS_PROF_ANCHOR, "anchor stage", launch_anchor_ff(a, c->st));
-  c->mb = nb;
+  const int nb = c->mb;  // the base of this iteration's increment stages
   IncArgs ia;
   std::memset(&ia, 0, sizeof(ia));
   ia.g = c->g;
@@ -1140,7 +1182,7 @@ static int alloc_mixed(ns_ctx* c) {
   if (c->G0[0]) return NS_OK;
   const size_t fb = (size_t)c->pitch * (c->N + 1) * sizeof(float);
   for (int m = 0; m < 2; ++m) {
-    float** ps[12] = {&c->G0[m], &c->E[0][m], &c->E[1][m], &c->BH[0][m], &c->BH[1][m], &c->BL[0][m],
+    float** ps[13] = {&c->G0[m], &c->G0b[m], &c->E[0][m], &c->E[1][m], &c->BH[0][m], &c->BH[1][m], &c->BL[0][m],
                       &c->BL[1][m], &c->SFh[m], &c->SFl[m], &c->PFh[m], &c->PFl[m], m == 0 ? &c->FFh : &c->FFl};
     for (float** p : ps) {
       if (cudaMalloc(p, fb) != cudaSuccess) return fail(c, NS_ERR_NOMEM, "cudaMalloc (mixed) failed");
@@ -1160,6 +1202,7 @@ int nsh::run_predictor(ns_ctx* c, ns_step_stats* sp) {
     if (ra != NS_OK) return ra;
   }
   c->mix_pending = false;
+  c->mix_it = 0;
   int r = ns_step_begin(c);
   if (r != NS_OK) return r;
   int countIter = 0;
