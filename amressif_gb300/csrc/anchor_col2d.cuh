@@ -71,12 +71,14 @@ __global__ void __launch_bounds__(NT) k_anchor_col2d(AnchorFFArgs A) {
     int kk = k < 0 ? -k - 1 : 2 * N - 1 - k;
     return kk < 0 ? 0 : (kk >= N ? N - 1 : kk);
   };
-  auto slot = [&](int k) { return ring + (size_t)(((k % kColRing) + kColRing) % kColRing) * kAncWords * 32; };
+  // ring slots count from the strip's first row (row r_first - 2 in slot 0); row
+  // k + kColRing is issued into the slot row k was just read from
+  auto slot_ptr = [&](int sl) { return ring + (size_t)sl * kAncWords * 32; };
   // words: 0-2 u face (ic): hi, lo, e4; 3-5 u face (ic+1); 6-8 v face (ic, kk);
   // 9-11 v face (ic, kk+1); 12-13 S_u (iface): hi, lo; 14-15 S_v (ic): hi, lo
-  auto issue_row = [&](int k) {
+  auto issue_row = [&](int k, int sl) {
     const long r0 = (long)row_of(k) * P;
-    float* d = slot(k);
+    float* d = slot_ptr(sl);
     cp_async4(d + 0 * 32, A.bh[0] + r0 + ic);
     cp_async4(d + 1 * 32, A.bl[0] + r0 + ic);
     cp_async4(d + 3 * 32, A.bh[0] + r0 + ic + 1);
@@ -109,20 +111,22 @@ __global__ void __launch_bounds__(NT) k_anchor_col2d(AnchorFFArgs A) {
     return u;
   };
   int k_next = 0, k_end = 0;
+  int rslot = 0;  // ring slot of the next row to read
   // consume row k: cell velocities (with ghosts), the u face (iface, k), the
   // lower v face (ic, k) and S at the lane's faces
   auto cell_row = [&](int k, CellFF& c, ff& uf, ff& vl, ff& su, ff& sv) {
     cp_async_wait<kColRing - 1>();
-    const float* d = slot(k);
+    const float* d = slot_ptr(rslot);
     const ff ua = ubase(d, 0), ub = ubase(d, 3), va = ubase(d, 6), vb = ubase(d, 9);
     su = ff_make(d[12 * 32], d[13 * 32]);
     sv = ff_make(d[14 * 32], d[15 * 32]);
     if (iface != ic) uf = ubase_direct(0, (long)row_of(k) * P + iface);  // boundary / periodic lanes only
     else uf = ua;
     vl = va;
-    if (k_next <= k_end) issue_row(k_next);
+    if (k_next <= k_end) issue_row(k_next, rslot);
     else cp_async_commit();
     ++k_next;
+    rslot = (rslot == kColRing - 1) ? 0 : rslot + 1;
     c.p0 = ff_scale2(ua + ub, 0.5f);
     c.p1 = ff_scale2(va + vb, 0.5f);
     if (warp_xghost) {
@@ -144,7 +148,7 @@ __global__ void __launch_bounds__(NT) k_anchor_col2d(AnchorFFArgs A) {
   k_next = r_first - 2;
   k_end = r_last + 2;
   for (int q = 0; q < kColRing; ++q) {
-    if (k_next <= k_end) issue_row(k_next);
+    if (k_next <= k_end) issue_row(k_next, q);
     else cp_async_commit();
     ++k_next;
   }

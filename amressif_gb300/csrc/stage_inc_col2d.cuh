@@ -50,7 +50,7 @@ template <int NT>
 constexpr size_t inc_col_smem() { return (size_t)(NT / 32) * kColRing * kColWords * 32 * sizeof(float); }
 
 template <int NT>
-__global__ void __launch_bounds__(NT) k_inc_col2d(IncArgs A) {
+__global__ void __launch_bounds__(NT, 6) k_inc_col2d(IncArgs A) {  // 6 blocks (24 warps) per SM
   constexpr unsigned FULL = 0xffffffffu;
   const Geom& g = A.g;
   const int N = g.N;
@@ -100,9 +100,11 @@ __global__ void __launch_bounds__(NT) k_inc_col2d(IncArgs A) {
       int kk = k < 0 ? -k - 1 : 2 * N - 1 - k;
       return kk < 0 ? 0 : (kk >= N ? N - 1 : kk);
     };
-    auto issue_row = [&](int k) {
+    // ring slots count from the strip's first row (row r_first - 2 in slot 0); row
+    // k + kColRing is issued into the slot row k was just read from
+    auto issue_row = [&](int k, int slot) {
       const long r0 = (long)row_of(k) * P;
-      float* d = ring + (size_t)(((k % kColRing) + kColRing) % kColRing) * kColWords * 32;
+      float* d = ring + (size_t)slot * kColWords * 32;
       cp_async4(d + 0 * 32, shu + r0 + ic);
       cp_async4(d + 1 * 32, shu + r0 + ic + 1);
       cp_async4(d + 2 * 32, eu + r0 + ic);
@@ -115,9 +117,9 @@ __global__ void __launch_bounds__(NT) k_inc_col2d(IncArgs A) {
       cp_async4(d + 9 * 32, A.g0[1] + r0 + ic);
       cp_async_commit();
     };
-    auto read_row = [&](int k, RawRow& R) {
+    auto read_row = [&](int k, int slot, RawRow& R) {
       cp_async_wait<kColRing - 1>();
-      const float* d = ring + (size_t)(((k % kColRing) + kColRing) % kColRing) * kColWords * 32;
+      const float* d = ring + (size_t)slot * kColWords * 32;
       R.ua = d[0 * 32]; R.ub = d[1 * 32]; R.ea = d[2 * 32]; R.eb = d[3 * 32];
       R.va = d[4 * 32]; R.vb = d[5 * 32]; R.fa = d[6 * 32]; R.fb = d[7 * 32];
       R.gu = d[8 * 32]; R.gv = d[9 * 32];
@@ -131,6 +133,7 @@ __global__ void __launch_bounds__(NT) k_inc_col2d(IncArgs A) {
       }
     };
     int k_next = 0, k_end = 0;  // next row to issue, last row of the strip
+    int slot = 0;               // ring slot of the next row to read
     auto finish_row = [&](const RawRow& R, int k, ColCells& c, float& ufb, float& ufe, float& vlb, float& vle) {
       c.p0 = 0.5f * (R.ua + R.ub);
       c.e0 = 0.5f * es * (R.ea + R.eb);
@@ -162,10 +165,11 @@ __global__ void __launch_bounds__(NT) k_inc_col2d(IncArgs A) {
     // consume row k (the oldest in flight) and put the next row in flight
     auto cell_row = [&](int k, ColCells& c, float& ufb, float& ufe, float& vlb, float& vle, float& gu, float& gv) {
       RawRow R;
-      read_row(k, R);
-      if (k_next <= k_end) issue_row(k_next);
+      read_row(k, slot, R);
+      if (k_next <= k_end) issue_row(k_next, slot);
       else cp_async_commit();  // empty group: the wait count stays one row per call
       ++k_next;
+      slot = (slot == kColRing - 1) ? 0 : slot + 1;
       finish_row(R, k, c, ufb, ufe, vlb, vle);
       gu = R.gu;
       gv = R.gv;
@@ -180,7 +184,7 @@ __global__ void __launch_bounds__(NT) k_inc_col2d(IncArgs A) {
     k_next = r_first - 2;
     k_end = r_last + 2;
     for (int q = 0; q < kColRing; ++q) {
-      if (k_next <= k_end) issue_row(k_next);
+      if (k_next <= k_end) issue_row(k_next, q);
       else cp_async_commit();
       ++k_next;
     }
