@@ -22,7 +22,7 @@
 namespace ns {
 
 constexpr int kColOut = 26;  // output columns per warp
-constexpr int kColH = 64;    // rows per strip
+constexpr int kColH = 40;    // rows per strip (a 4096^2 sweep of 16..128 rows peaked at 40)
 
 struct ColCells {
   float p0, p1, e0, e1;  // cart(u_b), cart(e_s)
