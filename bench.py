@@ -435,12 +435,17 @@ def bench_ours(args):
         uh, uph, ph = [bufs[0].a, bufs[1].a], [bufs[2].a, bufs[3].a], bufs[4].a
         s.step_host(uh, uph, ph)  # warm-up of the host path
         t0 = time.perf_counter()
-        for _ in range(E):
-            s.step_host(uh, uph, ph)
+        est = [s.step_host(uh, uph, ph) for _ in range(E)]
         te = time.perf_counter() - t0
         nbytes = 8 * (2 * shp[0][0] * shp[0][1] + 2 * shp[1][0] * shp[1][1] + n * n)
+        dev = statistics.mean(x["ms_predictor"] + x["ms_poisson"] + x["ms_project"] for x in est)
         e2e = {"value": world * E / te, "unit": "steps/s", "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
-               "steps": E, "path": "ns_step_host (pinned host u, u_prev, p in; u, u_prev, p out)"}
+               "steps": E, "path": "ns_step_host (pinned host u, u_prev, p in; u, u_prev, p out)",
+               "note": "the steps after the timed ones (their pseudo-iteration counts below differ from the timed "
+                       "steps'); device_ms_per_step is the same device timing as value, copy_and_host_ms_per_step "
+                       "the rest of the wall time (host<->device copies, host calls)",
+               "pseudo_iters": [x["pseudo_iters"] for x in est], "device_ms_per_step": dev,
+               "copy_and_host_ms_per_step": 1e3 * te / E - dev}
         for b in bufs:
             b.free()
 
