@@ -52,7 +52,7 @@ extern "C" {
 
 /* Inputs-file keys of the reference (main.cpp:89-157) plus GPU options. */
 typedef struct ns_params {
-  int dim;                   /* AMREX_SPACEDIM: 2 */
+  int dim;                   /* AMREX_SPACEDIM: 2 or 3 (3: the whole-step API and the adjoint pair) */
   int n_cell;
   int max_grid_size[3];      /* accepted for drop-in; the GPU runs one box */
   double prob_lo[3];         /* lo_phy_dim (default 0) */
@@ -123,8 +123,9 @@ int ns_put_box(ns_ctx* c, int field, int comp, const double* data, const int lo[
 int ns_get_box(ns_ctx* c, int field, int comp, double* data, const int lo[3], const int hi[3],
                long long jstride, long long kstride, int where_device);
 
-/* Whole-state convenience (dense host arrays, x fastest): u[d] are face
- * arrays of extent n_cell+1 along d, p is a cell array. */
+/* Whole-state convenience (dense host arrays, x fastest): u[d] (d < dim) are
+ * face arrays of extent n_cell+1 along d and n_cell along the others, p is a
+ * cell array. */
 int ns_set_state(ns_ctx* c, const double* const* u, const double* const* u_prev, const double* p, double time);
 int ns_get_state(ns_ctx* c, double* const* u, double* const* u_prev, double* p, double* phi);
 
@@ -239,7 +240,8 @@ typedef struct ns_adjoint_stats {
   long long adjoint_steps;
   long long lin_iters;      /* BiCGStab iterations, all solves */
   int lin_max_iters_seen;
-  double lin_max_res;       /* largest final ||r|| / ||b|| */
+  double lin_max_res;       /* largest final relative residual: ||r|| / ||b||, or max|r| / max|b| for the
+                               mixed-precision (refined) 3D solves */
   long long poisson_cycles; /* adjoint Poisson V-cycles */
   double ms_forward;        /* wall time of ns_step_adjoint_fwd */
   double ms_backward;       /* wall time of ns_step_adjoint_bwd */
@@ -254,8 +256,11 @@ int ns_set_controls(ns_ctx* c, int nseg, const double* controls);
 
 /* Forward half of the pair (the analogue of an autograd Function's forward):
  * sets the controls, runs opts->nsteps steps from the current state keeping
- * binomial snapshots (Griewank's revolve schedule with opts->nsnap slots),
- * and returns J. The context is left at the final state. */
+ * opts->nsnap snapshots (placed by a dynamic-programming schedule, the
+ * binomial one as fallback), and returns J. 2D: J = kinetic energy of the
+ * lower-left quarter, with nseg lid controls. 3D (periodic boxes,
+ * fix_quirks = 1): J = the final enstrophy 1/2 sum |curl u|^2 dV, nseg = 0.
+ * The context is left at the final state. */
 int ns_step_adjoint_fwd(ns_ctx* c, const ns_adjoint_opts* opts, int nseg, const double* controls, double* J,
                         ns_adjoint_stats* stats);
 
