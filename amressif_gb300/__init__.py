@@ -63,7 +63,7 @@ class PinnedArray:
 
 PROF_KINDS = ["stage_exact", "stage_fast", "anchor", "increment", "explicit", "step_begin", "poisson_rhs",
               "project", "mg_smooth0", "mg_smooth", "mg_restrict0", "mg_restrict", "mg_bottom", "mg_resnorm",
-              "dc_update", "other"]
+              "dc_update", "other", "mg_cycle"]
 
 
 class NsError(RuntimeError):

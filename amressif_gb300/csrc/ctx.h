@@ -79,6 +79,14 @@ struct ns_ctx {
   bool prof = false;
   std::vector<cudaEvent_t> evpool;
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pend;
+  // V-cycles captured once as CUDA graphs and replayed: [FP64 hierarchy][x0 starts at 0],
+  // keyed by the level-0 buffers the graph was captured with
+  struct VGraph {
+    cudaGraphExec_t exec = nullptr;
+    const void* key[4] = {nullptr, nullptr, nullptr, nullptr};
+    long long nlaunch = 0;
+    bool unusable = false;
+  } vg[2][2];
   double pms[NS_PROF_KINDS] = {0};
   long long pcnt[NS_PROF_KINDS] = {0};
   long long launches = 0;

@@ -134,6 +134,9 @@ void free_all(ns_ctx* c) {
   if (c->ev_ok) for (auto& e : c->ev) cudaEventDestroy(e);
   for (auto& p : c->pend) { cudaEventDestroy(p.second.first); cudaEventDestroy(p.second.second); }
   for (auto& e : c->evpool) cudaEventDestroy(e);
+  for (auto& row : c->vg)
+    for (auto& G : row)
+      if (G.exec) cudaGraphExecDestroy(G.exec);
   if (c->own_stream && c->st) cudaStreamDestroy(c->st);
 }
 
@@ -711,6 +714,51 @@ static int vcycle(ns_ctx* c, MGLevels<T>& M, int x0_zero) {
   return NS_OK;
 }
 
+// One V-cycle, replayed from a CUDA graph captured on first use: the ~22
+// launches of a cycle become one graph launch. The smoother's buffer swaps
+// leave every level's pointers as they were, so the captured arguments stay
+// valid; the graph is rebuilt when the level-0 buffers change (the FP64
+// hierarchy's level 0 is the caller's phi). If the stream cannot be captured
+// (the legacy default stream), the cycle runs as plain launches.
+template <typename T>
+static int vcycle_graph(ns_ctx* c, MGLevels<T>& M, int x0_zero) {
+  ns_ctx::VGraph& G = c->vg[sizeof(T) == 8 ? 1 : 0][x0_zero ? 1 : 0];
+  if (G.unusable) return vcycle<T>(c, M, x0_zero);
+  const void* key[4] = {M.x[0], M.x2[0], M.f[0], M.fmean};
+  if (G.exec && std::memcmp(key, G.key, sizeof(key)) != 0) {
+    cudaGraphExecDestroy(G.exec);
+    G.exec = nullptr;
+  }
+  if (!G.exec) {
+    if (cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+      cudaGetLastError();
+      G.unusable = true;
+      return vcycle<T>(c, M, x0_zero);
+    }
+    const long long l0 = c->launches;
+    const bool prof = c->prof;
+    c->prof = false;  // no event nodes inside the graph
+    const int r = vcycle<T>(c, M, x0_zero);
+    c->prof = prof;
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(c->st, &g);
+    if (r != NS_OK) {
+      if (g) cudaGraphDestroy(g);
+      return r;
+    }
+    CK(e, "V-cycle capture");
+    const cudaError_t ei = cudaGraphInstantiate(&G.exec, g, 0);
+    cudaGraphDestroy(g);
+    CK(ei, "V-cycle graph instantiate");
+    G.nlaunch = c->launches - l0;
+    c->launches = l0;
+    std::memcpy(G.key, key, sizeof(key));
+  }
+  LAUNCH(NS_PROF_MG_CYCLE, "V-cycle graph", cudaGraphLaunch(G.exec, c->st));
+  c->launches += G.nlaunch - 1;  // the kernels of the graph, as the library's launch count
+  return NS_OK;
+}
+
 // mean of f (singular problem, AMReX makes the RHS solvable) written to red[kRedMean]
 __global__ void k_set_mean(double* red, double inv_n) { red[kRedMean] = red[kRedSum] * inv_n; }
 
@@ -944,7 +992,7 @@ int ns_poisson_solve(ns_ctx* c, int precision, int* cycles, double* res) {
     int pc = 0;
     while (!done(rn) && rnorm0 > 0) {
       if (ncyc >= maxc) { status = NS_ERR_MG_STALL; break; }
-      int r2 = vcycle<float>(c, c->M32, 1);
+      int r2 = vcycle_graph<float>(c, c->M32, 1);
       if (r2 != NS_OK) return r2;
       if (ffmode) {
         q.first = 0;
@@ -1001,7 +1049,7 @@ int ns_poisson_solve(ns_ctx* c, int precision, int* cycles, double* res) {
     int stall = 0;
     while (!done(rn) && rnorm0 > 0) {
       if (ncyc >= maxc) { status = NS_ERR_MG_STALL; break; }
-      int r2 = vcycle<double>(c, c->M64, (ncyc == 0 && !warm) ? 1 : 0);
+      int r2 = vcycle_graph<double>(c, c->M64, (ncyc == 0 && !warm) ? 1 : 0);
       if (r2 != NS_OK) return r2;
       ++ncyc;
       LAUNCH(NS_PROF_MG_RESNORM, "resnorm", launch_mg_resnorm<double>(c->M64, c->part, c->counter, c->red + kRedRes, c->st));

@@ -50,7 +50,7 @@ template <int NT>
 constexpr size_t inc_col_smem() { return (size_t)(NT / 32) * kColRing * kColWords * 32 * sizeof(float); }
 
 template <int NT>
-__global__ void __launch_bounds__(NT, 6) k_inc_col2d(IncArgs A) {  // 6 blocks (24 warps) per SM
+__global__ void __launch_bounds__(NT, 768 / NT) k_inc_col2d(IncArgs A) {  // 24 warps per SM
   constexpr unsigned FULL = 0xffffffffu;
   const Geom& g = A.g;
   const int N = g.N;

@@ -167,7 +167,7 @@ def throughput_block(n, K, total_s, stats, prof, peak):
     kmean = statistics.mean(st["pseudo_iters"] for st in stats)
     cycles = sum(st["poisson_cycles"] for st in stats)
     algo = sum(ALGO_BYTES_PER_CELL[k] * n * n * c for k, (c, _) in prof.items() if k in ALGO_BYTES_PER_CELL)
-    mg_kinds = ("mg_smooth0", "mg_smooth", "mg_restrict0", "mg_restrict", "mg_bottom")
+    mg_kinds = ("mg_smooth0", "mg_smooth", "mg_restrict0", "mg_restrict", "mg_bottom", "mg_cycle")
     mg_ms = sum(prof[k][1] for k in mg_kinds if k in prof)
     dc_c, dc_ms = prof.get("dc_update", (0, 0.0))
     out = {"cell_updates_per_s": steps_per_s * n * n,

@@ -180,7 +180,8 @@ int ns_sync(ns_ctx* c);
 #define NS_PROF_MG_RESNORM 13
 #define NS_PROF_DC_UPDATE 14
 #define NS_PROF_OTHER 15
-#define NS_PROF_KINDS 16
+#define NS_PROF_MG_CYCLE 16 /* one V-cycle replayed as a CUDA graph (its kernels are not timed one by one) */
+#define NS_PROF_KINDS 17
 /* Poisson right-hand side without any device allocation. No counterpart in
  * the reference. For callers that cannot call cudaMalloc: a host whose device
  * memory all belongs to its own arena allocator (AMReX's), or a job whose
