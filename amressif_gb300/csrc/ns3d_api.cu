@@ -22,6 +22,8 @@ namespace nsh {
 void free3d(ns_ctx* c) {
   if (!c->s3) return;
   free_adj3(c);
+  for (auto& G : c->s3->vg3)
+    if (G.exec) cudaGraphExecDestroy(G.exec);
   for (void* p : c->s3->allocs) cudaFree(p);
   delete c->s3;
   c->s3 = nullptr;
@@ -109,6 +111,52 @@ int vcycle3(ns_ctx* c, MG3<T>& M) {
   return NS_OK;
 }
 
+// one V-cycle (FP32: preceded by zeroing the correction) replayed from a CUDA
+// graph captured on first use; plain launches if the stream cannot be captured
+template <typename T>
+int vcycle3_graph(ns_ctx* c, MG3<T>& M) {
+  State3D& S = *c->s3;
+  ns_ctx::VGraph& G = S.vg3[sizeof(T) == 8 ? 1 : 0];
+  auto body = [&]() -> int {
+    if (sizeof(T) == 4) CK(cudaMemsetAsync(M.x[0], 0, S.fb / 2, c->st), "memset e");  // each correction starts from zero
+    return vcycle3<T>(c, M);
+  };
+  if (G.unusable) return body();
+  const void* key[4] = {M.x[0], M.f[0], M.fmean, nullptr};
+  if (G.exec && std::memcmp(key, G.key, sizeof(key)) != 0) {
+    cudaGraphExecDestroy(G.exec);
+    G.exec = nullptr;
+  }
+  if (!G.exec) {
+    if (cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+      cudaGetLastError();
+      G.unusable = true;
+      return body();
+    }
+    const long long l0 = c->launches;
+    const bool prof = c->prof;
+    c->prof = false;
+    const int r = body();
+    c->prof = prof;
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(c->st, &g);
+    if (r != NS_OK) {
+      if (g) cudaGraphDestroy(g);
+      return r;
+    }
+    CK(e, "V-cycle capture");
+    const cudaError_t ei = cudaGraphInstantiate(&G.exec, g, 0);
+    cudaGraphDestroy(g);
+    CK(ei, "V-cycle graph instantiate");
+    G.nlaunch = c->launches - l0;
+    c->launches = l0;
+    std::memcpy(G.key, key, sizeof(key));
+  }
+  LAUNCH(NS_PROF_MG_CYCLE, "V-cycle graph", cudaGraphLaunch(G.exec, c->st));
+  c->launches += G.nlaunch - 1;
+  return NS_OK;
+}
+
 __global__ void k3_set_mean(double* red, double inv_n) { red[kRedMean] = red[kRedSum] * inv_n; }
 
 // phi solves L phi = f - mean(f) to poisson_tol_rel (and the divergence
@@ -168,10 +216,9 @@ int poisson3(ns_ctx* c, int* cycles, double* res, long long* fallbacks) {
   while (!done(rn) && r0 > 0) {
     if (ncyc >= maxc) { status = NS_ERR_MG_STALL; break; }
     if (mixed) {
-      CK(cudaMemsetAsync(S.M32.x[0], 0, S.fb / 2, c->st), "memset e");  // each correction starts from zero
-      r = vcycle3<float>(c, S.M32);
+      r = vcycle3_graph<float>(c, S.M32);  // zeroes the correction first
     } else {
-      r = vcycle3<double>(c, S.M64);
+      r = vcycle3_graph<double>(c, S.M64);
     }
     if (r != NS_OK) return r;
     ++ncyc;

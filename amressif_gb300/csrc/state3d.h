@@ -38,6 +38,7 @@ struct State3D {
   ns::MG3<double> M64;
   ns::MG3<float> M32;
   int base = -1, cur = -1;
+  ns_ctx::VGraph vg3[2];  // V-cycle graphs: [0] FP32 (with the memset of the correction), [1] FP64
   Adj3* adj = nullptr;
 };
 
