@@ -9,10 +9,12 @@
 #pragma once
 #include "anchor_ff2d.cuh"
 #include "ff.cuh"
-#include "stage_inc_col2d.cuh"
+#include "col2d.cuh"
 
 namespace ns {
 
+constexpr int kAncOut = 26;    // output columns per warp (lanes 3..28; 3 halo lanes each side)
+constexpr int kAncH = 40;      // rows per strip (a 4096^2 sweep of 16..128 rows peaked at 40)
 constexpr int kAncWords = 16;  // words per lane and row in the ring
 
 struct CellFF {
@@ -38,12 +40,12 @@ __global__ void __launch_bounds__(NT) k_anchor_col2d(AnchorFFArgs A) {
   const int N = g.N;
   const long P = g.pitch;
   const int lane = threadIdx.x & 31;
-  const int nsx = (N + 1 + kColOut - 1) / kColOut;
-  const int nsy = (N + kColH - 1) / kColH;
+  const int nsx = (N + 1 + kAncOut - 1) / kAncOut;
+  const int nsy = (N + kAncH - 1) / kAncH;
   const int gw = blockIdx.x * (NT / 32) + (threadIdx.x >> 5);
   if (gw >= nsx * nsy) return;  // warp-uniform; no block-wide barrier below
   const int sx = gw % nsx, sy = gw / nsx;
-  const int xs = sx * kColOut, ys = sy * kColH;
+  const int xs = sx * kAncOut, ys = sy * kAncH;
   const int i = xs - 3 + lane;
   const bool perx = g.periodic[0], pery = g.periodic[1];
   const bool has_e = A.e4[0] != nullptr;
@@ -144,7 +146,7 @@ __global__ void __launch_bounds__(NT) k_anchor_col2d(AnchorFFArgs A) {
     }
   };
 
-  const int r_first = ys - 2, r_last = (ys + kColH >= N) ? N : ys + kColH - 1;
+  const int r_first = ys - 2, r_last = (ys + kAncH >= N) ? N : ys + kAncH - 1;
   k_next = r_first - 2;
   k_end = r_last + 2;
   for (int q = 0; q < kColRing; ++q) {
@@ -163,7 +165,7 @@ __global__ void __launch_bounds__(NT) k_anchor_col2d(AnchorFFArgs A) {
   const ff c15 = ff_make(A.c15[0], A.c15[1]);
   const ff zero = ff_make(0.f, 0.f);
   const int fgx = g.flux_ghost[0], fgy = g.flux_ghost[1];
-  const bool out_lane = lane >= 3 && lane < 3 + kColOut;
+  const bool out_lane = lane >= 3 && lane < 3 + kAncOut;
   ff fyp0 = zero, fyp1 = zero, t1p = zero;
   for (int r = r_first; r <= r_last; ++r) {
     cell_row(r + 2, w[4], uf[2], vl[2], su[2], sv[2]);

@@ -15,7 +15,7 @@ namespace ns {
 cudaError_t launch_inc_stage(const IncArgs& a, cudaStream_t s) {
   constexpr int NT = 128;
   const int N = a.g.N;
-  const long warps = (long)((N + 1 + kColOut - 1) / kColOut) * ((N + kColH - 1) / kColH);
+  const long warps = (long)((N + 1 + kIncOut - 1) / kIncOut) * ((N + kIncH - 1) / kIncH);
   const unsigned blocks = (unsigned)((warps + NT / 32 - 1) / (NT / 32));
   constexpr size_t smem = inc_col_smem<NT>();
   static bool attr = false;
@@ -33,7 +33,7 @@ cudaError_t launch_inc_stage(const IncArgs& a, cudaStream_t s) {
 cudaError_t launch_anchor_ff(const AnchorFFArgs& a, cudaStream_t s) {
   constexpr int NT = 128;
   const int N = a.g.N;
-  const long warps = (long)((N + 1 + kColOut - 1) / kColOut) * ((N + kColH - 1) / kColH);
+  const long warps = (long)((N + 1 + kAncOut - 1) / kAncOut) * ((N + kAncH - 1) / kAncH);
   const unsigned blocks = (unsigned)((warps + NT / 32 - 1) / (NT / 32));
   constexpr size_t smem = anchor_col_smem<NT>();
   static bool attr = false;
