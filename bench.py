@@ -37,7 +37,8 @@ ALGO_BYTES_PER_CELL = {
     "stage_exact": 88.0,   # read u*, u_base, u^n, du^n (2 x 8 B each) + p; write u*
     "stage_fast": 64.0,    # read u*, u_base, S; write u*
     "anchor": 64.0,        # read base hi/lo, e4, S hi/lo (f32); write base hi/lo, G0 (f32)
-    "increment": 88.0 / 3, # stage 1: read u_b, G0, write e; stages 2-3 also read e (all FP32)
+    "increment": 30.0,     # stage 1: read u_b, G0, write e (24); stages 2-3 and the incremental anchor update
+                           # also read e (32); launch mix of 7 incremental + 1 exact anchor per 8 iterations
     "explicit": 88.0,
     "step_begin": 56.0,    # read u, u_prev, p; write du, S
     "poisson_rhs": 24.0,   # read 2 faces, write f
