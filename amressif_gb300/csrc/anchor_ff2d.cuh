@@ -73,28 +73,6 @@ static __global__ void __launch_bounds__(256) k_split_ff2d(Geom g, const double*
 }
 
 // u* = (hi + lo) + e (FP64) once the mixed iteration stops
-// float-float base update between exact anchors: (oh, ol) = (h, l) + e on every
-// face; thread a of block row b handles u face (a, b) (a <= N, b < N) and
-// v face (a, b) (a < N, b <= N)
-static __global__ void __launch_bounds__(256) k_ff_base_add2d(Geom g, const float* h0, const float* l0, const float* h1,
-                                                              const float* l1, const float* e0, const float* e1, float* oh0,
-                                                              float* ol0, float* oh1, float* ol1) {
-  const int N = g.N;
-  const int a = blockIdx.x * 256 + threadIdx.x, b = blockIdx.y;
-  if (a > N) return;
-  const long id = (long)b * g.pitch + a;
-  if (b < N) {
-    const ff v = ff_add_f(ff_make(h0[id], l0[id]), e0[id]);
-    oh0[id] = v.hi;
-    ol0[id] = v.lo;
-  }
-  if (a < N) {
-    const ff v = ff_add_f(ff_make(h1[id], l1[id]), e1[id]);
-    oh1[id] = v.hi;
-    ol1[id] = v.lo;
-  }
-}
-
 static __global__ void __launch_bounds__(256) k_ff_add_inc2d(Geom g, const float* h0, const float* l0, const float* h1,
                                                              const float* l1, const float* e0, const float* e1, double* o0,
                                                              double* o1) {

@@ -10,22 +10,34 @@
 
 namespace ns {
 
-// column-marching increment stage: one warp per 26-column x 64-row strip, a
-// cp.async ring of raw face rows per warp in shared memory
-cudaError_t launch_inc_stage(const IncArgs& a, cudaStream_t s) {
+// column-marching increment stage: one warp per 58-column x kIncH-row strip,
+// a cp.async ring of raw face rows per warp in shared memory; the incremental
+// anchor update (obh set) also writes the new float-float base
+template <bool BASE>
+static cudaError_t launch_inc_t(const IncArgs& a, cudaStream_t s) {
   constexpr int NT = 128;
   const int N = a.g.N;
   const long warps = (long)((N + 1 + kIncOut - 1) / kIncOut) * ((N + kIncH - 1) / kIncH);
   const unsigned blocks = (unsigned)((warps + NT / 32 - 1) / (NT / 32));
-  constexpr size_t smem = inc_col_smem<NT>();
+  constexpr size_t smem = inc_col_smem<NT, BASE>();
   static bool attr = false;
   if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(k_inc_col2d<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(k_inc_col2d<NT, BASE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     attr = true;
   }
-  k_inc_col2d<NT><<<blocks, NT, smem, s>>>(a);
+  k_inc_col2d<NT, BASE><<<blocks, NT, smem, s>>>(a);
   return cudaGetLastError();
+}
+
+cudaError_t launch_inc_stage(const IncArgs& a, cudaStream_t s) {
+  if (a.obh[0] != nullptr) {
+    if (a.bl[0] == nullptr || a.bl[1] == nullptr || a.obh[1] == nullptr || a.obl[0] == nullptr || a.obl[1] == nullptr ||
+        a.ein[0] == nullptr)
+      return cudaErrorInvalidValue;
+    return launch_inc_t<true>(a, s);
+  }
+  return launch_inc_t<false>(a, s);
 }
 
 // column-marching float-float anchor: one warp per 26-column x 64-row strip,
@@ -64,13 +76,6 @@ cudaError_t launch_rhs_ff(int n, long pitch, const double* f, const double* mean
 
 cudaError_t launch_ff_to_double(int n, long pitch, const float* h, const float* l, double* out, cudaStream_t s) {
   k_ff_to_double2d<<<1024, 256, 0, s>>>(n, pitch, h, l, out);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_ff_base_add(const Geom& g, const float* const* h, const float* const* l, const float* const* e,
-                               float* const* oh, float* const* ol, cudaStream_t s) {
-  const dim3 grid((g.N + 1 + 255) / 256, g.N + 1, 1);
-  k_ff_base_add2d<<<grid, 256, 0, s>>>(g, h[0], l[0], h[1], l[1], e[0], e[1], oh[0], ol[0], oh[1], ol[1]);
   return cudaGetLastError();
 }
 

@@ -43,8 +43,6 @@ cudaError_t launch_ff_to_double(int n, long pitch, const float* h, const float* 
 cudaError_t launch_inc_stage(const IncArgs& a, cudaStream_t s);
 cudaError_t launch_anchor_ff(const AnchorFFArgs& a, cudaStream_t s);
 cudaError_t launch_split_ff(const Geom& g, const double* const* x, float* const* h, float* const* l, cudaStream_t s);
-cudaError_t launch_ff_base_add(const Geom& g, const float* const* h, const float* const* l, const float* const* e,
-                               float* const* oh, float* const* ol, cudaStream_t s);
 cudaError_t launch_ff_add_inc(const Geom& g, const float* const* h, const float* const* l, const float* const* e,
                               double* const* out, cudaStream_t s);
 

@@ -1107,7 +1107,7 @@ static void split_const(double x, float* out) {
 // pseudo-increment norm of Error_Computation.
 // every kAnchorEvery-th pseudo-iteration evaluates the anchor exactly (float-float);
 // the others update it by an FP32 increment evaluation
-constexpr int kAnchorEvery = 8;
+constexpr int kAnchorEvery = 16;
 
 static int mixed_iteration(ns_ctx* c, double* norm) {
   if (!c->s_ff_valid) {
@@ -1146,9 +1146,10 @@ static int mixed_iteration(ns_ctx* c, double* norm) {
     c->mb = nb;
   } else {
     // incremental anchor: G0 + dG(u_b; e4) by the FP32 increment kernel with
-    // rk = 1 (its rounding error is relative to e4), then u_b + e4 in
-    // float-float; the exact float-float anchor of the next kAnchorEvery-th
-    // iteration removes whatever these updates accumulated
+    // rk = 1 (its rounding error is relative to e4); the same launch writes
+    // u_b + e4 in float-float to the other base buffer. The exact float-float
+    // anchor of the next kAnchorEvery-th iteration removes whatever these
+    // updates accumulated
     const int mb = c->mb, nb = 1 - c->mb;
     IncArgs u;
     std::memset(&u, 0, sizeof(u));
@@ -1161,6 +1162,9 @@ static int mixed_iteration(ns_ctx* c, double* norm) {
       u.g0[m] = c->G0[m];
       u.ein[m] = c->E[0][m];
       u.eout[m] = c->G0b[m];
+      u.bl[m] = c->BL[mb][m];
+      u.obh[m] = c->BH[nb][m];
+      u.obl[m] = c->BL[nb][m];
       u.inv_dx[m] = (float)c->g.inv_dx[m];
       u.vcoef[m] = (float)(1.0 / (c->g.ren * c->g.dx2[m]));
     }
@@ -1169,12 +1173,6 @@ static int mixed_iteration(ns_ctx* c, double* norm) {
     u.rk = 1.f;
     u.do_norm = 0;
     LAUNCH(NS_PROF_INC, "anchor update", launch_inc_stage(u, c->st));
-    const float* h[2] = {c->BH[mb][0], c->BH[mb][1]};
-    const float* l[2] = {c->BL[mb][0], c->BL[mb][1]};
-    const float* e[2] = {c->E[0][0], c->E[0][1]};
-    float* oh[2] = {c->BH[nb][0], c->BH[nb][1]};
-    float* ol[2] = {c->BL[nb][0], c->BL[nb][1]};
-    LAUNCH(NS_PROF_OTHER, "base update", launch_ff_base_add(c->g, h, l, e, oh, ol, c->st));
     for (int m = 0; m < 2; ++m) std::swap(c->G0[m], c->G0b[m]);
     c->mb = nb;
   }

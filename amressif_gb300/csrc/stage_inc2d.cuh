@@ -27,6 +27,12 @@ struct IncArgs {
   const float* ein[2];  // e_s (faces); nullptr => e_s = rk_prev * g0
   float rk_prev;
   float* eout[2];       // e_{s+1} = rk * (G0 + dG)
+  // incremental anchor update only (nullptr otherwise): the lo part of the
+  // float-float base, and the new base (hi, lo) = (sh, bl) + e_s written to
+  // the other buffer of the pair, at the faces the launch writes eout
+  const float* bl[2];
+  float* obh[2];
+  float* obl[2];
   float rk;
   float inv_dx[2];      // 1/dx, 1/dy
   float vcoef[2];       // 1/(ren dx^2), 1/(ren dy^2)

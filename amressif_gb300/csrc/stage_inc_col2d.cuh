@@ -14,6 +14,10 @@
 // Compared with one column per lane (26 output columns per warp) this issues
 // about a quarter fewer instructions per output face; it runs at 12 warps per
 // SM (150 registers), and at 4096^2 a launch takes 0.243 ms against 0.273.
+// The incremental anchor update (BASE = true) also writes the new float-float
+// base (hi, lo) + e_s at its output faces, into the other buffer of the pair:
+// the lo words of row k - 2 travel in row k's ring slot, so they arrive with
+// the cell values read in the iteration that writes the faces of row k - 2.
 // Boundary handling: wall / lid ghosts of the cell velocity
 // (utilities.cpp:62-349; x ghosts from the mirror lane, y ghosts from the
 // mirror row), face column N and face row N loaded as they are (the periodic
@@ -27,6 +31,7 @@
 // in k_inc_col2d.
 #pragma once
 #include "col2d.cuh"
+#include "ff.cuh"
 #include "ns_common.cuh"
 #include "stage_inc2d.cuh"
 
@@ -34,18 +39,21 @@ namespace ns {
 
 constexpr int kIncOut = 58;    // output columns per warp
 constexpr int kIncH = 24;      // rows per strip (a 4096^2 sweep of 12..56 rows peaked at 24)
-constexpr int kIncWords = 18;  // ring words per lane and row
+// ring words per lane and row: 8 float2 pairs and 2 singles, plus the two lo
+// pairs of the base update
+__host__ __device__ constexpr int inc_words(bool base) { return base ? 22 : 18; }
 
 struct ColCells2 {
   float p0[2], p1[2], e0[2], e1[2];  // cart(u_b), cart(e_s) of columns a, b
 };
 
-template <int NT>
-constexpr size_t inc_col_smem() { return (size_t)(NT / 32) * kColRing * kIncWords * 32 * sizeof(float); }
+template <int NT, bool BASE>
+constexpr size_t inc_col_smem() { return (size_t)(NT / 32) * kColRing * inc_words(BASE) * 32 * sizeof(float); }
 
-template <int NT>
+template <int NT, bool BASE>
 __global__ void __launch_bounds__(NT, 384 / NT) k_inc_col2d(IncArgs A) {  // 12 warps per SM
   constexpr unsigned FULL = 0xffffffffu;
+  constexpr int kWords = inc_words(BASE), kPairs = BASE ? 10 : 8;
   const Geom& g = A.g;
   const int N = g.N;
   const long P = g.pitch;
@@ -94,13 +102,14 @@ __global__ void __launch_bounds__(NT, 384 / NT) k_inc_col2d(IncArgs A) {  // 12 
 #pragma unroll
     for (int s = 0; s < 2; ++s) lid[s] = (g.lid_u != nullptr) ? (float)(2.0 * g.lid_u[icm[s]]) : (float)g.bc[3].add[0];
 
-    // ring slot layout (per warp): float2 pairs[8][32] then float singles[2][32];
-    // pairs: 0 shu(pc, pc+1), 1 eu, 2 shv row k, 3 shv row k+1, 4 ev row k,
-    // 5 ev row k+1, 6 g0u, 7 g0v; singles: 0 shu(pc+2), 1 eu(pc+2)
+    // ring slot layout (per warp): float2 pairs[kPairs][32] then float
+    // singles[2][32]; pairs: 0 shu(pc, pc+1), 1 eu, 2 shv row k, 3 shv row k+1,
+    // 4 ev row k, 5 ev row k+1, 6 g0u, 7 g0v, with BASE 8 base lo u row k-2,
+    // 9 base lo v row k-2; singles: 0 shu(pc+2), 1 eu(pc+2)
     extern __shared__ __align__(16) float inc_ring[];
-    float* wring = inc_ring + (size_t)(threadIdx.x >> 5) * kColRing * kIncWords * 32;
-    auto pair_ptr = [&](int sl, int w) { return reinterpret_cast<float2*>(wring + (size_t)sl * kIncWords * 32) + w * 32 + lane; };
-    auto single_ptr = [&](int sl, int w) { return wring + (size_t)sl * kIncWords * 32 + 16 * 32 + w * 32 + lane; };
+    float* wring = inc_ring + (size_t)(threadIdx.x >> 5) * kColRing * kWords * 32;
+    auto pair_ptr = [&](int sl, int w) { return reinterpret_cast<float2*>(wring + (size_t)sl * kWords * 32) + w * 32 + lane; };
+    auto single_ptr = [&](int sl, int w) { return wring + (size_t)sl * kWords * 32 + 2 * kPairs * 32 + w * 32 + lane; };
     auto row_of = [&](int k) {
       if (k >= 0 && k < N) return k;
       if (pery) return wrapi(k, N);
@@ -119,10 +128,16 @@ __global__ void __launch_bounds__(NT, 384 / NT) k_inc_col2d(IncArgs A) {  // 12 
       cp_async8(reinterpret_cast<float*>(pair_ptr(sl, 7)), A.g0[1] + r0);
       cp_async4(single_ptr(sl, 0), shu + r0 + 2);
       cp_async4(single_ptr(sl, 1), eu + r0 + 2);
+      if constexpr (BASE) {
+        const long r2 = (long)row_of(k - 2) * P + pc;
+        cp_async8(reinterpret_cast<float*>(pair_ptr(sl, 8)), A.bl[0] + r2);
+        cp_async8(reinterpret_cast<float*>(pair_ptr(sl, 9)), A.bl[1] + r2);
+      }
       cp_async_commit();
     };
     int k_next = 0, k_end = 0;  // next row to issue, last row of the strip
     int slot = 0;               // ring slot of the next row to read (row r_first - 2 in slot 0)
+    float blu[2] = {0.f, 0.f}, blv[2] = {0.f, 0.f};  // base lo of the u / v faces of row k - 2
     // consume row k: cell values of both columns (with ghosts), the u face
     // (iface), the lower v face and G0 at the lane's faces; put the next row in flight
     auto cell_row = [&](int k, ColCells2& c, float (&ufb)[2], float (&ufe)[2], float (&vlb)[2], float (&vle)[2],
@@ -131,6 +146,13 @@ __global__ void __launch_bounds__(NT, 384 / NT) k_inc_col2d(IncArgs A) {  // 12 
       const float2 U = *pair_ptr(slot, 0), E = *pair_ptr(slot, 1), Vk = *pair_ptr(slot, 2), Vk1 = *pair_ptr(slot, 3);
       const float2 Fk = *pair_ptr(slot, 4), Fk1 = *pair_ptr(slot, 5), GU = *pair_ptr(slot, 6), GV = *pair_ptr(slot, 7);
       const float U2 = *single_ptr(slot, 0), E2 = *single_ptr(slot, 1);
+      if constexpr (BASE) {
+        const float2 LU = *pair_ptr(slot, 8), LV = *pair_ptr(slot, 9);
+        blu[0] = LU.x;
+        blu[1] = LU.y;
+        blv[0] = LV.x;
+        blv[1] = LV.y;
+      }
       if (k_next <= k_end) issue_row(k_next, slot);
       else cp_async_commit();  // empty group: the wait count stays one row per call
       ++k_next;
@@ -279,19 +301,35 @@ __global__ void __launch_bounds__(NT, 384 / NT) k_inc_col2d(IncArgs A) {  // 12 
               const float e = rk * (gqu[0][s] + (avg - c15 * ufe[0][s]));
               A.eout[0][id] = e;
               n0 = fmaf(wgt_u[s] * e, e, n0);
+              if constexpr (BASE) {  // u_b + e_s at u face (i, r); face words off the pair loads directly
+                const float lo = (s == 0 ? irr0 : irr1) ? A.bl[0][id] : blu[s];
+                const ff nb = ff_add_f(ff_make(ufb[0][s], lo), ufe[0][s]);
+                A.obh[0][id] = nb.hi;
+                A.obl[0][id] = nb.lo;
+              }
             }
             if (out_v[s]) {  // v face (i, r), r <= N
               const bool edge_v = (r == 0 || r == N);
               float avg = 0.5f * (t1p[s] + t1[s]);
               if (fgy != kWrap && edge_v) avg = (fgy == kReflect) ? 0.f : 0.5f * (r == 0 ? t1[s] : t1p[s]);
               float ecur = vle[0][s], gcur = gqv[0][s];
+              float bh = vlb[0][s], bo = blv[s];
               if (r == N) {  // face row N as stored
                 ecur = es * ev[id];
                 gcur = A.g0[1][id];
+                if constexpr (BASE) {
+                  bh = shv[id];
+                  bo = A.bl[1][id];
+                }
               }
               const float e = rk * (gcur + (avg - c15 * ecur));
               A.eout[1][id] = e;
               n1 = fmaf(edge_v ? 0.5f * e : e, e, n1);
+              if constexpr (BASE) {  // u_b + e_s at v face (i, r)
+                const ff nb = ff_add_f(ff_make(bh, bo), ecur);
+                A.obh[1][id] = nb.hi;
+                A.obl[1][id] = nb.lo;
+              }
             }
           }
         }
