@@ -43,23 +43,52 @@ struct IncArgs {
   double* norm_out;
 };
 
-// QUICK flux difference F(ub + e, phi + eps) - F(ub, phi) (fn_flux_calc.cpp:66-76)
-// a, b, c, e: phi at i+1, i, i-1, i-2; pa..pe the same for eps. Branch-free.
-// udn = max(un, 0) and upn = min(un, 0) are the upwind parts of the new
-// velocity; dud = udn - max(ub, 0) is formed without a subtraction (eb when
-// both signs are positive), and dup = eb - dud (exact except after a sign
-// change from negative to positive, where it differs from -ub by one rounding).
-__device__ __forceinline__ float quick_dflux(float ub, float eb, float a, float b, float c, float e, float pa, float pb_,
-                                             float pc, float pe) {
-  const float un = ub + eb;
-  const float udn = fmaxf(un, 0.f), upn = fminf(un, 0.f);
-  const float dud = (ub > 0.f) ? ((un > 0.f) ? eb : -ub) : udn;
-  const float dup = eb - dud;
-  const float qr_phi = fmaf(0.125f, (-a - 2.f * b) + 3.f * c, b);
-  const float ql_phi = fmaf(0.125f, (-e - 2.f * c) + 3.f * b, c);
-  const float qr_eps = fmaf(0.125f, (-pa - 2.f * pb_) + 3.f * pc, pb_);
-  const float ql_eps = fmaf(0.125f, (-pe - 2.f * pc) + 3.f * pb_, pc);
-  return fmaf(dud, ql_phi, fmaf(udn, ql_eps, fmaf(dup, qr_phi, upn * qr_eps)));
+// Packed FP32 pairs (the add / mul / fma f32x2 instructions of sm_100 and
+// later, each lane of the pair rounded like the scalar operation): the
+// column-marching kernel keeps two adjacent columns per lane and evaluates
+// both with one instruction where the operands form register pairs.
+__device__ __forceinline__ float2 p_add(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 p_mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 p_fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 p_sub(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
+__device__ __forceinline__ float2 p_splat(float x) { return make_float2(x, x); }
+
+// Upwind split of the new advecting velocity un = ub + e and its change
+// against ub (fn_flux_calc.cpp:66-68): udn = max(un, 0) and upn = min(un, 0)
+// (formed as un - udn, exact); dud = udn - max(ub, 0) without a subtraction
+// (eb while both are positive, -ub after a sign change, max(eb, -ub) covers
+// both); dup = eb - dud (exact except after a sign change from negative to
+// positive, where it differs from -ub by one rounding).
+struct QSign2 {
+  float2 udn, upn, dud, dup;
+};
+
+__device__ __forceinline__ QSign2 quick_sign2(float2 ub, float2 eb) {
+  QSign2 q;
+  const float2 un = p_add(ub, eb);
+  q.udn = make_float2(fmaxf(un.x, 0.f), fmaxf(un.y, 0.f));
+  q.upn = p_sub(un, q.udn);
+  q.dud = make_float2(ub.x > 0.f ? fmaxf(eb.x, -ub.x) : q.udn.x, ub.y > 0.f ? fmaxf(eb.y, -ub.y) : q.udn.y);
+  q.dup = p_sub(eb, q.dud);
+  return q;
+}
+
+// QUICK face value (fn_flux_calc.cpp:71-76) mid + (-up - 2 mid + 3 dn) / 8 =
+// 0.75 mid + 0.375 dn - 0.125 up, for a pair of faces
+__device__ __forceinline__ float2 quick_q2(float2 up, float2 mid, float2 dn) {
+  return p_fma(up, p_splat(-0.125f), p_fma(dn, p_splat(0.375f), p_mul(mid, p_splat(0.75f))));
+}
+
+// QUICK flux difference F(ub + e, phi + eps) - F(ub, phi) at a pair of faces;
+// a, b, c, e: phi at i+1, i, i-1, i-2; pa..pe the same for eps:
+//   dF = dud Q_L(phi) + udn Q_L(eps) + dup Q_R(phi) + upn Q_R(eps)
+__device__ __forceinline__ float2 quick_dflux2(const QSign2& q, float2 a, float2 b, float2 c, float2 e, float2 pa,
+                                               float2 pb, float2 pc, float2 pe) {
+  const float2 qr_phi = quick_q2(a, b, c);
+  const float2 ql_phi = quick_q2(e, c, b);
+  const float2 qr_eps = quick_q2(pa, pb, pc);
+  const float2 ql_eps = quick_q2(pe, pc, pb);
+  return p_fma(q.dud, ql_phi, p_fma(q.udn, ql_eps, p_fma(q.dup, qr_phi, p_mul(q.upn, qr_eps))));
 }
 
 }  // namespace ns

@@ -44,7 +44,7 @@ constexpr int kIncH = 24;      // rows per strip (a 4096^2 sweep of 12..56 rows 
 __host__ __device__ constexpr int inc_words(bool base) { return base ? 22 : 18; }
 
 struct ColCells2 {
-  float p0[2], p1[2], e0[2], e1[2];  // cart(u_b), cart(e_s) of columns a, b
+  float2 p0, p1, e0, e1;  // cart(u_b), cart(e_s) of columns (a, b)
 };
 
 template <int NT, bool BASE>
@@ -73,6 +73,7 @@ __global__ void __launch_bounds__(NT, 384 / NT) k_inc_col2d(IncArgs A) {  // 12 
     const float* __restrict__ eu = e_from_g0 ? A.g0[0] : A.ein[0];
     const float* __restrict__ ev = e_from_g0 ? A.g0[1] : A.ein[1];
     const float es = e_from_g0 ? A.rk_prev : 1.f;
+    const float2 es2 = p_splat(es), hes2 = p_splat(0.5f * es), half2 = p_splat(0.5f);
     // per slot s (column a + s): icm = cell column of k_inc_col2d (wrapped, or
     // the clamped mirror of an x ghost), iface = face column of the x flux's
     // advecting velocity; the pair loads use the even column pc (the lane's
@@ -137,83 +138,66 @@ __global__ void __launch_bounds__(NT, 384 / NT) k_inc_col2d(IncArgs A) {  // 12 
     };
     int k_next = 0, k_end = 0;  // next row to issue, last row of the strip
     int slot = 0;               // ring slot of the next row to read (row r_first - 2 in slot 0)
-    float blu[2] = {0.f, 0.f}, blv[2] = {0.f, 0.f};  // base lo of the u / v faces of row k - 2
+    float2 blu = make_float2(0.f, 0.f), blv = make_float2(0.f, 0.f);  // base lo of the u / v faces of row k - 2
     // consume row k: cell values of both columns (with ghosts), the u face
     // (iface), the lower v face and G0 at the lane's faces; put the next row in flight
-    auto cell_row = [&](int k, ColCells2& c, float (&ufb)[2], float (&ufe)[2], float (&vlb)[2], float (&vle)[2],
-                        float (&gu)[2], float (&gv)[2]) {
+    auto cell_row = [&](int k, ColCells2& c, float2& ufb, float2& ufe, float2& vlb, float2& vle, float2& gu,
+                        float2& gv) {
       cp_async_wait<kColRing - 1>();
       const float2 U = *pair_ptr(slot, 0), E = *pair_ptr(slot, 1), Vk = *pair_ptr(slot, 2), Vk1 = *pair_ptr(slot, 3);
       const float2 Fk = *pair_ptr(slot, 4), Fk1 = *pair_ptr(slot, 5), GU = *pair_ptr(slot, 6), GV = *pair_ptr(slot, 7);
       const float U2 = *single_ptr(slot, 0), E2 = *single_ptr(slot, 1);
       if constexpr (BASE) {
-        const float2 LU = *pair_ptr(slot, 8), LV = *pair_ptr(slot, 9);
-        blu[0] = LU.x;
-        blu[1] = LU.y;
-        blv[0] = LV.x;
-        blv[1] = LV.y;
+        blu = *pair_ptr(slot, 8);
+        blv = *pair_ptr(slot, 9);
       }
       if (k_next <= k_end) issue_row(k_next, slot);
       else cp_async_commit();  // empty group: the wait count stays one row per call
       ++k_next;
       slot = (slot == kColRing - 1) ? 0 : slot + 1;
-      c.p0[0] = 0.5f * (U.x + U.y);
-      c.p0[1] = 0.5f * (U.y + U2);
-      c.e0[0] = 0.5f * es * (E.x + E.y);
-      c.e0[1] = 0.5f * es * (E.y + E2);
-      c.p1[0] = 0.5f * (Vk.x + Vk1.x);
-      c.p1[1] = 0.5f * (Vk.y + Vk1.y);
-      c.e1[0] = 0.5f * es * (Fk.x + Fk1.x);
-      c.e1[1] = 0.5f * es * (Fk.y + Fk1.y);
-      ufb[0] = U.x;
-      ufb[1] = U.y;
-      ufe[0] = es * E.x;
-      ufe[1] = es * E.y;
-      gu[0] = GU.x;
-      gu[1] = GU.y;
+      c.p0 = p_mul(half2, p_add(U, make_float2(U.y, U2)));
+      c.e0 = p_mul(hes2, p_add(E, make_float2(E.y, E2)));
+      c.p1 = p_mul(half2, p_add(Vk, Vk1));
+      c.e1 = p_mul(hes2, p_add(Fk, Fk1));
+      ufb = U;
+      ufe = p_mul(es2, E);
+      gu = GU;
       if (irr0 || irr1) {  // face N, the periodic image, wall faces: direct loads (edge lanes only)
         const long rr = (long)row_of(k) * P;
-        if (irr0) { ufb[0] = shu[rr + iface[0]]; ufe[0] = es * eu[rr + iface[0]]; gu[0] = A.g0[0][rr + iface[0]]; }
-        if (irr1) { ufb[1] = shu[rr + iface[1]]; ufe[1] = es * eu[rr + iface[1]]; gu[1] = A.g0[0][rr + iface[1]]; }
+        if (irr0) { ufb.x = shu[rr + iface[0]]; ufe.x = es * eu[rr + iface[0]]; gu.x = A.g0[0][rr + iface[0]]; }
+        if (irr1) { ufb.y = shu[rr + iface[1]]; ufe.y = es * eu[rr + iface[1]]; gu.y = A.g0[0][rr + iface[1]]; }
       }
-      vlb[0] = Vk.x;
-      vlb[1] = Vk.y;
-      vle[0] = es * Fk.x;
-      vle[1] = es * Fk.y;
-      gv[0] = GV.x;
-      gv[1] = GV.y;
+      vlb = Vk;
+      vle = p_mul(es2, Fk);
+      gv = GV;
       if (warp_xghost) {  // x ghosts: the mirror pair's values (slots swapped) under the side's rule
-        const float q00 = __shfl_sync(FULL, c.p0[1], src_lane), q01 = __shfl_sync(FULL, c.p0[0], src_lane);
-        const float q10 = __shfl_sync(FULL, c.p1[1], src_lane), q11 = __shfl_sync(FULL, c.p1[0], src_lane);
-        const float s00 = __shfl_sync(FULL, c.e0[1], src_lane), s01 = __shfl_sync(FULL, c.e0[0], src_lane);
-        const float s10 = __shfl_sync(FULL, c.e1[1], src_lane), s11 = __shfl_sync(FULL, c.e1[0], src_lane);
+        const float q00 = __shfl_sync(FULL, c.p0.y, src_lane), q01 = __shfl_sync(FULL, c.p0.x, src_lane);
+        const float q10 = __shfl_sync(FULL, c.p1.y, src_lane), q11 = __shfl_sync(FULL, c.p1.x, src_lane);
+        const float s00 = __shfl_sync(FULL, c.e0.y, src_lane), s01 = __shfl_sync(FULL, c.e0.x, src_lane);
+        const float s10 = __shfl_sync(FULL, c.e1.y, src_lane), s11 = __shfl_sync(FULL, c.e1.x, src_lane);
         if (xghost) {
-          c.p0[0] = cart_ghost_f(bx, 0, q00, false);
-          c.p0[1] = cart_ghost_f(bx, 0, q01, false);
-          c.p1[0] = cart_ghost_f(bx, 1, q10, false);
-          c.p1[1] = cart_ghost_f(bx, 1, q11, false);
-          c.e0[0] = cart_ghost_f(bx, 0, s00, true);
-          c.e0[1] = cart_ghost_f(bx, 0, s01, true);
-          c.e1[0] = cart_ghost_f(bx, 1, s10, true);
-          c.e1[1] = cart_ghost_f(bx, 1, s11, true);
+          c.p0 = make_float2(cart_ghost_f(bx, 0, q00, false), cart_ghost_f(bx, 0, q01, false));
+          c.p1 = make_float2(cart_ghost_f(bx, 1, q10, false), cart_ghost_f(bx, 1, q11, false));
+          c.e0 = make_float2(cart_ghost_f(bx, 0, s00, true), cart_ghost_f(bx, 0, s01, true));
+          c.e1 = make_float2(cart_ghost_f(bx, 1, s10, true), cart_ghost_f(bx, 1, s11, true));
         }
       }
       if (!pery && (k < 0 || k >= N)) {  // y ghosts from the mirror row; the lid profile on the north u
         const CartBC& by = g.bc[k < 0 ? 2 : 3];
-#pragma unroll
-        for (int s = 0; s < 2; ++s) {
-          if (k >= N && by.rule[0] == kInlet) c.p0[s] = lid[s] - c.p0[s];
-          else c.p0[s] = cart_ghost_f(by, 0, c.p0[s], false);
-          c.p1[s] = cart_ghost_f(by, 1, c.p1[s], false);
-          c.e0[s] = cart_ghost_f(by, 0, c.e0[s], true);
-          c.e1[s] = cart_ghost_f(by, 1, c.e1[s], true);
+        if (k >= N && by.rule[0] == kInlet) {
+          c.p0 = make_float2(lid[0] - c.p0.x, lid[1] - c.p0.y);
+        } else {
+          c.p0 = make_float2(cart_ghost_f(by, 0, c.p0.x, false), cart_ghost_f(by, 0, c.p0.y, false));
         }
+        c.p1 = make_float2(cart_ghost_f(by, 1, c.p1.x, false), cart_ghost_f(by, 1, c.p1.y, false));
+        c.e0 = make_float2(cart_ghost_f(by, 0, c.e0.x, true), cart_ghost_f(by, 0, c.e0.y, true));
+        c.e1 = make_float2(cart_ghost_f(by, 1, c.e1.x, true), cart_ghost_f(by, 1, c.e1.y, true));
       }
     };
 
     // w[0..4]: cell rows r-2 .. r+2; uf*/vl*/gq*[0..2]: faces of rows r .. r+2
     ColCells2 w[5];
-    float ufb[3][2], ufe[3][2], vlb[3][2], vle[3][2], gqu[3][2], gqv[3][2], xb[2], xe[2];
+    float2 ufb[3], ufe[3], vlb[3], vle[3], gqu[3], gqv[3], xb, xe;
     const int r_first = ys - 2;  // fy at face ys-1, then the totals of row ys-1
     const int r_last = (ys + kIncH >= N) ? N : ys + kIncH - 1;
     k_next = r_first - 2;
@@ -227,8 +211,9 @@ __global__ void __launch_bounds__(NT, 384 / NT) k_inc_col2d(IncArgs A) {  // 12 
     cell_row(r_first - 1, w[1], xb, xe, xb, xe, xb, xe);
     cell_row(r_first, w[2], ufb[0], ufe[0], vlb[0], vle[0], gqu[0], gqv[0]);
     cell_row(r_first + 1, w[3], ufb[1], ufe[1], vlb[1], vle[1], gqu[1], gqv[1]);
-    const float idx_ = A.inv_dx[0], idy_ = A.inv_dx[1], vx = A.vcoef[0], vy = A.vcoef[1];
-    const float c15 = A.c15, rk = A.rk;
+    const float2 idx2 = p_splat(A.inv_dx[0]), idy2 = p_splat(A.inv_dx[1]);
+    const float2 vx2 = p_splat(A.vcoef[0]), vy2 = p_splat(A.vcoef[1]), m2 = p_splat(-2.f);
+    const float2 mc15 = p_splat(-A.c15), rk2 = p_splat(A.rk);
     const int fgx = g.flux_ghost[0], fgy = g.flux_ghost[1];
     const bool out_lane = lane >= 2 && lane <= 30;  // columns xs .. xs + 57, both slots
     bool out_u[2], out_v[2], edge_u[2], rule_u[2];
@@ -242,111 +227,114 @@ __global__ void __launch_bounds__(NT, 384 / NT) k_inc_col2d(IncArgs A) {  // 12 
       rule_u[s] = fgx != kWrap && edge_u[s];
       wgt_u[s] = edge_u[s] ? 0.5f : 1.f;
     }
-    float fyp0[2] = {0.f, 0.f}, fyp1[2] = {0.f, 0.f};  // y flux at face r
-    float t1p[2] = {0.f, 0.f};                          // v total of row r-1
+    // x neighbours of a field X of columns (a, b): ip = columns (a+1, b+1),
+    // im = (a-1, b-1), imm = (a-2, b-2), from the lanes on either side
+    auto xnb = [&](float2 X, float2& ip, float2& im, float2& imm) {
+      const float u0 = __shfl_up_sync(FULL, X.x, 1), u1 = __shfl_up_sync(FULL, X.y, 1);
+      const float d0 = __shfl_down_sync(FULL, X.x, 1);
+      ip = make_float2(X.y, d0);
+      im = make_float2(u1, X.x);
+      imm = make_float2(u0, u1);
+    };
+    float2 fyp0 = make_float2(0.f, 0.f), fyp1 = make_float2(0.f, 0.f);  // y flux at face r
+    float2 t1p = make_float2(0.f, 0.f);                                 // v total of row r-1
     for (int r = r_first; r <= r_last; ++r) {
       cell_row(r + 2, w[4], ufb[2], ufe[2], vlb[2], vle[2], gqu[2], gqv[2]);
       // y flux at face r+1 (rows r, r+1), cells r-1 .. r+2; face row N as stored
-      float fy0[2], fy1[2];
-#pragma unroll
-      for (int s = 0; s < 2; ++s) {
-        float vfb = vlb[1][s], vfe = vle[1][s];
-        if (r + 1 == N) {
-          const long id = (long)N * P + pc + s;
-          vfb = shv[id];
-          vfe = es * ev[id];
-        }
-        fy0[s] = quick_dflux(vfb, vfe, w[4].p0[s], w[3].p0[s], w[2].p0[s], w[1].p0[s], w[4].e0[s], w[3].e0[s],
-                             w[2].e0[s], w[1].e0[s]);
-        fy1[s] = quick_dflux(vfb, vfe, w[4].p1[s], w[3].p1[s], w[2].p1[s], w[1].p1[s], w[4].e1[s], w[3].e1[s],
-                             w[2].e1[s], w[1].e1[s]);
+      float2 vfb = vlb[1], vfe = vle[1];
+      if (r + 1 == N) {
+        const long id = (long)N * P + pc;
+        vfb = make_float2(shv[id], shv[id + 1]);
+        vfe = p_mul(es2, make_float2(ev[id], ev[id + 1]));
       }
+      const QSign2 qy = quick_sign2(vfb, vfe);
+      const float2 fy0 = quick_dflux2(qy, w[4].p0, w[3].p0, w[2].p0, w[1].p0, w[4].e0, w[3].e0, w[2].e0, w[1].e0);
+      const float2 fy1 = quick_dflux2(qy, w[4].p1, w[3].p1, w[2].p1, w[1].p1, w[4].e1, w[3].e1, w[2].e1, w[1].e1);
       if (r >= ys - 1) {  // warp-uniform
         const ColCells2& c = w[2];
-        // x neighbours: U1 = column a - 1, U0 = column a - 2, D0 = column b + 1
-        const float p0U1 = __shfl_up_sync(FULL, c.p0[1], 1), p0U0 = __shfl_up_sync(FULL, c.p0[0], 1);
-        const float p0D0 = __shfl_down_sync(FULL, c.p0[0], 1);
-        const float p1U1 = __shfl_up_sync(FULL, c.p1[1], 1), p1U0 = __shfl_up_sync(FULL, c.p1[0], 1);
-        const float p1D0 = __shfl_down_sync(FULL, c.p1[0], 1);
-        const float e0U1 = __shfl_up_sync(FULL, c.e0[1], 1), e0U0 = __shfl_up_sync(FULL, c.e0[0], 1);
-        const float e0D0 = __shfl_down_sync(FULL, c.e0[0], 1);
-        const float e1U1 = __shfl_up_sync(FULL, c.e1[1], 1), e1U0 = __shfl_up_sync(FULL, c.e1[0], 1);
-        const float e1D0 = __shfl_down_sync(FULL, c.e1[0], 1);
-        // x fluxes at faces a (cells a-2 .. a+1) and b (cells b-2 .. b+1)
-        const float fx0a = quick_dflux(ufb[0][0], ufe[0][0], c.p0[1], c.p0[0], p0U1, p0U0, c.e0[1], c.e0[0], e0U1, e0U0);
-        const float fx1a = quick_dflux(ufb[0][0], ufe[0][0], c.p1[1], c.p1[0], p1U1, p1U0, c.e1[1], c.e1[0], e1U1, e1U0);
-        const float fx0b = quick_dflux(ufb[0][1], ufe[0][1], p0D0, c.p0[1], c.p0[0], p0U1, e0D0, c.e0[1], c.e0[0], e0U1);
-        const float fx1b = quick_dflux(ufb[0][1], ufe[0][1], p1D0, c.p1[1], c.p1[0], p1U1, e1D0, c.e1[1], c.e1[0], e1U1);
-        const float fx0r = __shfl_down_sync(FULL, fx0a, 1), fx1r = __shfl_down_sync(FULL, fx1a, 1);  // face b + 1
-        // totals of cells a and b
-        const float conv0a = (fx0b - fx0a) * idx_ + (fy0[0] - fyp0[0]) * idy_;
-        const float conv1a = (fx1b - fx1a) * idx_ + (fy1[0] - fyp1[0]) * idy_;
-        const float conv0b = (fx0r - fx0b) * idx_ + (fy0[1] - fyp0[1]) * idy_;
-        const float conv1b = (fx1r - fx1b) * idx_ + (fy1[1] - fyp1[1]) * idy_;
-        const float visc0a = (c.e0[1] - 2.f * c.e0[0] + e0U1) * vx + (w[3].e0[0] - 2.f * c.e0[0] + w[1].e0[0]) * vy;
-        const float visc1a = (c.e1[1] - 2.f * c.e1[0] + e1U1) * vx + (w[3].e1[0] - 2.f * c.e1[0] + w[1].e1[0]) * vy;
-        const float visc0b = (e0D0 - 2.f * c.e0[1] + c.e0[0]) * vx + (w[3].e0[1] - 2.f * c.e0[1] + w[1].e0[1]) * vy;
-        const float visc1b = (e1D0 - 2.f * c.e1[1] + c.e1[0]) * vx + (w[3].e1[1] - 2.f * c.e1[1] + w[1].e1[1]) * vy;
-        const float t0[2] = {visc0a - conv0a, visc0b - conv0b};
-        const float t1[2] = {visc1a - conv1a, visc1b - conv1b};
-        const float t0l[2] = {__shfl_up_sync(FULL, t0[1], 1), t0[0]};  // u total of cells a - 1 and a
+        float2 p0p, p0m, p0mm, p1p, p1m, p1mm, e0p, e0m, e0mm, e1p, e1m, e1mm;
+        xnb(c.p0, p0p, p0m, p0mm);
+        xnb(c.p1, p1p, p1m, p1mm);
+        xnb(c.e0, e0p, e0m, e0mm);
+        xnb(c.e1, e1p, e1m, e1mm);
+        // x fluxes at faces a and b (face i between cells i-1 and i)
+        const QSign2 qx = quick_sign2(ufb[0], ufe[0]);
+        const float2 fx0 = quick_dflux2(qx, p0p, c.p0, p0m, p0mm, e0p, c.e0, e0m, e0mm);
+        const float2 fx1 = quick_dflux2(qx, p1p, c.p1, p1m, p1mm, e1p, c.e1, e1m, e1mm);
+        const float2 fx0n = make_float2(fx0.y, __shfl_down_sync(FULL, fx0.x, 1));  // faces b, b + 1
+        const float2 fx1n = make_float2(fx1.y, __shfl_down_sync(FULL, fx1.x, 1));
+        // totals of cells a and b: viscous minus convective
+        const float2 conv0 = p_fma(p_sub(fx0n, fx0), idx2, p_mul(p_sub(fy0, fyp0), idy2));
+        const float2 conv1 = p_fma(p_sub(fx1n, fx1), idx2, p_mul(p_sub(fy1, fyp1), idy2));
+        const float2 visc0 = p_fma(p_fma(c.e0, m2, p_add(e0p, e0m)), vx2, p_mul(p_fma(c.e0, m2, p_add(w[3].e0, w[1].e0)), vy2));
+        const float2 visc1 = p_fma(p_fma(c.e1, m2, p_add(e1p, e1m)), vx2, p_mul(p_fma(c.e1, m2, p_add(w[3].e1, w[1].e1)), vy2));
+        const float2 t0 = p_sub(visc0, conv0), t1 = p_sub(visc1, conv1);
+        const float2 t0l = make_float2(__shfl_up_sync(FULL, t0.y, 1), t0.x);  // u total of cells a - 1 and a
         if (r >= ys) {  // warp-uniform
+          // u faces (a, r), (b, r); r < N
+          float2 avg = p_mul(half2, p_add(t0l, t0));
+          if (rule_u[0]) avg.x = (fgx == kReflect) ? 0.f : 0.5f * (a == 0 ? t0.x : t0l.x);
+          if (rule_u[1]) avg.y = (fgx == kReflect) ? 0.f : 0.5f * (a + 1 == 0 ? t0.y : t0l.y);
+          const float2 eu2 = p_mul(rk2, p_add(gqu[0], p_fma(ufe[0], mc15, avg)));
+          // v faces (a, r), (b, r); r <= N
+          const bool edge_v = (r == 0 || r == N);
+          float2 avgv = p_mul(half2, p_add(t1p, t1));
+          if (fgy != kWrap && edge_v) {
+            avgv.x = (fgy == kReflect) ? 0.f : 0.5f * (r == 0 ? t1.x : t1p.x);
+            avgv.y = (fgy == kReflect) ? 0.f : 0.5f * (r == 0 ? t1.y : t1p.y);
+          }
+          float2 ecur = vle[0], gcur = gqv[0], bh = vlb[0], bo = blv;
+          if (r == N) {  // face row N as stored
+            const long id = (long)N * P + a;
+#pragma unroll
+            for (int s = 0; s < 2; ++s) {
+              if (out_v[s]) {
+                (s ? ecur.y : ecur.x) = es * ev[id + s];
+                (s ? gcur.y : gcur.x) = A.g0[1][id + s];
+                if constexpr (BASE) {
+                  (s ? bh.y : bh.x) = shv[id + s];
+                  (s ? bo.y : bo.x) = A.bl[1][id + s];
+                }
+              }
+            }
+          }
+          const float2 ev2 = p_mul(rk2, p_add(gcur, p_fma(ecur, mc15, avgv)));
 #pragma unroll
           for (int s = 0; s < 2; ++s) {
             const int i = a + s;
             const long id = (long)r * P + i;
             if (out_u[s] && r < N) {  // u face (i, r)
-              float avg = 0.5f * (t0l[s] + t0[s]);
-              if (rule_u[s]) avg = (fgx == kReflect) ? 0.f : 0.5f * (i == 0 ? t0[s] : t0l[s]);
-              const float e = rk * (gqu[0][s] + (avg - c15 * ufe[0][s]));
+              const float e = s ? eu2.y : eu2.x;
               A.eout[0][id] = e;
               n0 = fmaf(wgt_u[s] * e, e, n0);
               if constexpr (BASE) {  // u_b + e_s at u face (i, r); face words off the pair loads directly
-                const float lo = (s == 0 ? irr0 : irr1) ? A.bl[0][id] : blu[s];
-                const ff nb = ff_add_f(ff_make(ufb[0][s], lo), ufe[0][s]);
+                const float lo = (s == 0 ? irr0 : irr1) ? A.bl[0][id] : (s ? blu.y : blu.x);
+                const ff nb = ff_add_f(ff_make(s ? ufb[0].y : ufb[0].x, lo), s ? ufe[0].y : ufe[0].x);
                 A.obh[0][id] = nb.hi;
                 A.obl[0][id] = nb.lo;
               }
             }
             if (out_v[s]) {  // v face (i, r), r <= N
-              const bool edge_v = (r == 0 || r == N);
-              float avg = 0.5f * (t1p[s] + t1[s]);
-              if (fgy != kWrap && edge_v) avg = (fgy == kReflect) ? 0.f : 0.5f * (r == 0 ? t1[s] : t1p[s]);
-              float ecur = vle[0][s], gcur = gqv[0][s];
-              float bh = vlb[0][s], bo = blv[s];
-              if (r == N) {  // face row N as stored
-                ecur = es * ev[id];
-                gcur = A.g0[1][id];
-                if constexpr (BASE) {
-                  bh = shv[id];
-                  bo = A.bl[1][id];
-                }
-              }
-              const float e = rk * (gcur + (avg - c15 * ecur));
+              const float e = s ? ev2.y : ev2.x;
               A.eout[1][id] = e;
               n1 = fmaf(edge_v ? 0.5f * e : e, e, n1);
               if constexpr (BASE) {  // u_b + e_s at v face (i, r)
-                const ff nb = ff_add_f(ff_make(bh, bo), ecur);
+                const ff nb = ff_add_f(ff_make(s ? bh.y : bh.x, s ? bo.y : bo.x), s ? ecur.y : ecur.x);
                 A.obh[1][id] = nb.hi;
                 A.obl[1][id] = nb.lo;
               }
             }
           }
         }
-        t1p[0] = t1[0];
-        t1p[1] = t1[1];
+        t1p = t1;
       }
-#pragma unroll
-      for (int s = 0; s < 2; ++s) {
-        fyp0[s] = fy0[s];
-        fyp1[s] = fy1[s];
-      }
+      fyp0 = fy0;
+      fyp1 = fy1;
       w[0] = w[1]; w[1] = w[2]; w[2] = w[3]; w[3] = w[4];
 #pragma unroll
-      for (int s = 0; s < 2; ++s) {
-        ufb[0][s] = ufb[1][s]; ufe[0][s] = ufe[1][s]; ufb[1][s] = ufb[2][s]; ufe[1][s] = ufe[2][s];
-        gqu[0][s] = gqu[1][s]; gqv[0][s] = gqv[1][s]; gqu[1][s] = gqu[2][s]; gqv[1][s] = gqv[2][s];
-        vlb[0][s] = vlb[1][s]; vle[0][s] = vle[1][s]; vlb[1][s] = vlb[2][s]; vle[1][s] = vle[2][s];
+      for (int q = 0; q < 2; ++q) {
+        ufb[q] = ufb[q + 1]; ufe[q] = ufe[q + 1]; gqu[q] = gqu[q + 1]; gqv[q] = gqv[q + 1];
+        vlb[q] = vlb[q + 1]; vle[q] = vle[q + 1];
       }
     }
     cp_async_wait<0>();
