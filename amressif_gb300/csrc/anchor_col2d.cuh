@@ -5,7 +5,7 @@
 // warp per strip of 32 columns (26 output columns), marching upward with a
 // 5-row register window of cell velocities, x neighbours by warp shuffles, and
 // the raw face rows streamed through a per-warp cp.async ring in shared
-// memory (kColRing rows in flight), so the loads never stall the arithmetic.
+// memory (kAncRing rows in flight), so the loads never stall the arithmetic.
 #pragma once
 #include "anchor_ff2d.cuh"
 #include "ff.cuh"
@@ -15,6 +15,7 @@ namespace ns {
 
 constexpr int kAncOut = 26;    // output columns per warp (lanes 3..28; 3 halo lanes each side)
 constexpr int kAncH = 40;      // rows per strip (a 4096^2 sweep of 16..128 rows peaked at 40)
+constexpr int kAncRing = 4;    // rows in flight per warp (6, 4 and 3 rows: 0.626, 0.620, 0.619 ms a launch at 4096^2)
 constexpr int kAncWords = 16;  // words per lane and row in the ring
 
 struct CellFF {
@@ -22,7 +23,7 @@ struct CellFF {
 };
 
 template <int NT>
-constexpr size_t anchor_col_smem() { return (size_t)(NT / 32) * kColRing * kAncWords * 32 * sizeof(float); }
+constexpr size_t anchor_col_smem() { return (size_t)(NT / 32) * kAncRing * kAncWords * 32 * sizeof(float); }
 
 __device__ __forceinline__ ff shfl_ff(ff x, int src) {
   return ff_make(__shfl_sync(0xffffffffu, x.hi, src), __shfl_sync(0xffffffffu, x.lo, src));
@@ -66,7 +67,7 @@ __global__ void __launch_bounds__(NT) k_anchor_col2d(AnchorFFArgs A) {
   const ff lid = (g.lid_u != nullptr) ? ff_from_double(2.0 * g.lid_u[ic]) : ff_from_double(g.bc[3].add[0]);
 
   extern __shared__ __align__(16) float anc_ring[];
-  float* ring = anc_ring + (size_t)(threadIdx.x >> 5) * kColRing * kAncWords * 32 + lane;
+  float* ring = anc_ring + (size_t)(threadIdx.x >> 5) * kAncRing * kAncWords * 32 + lane;
   auto row_of = [&](int k) {
     if (k >= 0 && k < N) return k;
     if (pery) return wrapi(k, N);
@@ -74,7 +75,7 @@ __global__ void __launch_bounds__(NT) k_anchor_col2d(AnchorFFArgs A) {
     return kk < 0 ? 0 : (kk >= N ? N - 1 : kk);
   };
   // ring slots count from the strip's first row (row r_first - 2 in slot 0); row
-  // k + kColRing is issued into the slot row k was just read from
+  // k + kAncRing is issued into the slot row k was just read from
   auto slot_ptr = [&](int sl) { return ring + (size_t)sl * kAncWords * 32; };
   // words: 0-2 u face (ic): hi, lo, e4; 3-5 u face (ic+1); 6-8 v face (ic, kk);
   // 9-11 v face (ic, kk+1); 12-13 S_u (iface): hi, lo; 14-15 S_v (ic): hi, lo
@@ -117,7 +118,7 @@ __global__ void __launch_bounds__(NT) k_anchor_col2d(AnchorFFArgs A) {
   // consume row k: cell velocities (with ghosts), the u face (iface, k), the
   // lower v face (ic, k) and S at the lane's faces
   auto cell_row = [&](int k, CellFF& c, ff& uf, ff& vl, ff& su, ff& sv) {
-    cp_async_wait<kColRing - 1>();
+    cp_async_wait<kAncRing - 1>();
     const float* d = slot_ptr(rslot);
     const ff ua = ubase(d, 0), ub = ubase(d, 3), va = ubase(d, 6), vb = ubase(d, 9);
     su = ff_make(d[12 * 32], d[13 * 32]);
@@ -128,7 +129,7 @@ __global__ void __launch_bounds__(NT) k_anchor_col2d(AnchorFFArgs A) {
     if (k_next <= k_end) issue_row(k_next, rslot);
     else cp_async_commit();
     ++k_next;
-    rslot = (rslot == kColRing - 1) ? 0 : rslot + 1;
+    rslot = (rslot == kAncRing - 1) ? 0 : rslot + 1;
     c.p0 = ff_scale2(ua + ub, 0.5f);
     c.p1 = ff_scale2(va + vb, 0.5f);
     if (warp_xghost) {
@@ -149,7 +150,7 @@ __global__ void __launch_bounds__(NT) k_anchor_col2d(AnchorFFArgs A) {
   const int r_first = ys - 2, r_last = (ys + kAncH >= N) ? N : ys + kAncH - 1;
   k_next = r_first - 2;
   k_end = r_last + 2;
-  for (int q = 0; q < kColRing; ++q) {
+  for (int q = 0; q < kAncRing; ++q) {
     if (k_next <= k_end) issue_row(k_next, q);
     else cp_async_commit();
     ++k_next;

@@ -1,15 +1,13 @@
 // Column-marching infrastructure shared by the 2D mixed-precision predictor
 // kernels (stage_inc_col2d.cuh, anchor_col2d.cuh): a warp owns a strip of
 // columns and marches up its rows; the raw face rows stream through a per-warp
-// ring of shared memory filled by cp.async (kColRing rows in flight), so the
+// ring of shared memory filled by cp.async (a few rows in flight), so the
 // loads of later rows are in flight while a row is computed and no block
 // barrier is needed.
 #pragma once
 #include <cuda_runtime.h>
 
 namespace ns {
-
-constexpr int kColRing = 6;  // rows in flight per warp
 
 __device__ __forceinline__ void cp_async4(float* sdst, const float* gsrc) {
   const unsigned s = (unsigned)__cvta_generic_to_shared(sdst);

@@ -42,13 +42,18 @@ constexpr int kIncH = 24;      // rows per strip (a 4096^2 sweep of 12..56 rows 
 // ring words per lane and row: 8 float2 pairs and 2 singles, plus the two lo
 // pairs of the base update
 __host__ __device__ constexpr int inc_words(bool base) { return base ? 22 : 18; }
+// rows in flight per warp. A shallow ring leaves most of the SM's unified
+// L1 / shared storage to L1, where the halo columns of neighbouring warps and
+// the single-word loads of the next lane's pair hit: at 4096^2 rings of 6, 5,
+// 4, 3 and 2 rows gave 0.239, 0.222, 0.219, 0.214 and 0.215 ms a launch.
+constexpr int kIncRing = 3;
 
 struct ColCells2 {
   float2 p0, p1, e0, e1;  // cart(u_b), cart(e_s) of columns (a, b)
 };
 
 template <int NT, bool BASE>
-constexpr size_t inc_col_smem() { return (size_t)(NT / 32) * kColRing * inc_words(BASE) * 32 * sizeof(float); }
+constexpr size_t inc_col_smem() { return (size_t)(NT / 32) * kIncRing * inc_words(BASE) * 32 * sizeof(float); }
 
 template <int NT, bool BASE>
 __global__ void __launch_bounds__(NT, 384 / NT) k_inc_col2d(IncArgs A) {  // 12 warps per SM
@@ -108,7 +113,7 @@ __global__ void __launch_bounds__(NT, 384 / NT) k_inc_col2d(IncArgs A) {  // 12 
     // 4 ev row k, 5 ev row k+1, 6 g0u, 7 g0v, with BASE 8 base lo u row k-2,
     // 9 base lo v row k-2; singles: 0 shu(pc+2), 1 eu(pc+2)
     extern __shared__ __align__(16) float inc_ring[];
-    float* wring = inc_ring + (size_t)(threadIdx.x >> 5) * kColRing * kWords * 32;
+    float* wring = inc_ring + (size_t)(threadIdx.x >> 5) * kIncRing * kWords * 32;
     auto pair_ptr = [&](int sl, int w) { return reinterpret_cast<float2*>(wring + (size_t)sl * kWords * 32) + w * 32 + lane; };
     auto single_ptr = [&](int sl, int w) { return wring + (size_t)sl * kWords * 32 + 2 * kPairs * 32 + w * 32 + lane; };
     auto row_of = [&](int k) {
@@ -143,7 +148,7 @@ __global__ void __launch_bounds__(NT, 384 / NT) k_inc_col2d(IncArgs A) {  // 12 
     // (iface), the lower v face and G0 at the lane's faces; put the next row in flight
     auto cell_row = [&](int k, ColCells2& c, float2& ufb, float2& ufe, float2& vlb, float2& vle, float2& gu,
                         float2& gv) {
-      cp_async_wait<kColRing - 1>();
+      cp_async_wait<kIncRing - 1>();
       const float2 U = *pair_ptr(slot, 0), E = *pair_ptr(slot, 1), Vk = *pair_ptr(slot, 2), Vk1 = *pair_ptr(slot, 3);
       const float2 Fk = *pair_ptr(slot, 4), Fk1 = *pair_ptr(slot, 5), GU = *pair_ptr(slot, 6), GV = *pair_ptr(slot, 7);
       const float U2 = *single_ptr(slot, 0), E2 = *single_ptr(slot, 1);
@@ -154,7 +159,7 @@ __global__ void __launch_bounds__(NT, 384 / NT) k_inc_col2d(IncArgs A) {  // 12 
       if (k_next <= k_end) issue_row(k_next, slot);
       else cp_async_commit();  // empty group: the wait count stays one row per call
       ++k_next;
-      slot = (slot == kColRing - 1) ? 0 : slot + 1;
+      slot = (slot == kIncRing - 1) ? 0 : slot + 1;
       c.p0 = p_mul(half2, p_add(U, make_float2(U.y, U2)));
       c.e0 = p_mul(hes2, p_add(E, make_float2(E.y, E2)));
       c.p1 = p_mul(half2, p_add(Vk, Vk1));
@@ -202,7 +207,7 @@ __global__ void __launch_bounds__(NT, 384 / NT) k_inc_col2d(IncArgs A) {  // 12 
     const int r_last = (ys + kIncH >= N) ? N : ys + kIncH - 1;
     k_next = r_first - 2;
     k_end = r_last + 2;
-    for (int q = 0; q < kColRing; ++q) {
+    for (int q = 0; q < kIncRing; ++q) {
       if (k_next <= k_end) issue_row(k_next, q);
       else cp_async_commit();
       ++k_next;
