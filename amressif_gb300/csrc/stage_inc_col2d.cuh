@@ -243,6 +243,10 @@ __global__ void __launch_bounds__(NT, 384 / NT) k_inc_col2d(IncArgs A) {  // 12 
     };
     float2 fyp0 = make_float2(0.f, 0.f), fyp1 = make_float2(0.f, 0.f);  // y flux at face r
     float2 t1p = make_float2(0.f, 0.f);                                 // v total of row r-1
+    // unrolled by two: half of the register window's copies become renames
+    // (0.214 -> 0.211 ms a launch at 4096^2; by four the code outgrows the
+    // instruction cache and a launch takes 0.251 ms)
+#pragma unroll 2
     for (int r = r_first; r <= r_last; ++r) {
       cell_row(r + 2, w[4], ufb[2], ufe[2], vlb[2], vle[2], gqu[2], gqv[2]);
       // y flux at face r+1 (rows r, r+1), cells r-1 .. r+2; face row N as stored
