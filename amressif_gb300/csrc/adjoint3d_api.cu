@@ -244,7 +244,6 @@ int scalars3(ns_ctx* c) {
   Adj3& A = *c->s3->adj;
   CK(cudaMemcpyAsync(A.sc_h, A.sc, kRfN * sizeof(double), cudaMemcpyDeviceToHost, c->st), "readback");
   CK(cudaStreamSynchronize(c->st), "stream sync");
-  if (c->prof) prof_resolve(c);
   return NS_OK;
 }
 

@@ -240,7 +240,6 @@ int read_scalars(ns_ctx* c) {
   AdjState& A = *c->adj;
   CK(cudaMemcpyAsync(A.sc_h, A.sc, kBcN * sizeof(double), cudaMemcpyDeviceToHost, c->st), "readback");
   CK(cudaStreamSynchronize(c->st), "stream sync");
-  if (c->prof) prof_resolve(c);
   return NS_OK;
 }
 

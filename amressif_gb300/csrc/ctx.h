@@ -134,6 +134,11 @@ int step3d(ns_ctx* c, ns_step_stats* s);
 
 inline double* face_ptr(ns_ctx* c, int id, int m) { return id < 0 ? c->UP[m] : c->B[id][m]; }
 
+// events created when profiling is switched on (two per launch), and the
+// pending launches after which the timings are read out (a stream sync)
+constexpr int kProfPool = 16384;
+constexpr int kProfPending = 8192;
+
 // Launch one kernel (a callable returning cudaError_t), counting it and, when
 // profiling is on, bracketing it with events on the context's stream.
 template <class F>
@@ -149,7 +154,7 @@ int launch(ns_ctx* c, int kind, const char* what, F&& f) {
   if (c->prof && a && b) {
     cudaEventRecord(b, c->st);
     c->pend.push_back({kind, {a, b}});
-    if (c->pend.size() > 4096) {
+    if (c->pend.size() > (size_t)kProfPending) {
       cudaStreamSynchronize(c->st);
       prof_resolve(c);
     }

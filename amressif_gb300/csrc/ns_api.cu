@@ -50,7 +50,6 @@ int alloc_field(ns_ctx* c, double** p) {
 int sync_red(ns_ctx* c, int first, int count) {
   CK(cudaMemcpyAsync(c->red_h + first, c->red + first, count * sizeof(double), cudaMemcpyDeviceToHost, c->st), "readback");
   CK(cudaStreamSynchronize(c->st), "stream sync");
-  if (c->prof) prof_resolve(c);
   return NS_OK;
 }
 
@@ -808,7 +807,6 @@ static int gmres_dots(ns_ctx* c, const std::vector<double*>& V, int nv, const do
   LAUNCH(NS_PROF_OTHER, "gmres dots", launch_gm_mdot(c->N, c->pitch, nv, vv, w, c->gm_part, c->counter, c->gm_dev, c->st));
   CK(cudaMemcpyAsync(c->gm_host, c->gm_dev, nv * sizeof(double), cudaMemcpyDeviceToHost, c->st), "readback");
   CK(cudaStreamSynchronize(c->st), "stream sync");
-  if (c->prof) prof_resolve(c);
   return NS_OK;
 }
 
@@ -1356,11 +1354,22 @@ int ns_step_host(ns_ctx* c, double* const* u, double* const* u_prev, double* p, 
 
 extern "C" {
 
+// The per-launch event pairs are resolved only here, in ns_profile_read and
+// when nsh::kProfPending launches are pending, never at the per-iteration
+// syncs of the step (the stream would idle while the host reads them). The
+// pool is filled when profiling is switched on, outside any timed region.
 int ns_profile_enable(ns_ctx* c, int on) {
   if (!c) return NS_ERR_ARG;
   CK(cudaStreamSynchronize(c->st), "stream sync");
   prof_resolve(c);
   c->prof = on != 0;
+  if (c->prof) {
+    while (c->evpool.size() < (size_t)nsh::kProfPool) {
+      cudaEvent_t e;
+      CK(cudaEventCreate(&e), "event create");
+      c->evpool.push_back(e);
+    }
+  }
   return NS_OK;
 }
 
