@@ -10,10 +10,14 @@
 //     columns on the left and 2 on the right);
 //   * the cell-indexed face words of a row come in 8-byte pairs: 10 cp.async
 //     copies per row for two columns;
-//   * x neighbours need three shuffles per field for both columns.
-// Compared with one column per lane (26 output columns per warp) this issues
-// about a quarter fewer instructions per output face; it runs at 12 warps per
-// SM (150 registers), and at 4096^2 a launch takes 0.243 ms against 0.273.
+//   * x neighbours need three shuffles per field for both columns;
+//   * the arithmetic of the two columns runs on packed FP32 pairs (the
+//     f32x2 add / mul / fma of stage_inc2d.cuh), one instruction for both;
+//     only the upwind selects and the boundary rules stay per column.
+// Compared with one column per lane (26 output columns per warp, 0.273 ms a
+// launch at 4096^2) the pair layout took a launch to 0.243 ms and the packed
+// arithmetic to 0.214 ms (with the 3-row ring; 12 warps per SM, ~150
+// registers).
 // The incremental anchor update (BASE = true) also writes the new float-float
 // base (hi, lo) + e_s at its output faces, into the other buffer of the pair:
 // the lo words of row k - 2 travel in row k's ring slot, so they arrive with
@@ -27,8 +31,7 @@
 // seam: after wrapping (periodic) or mirroring (wall ghosts) the two columns
 // stay adjacent, and a wall ghost pair mirrors onto one lane's pair with the
 // slots swapped. Face-indexed words whose face is not the lane's cell column
-// (face N, the periodic image, wall faces) are loaded directly, per slot, as
-// in k_inc_col2d.
+// (face N, the periodic image, wall faces) are loaded directly, per slot.
 #pragma once
 #include "col2d.cuh"
 #include "ff.cuh"

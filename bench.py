@@ -37,8 +37,9 @@ ALGO_BYTES_PER_CELL = {
     "stage_exact": 88.0,   # read u*, u_base, u^n, du^n (2 x 8 B each) + p; write u*
     "stage_fast": 64.0,    # read u*, u_base, S; write u*
     "anchor": 64.0,        # read base hi/lo, e4, S hi/lo (f32); write base hi/lo, G0 (f32)
-    "increment": 30.0,     # stage 1: read u_b, G0, write e (24); stages 2-3 and the incremental anchor update
-                           # also read e (32); launch mix of 7 incremental + 1 exact anchor per 8 iterations
+    "increment": 35.7,     # stage 1: read u_b, G0, write e (24); stages 2-3 also read e (32); the incremental
+                           # anchor update also reads the base lo part and writes the new base hi/lo (56);
+                           # launch mix of 15 incremental + 1 exact anchor per 16 iterations
     "explicit": 88.0,
     "step_begin": 56.0,    # read u, u_prev, p; write du, S
     "poisson_rhs": 24.0,   # read 2 faces, write f
@@ -161,22 +162,24 @@ def vcycle_bytes(n):
     return b
 
 
-def throughput_block(n, K, total_s, stats, prof, peak):
-    """cell-updates/s, whole-step algorithmic GB/s and V-cycle GB/s, each with
-    its fraction of the measured HBM peak"""
+def throughput_block(n, K, total_s, stats, prof, peak, stats_p):
+    """cell-updates/s (all K timed steps), whole-step algorithmic GB/s and
+    V-cycle GB/s (the profiled steps stats_p, whose launches prof counts), each
+    GB/s with its fraction of the measured HBM peak"""
     steps_per_s = K / total_s
     kmean = statistics.mean(st["pseudo_iters"] for st in stats)
-    cycles = sum(st["poisson_cycles"] for st in stats)
+    cycles = sum(st["poisson_cycles"] for st in stats_p)
+    prof_s = sum(st["ms_predictor"] + st["ms_poisson"] + st["ms_project"] for st in stats_p) / 1e3
     algo = sum(ALGO_BYTES_PER_CELL[k] * n * n * c for k, (c, _) in prof.items() if k in ALGO_BYTES_PER_CELL)
     mg_kinds = ("mg_smooth0", "mg_smooth", "mg_restrict0", "mg_restrict", "mg_bottom", "mg_cycle")
     mg_ms = sum(prof[k][1] for k in mg_kinds if k in prof)
     dc_c, dc_ms = prof.get("dc_update", (0, 0.0))
     out = {"cell_updates_per_s": steps_per_s * n * n,
            "rk_stage_cell_updates_per_s": steps_per_s * n * n * kmean * 4,
-           "step_algorithmic_gbs": algo / total_s / 1e9,
-           "step_algorithmic_frac": algo / total_s / 1e9 / peak,
+           "step_algorithmic_gbs": algo / prof_s / 1e9,
+           "step_algorithmic_frac": algo / prof_s / 1e9 / peak,
            "note": "algorithmic bytes of the kinds with a per-cell figure (ALGO_BYTES_PER_CELL) over the device "
-                   "time of the timed steps; the predictor kernels are issue-bound, not HBM-bound"}
+                   "time of the profiled steps; the predictor kernels are issue-bound, not HBM-bound"}
     if cycles > 0 and mg_ms > 0:
         vb = vcycle_bytes(n)
         t = mg_ms / cycles * 1e-3
@@ -366,7 +369,13 @@ def bench_ours(args):
     s = ns.Solver(workload_params(ns, n, ns.PREC_MIXED))
     s.init(ns.INIT_CAVITY)
     run_steps(s, W)
+    # per-launch events only over the last Kp of the K timed steps: an event
+    # pair around every launch costs about 2% of a step, which the headline
+    # value (all K steps) should not carry. Switching profiling on fills the
+    # event pool, so it is done once before the timed region.
+    Kp = max(1, K // 5)
     s.profile(True)
+    s.profile(False)
     s.profile_read(reset=True)
     s.sync()
     if dist:
@@ -376,7 +385,9 @@ def bench_ours(args):
     th = threading.Thread(target=clocks_sampler, args=(stop, samples), daemon=True)
     th.start()
     t0 = time.perf_counter()
-    stats = run_steps(s, K)
+    stats = run_steps(s, K - Kp)
+    s.profile(True)
+    stats += run_steps(s, Kp)
     s.sync()
     wall = time.perf_counter() - t0
     stop.set()
@@ -464,10 +475,14 @@ def bench_ours(args):
         roofline = {"kernel": kind, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                     "frac": achieved / peak, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
                     "traffic": (tr * n * n if tr else None), "algorithmic_bytes": algo,
-                    "ms_per_launch": per_launch_ms, "launches": cnt}
+                    "ms_per_launch": per_launch_ms, "launches": cnt,
+                    "timing": "CUDA events around each launch on the library's stream, over the last %d of "
+                              "the %d timed steps" % (Kp, K)}
+    stats_p = stats[K - Kp:]
+    dev_ms_p = sum(st["ms_predictor"] + st["ms_poisson"] + st["ms_project"] for st in stats_p)
     kernels = {k: {"launches": c, "ms_total": m, "ms_per_launch": (m / c if c else None),
-                   "share": m / max(dev_ms, 1e-9)} for k, (c, m) in prof.items() if c}
-    throughput = throughput_block(n, K, total_s, stats, prof, peak)
+                   "share": m / max(dev_ms_p, 1e-9)} for k, (c, m) in prof.items() if c}
+    throughput = throughput_block(n, K, total_s, stats, prof, peak, stats_p)
 
     # ---- CPU restatement timed on the host (rank 0, N=1) ----
     cpu = None
@@ -514,6 +529,7 @@ def bench_ours(args):
             "roofline": roofline,
             "throughput": throughput,
             "kernels": kernels,
+            "profiled_steps": Kp,
             "cpu_baseline": cpu,
             "clocks": summarize_clocks(samples),
         }
