@@ -53,6 +53,16 @@ __device__ __forceinline__ float2 p_fma(float2 a, float2 b, float2 c) { return _
 __device__ __forceinline__ float2 p_sub(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
 __device__ __forceinline__ float2 p_splat(float x) { return make_float2(x, x); }
 
+// float-float pair + FP32 pair, each lane as ff_add_f (two_sum of the hi
+// parts, then fast2sum with the lo parts)
+__device__ __forceinline__ void ff_add_f2(float2 h, float2 l, float2 y, float2& oh, float2& ol) {
+  const float2 s = p_add(h, y);
+  const float2 bb = p_sub(s, h);
+  const float2 t = p_add(p_add(p_sub(h, p_sub(s, bb)), p_sub(y, bb)), l);
+  oh = p_add(s, t);
+  ol = p_sub(t, p_sub(oh, s));
+}
+
 // Upwind split of the new advecting velocity un = ub + e and its change
 // against ub (fn_flux_calc.cpp:66-68): udn = max(un, 0) and upn = min(un, 0)
 // (formed as un - udn, exact); dud = udn - max(ub, 0) without a subtraction

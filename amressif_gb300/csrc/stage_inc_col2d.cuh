@@ -246,10 +246,11 @@ __global__ void __launch_bounds__(NT, 384 / NT) k_inc_col2d(IncArgs A) {  // 12 
     };
     float2 fyp0 = make_float2(0.f, 0.f), fyp1 = make_float2(0.f, 0.f);  // y flux at face r
     float2 t1p = make_float2(0.f, 0.f);                                 // v total of row r-1
-    // unrolled by two: half of the register window's copies become renames
-    // (0.214 -> 0.211 ms a launch at 4096^2; by four the code outgrows the
-    // instruction cache and a launch takes 0.251 ms)
-#pragma unroll 2
+    // the stages unrolled by two: half of the register window's copies
+    // become renames (0.214 -> 0.211 ms a launch at 4096^2; by four the code
+    // outgrows the instruction cache and a launch takes 0.251 ms); the longer
+    // base-update loop is not unrolled
+#pragma unroll (BASE ? 1 : 2)
     for (int r = r_first; r <= r_last; ++r) {
       cell_row(r + 2, w[4], ufb[2], ufe[2], vlb[2], vle[2], gqu[2], gqv[2]);
       // y flux at face r+1 (rows r, r+1), cells r-1 .. r+2; face row N as stored
@@ -311,6 +312,16 @@ __global__ void __launch_bounds__(NT, 384 / NT) k_inc_col2d(IncArgs A) {  // 12 
             }
           }
           const float2 ev2 = p_mul(rk2, p_add(gcur, p_fma(ecur, mc15, avgv)));
+          // new float-float base u_b + e_s of both columns (BASE); u face words
+          // off the pair loads come directly
+          float2 nuh, nul, nvh, nvl;
+          if constexpr (BASE) {
+            float2 lo = blu;
+            if (irr0 && out_u[0] && r < N) lo.x = A.bl[0][(long)r * P + a];
+            if (irr1 && out_u[1] && r < N) lo.y = A.bl[0][(long)r * P + a + 1];
+            ff_add_f2(ufb[0], lo, ufe[0], nuh, nul);
+            ff_add_f2(bh, bo, ecur, nvh, nvl);
+          }
 #pragma unroll
           for (int s = 0; s < 2; ++s) {
             const int i = a + s;
@@ -319,11 +330,9 @@ __global__ void __launch_bounds__(NT, 384 / NT) k_inc_col2d(IncArgs A) {  // 12 
               const float e = s ? eu2.y : eu2.x;
               A.eout[0][id] = e;
               n0 = fmaf(wgt_u[s] * e, e, n0);
-              if constexpr (BASE) {  // u_b + e_s at u face (i, r); face words off the pair loads directly
-                const float lo = (s == 0 ? irr0 : irr1) ? A.bl[0][id] : (s ? blu.y : blu.x);
-                const ff nb = ff_add_f(ff_make(s ? ufb[0].y : ufb[0].x, lo), s ? ufe[0].y : ufe[0].x);
-                A.obh[0][id] = nb.hi;
-                A.obl[0][id] = nb.lo;
+              if constexpr (BASE) {  // u_b + e_s at u face (i, r)
+                A.obh[0][id] = s ? nuh.y : nuh.x;
+                A.obl[0][id] = s ? nul.y : nul.x;
               }
             }
             if (out_v[s]) {  // v face (i, r), r <= N
@@ -331,9 +340,8 @@ __global__ void __launch_bounds__(NT, 384 / NT) k_inc_col2d(IncArgs A) {  // 12 
               A.eout[1][id] = e;
               n1 = fmaf(edge_v ? 0.5f * e : e, e, n1);
               if constexpr (BASE) {  // u_b + e_s at v face (i, r)
-                const ff nb = ff_add_f(ff_make(s ? bh.y : bh.x, s ? bo.y : bo.x), s ? ecur.y : ecur.x);
-                A.obh[1][id] = nb.hi;
-                A.obl[1][id] = nb.lo;
+                A.obh[1][id] = s ? nvh.y : nvh.x;
+                A.obl[1][id] = s ? nvl.y : nvl.x;
               }
             }
           }
