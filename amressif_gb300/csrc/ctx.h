@@ -61,7 +61,9 @@ struct ns_ctx {
   bool ev_ok = false;
   // mixed iteration: E[0] holds an increment not yet added to the base
   bool mix_pending = false;
-  int mix_it = 0;  // mixed pseudo-iterations of this step (every kAnchorEvery-th anchor is exact)
+  int mix_it = 0;          // mixed pseudo-iterations of this step
+  int mix_last_exact = 0;  // the iteration of the last exact anchor
+  double mix_norm = 0.0, mix_norm_exact = 0.0;  // pseudo-norm of the last iteration / of the last exact one
   // float-float pseudo-iterate (hi, lo) ping-pong and the split source S
   float* BH[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
   float* BL[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};

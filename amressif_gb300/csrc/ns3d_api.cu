@@ -297,7 +297,7 @@ int create3d(ns_ctx* c) {
     r = levels3<float>(c, S.M32, true);
     const size_t f32 = S.fb / 2, g32 = (size_t)(N + 4) * (N + 4) * (N + 4) * sizeof(float);
     for (int m = 0; m < 3 && r == NS_OK; ++m) {
-      float** fs[] = {&S.UB32[m], &S.G0[m], &S.E[0][m], &S.E[1][m]};
+      float** fs[] = {&S.UB32[m], &S.G0[m], &S.G0b[m], &S.E[0][m], &S.E[1][m]};
       for (float** p : fs)
         if (r == NS_OK) r = alloc3(c, p, f32);
       if (r == NS_OK) r = alloc3(c, &S.PHB32[m], g32);
@@ -359,11 +359,69 @@ void split2(double x, float* out) {
   out[1] = (float)(x - (double)out[0]);
 }
 
+// the anchor is evaluated exactly (float-float) on the first iteration, at
+// most kAnchorEvery3 iterations after the last exact one, and once the
+// pseudo-norm has fallen below kAnchorDrop3 times its value after the last
+// exact one; the others update it by an FP32 increment evaluation, as in the
+// 2D predictor. (A drop of 1e-2 left 1.1e-11 relative error in the small w of
+// a 16^3 cavity after four steps; 1e-1 leaves 1.8e-12.)
+constexpr int kAnchorEvery3 = 16;
+constexpr double kAnchorDrop3 = 1e-1;
+
 // One pseudo-iteration of the mixed-precision predictor (ns3d_mixed.cuh):
-// the float-float anchor G0 = G(u_b), three FP32 increment stages, u_b + e4
-// (FP64) into a free buffer, the pseudo-norm of e4 into red[kRedNorm]
+// the anchor G0 = G(u_b), three FP32 increment stages, u_b + e4 (float-float)
+// into the other base buffer, the pseudo-norm of e4 into red[kRedNorm].
+// The anchor is exact (the float-float passes) on the first and every
+// kAnchorEvery3-th iteration. In between it is updated:
+//   G(u_b + e4) = G(u_b) + dG(u_b; e4),
+// with dG from the FP32 increment passes at the old base (rk = 1, e4 kept by
+// the previous iteration's last stage). The FP32 copies of the moved base are
+// then rebuilt from its float-float pairs. Each update rounds the stored G0
+// to FP32, an error relative to |G0| at that iteration; the errors add up
+// until the next exact anchor and shift the converged u* by their sum over
+// 1.5/dt. Refreshing the anchor whenever the pseudo-norm has dropped by
+// kAnchorDrop3 keeps that sum within a small multiple of the final norm,
+// however few iterations the step takes.
 int mixed_iteration3(ns_ctx* c) {
   State3D& S = *c->s3;
+  const bool exact = S.bf < 0 || S.mix_it - S.mix_last_exact >= kAnchorEvery3 ||
+                     !(S.mix_norm >= kAnchorDrop3 * S.mix_norm_exact);
+  if (exact) S.mix_last_exact = S.mix_it;
+  S.mix_exact = exact;
+  ++S.mix_it;
+  if (!exact) {
+    Inc3 u;
+    std::memset(&u, 0, sizeof(u));
+    u.g = c->g;
+    for (int m = 0; m < 3; ++m) {
+      u.ub[m] = S.UB32[m];
+      u.g0[m] = S.G0[m];
+      u.phb[m] = S.PHB32[m];
+      u.phe[m] = reinterpret_cast<float*>(S.PH[m]);
+      u.dt[m] = reinterpret_cast<float*>(S.T[m]);
+      for (int d = 0; d < 3; ++d) u.dfl[d][m] = reinterpret_cast<float*>(S.FL[d][m]);
+      u.ein[m] = S.E[1][m];
+      u.eout[m] = S.G0b[m];
+      u.inv_dx[m] = (float)c->g.inv_dx[m];
+      u.vcoef[m] = (float)(c->g.inv_dx2[m] * c->g.inv_ren);
+    }
+    u.c15 = (float)c->g.c15;
+    u.rk_prev = 1.f;
+    u.rk = 1.f;
+    LAUNCH(NS_PROF_INC, "anchor update cart 3d", launch3i_cart(u, c->st));
+    LAUNCH(NS_PROF_INC, "anchor update total 3d", launch3i_total(u, c->st));
+    LAUNCH(NS_PROF_INC, "anchor update face 3d", launch3i_face(u, c->st));
+    for (int m = 0; m < 3; ++m) std::swap(S.G0[m], S.G0b[m]);
+    AncFF b;
+    std::memset(&b, 0, sizeof(b));
+    b.g = c->g;
+    for (int m = 0; m < 3; ++m) {
+      b.uff[m] = S.BF[S.bf][m];
+      b.ph32[m] = S.PHB32[m];
+      b.ub[m] = S.UB32[m];
+    }
+    LAUNCH(NS_PROF_OTHER, "fp32 base 3d", launch3f_base32(b, c->st));
+  }
   AncFF f;
   std::memset(&f, 0, sizeof(f));
   f.g = c->g;
@@ -382,9 +440,11 @@ int mixed_iteration3(ns_ctx* c) {
     split2(c->g.inv_dx2[m] * c->g.inv_ren, f.vcoef[m]);
   }
   split2(c->g.c15, f.c15);
-  LAUNCH(NS_PROF_ANCHOR, "anchor cart 3d", launch3f_cart(f, c->st));
-  LAUNCH(NS_PROF_ANCHOR, "anchor total 3d", launch3f_total(f, c->st));
-  LAUNCH(NS_PROF_ANCHOR, "anchor face 3d", launch3f_face(f, c->st));
+  if (exact) {
+    LAUNCH(NS_PROF_ANCHOR, "anchor cart 3d", launch3f_cart(f, c->st));
+    LAUNCH(NS_PROF_ANCHOR, "anchor total 3d", launch3f_total(f, c->st));
+    LAUNCH(NS_PROF_ANCHOR, "anchor face 3d", launch3f_face(f, c->st));
+  }
   Inc3 q;
   std::memset(&q, 0, sizeof(q));
   q.g = c->g;
@@ -413,6 +473,7 @@ int mixed_iteration3(ns_ctx* c) {
     q.rk_prev = (float)c->rk[s - 1];
     q.rk = (float)c->rk[s];
     q.last = s == 3;
+    q.keep_e = s == 3;
     LAUNCH(NS_PROF_INC, "increment cart 3d", launch3i_cart(q, c->st));
     LAUNCH(NS_PROF_INC, "increment total 3d", launch3i_total(q, c->st));
     LAUNCH(NS_PROF_INC, "increment face 3d", launch3i_face(q, c->st));
@@ -459,6 +520,8 @@ int predictor3d(ns_ctx* c, ns_step_stats* sp) {
   // ---- dual-time pseudo-iterations (main.cpp:898-1040)
   const bool mixed = c->P.precision == NS_PREC_MIXED;
   S.bf = -1;
+  S.mix_it = 0;
+  S.mix_last_exact = 0;
   int count = 0;
   double norm = 1.e9;
   while (norm > c->P.momentum_tolerance) {
@@ -485,6 +548,10 @@ int predictor3d(ns_ctx* c, ns_step_stats* sp) {
     int r = sync_red(c, kRedNorm, 1);
     if (r != NS_OK) return r;
     norm = c->red_h[kRedNorm];
+    if (mixed) {
+      S.mix_norm = norm;
+      if (S.mix_exact) S.mix_norm_exact = norm;
+    }
     S.base = S.cur;
     count++;
     if (count > c->P.iter_num) { s.status = NS_WARN_PSEUDO_MAXITER; break; }

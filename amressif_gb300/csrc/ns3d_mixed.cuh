@@ -41,6 +41,7 @@ struct Inc3 {
   float rk_prev, rk, c15;
   float inv_dx[3], vcoef[3];  // 1/dx, 1/(Re dx^2)
   int last;
+  int keep_e;              // last stage: also store e4 in eout (the next incremental anchor reads it)
   double* part;
   unsigned* counter;
   double* norm_out;
@@ -130,8 +131,23 @@ __global__ void __launch_bounds__(256) k3f_cart(AncFF A) {
         else if (r == kNeg) v = -v;
       }
     }
-    st2(A.ph[m], gi, v);
+    if (A.ph[m] != nullptr) st2(A.ph[m], gi, v);
     A.ph32[m][gi] = ff_round(v);
+  }
+}
+
+// u_b rounded to FP32 at the faces (k3f_face's rounding of u_b), for the
+// incremental anchors: with k3f_cart (ph unset) it refreshes the FP32 base
+// that the increment stages read after the float-float base has moved
+__global__ void __launch_bounds__(256) k3f_ub(AncFF A) {
+  const Geom& g = A.g;
+  const int N = g.N;
+  NS3_IJK(0, 0, 0)
+  for (int m = 0; m < 3; ++m) {
+    const int lim[3] = {N + (m == 0), N + (m == 1), N + (m == 2)};
+    if (i >= lim[0] || j >= lim[1] || k >= lim[2]) continue;
+    const long id = id3(g, i, j, k);
+    A.ub[m][id] = ff_round(ld_base(A, m, id));
   }
 }
 
@@ -366,6 +382,7 @@ __global__ void __launch_bounds__(256) k3i_face(Inc3 A) {
       if (A.last) {
         const ff b = A.baseff[m] ? ld2(A.baseff[m], id) : ld_ff(A.base64[m], id);
         st2(A.outff[m], id, ff_add_f(b, eo));
+        if (A.keep_e) A.eout[m][id] = eo;
         const float w = (a == 0 || a == N) ? 0.5f : 1.f;
         nrm[m] += eo * eo * w;
       } else {

@@ -1103,9 +1103,17 @@ static void split_const(double x, float* out) {
 // increment of the previous iteration), then three FP32 increment stages; the
 // fourth stage's increment e4 stays in E[0] and its norm is the
 // pseudo-increment norm of Error_Computation.
-// every kAnchorEvery-th pseudo-iteration evaluates the anchor exactly (float-float);
-// the others update it by an FP32 increment evaluation
+// the anchor is evaluated exactly (float-float) on the first iteration, at
+// most kAnchorEvery iterations after the last exact one, and once the
+// pseudo-norm has fallen below kAnchorDrop times its value after the last
+// exact one; the others update it by an FP32 increment evaluation. Each
+// update rounds the stored G0 to FP32, an error relative to |G0| at that
+// iteration; the errors add up until the next exact anchor and shift the
+// converged u* by their sum over 1.5/dt, so the refresh on a falling norm
+// keeps that sum within a small multiple of the final norm however few
+// iterations the step takes.
 constexpr int kAnchorEvery = 16;
+constexpr double kAnchorDrop = 1e-2;
 
 static int mixed_iteration(ns_ctx* c, double* norm) {
   if (!c->s_ff_valid) {
@@ -1120,7 +1128,9 @@ static int mixed_iteration(ns_ctx* c, double* norm) {
     c->base_ff_valid = true;
     c->mix_pending = false;
   }
-  const bool exact = !c->mix_pending || (c->mix_it % kAnchorEvery) == 0;
+  const bool exact = !c->mix_pending || c->mix_it - c->mix_last_exact >= kAnchorEvery ||
+                     !(c->mix_norm >= kAnchorDrop * c->mix_norm_exact);
+  if (exact) c->mix_last_exact = c->mix_it;
   ++c->mix_it;
   if (exact) {
     AnchorFFArgs a;
@@ -1203,6 +1213,8 @@ static int mixed_iteration(ns_ctx* c, double* norm) {
   int r = sync_red(c, kRedNorm, 1);
   if (r != NS_OK) return r;
   *norm = c->red_h[kRedNorm];
+  c->mix_norm = *norm;
+  if (exact) c->mix_norm_exact = *norm;
   return NS_OK;
 }
 
@@ -1247,6 +1259,7 @@ int nsh::run_predictor(ns_ctx* c, ns_step_stats* sp) {
   }
   c->mix_pending = false;
   c->mix_it = 0;
+  c->mix_last_exact = 0;
   int r = ns_step_begin(c);
   if (r != NS_OK) return r;
   int countIter = 0;

@@ -29,6 +29,11 @@ struct State3D {
   // cell velocity; the flux / total / cell-velocity increments reuse FL, T, PH
   float* UB32[3] = {nullptr, nullptr, nullptr};
   float* G0[3] = {nullptr, nullptr, nullptr};
+  float* G0b[3] = {nullptr, nullptr, nullptr};  // G0 of an incremental anchor update
+  int mix_it = 0;          // mixed pseudo-iterations of this step
+  int mix_last_exact = 0;  // the iteration of the last exact anchor
+  bool mix_exact = false;  // the current iteration's anchor is exact
+  double mix_norm = 0.0, mix_norm_exact = 0.0;  // pseudo-norm of the last iteration / of the last exact one
   float* E[2][3] = {};
   float* PHB32[3] = {nullptr, nullptr, nullptr};
   float2* BF[2][3] = {};  // u_b as float-float pairs between pseudo-iterations
