@@ -54,40 +54,39 @@ __device__ __forceinline__ ff cart_ghost_ff(const CartBC& b, int m, ff q) {
   return r == kNeg ? -q : q;
 }
 
-// FP64 field -> float-float (hi, lo) arrays, integer split (no FP64 pipe)
+// FP64 field -> float-float (hi, lo) arrays, integer split (no FP64 pipe), on
+// every face. Thread a of block row b takes the
+// u face (a, b) (a <= N, b < N) and the v face (a, b) (a < N, b <= N); grid
+// ((N + 1 + 255) / 256, N + 1).
 static __global__ void __launch_bounds__(256) k_split_ff2d(Geom g, const double* x0, const double* x1, float* h0, float* l0,
                                                            float* h1, float* l1) {
   const int N = g.N;
-  const long P = g.pitch;
-  const long nu = (long)(N + 1) * N;
-  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < 2 * nu; t += (long)gridDim.x * blockDim.x) {
-    const int m = (t < nu) ? 0 : 1;
-    const long q = (m == 0) ? t : t - nu;
-    const int a = (m == 0) ? (int)(q % (N + 1)) : (int)(q % N);
-    const int b = (m == 0) ? (int)(q / (N + 1)) : (int)(q / N);
-    const long id = (long)b * P + a;
-    const ff v = ff_from_double(m == 0 ? x0[id] : x1[id]);
-    if (m == 0) { h0[id] = v.hi; l0[id] = v.lo; }
-    else { h1[id] = v.hi; l1[id] = v.lo; }
+  const int a = blockIdx.x * 256 + threadIdx.x, b = blockIdx.y;
+  if (a > N) return;
+  const long id = (long)b * g.pitch + a;
+  if (b < N) {
+    const ff v = ff_from_double(x0[id]);
+    h0[id] = v.hi;
+    l0[id] = v.lo;
+  }
+  if (a < N) {
+    const ff v = ff_from_double(x1[id]);
+    h1[id] = v.hi;
+    l1[id] = v.lo;
   }
 }
 
-// u* = (hi + lo) + e (FP64) once the mixed iteration stops
+// u* = (hi + lo) + e (FP64) once the mixed iteration stops; the face layout
+// and grid of k_split_ff2d
 static __global__ void __launch_bounds__(256) k_ff_add_inc2d(Geom g, const float* h0, const float* l0, const float* h1,
                                                              const float* l1, const float* e0, const float* e1, double* o0,
                                                              double* o1) {
   const int N = g.N;
-  const long P = g.pitch;
-  const long nu = (long)(N + 1) * N;
-  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < 2 * nu; t += (long)gridDim.x * blockDim.x) {
-    const int m = (t < nu) ? 0 : 1;
-    const long q = (m == 0) ? t : t - nu;
-    const int a = (m == 0) ? (int)(q % (N + 1)) : (int)(q % N);
-    const int b = (m == 0) ? (int)(q / (N + 1)) : (int)(q / N);
-    const long id = (long)b * P + a;
-    if (m == 0) o0[id] = ((double)h0[id] + (double)l0[id]) + (e0 ? (double)e0[id] : 0.0);
-    else o1[id] = ((double)h1[id] + (double)l1[id]) + (e1 ? (double)e1[id] : 0.0);
-  }
+  const int a = blockIdx.x * 256 + threadIdx.x, b = blockIdx.y;
+  if (a > N) return;
+  const long id = (long)b * g.pitch + a;
+  if (b < N) o0[id] = ((double)h0[id] + (double)l0[id]) + (e0 ? (double)e0[id] : 0.0);
+  if (a < N) o1[id] = ((double)h1[id] + (double)l1[id]) + (e1 ? (double)e1[id] : 0.0);
 }
 
 }  // namespace ns

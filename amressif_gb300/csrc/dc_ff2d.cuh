@@ -77,23 +77,24 @@ static __global__ void __launch_bounds__(256) k_dc_update_ff2d(DCffArgs A) {
 }
 
 // (f - mean) -> float-float, integer split of both (no FP64 instruction)
+// grid ((n + 255) / 256, n): thread a of block row b takes cell (a, b)
 static __global__ void __launch_bounds__(256) k_rhs_ff2d(int n, long P, const double* f, const double* mean, float* fh,
                                                          float* fl) {
+  const int a = blockIdx.x * 256 + threadIdx.x, b = blockIdx.y;
+  if (a >= n) return;
   const ff m = ff_from_double(*mean);
-  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < (long)n * n; t += (long)gridDim.x * blockDim.x) {
-    const long id = (t / n) * P + (t % n);
-    const ff r = ff_from_double(f[id]) - m;
-    fh[id] = r.hi;
-    fl[id] = r.lo;
-  }
+  const long id = (long)b * P + a;
+  const ff r = ff_from_double(f[id]) - m;
+  fh[id] = r.hi;
+  fl[id] = r.lo;
 }
 
 // phi (FP64) = hi + lo
 static __global__ void __launch_bounds__(256) k_ff_to_double2d(int n, long P, const float* h, const float* l, double* out) {
-  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < (long)n * n; t += (long)gridDim.x * blockDim.x) {
-    const long id = (t / n) * P + (t % n);
-    out[id] = (double)h[id] + (double)l[id];
-  }
+  const int a = blockIdx.x * 256 + threadIdx.x, b = blockIdx.y;
+  if (a >= n) return;
+  const long id = (long)b * P + a;
+  out[id] = (double)h[id] + (double)l[id];
 }
 
 }  // namespace ns

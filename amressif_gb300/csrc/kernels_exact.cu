@@ -19,19 +19,18 @@ cudaError_t launch_stage_exact(int mode, const StageArgs& a, cudaStream_t s) {
 }
 
 cudaError_t launch_step_begin_exact(const ProjArgs& a, cudaStream_t s) {
-  k_step_begin2d<ArithExact, false><<<1024, 256, 0, s>>>(a);
+  k_step_begin2d<ArithExact, false><<<proj_face_grid(a.g), 256, 0, s>>>(a);
   return cudaGetLastError();
 }
 
-static inline dim3 cell_grid(const Geom& g) { return dim3((g.N + 31) / 32, (g.N + 7) / 8, 1); }
 
 cudaError_t launch_poisson_rhs_exact(const ProjArgs& a, cudaStream_t s) {
-  k_poisson_rhs2d<ArithExact><<<cell_grid(a.g), 256, 0, s>>>(a);
+  k_poisson_rhs2d<ArithExact><<<proj_grid(a.g.N), 256, 0, s>>>(a);
   return cudaGetLastError();
 }
 
 cudaError_t launch_project_exact(const ProjArgs& a, cudaStream_t s) {
-  k_project2d<ArithExact><<<cell_grid(a.g), 256, 0, s>>>(a);
+  k_project2d<ArithExact><<<proj_grid(a.g.N), 256, 0, s>>>(a);
   return cudaGetLastError();
 }
 

@@ -8,7 +8,6 @@ namespace ns {
 static inline dim3 stage_grid(const Geom& g) {
   return dim3((g.N + kStageTX - 1) / kStageTX, (g.N + kStageTY - 1) / kStageTY, 1);
 }
-static inline dim3 cell_grid(const Geom& g) { return dim3((g.N + 31) / 32, (g.N + 7) / 8, 1); }
 
 cudaError_t launch_stage_fast(int mode, const StageArgs& a, cudaStream_t s) {
   if (mode == kFastRK)
@@ -21,17 +20,17 @@ cudaError_t launch_stage_fast(int mode, const StageArgs& a, cudaStream_t s) {
 }
 
 cudaError_t launch_step_begin_fast(const ProjArgs& a, cudaStream_t s) {
-  k_step_begin2d<ArithFast, true><<<1024, 256, 0, s>>>(a);
+  k_step_begin2d<ArithFast, true><<<proj_face_grid(a.g), 256, 0, s>>>(a);
   return cudaGetLastError();
 }
 
 cudaError_t launch_poisson_rhs_fast(const ProjArgs& a, cudaStream_t s) {
-  k_poisson_rhs2d<ArithFast><<<cell_grid(a.g), 256, 0, s>>>(a);
+  k_poisson_rhs2d<ArithFast><<<proj_grid(a.g.N), 256, 0, s>>>(a);
   return cudaGetLastError();
 }
 
 cudaError_t launch_project_fast(const ProjArgs& a, cudaStream_t s) {
-  k_project2d<ArithFast><<<cell_grid(a.g), 256, 0, s>>>(a);
+  k_project2d<ArithFast><<<proj_grid(a.g.N), 256, 0, s>>>(a);
   return cudaGetLastError();
 }
 

@@ -59,7 +59,7 @@ cudaError_t launch_anchor_ff(const AnchorFFArgs& a, cudaStream_t s) {
 }
 
 cudaError_t launch_split_ff(const Geom& g, const double* const* x, float* const* h, float* const* l, cudaStream_t s) {
-  k_split_ff2d<<<1024, 256, 0, s>>>(g, x[0], x[1], h[0], l[0], h[1], l[1]);
+  k_split_ff2d<<<dim3((g.N + 1 + 255) / 256, g.N + 1), 256, 0, s>>>(g, x[0], x[1], h[0], l[0], h[1], l[1]);
   return cudaGetLastError();
 }
 
@@ -70,18 +70,18 @@ cudaError_t launch_dc_update_ff(const DCffArgs& a, cudaStream_t s) {
 }
 
 cudaError_t launch_rhs_ff(int n, long pitch, const double* f, const double* mean, float* fh, float* fl, cudaStream_t s) {
-  k_rhs_ff2d<<<1024, 256, 0, s>>>(n, pitch, f, mean, fh, fl);
+  k_rhs_ff2d<<<dim3((n + 255) / 256, n), 256, 0, s>>>(n, pitch, f, mean, fh, fl);
   return cudaGetLastError();
 }
 
 cudaError_t launch_ff_to_double(int n, long pitch, const float* h, const float* l, double* out, cudaStream_t s) {
-  k_ff_to_double2d<<<1024, 256, 0, s>>>(n, pitch, h, l, out);
+  k_ff_to_double2d<<<dim3((n + 255) / 256, n), 256, 0, s>>>(n, pitch, h, l, out);
   return cudaGetLastError();
 }
 
 cudaError_t launch_ff_add_inc(const Geom& g, const float* const* h, const float* const* l, const float* const* e,
                               double* const* out, cudaStream_t s) {
-  k_ff_add_inc2d<<<1024, 256, 0, s>>>(g, h[0], l[0], h[1], l[1], e[0], e[1], out[0], out[1]);
+  k_ff_add_inc2d<<<dim3((g.N + 1 + 255) / 256, g.N + 1), 256, 0, s>>>(g, h[0], l[0], h[1], l[1], e[0], e[1], out[0], out[1]);
   return cudaGetLastError();
 }
 

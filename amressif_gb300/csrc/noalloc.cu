@@ -85,8 +85,7 @@ extern "C" int ns_poisson_rhs_noalloc(const double* u, const double* v, double* 
   a.part = part;
   a.counter = counter;
   a.red_out = result;
-  dim3 grid((n_cell + 31) / 32, (n_cell + 7) / 8, 1);
-  k_poisson_rhs2d<ArithExact><<<grid, 256, 0, st>>>(a);
+  k_poisson_rhs2d<ArithExact><<<proj_grid(n_cell), 256, 0, st>>>(a);
   if (cudaGetLastError() != cudaSuccess) return NS_ERR_CUDA;
   if (cudaMemcpyAsync(divmax_sum, result, 2 * sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess) return NS_ERR_CUDA;
   if (cudaStreamSynchronize(st) != cudaSuccess) return NS_ERR_CUDA;
