@@ -1112,7 +1112,9 @@ static void split_const(double x, float* out) {
 // converged u* by their sum over 1.5/dt, so the refresh on a falling norm
 // keeps that sum within a small multiple of the final norm however few
 // iterations the step takes.
-constexpr int kAnchorEvery = 16;
+// (4096^2 cavity: a cap of 16 gives 5 exact anchors a step, 32 gives 3 and
+// 0.8% more steps/s.)
+constexpr int kAnchorEvery = 32;
 constexpr double kAnchorDrop = 1e-2;
 
 static int mixed_iteration(ns_ctx* c, double* norm) {
