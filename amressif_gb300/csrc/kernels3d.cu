@@ -51,7 +51,6 @@ cudaError_t launch3f_cart(const AncFF& a, cudaStream_t s) {
 cudaError_t launch3f_base32(const AncFF& a, cudaStream_t s) {
   const int N = a.g.N;
   k3f_cart<<<grid3(N + 4, N + 4, N + 4), 256, 0, s>>>(a);
-  k3f_ub<<<grid3(N + 1, N + 1, N + 1), 256, 0, s>>>(a);
   return cudaGetLastError();
 }
 cudaError_t launch3f_total(const AncFF& a, cudaStream_t s) {

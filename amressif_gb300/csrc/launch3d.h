@@ -19,7 +19,7 @@ cudaError_t launch3_div(const Arg3& a, cudaStream_t s);
 long blocks3_face(int N);  // blocks of the largest reducing launch
 // mixed-precision predictor (ns3d_mixed.cuh)
 cudaError_t launch3f_cart(const AncFF& a, cudaStream_t s);
-cudaError_t launch3f_base32(const AncFF& a, cudaStream_t s);  // FP32 copies of a moved float-float base
+cudaError_t launch3f_base32(const AncFF& a, cudaStream_t s);  // FP32 cell velocity of a moved float-float base
 cudaError_t launch3f_total(const AncFF& a, cudaStream_t s);  // fluxes, then cell totals
 cudaError_t launch3f_face(const AncFF& a, cudaStream_t s);
 cudaError_t launch3f_store(const Geom& g, const float2* const* in, double* const* out, cudaStream_t s);

@@ -297,7 +297,7 @@ int create3d(ns_ctx* c) {
     r = levels3<float>(c, S.M32, true);
     const size_t f32 = S.fb / 2, g32 = (size_t)(N + 4) * (N + 4) * (N + 4) * sizeof(float);
     for (int m = 0; m < 3 && r == NS_OK; ++m) {
-      float** fs[] = {&S.UB32[m], &S.G0[m], &S.G0b[m], &S.E[0][m], &S.E[1][m]};
+      float** fs[] = {&S.UB32[m], &S.UB32b[m], &S.G0[m], &S.G0b[m], &S.E[0][m], &S.E[1][m]};
       for (float** p : fs)
         if (r == NS_OK) r = alloc3(c, p, f32);
       if (r == NS_OK) r = alloc3(c, &S.PHB32[m], g32);
@@ -375,8 +375,9 @@ constexpr double kAnchorDrop3 = 1e-1;
 // kAnchorEvery3-th iteration. In between it is updated:
 //   G(u_b + e4) = G(u_b) + dG(u_b; e4),
 // with dG from the FP32 increment passes at the old base (rk = 1, e4 kept by
-// the previous iteration's last stage). The FP32 copies of the moved base are
-// then rebuilt from its float-float pairs. Each update rounds the stored G0
+// the previous iteration's last stage, which also wrote the moved base rounded
+// to FP32 into the other buffer of the UB32 pair). The FP32 cell velocity of
+// the moved base is then rebuilt from its float-float pairs. Each update rounds the stored G0
 // to FP32, an error relative to |G0| at that iteration; the errors add up
 // until the next exact anchor and shift the converged u* by their sum over
 // 1.5/dt. Refreshing the anchor whenever the pseudo-norm has dropped by
@@ -394,7 +395,7 @@ int mixed_iteration3(ns_ctx* c) {
     std::memset(&u, 0, sizeof(u));
     u.g = c->g;
     for (int m = 0; m < 3; ++m) {
-      u.ub[m] = S.UB32[m];
+      u.ub[m] = S.UB32b[m];  // the old base (the pair was swapped after the last stage)
       u.g0[m] = S.G0[m];
       u.phb[m] = S.PHB32[m];
       u.phe[m] = reinterpret_cast<float*>(S.PH[m]);
@@ -418,7 +419,6 @@ int mixed_iteration3(ns_ctx* c) {
     for (int m = 0; m < 3; ++m) {
       b.uff[m] = S.BF[S.bf][m];
       b.ph32[m] = S.PHB32[m];
-      b.ub[m] = S.UB32[m];
     }
     LAUNCH(NS_PROF_OTHER, "fp32 base 3d", launch3f_base32(b, c->st));
   }
@@ -474,11 +474,13 @@ int mixed_iteration3(ns_ctx* c) {
     q.rk = (float)c->rk[s];
     q.last = s == 3;
     q.keep_e = s == 3;
+    for (int m = 0; m < 3; ++m) q.ubout[m] = s == 3 ? S.UB32b[m] : nullptr;
     LAUNCH(NS_PROF_INC, "increment cart 3d", launch3i_cart(q, c->st));
     LAUNCH(NS_PROF_INC, "increment total 3d", launch3i_total(q, c->st));
     LAUNCH(NS_PROF_INC, "increment face 3d", launch3i_face(q, c->st));
   }
   S.bf = nb;
+  for (int m = 0; m < 3; ++m) std::swap(S.UB32[m], S.UB32b[m]);  // UB32: the moved base, UB32b: the old one
   return NS_OK;
 }
 

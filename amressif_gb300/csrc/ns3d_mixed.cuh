@@ -38,6 +38,7 @@ struct Inc3 {
   const double* base64[3]; // u_b in FP64 (last stage of the first iteration) ...
   const float2* baseff[3]; // ... or as float-float pairs (later iterations)
   float2* outff[3];        // u_b + e4 (last stage)
+  float* ubout[3];         // u_b + e4 rounded to FP32 (last stage; nullptr: not written)
   float rk_prev, rk, c15;
   float inv_dx[3], vcoef[3];  // 1/dx, 1/(Re dx^2)
   int last;
@@ -136,20 +137,7 @@ __global__ void __launch_bounds__(256) k3f_cart(AncFF A) {
   }
 }
 
-// u_b rounded to FP32 at the faces (k3f_face's rounding of u_b), for the
-// incremental anchors: with k3f_cart (ph unset) it refreshes the FP32 base
-// that the increment stages read after the float-float base has moved
-__global__ void __launch_bounds__(256) k3f_ub(AncFF A) {
-  const Geom& g = A.g;
-  const int N = g.N;
-  NS3_IJK(0, 0, 0)
-  for (int m = 0; m < 3; ++m) {
-    const int lim[3] = {N + (m == 0), N + (m == 1), N + (m == 2)};
-    if (i >= lim[0] || j >= lim[1] || k >= lim[2]) continue;
-    const long id = id3(g, i, j, k);
-    A.ub[m][id] = ff_round(ld_base(A, m, id));
-  }
-}
+
 
 // u > 0: 3/4 x(-1) + 3/8 x(0) - 1/8 x(-2); u <= 0: 3/8 x(-1) + 3/4 x(0) - 1/8 x(+1)
 __device__ __forceinline__ ff q3p_ff(ff x2, ff x1, ff x0) { return (0.75f * x1 + 0.375f * x0) + ff_scale2(x2, -0.125f); }
@@ -381,7 +369,9 @@ __global__ void __launch_bounds__(256) k3i_face(Inc3 A) {
       const float eo = A.rk * G;
       if (A.last) {
         const ff b = A.baseff[m] ? ld2(A.baseff[m], id) : ld_ff(A.base64[m], id);
-        st2(A.outff[m], id, ff_add_f(b, eo));
+        const ff nb = ff_add_f(b, eo);
+        st2(A.outff[m], id, nb);
+        if (A.ubout[m] != nullptr) A.ubout[m][id] = ff_round(nb);
         if (A.keep_e) A.eout[m][id] = eo;
         const float w = (a == 0 || a == N) ? 0.5f : 1.f;
         nrm[m] += eo * eo * w;

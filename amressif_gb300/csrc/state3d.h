@@ -28,6 +28,7 @@ struct State3D {
   // mixed-precision predictor (FP32): u_b copy, anchor G0, increments, base
   // cell velocity; the flux / total / cell-velocity increments reuse FL, T, PH
   float* UB32[3] = {nullptr, nullptr, nullptr};
+  float* UB32b[3] = {nullptr, nullptr, nullptr};  // the other FP32 base: the last stage writes the moved base here
   float* G0[3] = {nullptr, nullptr, nullptr};
   float* G0b[3] = {nullptr, nullptr, nullptr};  // G0 of an incremental anchor update
   int mix_it = 0;          // mixed pseudo-iterations of this step
