@@ -205,6 +205,11 @@ int ns_poisson_rhs_noalloc(const double* u, const double* v, double* f, int n_ce
 void* ns_host_alloc(unsigned long long bytes);
 void ns_host_free(void* p);
 
+/* ns_profile_enable(c, 1) waits for the stream and creates the event pool
+ * (two events per launch, filled once), so switch it on outside a timed
+ * region. The event pairs are read out only by ns_profile_read (which waits
+ * for the stream), by ns_profile_enable, and when several thousand launches
+ * are pending, never at the syncs inside a step. */
 int ns_profile_enable(ns_ctx* c, int on);
 int ns_profile_read(ns_ctx* c, double* ms, long long* counts, int nkinds, int reset);
 long long ns_launch_count(const ns_ctx* c);
