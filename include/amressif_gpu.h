@@ -30,7 +30,7 @@ extern "C" {
 #define NS_ERR_MG_STALL -4        /* Poisson residual stopped decreasing before the tolerance */
 #define NS_ERR_NOMEM -5           /* device allocation failed */
 #define NS_ERR_STATE -6           /* call out of sequence (e.g. stage before step_begin) */
-#define NS_ERR_UNSUPPORTED -7     /* valid reference input this build does not implement */
+#define NS_ERR_UNSUPPORTED -7     /* valid reference input the library does not implement */
 
 /* ---- precision modes ----------------------------------------------------- */
 #define NS_PREC_FP64_EXACT 0 /* reference operation order, no FMA: bit-exact stages */
