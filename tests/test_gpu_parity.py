@@ -42,6 +42,12 @@ CASES = {
                              bc_lo=(111,) * 3, bc_hi=(111,) * 3, fix_quirks=1),
                     dict(ren=1000.0, fixed_dt=0.5 * 2 * math.pi / 64, prob_hi=(2 * math.pi,) * 3,
                          bc_lo=(111,) * 3, bc_hi=(111,) * 3, fix_quirks=1), 1),
+    # periodic with partial strips and tiles: 40 is not a multiple of the 32-, 58- or 64-column
+    # strips, so the wrap is taken inside a strip and by a lane other than the last
+    "tgv40_partial_tiles": (40, dict(ren=1000.0, dt=0.5 * 2 * math.pi / 40, prob_hi=(2 * math.pi,) * 3,
+                                     bc_lo=(111,) * 3, bc_hi=(111,) * 3, fix_quirks=1),
+                            dict(ren=1000.0, fixed_dt=0.5 * 2 * math.pi / 40, prob_hi=(2 * math.pi,) * 3,
+                                 bc_lo=(111,) * 3, bc_hi=(111,) * 3, fix_quirks=1), 1),
 }
 
 
@@ -61,7 +67,8 @@ def sync_state(o, s):
     o.set_state(u, up, p)
 
 
-@pytest.mark.parametrize("name", ["cavity32", "cavity40_partial_tiles", "cavity128_cfg1", "tgv64_parity", "tgv64_fixed"])
+@pytest.mark.parametrize("name", ["cavity32", "cavity40_partial_tiles", "cavity128_cfg1", "tgv64_parity", "tgv64_fixed",
+                                  "tgv40_partial_tiles"])
 def test_rk_stages_bit_exact(gpu_lib, oracle_lib, name):
     o, s = make_pair(name)
     for _ in range(3):
@@ -181,7 +188,8 @@ def test_free_running_matches_golden(gpu_lib):
         assert relp(pp, g["p_%d" % step]) <= TOL_STEP
 
 
-@pytest.mark.parametrize("name", ["cavity128_cfg1", "tgv64_parity", "tgv64_fixed", "cavity40_partial_tiles"])
+@pytest.mark.parametrize("name", ["cavity128_cfg1", "tgv64_parity", "tgv64_fixed", "cavity40_partial_tiles",
+                                  "tgv40_partial_tiles"])
 def test_mixed_predictor_matches_fp64(gpu_lib, name):
     """Float-float anchor + FP32 increments reproduce the FP64 iterates.
 
