@@ -146,6 +146,24 @@ def dist_setup():
     return 1, 0, None
 
 
+def max_over_ranks(dist, seconds):
+    """The slowest rank's time of the timed region (all ranks, gloo); the
+    time itself without a process group."""
+    if not dist:
+        return seconds
+    import torch
+
+    t = torch.tensor([seconds], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_rate(world, steps, seconds):
+    """Whole-job steps/s of `world` independent replicas that each ran `steps`
+    steps, timed by the slowest (weak scaling: the work per GPU is fixed)."""
+    return world * steps / seconds
+
+
 def vcycle_bytes(n):
     """Algorithmic bytes of one FP32 V-cycle of the 2D hierarchy: per tiled
     level (n_l >= 64) the pre-smoothing reads f and writes x (8 B/cell, x
@@ -396,14 +414,8 @@ def bench_ours(args):
     prof = s.profile_read()
     s.profile(False)
     dev_ms = sum(st["ms_predictor"] + st["ms_poisson"] + st["ms_project"] for st in stats)
-    total_s = dev_ms / 1e3
-    if dist:
-        import torch
-
-        t = torch.tensor([total_s], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_s = float(t.item())
-    value = world * K / total_s
+    total_s = max_over_ranks(dist, dev_ms / 1e3)
+    value = replica_rate(world, K, total_s)
     ms_per_step = 1e3 * total_s / K
     # the mixed state after the W + K steps, for the comparison with the FP64 run
     state_timed = s.get_state() if not args.no_fp64 else None
@@ -570,7 +582,9 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--n", type=int, default=4096)
+    # --grid: the same option for use under torch.distributed.run, whose own
+    # parser takes --n for an abbreviation of --nnodes / --nproc-per-node
+    ap.add_argument("--n", "--grid", dest="n", type=int, default=4096)
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-steps", type=int, default=1)
     ap.add_argument("--no-fp64", action="store_true")
