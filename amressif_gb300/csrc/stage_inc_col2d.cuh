@@ -15,9 +15,9 @@
 //     f32x2 add / mul / fma of stage_inc2d.cuh), one instruction for both;
 //     only the upwind selects and the boundary rules stay per column.
 // Compared with one column per lane (26 output columns per warp, 0.273 ms a
-// launch at 4096^2) the pair layout took a launch to 0.243 ms and the packed
-// arithmetic to 0.214 ms (with the 3-row ring; 12 warps per SM, ~150
-// registers).
+// launch at 4096^2) the pair layout took a launch to 0.243 ms, the packed
+// arithmetic with the 3-row ring to 0.214 ms and the unrolled row loop to
+// 0.211 ms (12 warps per SM; 167 registers, 156 for the base update).
 // The incremental anchor update (BASE = true) also writes the new float-float
 // base (hi, lo) + e_s at its output faces, into the other buffer of the pair:
 // the lo words of row k - 2 travel in row k's ring slot, so they arrive with
