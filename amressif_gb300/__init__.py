@@ -25,6 +25,7 @@ NS_ERR_MG_STALL = -4
 NS_ERR_NOMEM = -5
 NS_ERR_STATE = -6
 NS_ERR_UNSUPPORTED = -7
+NS_ERR_NONFINITE = -8
 
 PREC_FP64_EXACT, PREC_FP64, PREC_MIXED = 0, 1, 2
 INIT_CAVITY, INIT_TGV = 0, 1
@@ -98,6 +99,7 @@ class NsParams(ctypes.Structure):
         ("dtau_clip", ctypes.c_int),
         ("poisson_solver", ctypes.c_int),
         ("gmres_restart", ctypes.c_int),
+        ("dc_residual", ctypes.c_int),
     ]
 
 
@@ -115,6 +117,8 @@ class NsStepStats(ctypes.Structure):
         ("ms_poisson", ctypes.c_double),
         ("ms_project", ctypes.c_double),
         ("poisson_fp64_fallback", ctypes.c_int),
+        ("ms_h2d", ctypes.c_double),
+        ("ms_d2h", ctypes.c_double),
     ]
 
 

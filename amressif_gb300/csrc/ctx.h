@@ -57,7 +57,7 @@ struct ns_ctx {
   unsigned* counter = nullptr;
   double* red = nullptr;    // device scalars
   double* red_h = nullptr;  // pinned mirror
-  cudaEvent_t ev[4];
+  cudaEvent_t ev[8];  // 0..3: phases of ns_step; 4..7: the copies of ns_step_host
   bool ev_ok = false;
   // mixed iteration: E[0] holds an increment not yet added to the base
   bool mix_pending = false;
@@ -133,6 +133,9 @@ void free3d(ns_ctx* c);
 int set_state3d(ns_ctx* c, const double* const* u, const double* const* up, const double* p, double time);
 int get_state3d(ns_ctx* c, double* const* u, double* const* up, double* p, double* phi);
 int step3d(ns_ctx* c, ns_step_stats* s);
+// device array of an NS_FIELD_* of a 3D context (nullptr if the field has no
+// 3D array); *is_face tells whether it is a face field of direction comp
+double* field_ptr3d(ns_ctx* c, int field, int comp, bool* is_face);
 
 inline double* face_ptr(ns_ctx* c, int id, int m) { return id < 0 ? c->UP[m] : c->B[id][m]; }
 

@@ -9,8 +9,8 @@
 // like kernels_exact.cu, so its results are bit-identical to ns_poisson_rhs.
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstring>
-#include <mutex>
 
 #include "../../include/amressif_gpu.h"
 #include "project2d.cuh"
@@ -19,37 +19,20 @@
 namespace ns {
 namespace {
 
-// Largest grid: 4096 x 4096 cells = 128 x 512 blocks of 32 x 8 cells.
+// Largest grid: 4096 x 4096 cells. k_poisson_rhs2d runs on proj_grid(n):
+// blocks of 32 columns x (8 warps x kProjRows rows), 128 x 64 = 8192 blocks
+// at n = 4096, each leaving two partials (max|div|, sum f).
 constexpr int kNoAllocMaxCells = 4096;
-constexpr int kNoAllocMaxBlocks = (kNoAllocMaxCells / 32) * (kNoAllocMaxCells / 8);
+constexpr int kNoAllocMaxBlocks =
+    ((kNoAllocMaxCells + 31) / 32) * ((kNoAllocMaxCells + 8 * kProjRows - 1) / (8 * kProjRows));
+static_assert(kNoAllocMaxBlocks == 8192, "proj_grid(4096) sizing changed: resize the scratch");
 // layout: 2 * kNoAllocMaxBlocks doubles of block partials, 2 result doubles,
 // one counter (must be zero when a launch starts)
 constexpr size_t kNoAllocBytes = (2 * (size_t)kNoAllocMaxBlocks + 2) * sizeof(double) + 256;
 
-// Held by every GPU that loads the library until the process exits (1 MB).
+// Held by every GPU that loads the library until the process exits (about
+// 128 KB).
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
-
-constexpr int kMaxDevices = 64;
-std::mutex g_setup_mu;
-unsigned char* g_scratch_ptr[kMaxDevices] = {nullptr};
-
-// Device address of the scratch array for the current device (looked up once
-// per device; the host-side symbol itself is not a device address).
-cudaError_t scratch_for_current_device(unsigned char** out) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return e;
-  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
-  std::lock_guard<std::mutex> lk(g_setup_mu);
-  if (!g_scratch_ptr[dev]) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess) return e;
-    g_scratch_ptr[dev] = static_cast<unsigned char*>(p);
-  }
-  *out = g_scratch_ptr[dev];
-  return cudaSuccess;
-}
 
 }  // namespace
 }  // namespace ns
@@ -57,12 +40,20 @@ cudaError_t scratch_for_current_device(unsigned char** out) {
 extern "C" int ns_poisson_rhs_noalloc(const double* u, const double* v, double* f, int n_cell, long long pitch,
                                       double dx, double dy, double dt, double* divmax_sum, void* stream) {
   using namespace ns;
-  if (!u || !v || !f || !divmax_sum || n_cell < 1 || pitch < n_cell + 1 || dx <= 0 || dy <= 0 || dt <= 0)
+  // NaN and infinite spacings or time steps fail these tests too
+  if (!u || !v || !f || !divmax_sum || n_cell < 1 || pitch < n_cell + 1 || !(dx > 0 && std::isfinite(dx)) ||
+      !(dy > 0 && std::isfinite(dy)) || !(dt > 0 && std::isfinite(dt)))
     return NS_ERR_ARG;
   if (n_cell > kNoAllocMaxCells) return NS_ERR_UNSUPPORTED;  // beyond the fixed scratch
+  const dim3 grid = proj_grid(n_cell);
+  if ((size_t)grid.x * grid.y > (size_t)kNoAllocMaxBlocks) return NS_ERR_UNSUPPORTED;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  unsigned char* base = nullptr;
-  if (scratch_for_current_device(&base) != cudaSuccess) return NS_ERR_CUDA;
+  // The array's name is a host-side stand-in: its device address on the
+  // current device is looked up on every call (cheap, and still right after
+  // a cudaDeviceReset has reloaded the module).
+  void* sym = nullptr;
+  if (cudaGetSymbolAddress(&sym, g_noalloc_scratch) != cudaSuccess) return NS_ERR_CUDA;
+  unsigned char* base = static_cast<unsigned char*>(sym);
   double* part = reinterpret_cast<double*>(base);
   double* result = part + 2 * (size_t)kNoAllocMaxBlocks;
   unsigned* counter = reinterpret_cast<unsigned*>(result + 2);
@@ -85,7 +76,7 @@ extern "C" int ns_poisson_rhs_noalloc(const double* u, const double* v, double* 
   a.part = part;
   a.counter = counter;
   a.red_out = result;
-  k_poisson_rhs2d<ArithExact><<<proj_grid(n_cell), 256, 0, st>>>(a);
+  k_poisson_rhs2d<ArithExact><<<grid, 256, 0, st>>>(a);
   if (cudaGetLastError() != cudaSuccess) return NS_ERR_CUDA;
   if (cudaMemcpyAsync(divmax_sum, result, 2 * sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess) return NS_ERR_CUDA;
   if (cudaStreamSynchronize(st) != cudaSuccess) return NS_ERR_CUDA;

@@ -188,7 +188,7 @@ __global__ void __launch_bounds__(256) k3_face(Arg3 A) {
   if (A.do_norm && grid_reduce_last<3>(nrm, A.part, A.counter, 0u) && threadIdx.x == 0) {
     const double npts = (double)N * N * N;
     double e = 0.0;
-    for (int m = 0; m < 3; ++m) e = fmax(e, sqrt(nrm[m]) / sqrt(npts));
+    for (int m = 0; m < 3; ++m) e = max_keep_nan(e, sqrt(nrm[m]) / sqrt(npts));
     *A.red_out = e;
   }
 }

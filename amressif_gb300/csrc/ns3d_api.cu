@@ -344,6 +344,21 @@ int get_state3d(ns_ctx* c, double* const* u, double* const* up, double* p, doubl
 
 double* face3_ptr(ns_ctx* c, int id, int m) { return face3(c, id, m); }
 
+double* field_ptr3d(ns_ctx* c, int field, int comp, bool* is_face) {
+  State3D& S = *c->s3;
+  *is_face = false;
+  if (comp < 0 || comp > 2) return nullptr;
+  switch (field) {
+    case NS_FIELD_VEL: *is_face = true; return S.U[comp];
+    case NS_FIELD_VEL_PREV: *is_face = true; return S.UP[comp];
+    case NS_FIELD_VEL_STAR: *is_face = true; return face3(c, S.cur, comp);
+    case NS_FIELD_PRESSURE: return S.Pp;
+    case NS_FIELD_PHI: return S.PHI;
+    case NS_FIELD_POISSON_RHS: return S.F;
+    default: return nullptr;
+  }
+}
+
 int poisson3d(ns_ctx* c, int* cycles, double* res) {
   long long fb = 0;
   return poisson3(c, cycles, res, &fb);
@@ -556,6 +571,7 @@ int predictor3d(ns_ctx* c, ns_step_stats* sp) {
     }
     S.base = S.cur;
     count++;
+    if (std::isnan(norm)) return fail(c, NS_ERR_NONFINITE, "pseudo-increment norm is NaN (non-finite fields)");
     if (count > c->P.iter_num) { s.status = NS_WARN_PSEUDO_MAXITER; break; }
     if (norm > 1.e2) { s.status = NS_WARN_PSEUDO_DIVERGED; break; }
   }
@@ -583,6 +599,8 @@ int step3d(ns_ctx* c, ns_step_stats* stats) {
   if (r != NS_OK) return r;
   s.div_before = c->red_h[kRedDivBefore];
   s.rhs_sum = c->red_h[kRedSum];
+  if (!std::isfinite(s.div_before) || !std::isfinite(s.rhs_sum))
+    return fail(c, NS_ERR_NONFINITE, "Poisson right-hand side is not finite");
   long long fb = 0;
   const int mg = poisson3(c, &s.poisson_cycles, &s.poisson_res, &fb);
   if (mg != NS_OK && mg != NS_ERR_MG_STALL) return mg;

@@ -385,7 +385,7 @@ __global__ void __launch_bounds__(256) k3i_face(Inc3 A) {
       threadIdx.x == 0) {
     const double npts = (double)N * N * N;
     double e = 0.0;
-    for (int m = 0; m < 3; ++m) e = fmax(e, sqrt(tot[m]) / sqrt(npts));
+    for (int m = 0; m < 3; ++m) e = max_keep_nan(e, sqrt(tot[m]) / sqrt(npts));
     *A.norm_out = e;
   }
 }

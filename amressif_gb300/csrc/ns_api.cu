@@ -235,6 +235,7 @@ void ns_params_default(ns_params* p) {
   p->dtau_clip = 0;
   p->poisson_solver = 0;
   p->gmres_restart = 30;
+  p->dc_residual = 0;
 }
 
 int ns_params_parse_file(ns_params* p, const char* path) {
@@ -289,7 +290,16 @@ int ns_ctx_create(const ns_params* p, void* stream, ns_ctx** out) {
   if (p->dim != 2 && p->dim != 3) return NS_ERR_UNSUPPORTED;
   if (p->n_cell < 8 || p->n_cell % 8 != 0) return NS_ERR_ARG;
   const int D = p->dim;
-  if (p->ren <= 0) return NS_ERR_ARG;
+  {
+    // the multigrid halves n while n % 4 == 0 and n > 4; its coarsest level
+    // must fit the single-block bottom solve (2D: <= 32, 3D: <= 24)
+    int nc = p->n_cell;
+    while (nc % 4 == 0 && nc > 4) nc /= 2;
+    if (nc > (D == 2 ? kBottomN : 24)) return NS_ERR_UNSUPPORTED;
+  }
+  if (!(p->ren > 0)) return NS_ERR_ARG;
+  if (p->dc_residual != 0 && p->dc_residual != 1) return NS_ERR_ARG;
+  if (D == 3 && p->dc_residual == 1) return NS_ERR_UNSUPPORTED;  // the 3D defect correction is float-float
   ns_ctx* c = new ns_ctx();
   c->P = *p;
   const int N = p->n_cell;
@@ -435,12 +445,18 @@ static double* field_ptr(ns_ctx* c, int field, int comp, bool* is_face) {
   }
 }
 
+// One box [lo, hi] of a field between the caller's Array4-style view and the
+// device: one pitched 2D copy per k plane. The index box must lie inside the
+// field's own index space; jstride must hold a row of the box, and in 3D
+// kstride a plane of it (AMReX's Array4 strides satisfy both). A 2D context
+// takes the single plane k = 0 (kstride is then unused).
 static int box_copy(ns_ctx* c, int field, int comp, double* data, const int lo[3], const int hi[3], long long jstride,
                     long long kstride, int where_device, bool put) {
-  (void)kstride;
-  if (!c || !data || !lo || !hi || comp < 0 || comp > 1) return NS_ERR_ARG;
-  if (c->P.dim == 3) return fail(c, NS_ERR_UNSUPPORTED, "3D boxes: use ns_set_state / ns_get_state");
+  if (!c || !data || !lo || !hi) return NS_ERR_ARG;
+  const int D = c->P.dim;
+  if (comp < 0 || comp >= D) return fail(c, NS_ERR_ARG, "box copy: component out of range");
   if (field == NS_FIELD_CART) {
+    if (D == 3) return fail(c, NS_ERR_UNSUPPORTED, "3D: no cell-velocity override (the first stage rebuilds it)");
     if (!put) return NS_ERR_ARG;
     for (int m = 0; m < 2; ++m)
       if (!c->CART[m]) {
@@ -450,18 +466,30 @@ static int box_copy(ns_ctx* c, int field, int comp, double* data, const int lo[3
     c->cart_pending = true;
   }
   bool face = false;
-  double* dev = (field == NS_FIELD_CART) ? c->CART[comp] : field_ptr(c, field, comp, &face);
-  if (!dev) return NS_ERR_ARG;
-  const int ni = c->N + ((face && comp == 0) ? 1 : 0);
-  const int nj = c->N + ((face && comp == 1) ? 1 : 0);
-  if (lo[0] < 0 || lo[1] < 0 || hi[0] >= ni || hi[1] >= nj || hi[0] < lo[0] || hi[1] < lo[1]) return NS_ERR_ARG;
-  const size_t w = (size_t)(hi[0] - lo[0] + 1) * sizeof(double);
-  const size_t h = (size_t)(hi[1] - lo[1] + 1);
-  double* d = dev + (long)lo[1] * c->pitch + lo[0];
+  double* dev = nullptr;
+  if (D == 3) dev = field_ptr3d(c, field, comp, &face);
+  else dev = (field == NS_FIELD_CART) ? c->CART[comp] : field_ptr(c, field, comp, &face);
+  if (!dev) return fail(c, NS_ERR_ARG, "box copy: unknown field");
+  int ext[3];
+  for (int d = 0; d < 3; ++d) ext[d] = (d < D) ? c->N + ((face && comp == d) ? 1 : 0) : 1;
+  for (int d = 0; d < 3; ++d)
+    if (lo[d] < 0 || hi[d] >= ext[d] || hi[d] < lo[d]) return fail(c, NS_ERR_ARG, "box copy: index box outside the field");
+  const long long wcells = hi[0] - lo[0] + 1, hrows = hi[1] - lo[1] + 1, nplanes = hi[2] - lo[2] + 1;
+  if (jstride < wcells) return fail(c, NS_ERR_ARG, "box copy: jstride smaller than the box width");
+  if (nplanes > 1 && kstride < jstride * hrows) return fail(c, NS_ERR_ARG, "box copy: kstride smaller than a box plane");
+  const size_t w = (size_t)wcells * sizeof(double);
+  const long P = c->pitch;
+  const long plane = (long)P * (c->N + 1);  // 3D: (i, j, k) at (k (N + 1) + j) P + i
   const cudaMemcpyKind kind = where_device ? cudaMemcpyDeviceToDevice : (put ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost);
-  cudaError_t e = put ? cudaMemcpy2DAsync(d, c->pitch * sizeof(double), data, (size_t)jstride * sizeof(double), w, h, kind, c->st)
-                      : cudaMemcpy2DAsync(data, (size_t)jstride * sizeof(double), d, c->pitch * sizeof(double), w, h, kind, c->st);
-  return cuda_check(c, e, "box copy");
+  for (long long k = 0; k < nplanes; ++k) {
+    double* d = dev + (D == 3 ? (long)(lo[2] + k) * plane : 0) + (long)lo[1] * P + lo[0];
+    double* h = data + k * kstride;
+    cudaError_t e = put ? cudaMemcpy2DAsync(d, P * sizeof(double), h, (size_t)jstride * sizeof(double), w, (size_t)hrows, kind, c->st)
+                        : cudaMemcpy2DAsync(h, (size_t)jstride * sizeof(double), d, P * sizeof(double), w, (size_t)hrows, kind, c->st);
+    int r = cuda_check(c, e, "box copy");
+    if (r != NS_OK) return r;
+  }
+  return NS_OK;
 }
 
 int ns_put_box(ns_ctx* c, int field, int comp, const double* data, const int lo[3], const int hi[3], long long jstride,
@@ -478,9 +506,8 @@ int ns_get_box(ns_ctx* c, int field, int comp, double* data, const int lo[3], co
   return r;
 }
 
-int ns_set_state(ns_ctx* c, const double* const* u, const double* const* u_prev, const double* p, double time) {
-  if (!c || !u || !u_prev || !p) return NS_ERR_ARG;
-  if (c->P.dim == 3) return set_state3d(c, u, u_prev, p, time);
+// the copies and resets of ns_set_state, enqueued without waiting (2D)
+static int set_state_async(ns_ctx* c, const double* const* u, const double* const* u_prev, const double* p, double time) {
   const int N = c->N;
   for (int m = 0; m < 2; ++m) {
     const int lo[3] = {0, 0, 0};
@@ -497,12 +524,18 @@ int ns_set_state(ns_ctx* c, const double* const* u, const double* const* u_prev,
   c->time = time;
   c->in_step = false;
   c->cart_pending = false;
-  return ns_sync(c);
+  return NS_OK;
 }
 
-int ns_get_state(ns_ctx* c, double* const* u, double* const* u_prev, double* p, double* phi) {
-  if (!c) return NS_ERR_ARG;
-  if (c->P.dim == 3) return get_state3d(c, u, u_prev, p, phi);
+int ns_set_state(ns_ctx* c, const double* const* u, const double* const* u_prev, const double* p, double time) {
+  if (!c || !u || !u_prev || !p) return NS_ERR_ARG;
+  if (c->P.dim == 3) return set_state3d(c, u, u_prev, p, time);
+  const int r = set_state_async(c, u, u_prev, p, time);
+  return r != NS_OK ? r : ns_sync(c);
+}
+
+// the copies of ns_get_state, enqueued without waiting (2D)
+static int get_state_async(ns_ctx* c, double* const* u, double* const* u_prev, double* p, double* phi) {
   const int N = c->N;
   for (int m = 0; m < 2; ++m) {
     const int lo[3] = {0, 0, 0};
@@ -514,7 +547,14 @@ int ns_get_state(ns_ctx* c, double* const* u, double* const* u_prev, double* p, 
   const int lo[3] = {0, 0, 0}, hi[3] = {N - 1, N - 1, 0};
   if (p) { int r = box_copy(c, NS_FIELD_PRESSURE, 0, p, lo, hi, N, 0, 0, false); if (r) return r; }
   if (phi) { int r = box_copy(c, NS_FIELD_PHI, 0, phi, lo, hi, N, 0, 0, false); if (r) return r; }
-  return ns_sync(c);
+  return NS_OK;
+}
+
+int ns_get_state(ns_ctx* c, double* const* u, double* const* u_prev, double* p, double* phi) {
+  if (!c) return NS_ERR_ARG;
+  if (c->P.dim == 3) return get_state3d(c, u, u_prev, p, phi);
+  const int r = get_state_async(c, u, u_prev, p, phi);
+  return r != NS_OK ? r : ns_sync(c);
 }
 
 int ns_init_fields(ns_ctx* c, int init_case) {
@@ -972,12 +1012,22 @@ int ns_poisson_solve(ns_ctx* c, int precision, int* cycles, double* res) {
     q.part = c->part;
     q.counter = c->counter;
     q.red_out = c->red + kRedRes;
-    LAUNCH(NS_PROF_OTHER, "rhs split", launch_rhs_ff(c->N, c->pitch, c->F, c->red + kRedMean, c->FFh, c->FFl, c->st));
+    const bool ff_start = c->P.dc_residual == 0;
     int pf = 0;
-    q.first = 1;
-    q.phin[0] = c->PFh[0]; q.phin[1] = c->PFl[0];
-    q.phout[0] = c->PFh[0]; q.phout[1] = c->PFl[0];
-    LAUNCH(NS_PROF_DC_UPDATE, "dc update", launch_dc_update_ff(q, c->st));
+    int pc = 0;
+    if (ff_start) {
+      LAUNCH(NS_PROF_OTHER, "rhs split", launch_rhs_ff(c->N, c->pitch, c->F, c->red + kRedMean, c->FFh, c->FFl, c->st));
+      q.first = 1;
+      q.phin[0] = c->PFh[0]; q.phin[1] = c->PFl[0];
+      q.phout[0] = c->PFh[0]; q.phout[1] = c->PFl[0];
+      LAUNCH(NS_PROF_DC_UPDATE, "dc update", launch_dc_update_ff(q, c->st));
+    } else {
+      // FP64 phi and residual from the first sweep: phi = 0, r = f - mean f
+      d.first = 1;
+      d.phi_in = c->PHI[0];
+      d.phi_out = c->PHI[0];
+      LAUNCH(NS_PROF_DC_UPDATE, "dc update", launch_dc_update(d, c->st));
+    }
     r = sync_red(c, kRedRes, 1);
     if (r != NS_OK) return r;
     rnorm0 = c->red_h[kRedRes];
@@ -986,8 +1036,7 @@ int ns_poisson_solve(ns_ctx* c, int precision, int* cycles, double* res) {
     auto done = [&](double x) { return x <= tol && (div_tol_res <= 0 || x <= div_tol_res); };
     double best = rn;
     int stall = 0;
-    bool ffmode = true;
-    int pc = 0;
+    bool ffmode = ff_start;
     while (!done(rn) && rnorm0 > 0) {
       if (ncyc >= maxc) { status = NS_ERR_MG_STALL; break; }
       int r2 = vcycle_graph<float>(c, c->M32, 1);
@@ -1288,6 +1337,10 @@ int nsh::run_predictor(ns_ctx* c, ns_step_stats* sp) {
       if (r != NS_OK) return r;
     }
     countIter++;
+    if (std::isnan(normError)) {
+      c->in_step = false;
+      return fail(c, NS_ERR_NONFINITE, "pseudo-increment norm is NaN (non-finite fields)");
+    }
     if (countIter > c->P.iter_num) { s.status = NS_WARN_PSEUDO_MAXITER; break; }
     if (normError > 1.e2) { s.status = NS_WARN_PSEUDO_DIVERGED; break; }
   }
@@ -1309,6 +1362,10 @@ int ns_step(ns_ctx* c, ns_step_stats* stats) {
   if (c->ev_ok) cudaEventRecord(c->ev[1], c->st);
   r = ns_poisson_rhs(c, &s.div_before, &s.rhs_sum);
   if (r != NS_OK) return r;
+  if (!std::isfinite(s.div_before) || !std::isfinite(s.rhs_sum)) {
+    c->in_step = false;
+    return fail(c, NS_ERR_NONFINITE, "Poisson right-hand side is not finite");
+  }
   const int prec = (c->P.precision == NS_PREC_MIXED) ? NS_PREC_MIXED : NS_PREC_FP64;
   const long long fb0 = c->dc_fallbacks;
   r = ns_poisson_solve(c, prec, &s.poisson_cycles, &s.poisson_res);
@@ -1354,15 +1411,40 @@ int ns_checkpoint_put(ns_ctx* c, const double* const* u, const double* const* u_
 
 long long ns_get_step(const ns_ctx* c) { return c ? c->step : -1; }
 
+// The copies in and out are enqueued on the context's stream with the step
+// between them: nothing waits for the upload (the step's kernels follow it in
+// stream order), and one synchronisation ends the call. CUDA events around
+// the two copy phases give ms_h2d and ms_d2h.
 int ns_step_host(ns_ctx* c, double* const* u, double* const* u_prev, double* p, ns_step_stats* stats) {
   if (!c || !u || !u_prev || !p) return NS_ERR_ARG;
   const double t = c->time;
-  int r = ns_set_state(c, u, u_prev, p, t);
+  const bool two_d = c->P.dim == 2;
+  if (c->ev_ok) cudaEventRecord(c->ev[4], c->st);
+  int r = two_d ? set_state_async(c, u, u_prev, p, t) : ns_set_state(c, u, u_prev, p, t);
   if (r != NS_OK) return r;
-  const int st = ns_step(c, stats);
-  if (st < 0) return st;
-  r = ns_get_state(c, u, u_prev, p, nullptr);
-  return r != NS_OK ? r : st;
+  if (c->ev_ok) cudaEventRecord(c->ev[5], c->st);
+  ns_step_stats s;
+  std::memset(&s, 0, sizeof(s));
+  const int st = ns_step(c, &s);
+  if (st < 0) {
+    if (stats) *stats = s;
+    return st;
+  }
+  if (c->ev_ok) cudaEventRecord(c->ev[6], c->st);
+  r = two_d ? get_state_async(c, u, u_prev, p, nullptr) : ns_get_state(c, u, u_prev, p, nullptr);
+  if (r != NS_OK) return r;
+  if (c->ev_ok) cudaEventRecord(c->ev[7], c->st);
+  r = ns_sync(c);
+  if (r != NS_OK) return r;
+  if (c->ev_ok) {
+    float a = 0.f, b = 0.f;
+    cudaEventElapsedTime(&a, c->ev[4], c->ev[5]);
+    cudaEventElapsedTime(&b, c->ev[6], c->ev[7]);
+    s.ms_h2d = a;
+    s.ms_d2h = b;
+  }
+  if (stats) *stats = s;
+  return st;
 }
 
 }  // extern "C"

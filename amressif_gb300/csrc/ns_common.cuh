@@ -12,6 +12,11 @@
 
 namespace ns {
 
+// max of two pseudo-norm components that keeps a NaN (fmax drops it), so a
+// non-finite field shows in the norm the host reads; equal to fmax otherwise
+__device__ __forceinline__ double max_keep_nan(double a, double b) { return (a != a) ? a : ((b != b) ? b : fmax(a, b)); }
+
+
 // Ghost rule of the cell-centred velocity on one domain side for one
 // component (utilities.cpp:62-349): ghost = -q, +q, or add - q (inlets), with
 // q the mirror cell value.

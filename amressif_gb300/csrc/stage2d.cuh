@@ -296,7 +296,7 @@ __global__ void __launch_bounds__(256) k_stage2d(StageArgs A) {
     if (grid_reduce_last<2>(nrm, A.part, A.counter, 0u) && threadIdx.x == 0) {
       const double npts = (double)N * (double)N;
       const double ex = sqrt(nrm[0]) / sqrt(npts), ey = sqrt(nrm[1]) / sqrt(npts);
-      *A.norm_out = fmax(ex, ey);
+      *A.norm_out = max_keep_nan(ex, ey);
     }
   }
 }

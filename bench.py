@@ -109,15 +109,16 @@ def ncu_traffic_per_cell():
         return {}
 
 
-def workload_params(ns, n, precision):
+def workload_params(ns, n, precision, **extra):
     return ns.default_params(n_cell=n, ren=1000.0, fixed_dt=0.5 / n, iter_num=100, momentum_tolerance=1e-10,
                              max_grid_size=(n, n, n), bc_lo=(135, 135, 135), bc_hi=(135, 165, 135),
                              inflow_waveform=(1.0, 0.0, 0.0), precision=precision, poisson_tol_rel=1e-10,
-                             poisson_tol_div=1e-10, poisson_max_cycles=200, dtau_clip=1)
+                             poisson_tol_div=1e-10, poisson_max_cycles=200, dtau_clip=1, **extra)
 
 
-def cpu_sample(n, steps, threads):
-    """The oracle (CPU restatement of the reference) on host cores."""
+def cpu_sample(n, steps, threads, keep_state=False):
+    """The oracle (CPU restatement of the reference) on host cores: `steps`
+    steps of the cavity from rest; with keep_state also its final (u, p)."""
     from oracle.orc import Oracle
 
     o = Oracle(n, ren=1000.0, dt=0.5 / n, iter_num=100, dtau_clip=1, poisson_tol=1e-10,
@@ -128,8 +129,36 @@ def cpu_sample(n, steps, threads):
     for _ in range(steps):
         ks.append(o.step()["pseudo_iters"])
     dt = time.perf_counter() - t0
+    state = None
+    if keep_state:
+        u, _, p, _ = o.get_state()
+        state = (u, p)
     o.close()
-    return steps / dt, ks, dt
+    return steps / dt, ks, dt, state
+
+
+def parity_first_steps(ns, n, oracle_state, steps, oracle_ks):
+    """The GPU solvers' first `steps` steps from rest against the oracle's
+    state after the same steps (the oracle run of the CPU baseline): relative
+    L2 of u, v and p (p modulo its constant) and the pseudo-iteration counts."""
+    import numpy as np
+
+    uo, po = oracle_state
+
+    def rel(a, b):
+        return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+    out = {"steps": steps, "oracle_pseudo_iters": oracle_ks}
+    for name, prec in (("fp64_exact", ns.PREC_FP64_EXACT), ("fp64", ns.PREC_FP64), ("mixed", ns.PREC_MIXED)):
+        s = ns.Solver(workload_params(ns, n, prec))
+        s.init(ns.INIT_CAVITY)
+        ks = [s.step()["pseudo_iters"] for _ in range(steps)]
+        u, _, p, _ = s.get_state()
+        s.close()
+        out[name] = {"pseudo_iters": ks, "rel_l2_u": rel(u[0], uo[0]), "rel_l2_v": rel(u[1], uo[1]),
+                     "rel_l2_p": rel(p - p.mean(), po - po.mean())}
+    out["max_rel_l2_fp64"] = max(out[k][q] for k in ("fp64_exact", "fp64") for q in ("rel_l2_u", "rel_l2_v", "rel_l2_p"))
+    return out
 
 
 def dist_setup():
@@ -211,6 +240,19 @@ def throughput_block(n, K, total_s, stats, prof, peak, stats_p):
     return out
 
 
+WORKLOAD = "lid-driven cavity %dx%d, Re=1000, dt=0.5dx, 1000-step run from rest"
+DTYPE_MIXED = ("mixed: float-float anchors and fp32 increment stages in the predictor; fp32 V-cycles inside a "
+               "defect correction with a float-float residual and phi (fp64 once its floor is reached); fp64 "
+               "projection, pressure update and divergence check")
+
+
+def bench_config(n, world):
+    """The `config` of both arms (the same dict, so that the two lines name
+    the same workload); the window of timed steps is a key of its own."""
+    return {"workload": WORKLOAD % (n, n), "n_cell": n, "parallelism": "replicas" if world > 1 else "single GPU",
+            "l2_flush": "inputs larger than L2 (every field is >=67 MB, the step touches >1 GB)"}
+
+
 def run_steps(s, k):
     stats = [s.step() for _ in range(k)]
     return stats
@@ -281,6 +323,33 @@ def adjoint_section(ns, args):
             errs.append(abs(fd - ad) / abs(ad))
         out["fd_check"] = {"directions": args.adj_fd, "eps": 1e-6, "max_rel_err": max(errs), "rel_errs": errs,
                            "forward_tolerance": 1e-13}
+        if args.adj_tlm:
+            # tangent-linear model along one more seeded direction: the state
+            # tangent starts at zero and ns_step_jvp carries it over the run at
+            # the trajectory's own states; dJ = sum (phi . dphi) dx dy over
+            # the cells of the lower-left quarter at the final step
+            d = rng.standard_normal(nseg)
+            d /= np.linalg.norm(d)
+            t = solver(1e-13)
+            t.set_controls(c)
+            z = [np.zeros(t.face_shape(0)), np.zeros(t.face_shape(1))]
+            du, dup, dpp = [a.copy() for a in z], [a.copy() for a in z], np.zeros((n, n))
+            t0 = time.perf_counter()
+            for _ in range(L):
+                du, dup, dpp = t.step_jvp(du, dup, dpp, d)
+                t.step()
+            tlm_s = time.perf_counter() - t0
+            uf, _, _, _ = t.get_state()
+            t.close()
+            hh = n // 2
+            cu = 0.5 * (uf[0][:hh, :hh] + uf[0][:hh, 1:hh + 1])
+            cv = 0.5 * (uf[1][:hh, :hh] + uf[1][1:hh + 1, :hh])
+            dcu = 0.5 * (du[0][:hh, :hh] + du[0][:hh, 1:hh + 1])
+            dcv = 0.5 * (du[1][:hh, :hh] + du[1][1:hh + 1, :hh])
+            dj = float(np.sum(cu * dcu + cv * dcv)) / (n * n)
+            ad = float(g @ d)
+            out["tlm_dot_check"] = {"tlm_dJ": dj, "adjoint_dJ": ad, "rel_err": abs(dj - ad) / abs(ad),
+                                    "steps": L, "seconds": tlm_s}
     return out
 
 
@@ -438,12 +507,17 @@ def bench_ours(args):
         te = time.perf_counter() - t0
         nbytes = 8 * (2 * shp[0][0] * shp[0][1] + 2 * shp[1][0] * shp[1][1] + n * n)
         dev = statistics.mean(x["ms_predictor"] + x["ms_poisson"] + x["ms_project"] for x in est)
+        h2d = statistics.mean(x["ms_h2d"] for x in est)
+        d2h = statistics.mean(x["ms_d2h"] for x in est)
         e2e = {"value": world * E / te, "unit": "steps/s", "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
                "steps": E, "path": "ns_step_host (pinned host u, u_prev, p in; u, u_prev, p out)",
                "note": "the steps after the timed ones (their pseudo-iteration counts below differ from the timed "
-                       "steps'); device_ms_per_step is the same device timing as value, copy_and_host_ms_per_step "
-                       "the rest of the wall time (host<->device copies, host calls)",
+                       "steps'); device_ms_per_step is the same device timing as value, h2d_ms / d2h_ms the "
+                       "CUDA-event time of the copies, copy_and_host_ms_per_step the wall time beyond the step's "
+                       "device time",
                "pseudo_iters": [x["pseudo_iters"] for x in est], "device_ms_per_step": dev,
+               "h2d_ms": h2d, "d2h_ms": d2h, "h2d_gbs": nbytes / (h2d * 1e-3) / 1e9 if h2d > 0 else None,
+               "d2h_gbs": nbytes / (d2h * 1e-3) / 1e9 if d2h > 0 else None,
                "copy_and_host_ms_per_step": 1e3 * te / E - dev}
         for b in bufs:
             b.free()
@@ -476,6 +550,47 @@ def bench_ours(args):
         }
         s64.close()
 
+    # ---- the mixed solver with an FP64 defect-correction residual (and FP64
+    # phi) from the first sweep, on the same steps: the A/B of the residual's
+    # arithmetic ----
+    dc_ab = None
+    if not args.no_dc_ab:
+        import numpy as np
+
+        sdc = ns.Solver(workload_params(ns, n, ns.PREC_MIXED, dc_residual=1))
+        sdc.init(ns.INIT_CAVITY)
+        run_steps(sdc, W)
+        sdc.profile(True)
+        sdc.profile(False)
+        sdc.profile_read(reset=True)
+        stdc = run_steps(sdc, K - Kp)
+        sdc.profile(True)
+        stdc += run_steps(sdc, Kp)
+        pdc = sdc.profile_read()
+        sdc.profile(False)
+        msdc = sum(st["ms_predictor"] + st["ms_poisson"] + st["ms_project"] for st in stdc) / K
+        udc, _, pdcs, _ = sdc.get_state()
+        sdc.close()
+        c_ff, m_ff = prof.get("dc_update", (0, 0.0))
+        c_64, m_64 = pdc.get("dc_update", (0, 0.0))
+        dc_ab = {
+            "fp64_residual": {"steps_per_s": 1e3 / msdc, "ms_per_step": msdc,
+                              "poisson_ms_per_step": statistics.mean(st["ms_poisson"] for st in stdc),
+                              "poisson_cycles_mean": statistics.mean(st["poisson_cycles"] for st in stdc),
+                              "dc_ms_per_launch": m_64 / c_64 if c_64 else None},
+            "float_float_residual": {"steps_per_s": value / world, "ms_per_step": ms_per_step,
+                                     "poisson_ms_per_step": statistics.mean(st["ms_poisson"] for st in stats),
+                                     "poisson_cycles_mean": statistics.mean(st["poisson_cycles"] for st in stats),
+                                     "dc_ms_per_launch": m_ff / c_ff if c_ff else None},
+            "note": "dc_residual = 1 (FP64 residual and phi) against the default dc_residual = 0, the same steps; "
+                    "dc_ms_per_launch over the last %d steps" % Kp,
+        }
+        if fp64 is not None:
+            def rel(a, b):
+                return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+            dc_ab["fp64_residual"]["vs_fp64_rel_l2"] = {"u": rel(udc[0], u64[0]), "v": rel(udc[1], u64[1]),
+                                                        "p": rel(pdcs - pdcs.mean(), p64 - p64.mean())}
+
     # ---- roofline of the dominant kernel ----
     peak, peak_kind = measured_peak_hbm()
     dom = max(prof.items(), key=lambda kv: kv[1][1])
@@ -501,12 +616,14 @@ def bench_ours(args):
 
     # ---- CPU restatement timed on the host (rank 0, N=1) ----
     cpu = None
+    parity = None
     if rank == 0 and world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
-        v, ks, secs = cpu_sample(n, args.cpu_steps, threads)
+        v, ks, secs, ostate = cpu_sample(n, args.cpu_steps, threads, keep_state=True)
         cpu = {"value": v, "unit": "steps/s", "cores": threads, "kind": "port",
                "sample": "%d step(s) from rest of the same %d^2 cavity (%.1f s, K=%s), oracle/ C++ restatement, "
                          "OpenMP" % (args.cpu_steps, n, secs, ks)}
+        parity = parity_first_steps(ns, n, ostate, args.cpu_steps, ks)
 
     adjoint = None
     if rank == 0 and not args.no_adjoint:
@@ -521,11 +638,10 @@ def bench_ours(args):
         line = {
             "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": K, "warmup": W,
             "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "mixed (fp64 anchors, fp32 increments and V-cycles)", "data": "synthetic (cavity from rest)",
-            "config": {"workload": "lid-driven cavity %dx%d, Re=1000, dt=0.5dx, steps %d..%d of a 1000-step run from rest"
-                       % (n, n, W + 1, W + K), "n_cell": n, "precision": "mixed",
-                       "parallelism": "replicas" if world > 1 else "single GPU",
-                       "l2_flush": "inputs larger than L2 (every field is >=67 MB, the step touches >1 GB)"},
+            "dtype": DTYPE_MIXED, "data": "synthetic (cavity from rest)",
+            "config": bench_config(n, world),
+            "window": "steps %d..%d of the run (W = %d untimed warm-up steps first)" % (W + 1, W + K, W),
+            "pseudo_iters": [st["pseudo_iters"] for st in stats],
             "pseudo_iters_mean": statistics.mean(st["pseudo_iters"] for st in stats),
             "poisson_cycles_mean": statistics.mean(st["poisson_cycles"] for st in stats),
             "div_after_max": max(st["div_after"] for st in stats),
@@ -536,6 +652,8 @@ def bench_ours(args):
                                   "project": statistics.mean(st["ms_project"] for st in stats)},
             "wall_ms_per_step": 1e3 * wall / K,
             "fp64_mg": fp64,
+            "dc_residual_ab": dc_ab,
+            "parity_4096_first_steps": parity,
             "adjoint_forward_ratio": adjoint["ratio"] if adjoint else None,
             "adjoint": adjoint,
             "taylor_green_3d": cfg5,
@@ -561,13 +679,15 @@ def bench_reference(args):
         return
     threads = os.cpu_count() or 1
     steps = max(1, min(args.steps, args.cpu_steps))
-    v, ks, secs = cpu_sample(args.n, steps, threads)
+    v, ks, secs, _ = cpu_sample(args.n, steps, threads)
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "steps/s", "n_gpus": world, "steps": steps,
         "warmup": 0, "ms_per_step": 1e3 * secs / steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (cavity from rest)",
-        "config": {"workload": "lid-driven cavity %dx%d, Re=1000, dt=0.5dx, steps 1..%d of a 1000-step run from rest"
-                   % (args.n, args.n, steps), "n_cell": args.n},
+        "config": bench_config(args.n, world),
+        "window": "steps 1..%d of the run (a step of the oracle takes about a minute at this size, so the "
+                  "bounded sample is the first step(s))" % steps,
+        "pseudo_iters": ks,
         "cpu_baseline": {"value": v, "unit": "steps/s", "cores": threads, "kind": "port",
                          "sample": "%d step(s) from rest, K=%s (%.1f s); the AMReX reference does not build here "
                                    "(AMReX not vendored), so its C++ restatement oracle/ is timed" % (steps, ks, secs)},
@@ -589,6 +709,7 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=1)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-dc-ab", action="store_true", help="skip the FP64 defect-correction residual A/B")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-cfg5", action="store_true")
@@ -604,8 +725,9 @@ def main():
     ap.add_argument("--adj-n", type=int, default=512)
     ap.add_argument("--adj-steps", type=int, default=400)
     ap.add_argument("--adj-snap", type=int, default=20)
-    ap.add_argument("--adj-fd", type=int, default=2, help="finite-difference directions of the gradient check")
+    ap.add_argument("--adj-fd", type=int, default=8, help="finite-difference directions of the gradient check")
     ap.add_argument("--adj-store-all", type=int, default=1, help="also time the store-every-step schedule")
+    ap.add_argument("--adj-tlm", type=int, default=1, help="tangent-linear check of the gradient along one direction")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

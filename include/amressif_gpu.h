@@ -31,11 +31,17 @@ extern "C" {
 #define NS_ERR_NOMEM -5           /* device allocation failed */
 #define NS_ERR_STATE -6           /* call out of sequence (e.g. stage before step_begin) */
 #define NS_ERR_UNSUPPORTED -7     /* valid reference input the library does not implement */
+#define NS_ERR_NONFINITE -8       /* NaN in the pseudo-increment norm, or a non-finite Poisson right-hand side
+                                     (e.g. NaN in the input fields): the step is abandoned where it was
+                                     found; set a state before the next step. The reference's loop test
+                                     (main.cpp:898) is false for NaN, so it would carry the NaN on silently */
 
 /* ---- precision modes ----------------------------------------------------- */
 #define NS_PREC_FP64_EXACT 0 /* reference operation order, no FMA: bit-exact stages */
 #define NS_PREC_FP64 1       /* FP64 everywhere, FMA and reciprocal multiplies */
-#define NS_PREC_MIXED 2      /* FP64 anchors + FP32 increments; FP32 V-cycles in FP64 defect correction */
+#define NS_PREC_MIXED 2      /* float-float anchors + FP32 increments in the predictor; FP32 V-cycles inside a
+                                defect correction whose residual is float-float (dc_residual = 0) or FP64
+                                (dc_residual = 1); FP64 projection, pressure update and divergence check */
 
 /* ---- initial conditions of hybrid_grid_init (fn_init.cpp:30-631) ------- */
 #define NS_INIT_CAVITY 0 /* all zero (the shipped source) */
@@ -53,7 +59,11 @@ extern "C" {
 /* Inputs-file keys of the reference (main.cpp:89-157) plus GPU options. */
 typedef struct ns_params {
   int dim;                   /* AMREX_SPACEDIM: 2 or 3 (3: the whole-step API and the adjoint pair) */
-  int n_cell;
+  int n_cell;                /* cells per direction. Deviation: the reference takes any n_cell
+                                (main.cpp:310-324); here it must be a multiple of 8 (else NS_ERR_ARG)
+                                whose multigrid hierarchy, halving while n % 4 == 0 and n > 4, ends at
+                                32 or less in 2D and 24 or less in 3D (else NS_ERR_UNSUPPORTED): e.g.
+                                40, 128, 4096 are taken, 808 is not */
   int max_grid_size[3];      /* accepted for drop-in; the GPU runs one box */
   double prob_lo[3];         /* lo_phy_dim (default 0) */
   double prob_hi[3];         /* hi_phy_dim (default 1) */
@@ -77,6 +87,9 @@ typedef struct ns_params {
   int poisson_solver;        /* 0: multigrid V-cycles; 1: restarted GMRES with one FP64 V-cycle as right
                                 preconditioner (the GMRES option of GMRES_Poisson.cpp:56-131) */
   int gmres_restart;         /* Krylov vectors per GMRES cycle (<= 31) */
+  int dc_residual;           /* NS_PREC_MIXED Poisson: the defect correction's residual and phi in
+                                0 = float-float (about 48 bits; FP64 once its floor is reached),
+                                1 = FP64 from the first sweep (2D; NS_ERR_UNSUPPORTED in 3D) */
 } ns_params;
 
 typedef struct ns_step_stats {
@@ -90,6 +103,8 @@ typedef struct ns_step_stats {
   int status;         /* NS_OK or NS_WARN_* */
   double ms_predictor, ms_poisson, ms_project; /* device time of the phases */
   int poisson_fp64_fallback; /* mixed solve: 1 if the float-float residual floor forced FP64 sweeps */
+  double ms_h2d, ms_d2h;      /* ns_step_host: device time of the host->device copies of (u, u_prev, p) and
+                                 of the device->host copies of the result (0 for ns_step) */
 } ns_step_stats;
 
 typedef struct ns_ctx ns_ctx;
@@ -113,11 +128,17 @@ double ns_get_time(const ns_ctx* c);
 int ns_init_fields(ns_ctx* c, int init_case);
 
 /* Move one box of a field between the caller and the device
- * (MultiFab::array(mfi) views). data is indexed
+ * (MultiFab::array(mfi) views, 2D and 3D). data is indexed
  *   data[(i-lo[0]) + (j-lo[1])*jstride + (k-lo[2])*kstride]
  * over the inclusive index box [lo, hi] in the field's own index space
- * (face fields extend to n_cell along their direction). where_device = 1 if
- * data is device memory. */
+ * (face fields extend to n_cell along their direction). An AMReX host passes
+ * the Array4 of a ghosted FArrayBox offset to the valid box's lo, with the
+ * Array4's jstride and kstride. NS_ERR_ARG if the box leaves the field, if
+ * jstride is below the box width or, for boxes of more than one plane,
+ * kstride below jstride times the box height; a 2D context takes only the
+ * plane lo[2] = hi[2] = 0 (kstride unused). where_device = 1 if data is
+ * device memory. ns_put_box from host memory and ns_get_box wait for the
+ * stream before they return. NS_FIELD_CART is 2D only. */
 int ns_put_box(ns_ctx* c, int field, int comp, const double* data, const int lo[3], const int hi[3],
                long long jstride, long long kstride, int where_device);
 int ns_get_box(ns_ctx* c, int field, int comp, double* data, const int lo[3], const int hi[3],
@@ -186,17 +207,21 @@ int ns_sync(ns_ctx* c);
  * the reference. For callers that cannot call cudaMalloc: a host whose device
  * memory all belongs to its own arena allocator (AMReX's), or a job whose
  * memory budget is fixed once it starts. Computes f = (1.5/dt) div u from
- * caller-owned device arrays u (x faces), v (y faces) and f (cells), all with
- * row pitch `pitch` elements (u(i,j) at j*pitch+i, pitch >= n_cell+1), and
- * returns {max|div u|, sum f} in divmax_sum[2] (host memory) after
- * synchronising `stream` (a cudaStream_t, NULL = default stream). The
- * reduction scratch is a fixed 1 MB device array inside the library, held on
- * every GPU that loads it until the process exits: n_cell above 4096 is
- * rejected with NS_ERR_UNSUPPORTED. The first call on each device looks up
- * that array's device address; make it before any stream capture. All calls
- * share the array, so calls that overlap on the GPU (other streams, other
- * threads) race and must be serialised by the caller. Results are
- * bit-identical to ns_poisson_rhs. */
+ * caller-owned device arrays, all with row pitch `pitch` elements
+ * (pitch >= n_cell + 1; element (i, j) at j * pitch + i):
+ *   u: x faces, n_cell rows of n_cell + 1 values;
+ *   v: y faces, n_cell + 1 rows of n_cell values;
+ *   f: cells, n_cell rows of n_cell values (written).
+ * Returns {max|div u|, sum f} in divmax_sum[2] (host memory). The call
+ * synchronises `stream` (a cudaStream_t, NULL = default stream) before it
+ * returns, so it cannot be made during a stream capture. dx, dy and dt must be
+ * finite and positive (NS_ERR_ARG otherwise). The reduction scratch is a fixed
+ * device array of about 128 KB inside the library, held on every GPU that
+ * loads it until the process exits: n_cell above 4096 is rejected with
+ * NS_ERR_UNSUPPORTED. Each call looks up that array's device address on the
+ * current device and clears its counter. All calls share the array, so calls
+ * that overlap on the GPU (other streams, other threads) race and must be
+ * serialised by the caller. Results are bit-identical to ns_poisson_rhs. */
 int ns_poisson_rhs_noalloc(const double* u, const double* v, double* f, int n_cell, long long pitch, double dx, double dy,
                            double dt, double* divmax_sum, void* stream);
 

@@ -25,11 +25,11 @@ def rel(a, b):
     return float(np.linalg.norm(a - b) / np.linalg.norm(b))
 
 
-def one_step(precision, case):
+def one_step(precision, case, dc_residual=0):
     if case == "cavity":
         p = ns.default_params(n_cell=N, ren=1000.0, fixed_dt=0.5 / N, iter_num=100, momentum_tolerance=1e-10,
                               max_grid_size=(N, N, N), precision=precision, poisson_tol_rel=1e-11,
-                              poisson_tol_div=1e-10, poisson_max_cycles=200, dtau_clip=1)
+                              poisson_tol_div=1e-10, poisson_max_cycles=200, dtau_clip=1, dc_residual=dc_residual)
         s = ns.Solver(p)
         s.init(ns.INIT_CAVITY)
         s.step()  # a developed right-hand side
@@ -38,7 +38,7 @@ def one_step(precision, case):
         p = ns.default_params(n_cell=N, ren=1000.0, fixed_dt=0.5 * h, iter_num=100, momentum_tolerance=1e-10,
                               prob_hi=(2 * math.pi,) * 3, bc_lo=(111,) * 3, bc_hi=(111,) * 3, fix_quirks=1,
                               max_grid_size=(N, N, N), precision=precision, poisson_tol_rel=1e-11,
-                              poisson_tol_div=1e-10, poisson_max_cycles=200)
+                              poisson_tol_div=1e-10, poisson_max_cycles=200, dc_residual=dc_residual)
         s = ns.Solver(p)
         s.set_state(*wl.tgv_perturbed_state(N, amp=1e-3, seed=0))
     st = s.step()
@@ -47,9 +47,11 @@ def one_step(precision, case):
     return st, u, pp
 
 
+@pytest.mark.parametrize("dc_residual", [0, 1])
 @pytest.mark.parametrize("case", ["cavity", "tgv"])
-def test_fine_level_smoother_mixed_matches_fp64(gpu_lib, case):
-    sm, um, pm = one_step(ns.PREC_MIXED, case)
+def test_fine_level_smoother_mixed_matches_fp64(gpu_lib, case, dc_residual):
+    """dc_residual 0: float-float residual and phi; 1: FP64 from the first sweep"""
+    sm, um, pm = one_step(ns.PREC_MIXED, case, dc_residual)
     sd, ud, pd = one_step(ns.PREC_FP64, case)
     assert sm["div_after"] <= 1e-10, sm["div_after"]
     assert rel(pm - pm.mean(), pd - pd.mean()) <= 1e-10

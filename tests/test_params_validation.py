@@ -18,7 +18,13 @@ def create(gpu_lib, **kw):
 @pytest.mark.parametrize("kw,code", [
     (dict(n_cell=20), ns.NS_ERR_ARG),                 # not a multiple of 8
     (dict(n_cell=4), ns.NS_ERR_ARG),                  # too small for the box layout
+    # multiple of 8, but the hierarchy stops at 202 (808 -> 404 -> 202): too large for the bottom block
+    (dict(n_cell=808), ns.NS_ERR_UNSUPPORTED),
+    (dict(dim=3, n_cell=104), ns.NS_ERR_UNSUPPORTED),  # 104 -> 52 -> 26 > 24
     (dict(ren=0.0), ns.NS_ERR_ARG),
+    (dict(ren=float("nan")), ns.NS_ERR_ARG),
+    (dict(dc_residual=2), ns.NS_ERR_ARG),
+    (dict(dim=3, n_cell=16, dc_residual=1), ns.NS_ERR_UNSUPPORTED),
     (dict(dim=4), ns.NS_ERR_UNSUPPORTED),
     # periodic on one side only: the reference makes a direction periodic only when both
     # codes are 111 (main.cpp:160-162) yet gives the 111 side an interior BC type
