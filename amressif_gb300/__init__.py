@@ -41,7 +41,7 @@ EXPORTS = [
     "ns_poisson_rhs_noalloc",
     "ns_adjoint_opts_default", "ns_set_controls", "ns_step_adjoint_fwd", "ns_step_adjoint_bwd",
     "ns_adjoint_get_state_grad", "ns_step_jvp", "ns_step_vjp", "ns_adjoint_op",
-    "ns_checkpoint_get", "ns_checkpoint_put", "ns_get_step",
+    "ns_checkpoint_get", "ns_checkpoint_put", "ns_get_step", "ns_get_cell_velocity",
 ]
 
 
@@ -211,6 +211,7 @@ def lib():
         L.ns_adjoint_op.argtypes = [vp, ctypes.c_int, P(dp), dp, P(dp), dp]
         L.ns_checkpoint_get.argtypes = [vp, P(dp), P(dp), dp, dp, P(ctypes.c_longlong)]
         L.ns_checkpoint_put.argtypes = [vp, P(dp), P(dp), dp, ctypes.c_double, ctypes.c_longlong]
+        L.ns_get_cell_velocity.argtypes = [vp, P(dp)]
         L.ns_get_step.argtypes = [vp]
         L.ns_get_step.restype = ctypes.c_longlong
         _lib = L
@@ -322,20 +323,26 @@ class Solver:
         self._check(lib().ns_get_state(self.h, au, aup, _dp(p), _dp(phi)), "ns_get_state")
         return u, up, p, phi
 
+    @staticmethod
+    def _box(arr):
+        """(lo, hi, jstride, kstride) of a whole dense array (x fastest)."""
+        sh = arr.shape
+        lo = (ctypes.c_int * 3)(0, 0, 0)
+        hi = (ctypes.c_int * 3)(sh[-1] - 1, sh[-2] - 1, sh[-3] - 1 if arr.ndim == 3 else 0)
+        return lo, hi, sh[-1], sh[-1] * sh[-2] if arr.ndim == 3 else 0
+
     def put_field(self, field, comp, arr):
         arr = np.ascontiguousarray(arr, dtype=np.float64)
-        lo = (ctypes.c_int * 3)(0, 0, 0)
-        hi = (ctypes.c_int * 3)(arr.shape[1] - 1, arr.shape[0] - 1, 0)
-        self._check(lib().ns_put_box(self.h, field, comp, _dp(arr), lo, hi, arr.shape[1], 0, 0), "ns_put_box")
+        lo, hi, js, ks = self._box(arr)
+        self._check(lib().ns_put_box(self.h, field, comp, _dp(arr), lo, hi, js, ks, 0), "ns_put_box")
 
     def get_field(self, field, comp=0):
         if field in (FIELD_VEL, FIELD_VEL_PREV, FIELD_VEL_STAR):
             out = np.zeros(self.face_shape(comp))
         else:
-            out = np.zeros((self.n, self.n))
-        lo = (ctypes.c_int * 3)(0, 0, 0)
-        hi = (ctypes.c_int * 3)(out.shape[1] - 1, out.shape[0] - 1, 0)
-        self._check(lib().ns_get_box(self.h, field, comp, _dp(out), lo, hi, out.shape[1], 0, 0), "ns_get_box")
+            out = np.zeros(self.cell_shape())
+        lo, hi, js, ks = self._box(out)
+        self._check(lib().ns_get_box(self.h, field, comp, _dp(out), lo, hi, js, ks, 0), "ns_get_box")
         return out
 
     def step(self, allow_warn=True):
@@ -416,6 +423,12 @@ class Solver:
         self._check(lib().ns_checkpoint_get(self.h, self._vec(u), self._vec(up), _dp(p), ctypes.byref(t), ctypes.byref(k)),
                     "ns_checkpoint_get")
         return u, up, p, t.value, k.value
+
+    def cell_velocity(self):
+        """velCart (the face averages of u^n) from the device, one cell array per component"""
+        out = [np.zeros(self.cell_shape()) for _ in range(self.dim)]
+        self._check(lib().ns_get_cell_velocity(self.h, self._vec(out)), "ns_get_cell_velocity")
+        return out
 
     def checkpoint_put(self, u, u_prev, p, time, step):
         u = [np.ascontiguousarray(a, dtype=np.float64) for a in u]

@@ -105,6 +105,8 @@ struct ns_ctx {
   double* gm_part = nullptr;
   double* gm_dev = nullptr;   // device scalars: dot products, coefficients
   double* gm_host = nullptr;  // pinned mirror
+  // cell-velocity output of ns_get_cell_velocity (lazily allocated)
+  double* cell_tmp = nullptr;
   // lid profile (one value per cell column) when controls are set
   double* lid_col = nullptr;
   int nseg = 0;
@@ -133,6 +135,13 @@ void free3d(ns_ctx* c);
 int set_state3d(ns_ctx* c, const double* const* u, const double* const* up, const double* p, double time);
 int get_state3d(ns_ctx* c, double* const* u, double* const* up, double* p, double* phi);
 int step3d(ns_ctx* c, ns_step_stats* s);
+// the per-call-site building blocks of a 3D context
+int step_begin3d(ns_ctx* c);
+int rk_stage3d(ns_ctx* c, int sub);
+int pseudo_norm3d(ns_ctx* c, double* norm);
+int poisson_rhs3d(ns_ctx* c, double* divmax, double* sum);
+int poisson_solve3d(ns_ctx* c, int precision, int* cycles, double* res);
+int project3d(ns_ctx* c, double* divmax);
 // device array of an NS_FIELD_* of a 3D context (nullptr if the field has no
 // 3D array); *is_face tells whether it is a face field of direction comp
 double* field_ptr3d(ns_ctx* c, int field, int comp, bool* is_face);

@@ -169,4 +169,25 @@ cudaError_t launch_dc_update(const DCArgs& a, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+// velCart of cont2cart (utilities.cpp:49-53) without ghosts: component d of
+// the cell velocity, 0.5 (u_d(c) + u_d(c + e_d)), for 2D (plane = 0, one k)
+// and 3D grids of the shared face / cell index map
+__global__ void __launch_bounds__(256) k_cell_velocity(const double* u, double* out, int n, long pitch, long plane,
+                                                      int d, int nk) {
+  const int i = blockIdx.x * 32 + (threadIdx.x & 31);
+  const int j = blockIdx.y * 8 + (threadIdx.x >> 5);
+  const int k = blockIdx.z;
+  if (i >= n || j >= n || k >= nk) return;
+  const long id = (long)k * plane + (long)j * pitch + i;
+  const long st = d == 0 ? 1 : (d == 1 ? pitch : plane);
+  out[id] = 0.5 * (u[id] + u[id + st]);
+}
+
+cudaError_t launch_cell_velocity(const double* u, double* out, int n, long pitch, long plane, int d, int dim,
+                                 cudaStream_t s) {
+  const int nk = dim == 3 ? n : 1;
+  k_cell_velocity<<<dim3((n + 31) / 32, (n + 7) / 8, nk), 256, 0, s>>>(u, out, n, pitch, plane, d, nk);
+  return cudaGetLastError();
+}
+
 }  // namespace ns

@@ -98,5 +98,8 @@ struct DCArgs {
   double* red_out;     // {max |r|}
 };
 cudaError_t launch_dc_update(const DCArgs& a, cudaStream_t s);
+// the cell velocity (face average) of component d, 2D or 3D index map
+cudaError_t launch_cell_velocity(const double* u, double* out, int n, long pitch, long plane, int d, int dim,
+                                 cudaStream_t s);
 
 }  // namespace ns

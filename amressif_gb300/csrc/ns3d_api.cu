@@ -1,8 +1,10 @@
 // Host driver of the 3D advance (dim = 3): the time loop of main_main
 // (main.cpp:875-1180) over the kernels of ns3d.cuh (FP64 predictor) and
 // ns3d_mixed.cuh (mixed-precision predictor). The 3D context supports the
-// whole-step API (ns_step, ns_set_state / ns_get_state, checkpoints) and the
-// adjoint (adjoint3d_api.cu); the per-call-site building blocks are 2D only.
+// whole-step API (ns_step, ns_set_state / ns_get_state, checkpoints), the
+// per-call-site building blocks (step begin, FP64 RK stage, pseudo-norm,
+// Poisson right-hand side and solve, projection; the explicit predictor is
+// not built in 3D), the box transfers and the adjoint (adjoint3d_api.cu).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -161,7 +163,7 @@ __global__ void k3_set_mean(double* red, double inv_n) { red[kRedMean] = red[kRe
 
 // phi solves L phi = f - mean(f) to poisson_tol_rel (and the divergence
 // tolerance); FP64 V-cycles, or FP32 V-cycles inside an FP64 defect correction
-int poisson3(ns_ctx* c, int* cycles, double* res, long long* fallbacks) {
+int poisson3(ns_ctx* c, bool mixed, int* cycles, double* res, long long* fallbacks) {
   State3D& S = *c->s3;
   const double n3 = (double)c->N * c->N * c->N;
   LAUNCH(NS_PROF_OTHER, "set mean", (k3_set_mean<<<1, 1, 0, c->st>>>(c->red, 1.0 / n3), cudaGetLastError()));
@@ -169,7 +171,6 @@ int poisson3(ns_ctx* c, int* cycles, double* res, long long* fallbacks) {
   S.M64.f[0] = S.F;
   S.M64.fmean = c->red + kRedMean;
   CK(cudaMemsetAsync(S.PHI, 0, S.fb, c->st), "memset phi");
-  const bool mixed = c->P.precision == NS_PREC_MIXED;
   const int maxc = std::max(1, c->P.poisson_max_cycles);
   const double div_tol_res = c->P.poisson_tol_div > 0 ? c->P.poisson_tol_div * 1.5 / c->dt : 0.0;
   // mixed: phi as float-float pairs in PHF[pf]; each sweep adds the FP32
@@ -361,7 +362,7 @@ double* field_ptr3d(ns_ctx* c, int field, int comp, bool* is_face) {
 
 int poisson3d(ns_ctx* c, int* cycles, double* res) {
   long long fb = 0;
-  return poisson3(c, cycles, res, &fb);
+  return poisson3(c, c->P.precision == NS_PREC_MIXED, cycles, res, &fb);
 }
 
 }  // namespace nsh
@@ -516,12 +517,15 @@ int mixed_finalize3(ns_ctx* c) {
 
 namespace nsh {
 
-// step begin and the dual-time pseudo-iterations: u* in face3(c, S.cur); the
-// state (U, UP, time) is rotated as in ns_step_begin
-int predictor3d(ns_ctx* c, ns_step_stats* sp) {
+// ---- the per-call-site building blocks in 3D (the 2D entry points dispatch
+// here). The RK stage is the FP64 stage of the context's own predictor (three
+// passes: ghosted cell velocity, fluxes and totals, face update with the
+// pseudo-norm), so a step assembled from the blocks equals ns_step in FP64.
+
+// main.cpp:879-887: du, S from (u^n, u^{n-1}, p); the u^{n-1} buffer becomes
+// the target of the projection
+int step_begin3d(ns_ctx* c) {
   State3D& S = *c->s3;
-  ns_step_stats& s = *sp;
-  // ---- step begin: du, S from (u^n, u^{n-1}, p); u^{n-1} buffer becomes the target
   Arg3 a = args(c);
   for (int m = 0; m < 3; ++m) {
     a.un[m] = S.U[m];
@@ -534,6 +538,102 @@ int predictor3d(ns_ctx* c, ns_step_stats* sp) {
   for (int m = 0; m < 3; ++m) std::swap(S.U[m], S.UP[m]);
   c->time += c->dt;
   S.base = S.cur = -1;
+  c->in_step = true;
+  c->norm_ready = false;
+  return NS_OK;
+}
+
+// main.cpp:931-1017, one RK pseudo-stage (FP64)
+int rk_stage3d(ns_ctx* c, int sub) {
+  State3D& S = *c->s3;
+  const int outb = pick3(S.base, S.cur);
+  Arg3 b = args(c);
+  for (int m = 0; m < 3; ++m) {
+    b.u[m] = face3(c, S.cur, m);
+    b.ub[m] = face3(c, S.base, m);
+    b.S[m] = S.S[m];
+    b.out[m] = S.B[outb][m];
+  }
+  b.rk = c->rk[sub];
+  b.do_norm = (sub == 3);
+  b.red_out = c->red + kRedNorm;
+  LAUNCH(NS_PROF_STAGE_FAST, "cart 3d", launch3_cart(b, c->st));
+  LAUNCH(NS_PROF_STAGE_FAST, "total 3d", launch3_total(b, c->st));
+  LAUNCH(NS_PROF_STAGE_FAST, "face 3d", launch3_face(b, c->st));
+  S.cur = outb;
+  if (sub == 3) c->norm_ready = true;
+  return NS_OK;
+}
+
+// Error_Computation and velCont <- velStar (main.cpp:1019-1026)
+int pseudo_norm3d(ns_ctx* c, double* norm) {
+  State3D& S = *c->s3;
+  int r = sync_red(c, kRedNorm, 1);
+  if (r != NS_OK) return r;
+  if (norm) *norm = c->red_h[kRedNorm];
+  S.base = S.cur;
+  c->norm_ready = false;
+  return NS_OK;
+}
+
+// poisson_righthand_side_calc (fn_rhs.cpp:71-125) on u*
+int poisson_rhs3d(ns_ctx* c, double* divmax, double* sum) {
+  State3D& S = *c->s3;
+  Arg3 p = args(c);
+  for (int m = 0; m < 3; ++m) p.u[m] = face3(c, S.cur, m);
+  p.f = S.F;
+  p.red_out = c->red + kRedDivBefore;
+  LAUNCH(NS_PROF_POISSON_RHS, "rhs 3d", launch3_rhs(p, c->st));
+  int r = sync_red(c, kRedDivBefore, 2);
+  if (r != NS_OK) return r;
+  if (divmax) *divmax = c->red_h[kRedDivBefore];
+  if (sum) *sum = c->red_h[kRedSum];
+  return NS_OK;
+}
+
+// poisson_advance (poisson.cpp:41-186): FP64 V-cycles, or (NS_PREC_MIXED in a
+// mixed context) FP32 V-cycles inside the float-float defect correction
+int poisson_solve3d(ns_ctx* c, int precision, int* cycles, double* res) {
+  State3D& S = *c->s3;
+  const bool mixed = precision == NS_PREC_MIXED && S.M32.L > 0;
+  long long fb = 0;
+  int cyc = 0;
+  double rr = 0.0;
+  const int r = poisson3(c, mixed, &cyc, &rr, &fb);
+  if (cycles) *cycles = cyc;
+  if (res) *res = rr;
+  return r;
+}
+
+// main.cpp:1078-1164 (phi ghosts, update_solution) + the divergence check of
+// main.cpp:1180
+int project3d(ns_ctx* c, double* divmax) {
+  State3D& S = *c->s3;
+  Arg3 p = args(c);
+  for (int m = 0; m < 3; ++m) {
+    p.u[m] = face3(c, S.cur, m);
+    p.out[m] = S.U[m];
+  }
+  p.p = S.Pp;
+  p.pw = S.Pp;
+  p.phi = S.PHI;
+  p.red_out = c->red + kRedDivAfter;
+  LAUNCH(NS_PROF_PROJECT, "project 3d", launch3_project(p, c->st));
+  LAUNCH(NS_PROF_PROJECT, "div 3d", launch3_div(p, c->st));
+  int r = sync_red(c, kRedDivAfter, 1);
+  if (r != NS_OK) return r;
+  if (divmax) *divmax = c->red_h[kRedDivAfter];
+  c->in_step = false;
+  return NS_OK;
+}
+
+// step begin and the dual-time pseudo-iterations: u* in face3(c, S.cur); the
+// state (U, UP, time) is rotated as in ns_step_begin
+int predictor3d(ns_ctx* c, ns_step_stats* sp) {
+  State3D& S = *c->s3;
+  ns_step_stats& s = *sp;
+  int r = step_begin3d(c);
+  if (r != NS_OK) return r;
   // ---- dual-time pseudo-iterations (main.cpp:898-1040)
   const bool mixed = c->P.precision == NS_PREC_MIXED;
   S.bf = -1;
@@ -543,33 +643,22 @@ int predictor3d(ns_ctx* c, ns_step_stats* sp) {
   double norm = 1.e9;
   while (norm > c->P.momentum_tolerance) {
     if (mixed) {
-      int r = mixed_iteration3(c);
+      r = mixed_iteration3(c);
       if (r != NS_OK) return r;
-    } else for (int sub = 0; sub < 4; ++sub) {
-      const int outb = pick3(S.base, S.cur);
-      Arg3 b = args(c);
-      for (int m = 0; m < 3; ++m) {
-        b.u[m] = face3(c, S.cur, m);
-        b.ub[m] = face3(c, S.base, m);
-        b.S[m] = S.S[m];
-        b.out[m] = S.B[outb][m];
-      }
-      b.rk = c->rk[sub];
-      b.do_norm = (sub == 3);
-      b.red_out = c->red + kRedNorm;
-      LAUNCH(NS_PROF_STAGE_FAST, "cart 3d", launch3_cart(b, c->st));
-      LAUNCH(NS_PROF_STAGE_FAST, "total 3d", launch3_total(b, c->st));
-      LAUNCH(NS_PROF_STAGE_FAST, "face 3d", launch3_face(b, c->st));
-      S.cur = outb;
-    }
-    int r = sync_red(c, kRedNorm, 1);
-    if (r != NS_OK) return r;
-    norm = c->red_h[kRedNorm];
-    if (mixed) {
+      r = sync_red(c, kRedNorm, 1);
+      if (r != NS_OK) return r;
+      norm = c->red_h[kRedNorm];
       S.mix_norm = norm;
       if (S.mix_exact) S.mix_norm_exact = norm;
+      S.base = S.cur;
+    } else {
+      for (int sub = 0; sub < 4; ++sub) {
+        r = rk_stage3d(c, sub);
+        if (r != NS_OK) return r;
+      }
+      r = pseudo_norm3d(c, &norm);
+      if (r != NS_OK) return r;
     }
-    S.base = S.cur;
     count++;
     if (std::isnan(norm)) return fail(c, NS_ERR_NONFINITE, "pseudo-increment norm is NaN (non-finite fields)");
     if (count > c->P.iter_num) { s.status = NS_WARN_PSEUDO_MAXITER; break; }
@@ -581,7 +670,6 @@ int predictor3d(ns_ctx* c, ns_step_stats* sp) {
 }
 
 int step3d(ns_ctx* c, ns_step_stats* stats) {
-  State3D& S = *c->s3;
   if (c->P.pseudo_timestepping == 0) return fail(c, NS_ERR_UNSUPPORTED, "3D: the explicit predictor is not built");
   ns_step_stats s;
   std::memset(&s, 0, sizeof(s));
@@ -590,31 +678,16 @@ int step3d(ns_ctx* c, ns_step_stats* stats) {
   if (r != NS_OK) return r;
   if (c->ev_ok) cudaEventRecord(c->ev[1], c->st);
   // ---- Poisson right-hand side, solve, projection
-  Arg3 p = args(c);
-  for (int m = 0; m < 3; ++m) p.u[m] = face3(c, S.cur, m);
-  p.f = S.F;
-  p.red_out = c->red + kRedDivBefore;
-  LAUNCH(NS_PROF_POISSON_RHS, "rhs 3d", launch3_rhs(p, c->st));
-  r = sync_red(c, kRedDivBefore, 2);
+  r = poisson_rhs3d(c, &s.div_before, &s.rhs_sum);
   if (r != NS_OK) return r;
-  s.div_before = c->red_h[kRedDivBefore];
-  s.rhs_sum = c->red_h[kRedSum];
   if (!std::isfinite(s.div_before) || !std::isfinite(s.rhs_sum))
     return fail(c, NS_ERR_NONFINITE, "Poisson right-hand side is not finite");
   long long fb = 0;
-  const int mg = poisson3(c, &s.poisson_cycles, &s.poisson_res, &fb);
+  const int mg = poisson3(c, c->P.precision == NS_PREC_MIXED, &s.poisson_cycles, &s.poisson_res, &fb);
   if (mg != NS_OK && mg != NS_ERR_MG_STALL) return mg;
   if (c->ev_ok) cudaEventRecord(c->ev[2], c->st);
-  for (int m = 0; m < 3; ++m) p.out[m] = S.U[m];
-  p.p = S.Pp;
-  p.pw = S.Pp;
-  p.phi = S.PHI;
-  p.red_out = c->red + kRedDivAfter;
-  LAUNCH(NS_PROF_PROJECT, "project 3d", launch3_project(p, c->st));
-  LAUNCH(NS_PROF_PROJECT, "div 3d", launch3_div(p, c->st));
-  r = sync_red(c, kRedDivAfter, 1);
+  r = project3d(c, &s.div_after);
   if (r != NS_OK) return r;
-  s.div_after = c->red_h[kRedDivAfter];
   c->step++;
   if (c->ev_ok) {
     cudaEventRecord(c->ev[3], c->st);

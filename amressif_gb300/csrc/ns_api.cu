@@ -120,6 +120,7 @@ void free_all(ns_ctx* c) {
   F(c->FFh); F(c->FFl);
   F(c->Pp); F(c->F);
   F(c->lid_col);
+  F(c->cell_tmp);
   free3d(c);
   for (double* v : c->gm_v) F(v);
   F(c->gm_w); F(c->gm_z); F(c->gm_b); F(c->gm_part); F(c->gm_dev);
@@ -615,7 +616,7 @@ int ns_init_fields(ns_ctx* c, int init_case) {
 
 int ns_step_begin(ns_ctx* c) {
   if (!c) return NS_ERR_ARG;
-  if (c->P.dim == 3) return fail(c, NS_ERR_UNSUPPORTED, "building blocks are 2D only: use ns_step in 3D");
+  if (c->P.dim == 3) return step_begin3d(c);
   ProjArgs a;
   std::memset(&a, 0, sizeof(a));
   a.g = c->g;
@@ -663,8 +664,8 @@ static int launch_rk(ns_ctx* c, int sub, bool use_cart) {
 
 int ns_rk_stage(ns_ctx* c, int sub) {
   if (!c || sub < 0 || sub > 3) return NS_ERR_ARG;
-  if (c->P.dim == 3) return fail(c, NS_ERR_UNSUPPORTED, "building blocks are 2D only: use ns_step in 3D");
   if (!c->in_step) return fail(c, NS_ERR_STATE, "ns_rk_stage before ns_step_begin");
+  if (c->P.dim == 3) return rk_stage3d(c, sub);
   const bool use_cart = c->cart_pending;
   int r = launch_rk(c, sub, use_cart);
   if (r == NS_OK && use_cart) c->cart_pending = false;
@@ -674,8 +675,8 @@ int ns_rk_stage(ns_ctx* c, int sub) {
 
 int ns_pseudo_norm(ns_ctx* c, double* norm) {
   if (!c) return NS_ERR_ARG;
-  if (c->P.dim == 3) return fail(c, NS_ERR_UNSUPPORTED, "building blocks are 2D only: use ns_step in 3D");
   if (!c->norm_ready) return fail(c, NS_ERR_STATE, "ns_pseudo_norm needs stage 3 first");
+  if (c->P.dim == 3) return pseudo_norm3d(c, norm);
   int r = sync_red(c, kRedNorm, 1);
   if (r != NS_OK) return r;
   if (norm) *norm = c->red_h[kRedNorm];
@@ -686,7 +687,7 @@ int ns_pseudo_norm(ns_ctx* c, double* norm) {
 
 int ns_explicit_predictor(ns_ctx* c, double* norm) {
   if (!c) return NS_ERR_ARG;
-  if (c->P.dim == 3) return fail(c, NS_ERR_UNSUPPORTED, "building blocks are 2D only: use ns_step in 3D");
+  if (c->P.dim == 3) return fail(c, NS_ERR_UNSUPPORTED, "3D: the explicit predictor is not built");
   if (!c->in_step) return fail(c, NS_ERR_STATE, "explicit predictor before ns_step_begin");
   const int in = c->cur;
   const int outb = pick_out(c->base, in);
@@ -724,7 +725,7 @@ static int poisson_rhs_async(ns_ctx* c) {
 
 int ns_poisson_rhs(ns_ctx* c, double* divmax, double* sum) {
   if (!c) return NS_ERR_ARG;
-  if (c->P.dim == 3) return fail(c, NS_ERR_UNSUPPORTED, "building blocks are 2D only: use ns_step in 3D");
+  if (c->P.dim == 3) return poisson_rhs3d(c, divmax, sum);
   int r = poisson_rhs_async(c);
   if (r == NS_OK) r = sync_red(c, kRedDivBefore, 2);
   if (r != NS_OK) return r;
@@ -965,7 +966,7 @@ static void split_const(double x, float* out);
 
 int ns_poisson_solve(ns_ctx* c, int precision, int* cycles, double* res) {
   if (!c) return NS_ERR_ARG;
-  if (c->P.dim == 3) return fail(c, NS_ERR_UNSUPPORTED, "building blocks are 2D only: use ns_step in 3D");
+  if (c->P.dim == 3) return poisson_solve3d(c, precision, cycles, res);
   const double nn = (double)c->N * (double)c->N;
   LAUNCH(NS_PROF_OTHER, "set mean", (k_set_mean<<<1, 1, 0, c->st>>>(c->red, 1.0 / nn), cudaGetLastError()));
   const int maxc = std::max(1, c->P.poisson_max_cycles);
@@ -1133,7 +1134,7 @@ static int project_async(ns_ctx* c) {
 
 int ns_project(ns_ctx* c, double* divmax) {
   if (!c) return NS_ERR_ARG;
-  if (c->P.dim == 3) return fail(c, NS_ERR_UNSUPPORTED, "building blocks are 2D only: use ns_step in 3D");
+  if (c->P.dim == 3) return project3d(c, divmax);
   int r = project_async(c);
   if (r == NS_OK) r = sync_red(c, kRedDivAfter, 1);
   if (r != NS_OK) return r;
@@ -1388,6 +1389,31 @@ int ns_step(ns_ctx* c, ns_step_stats* stats) {
   if (stats) *stats = s;
   if (mg_status != NS_OK) return mg_status;
   return s.status;
+}
+
+int ns_get_cell_velocity(ns_ctx* c, double* const* cart) {
+  if (!c || !cart) return NS_ERR_ARG;
+  if (c->in_step) return fail(c, NS_ERR_STATE, "cell velocity inside a step");
+  const int D = c->P.dim;
+  for (int d = 0; d < D; ++d)
+    if (!cart[d]) return NS_ERR_ARG;
+  if (!c->cell_tmp) {
+    if (cudaMalloc(&c->cell_tmp, c->fbytes) != cudaSuccess) return fail(c, NS_ERR_NOMEM, "cudaMalloc failed");
+  }
+  const int N = c->N;
+  const long plane = D == 3 ? (long)c->pitch * (N + 1) : 0;
+  for (int d = 0; d < D; ++d) {
+    bool face = false;
+    const double* u = D == 3 ? field_ptr3d(c, NS_FIELD_VEL, d, &face) : c->U[d];
+    LAUNCH(NS_PROF_OTHER, "cell velocity", launch_cell_velocity(u, c->cell_tmp, N, c->pitch, plane, d, D, c->st));
+    // the dense host copy: N planes (3D) of N rows of N values
+    for (int k = 0; k < (D == 3 ? N : 1); ++k)
+      CK(cudaMemcpy2DAsync(cart[d] + (size_t)k * N * N, (size_t)N * sizeof(double), c->cell_tmp + k * plane,
+                           (size_t)c->pitch * sizeof(double), (size_t)N * sizeof(double), (size_t)N,
+                           cudaMemcpyDeviceToHost, c->st),
+         "cell velocity copy");
+  }
+  return ns_sync(c);
 }
 
 int ns_checkpoint_get(ns_ctx* c, double* const* u, double* const* u_prev, double* p, double* time, long long* step) {

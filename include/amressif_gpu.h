@@ -162,6 +162,12 @@ int ns_checkpoint_put(ns_ctx* c, const double* const* u, const double* const* u_
                       long long step);
 long long ns_get_step(const ns_ctx* c);
 
+/* The cell-centred velocity velCart that Export_Flow_Field plots
+ * (utilities.cpp:534-570): the face averages of cont2cart
+ * (utilities.cpp:49-53) of the current u^n, computed on the device. cart[d]
+ * (d < dim) are dense host arrays of n_cell^dim values, x fastest. */
+int ns_get_cell_velocity(ns_ctx* c, double* const* cart);
+
 /* ---- building blocks, one per reference call site ------------------------ */
 int ns_step_begin(ns_ctx* c);                              /* main.cpp:879-887 */
 int ns_rk_stage(ns_ctx* c, int sub);                       /* main.cpp:931-1017 (fused) */

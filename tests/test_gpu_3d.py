@@ -118,9 +118,67 @@ def test_3d_mixed_predictor_matches_fp64(gpu_lib, name):
     assert relp(pb, pa) <= 1e-11, relp(pb, pa)
 
 
-def test_3d_building_blocks_are_2d_only(gpu_lib):
-    p = ns.default_params(dim=3, n_cell=16, fixed_dt=1e-3)
-    s = ns.Solver(p)
-    s.init(ns.INIT_CAVITY)
+@pytest.mark.parametrize("name", sorted(CASES3))
+def test_3d_building_blocks(gpu_lib, oracle_lib, name):
+    """The per-call-site entry points on a 3D context (main.cpp:879-1180):
+    the RK stages against the oracle's 3D stages (the GPU's FP64 stage uses
+    FMA, so agreement is to round-off, 1e-13 relative), the pseudo-norm, the
+    Poisson right-hand side, solve and projection against the oracle's
+    (1e-10); and a step assembled from the blocks equal, bit for bit, to
+    ns_step on another context from the same state."""
+    from oracle.orc import FIELD_PRHS, FIELD_STAR, Oracle
+
+    n, kw, tgv = CASES3[name]
+    dt = dt_of(n, kw)
+    o = Oracle(n, dim=3, dt=dt, iter_num=100, poisson_tol=1e-13, max_grid_size=(n, n, n), **kw)
+    mk = lambda: ns.Solver(ns.default_params(dim=3, n_cell=n, fixed_dt=dt, iter_num=100, precision=ns.PREC_FP64,
+                                             poisson_tol_rel=1e-13, max_grid_size=(n, n, n), **kw))
+    s, t = mk(), mk()
+    u, up, pp = state3(n, tgv)
+    o.set_state(u, up, pp)
+    o.step()
+    uo, upo, po, _ = o.get_state()
+    for x in (o, s, t):
+        x.set_state(uo, upo, po)
+    o.step_begin()
+    s.step_begin()
+    K = 0
+    while True:
+        for sub in range(4):
+            o.rk_stage(sub)
+            s.rk_stage(sub)
+        if K == 0:
+            for d in range(3):
+                assert rel(s.get_field(ns.FIELD_VEL_STAR, d), o.field(FIELD_STAR, d)) <= 1e-13
+        eo, eg = o.pseudo_norm(), s.pseudo_norm()
+        assert abs(eg - eo) <= 1e-9 * eo, (K, eg, eo)
+        K += 1
+        if eo <= 1e-10 or K > 100:
+            break
+    assert eg <= 1e-10
+    do, so_ = o.poisson_rhs()
+    dg, sg = s.poisson_rhs()
+    assert abs(dg - do) <= 1e-10 * abs(do)
+    assert rel(s.get_field(ns.FIELD_POISSON_RHS), o.field(FIELD_PRHS)) <= 1e-10
+    o.poisson_solve()
+    cyc, res = s.poisson_solve(ns.PREC_FP64)
+    assert res <= 1e-13 and cyc >= 1
+    o.project()
+    dag = s.project()
+    ug, _, pg, _ = s.get_state()
+    uo, _, po, _ = o.get_state()
+    for d in range(3):
+        assert rel(ug[d], uo[d]) <= 1e-10, (d, rel(ug[d], uo[d]))
+    assert relp(pg, po) <= 1e-10
+    if kw.get("fix_quirks") or not tgv:
+        assert dag <= 1e-10
+    # the same step through ns_step
+    st = t.step()
+    assert st["pseudo_iters"] == K
+    ut, _, pt, _ = t.get_state()
+    for d in range(3):
+        np.testing.assert_array_equal(ug[d], ut[d])
+    np.testing.assert_array_equal(pg, pt)
     with pytest.raises(ns.NsError):
-        s.step_begin()
+        s.explicit_predictor()  # not built in 3D
+    o.close()
