@@ -355,10 +355,8 @@ class Solver:
 
     def step_host(self, u, u_prev, p):
         """End-to-end step from/to host arrays (modified in place)."""
-        au = (ctypes.POINTER(ctypes.c_double) * 2)(*[_dp(a) for a in u])
-        aup = (ctypes.POINTER(ctypes.c_double) * 2)(*[_dp(a) for a in u_prev])
         st = NsStepStats()
-        rc = lib().ns_step_host(self.h, au, aup, _dp(p), ctypes.byref(st))
+        rc = lib().ns_step_host(self.h, self._vec(u), self._vec(u_prev), _dp(p), ctypes.byref(st))
         self._check(rc, "ns_step_host", allow_warn=True)
         return stats_dict(st)
 

@@ -14,7 +14,9 @@
 namespace ns {
 
 constexpr int kAncOut = 26;    // output columns per warp (lanes 3..28; 3 halo lanes each side)
-constexpr int kAncH = 40;      // rows per strip (a 4096^2 sweep of 16..128 rows peaked at 40)
+// rows per strip (passed as A.rows; a 4096^2 sweep of 16..128 rows peaked at
+// 40; one-wave strips of 274 rows took a launch from 0.615 to 0.731 ms)
+constexpr int kAncH = 40;
 constexpr int kAncRing = 4;    // rows in flight per warp (6, 4 and 3 rows: 0.626, 0.620, 0.619 ms a launch at 4096^2)
 constexpr int kAncWords = 16;  // words per lane and row in the ring
 
@@ -42,11 +44,12 @@ __global__ void __launch_bounds__(NT) k_anchor_col2d(AnchorFFArgs A) {
   const long P = g.pitch;
   const int lane = threadIdx.x & 31;
   const int nsx = (N + 1 + kAncOut - 1) / kAncOut;
-  const int nsy = (N + kAncH - 1) / kAncH;
+  const int H = A.rows;
+  const int nsy = (N + H - 1) / H;
   const int gw = blockIdx.x * (NT / 32) + (threadIdx.x >> 5);
   if (gw >= nsx * nsy) return;  // warp-uniform; no block-wide barrier below
   const int sx = gw % nsx, sy = gw / nsx;
-  const int xs = sx * kAncOut, ys = sy * kAncH;
+  const int xs = sx * kAncOut, ys = sy * H;
   const int i = xs - 3 + lane;
   const bool perx = g.periodic[0], pery = g.periodic[1];
   const bool has_e = A.e4[0] != nullptr;
@@ -147,7 +150,7 @@ __global__ void __launch_bounds__(NT) k_anchor_col2d(AnchorFFArgs A) {
     }
   };
 
-  const int r_first = ys - 2, r_last = (ys + kAncH >= N) ? N : ys + kAncH - 1;
+  const int r_first = ys - 2, r_last = (ys + H >= N) ? N : ys + H - 1;
   k_next = r_first - 2;
   k_end = r_last + 2;
   for (int q = 0; q < kAncRing; ++q) {

@@ -27,6 +27,7 @@ struct AnchorFFArgs {
   float* g0[2];         // G(u_base) rounded to FP32
   // constants as float-float (hi, lo) pairs
   float inv_dx[2][2], vcoef[2][2], c15[2];
+  int rows;             // rows per strip of the column-marching kernel (set by its launcher)
 };
 
 __device__ __forceinline__ ff anchor_u(const AnchorFFArgs& A, int m, long id) {

@@ -105,6 +105,12 @@ struct ns_ctx {
   double* gm_part = nullptr;
   double* gm_dev = nullptr;   // device scalars: dot products, coefficients
   double* gm_host = nullptr;  // pinned mirror
+  // ns_step_host: a second stream that copies u_prev back while the step
+  // runs (the buffer holds the step's input u^n, unchanged by the step), and
+  // the host destinations of that copy, set only for the duration of the call
+  cudaStream_t side = nullptr;
+  cudaEvent_t side_ev[2] = {nullptr, nullptr};
+  double* const* early_uprev = nullptr;
   // cell-velocity output of ns_get_cell_velocity (lazily allocated)
   double* cell_tmp = nullptr;
   // lid profile (one value per cell column) when controls are set

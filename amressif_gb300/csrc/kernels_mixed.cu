@@ -14,10 +14,12 @@ namespace ns {
 // a cp.async ring of raw face rows per warp in shared memory; the incremental
 // anchor update (obh set) also writes the new float-float base
 template <bool BASE>
-static cudaError_t launch_inc_t(const IncArgs& a, cudaStream_t s) {
+static cudaError_t launch_inc_t(const IncArgs& a0, cudaStream_t s) {
   constexpr int NT = 128;
+  IncArgs a = a0;
+  a.rows = kIncH;
   const int N = a.g.N;
-  const long warps = (long)((N + 1 + kIncOut - 1) / kIncOut) * ((N + kIncH - 1) / kIncH);
+  const long warps = (long)((N + 1 + kIncOut - 1) / kIncOut) * ((N + a.rows - 1) / a.rows);
   const unsigned blocks = (unsigned)((warps + NT / 32 - 1) / (NT / 32));
   constexpr size_t smem = inc_col_smem<NT, BASE>();
   static bool attr = false;
@@ -40,12 +42,14 @@ cudaError_t launch_inc_stage(const IncArgs& a, cudaStream_t s) {
   return launch_inc_t<false>(a, s);
 }
 
-// column-marching float-float anchor: one warp per 26-column x 64-row strip,
+// column-marching float-float anchor: one warp per 26-column x kAncH-row strip,
 // a cp.async ring of raw face rows per warp in shared memory
-cudaError_t launch_anchor_ff(const AnchorFFArgs& a, cudaStream_t s) {
+cudaError_t launch_anchor_ff(const AnchorFFArgs& a0, cudaStream_t s) {
   constexpr int NT = 128;
+  AnchorFFArgs a = a0;
+  a.rows = kAncH;
   const int N = a.g.N;
-  const long warps = (long)((N + 1 + kAncOut - 1) / kAncOut) * ((N + kAncH - 1) / kAncH);
+  const long warps = (long)((N + 1 + kAncOut - 1) / kAncOut) * ((N + a.rows - 1) / a.rows);
   const unsigned blocks = (unsigned)((warps + NT / 32 - 1) / (NT / 32));
   constexpr size_t smem = anchor_col_smem<NT>();
   static bool attr = false;

@@ -138,6 +138,9 @@ void free_all(ns_ctx* c) {
     for (auto& G : row)
       if (G.exec) cudaGraphExecDestroy(G.exec);
   if (c->own_stream && c->st) cudaStreamDestroy(c->st);
+  for (auto& e : c->side_ev)
+    if (e) cudaEventDestroy(e);
+  if (c->side) cudaStreamDestroy(c->side);
 }
 
 template <typename T>
@@ -1314,6 +1317,21 @@ int nsh::run_predictor(ns_ctx* c, ns_step_stats* sp) {
   c->mix_last_exact = 0;
   int r = ns_step_begin(c);
   if (r != NS_OK) return r;
+  if (c->early_uprev) {
+    // ns_step_host: the new u^{n-1} (UP, the step's input u^n) goes back to
+    // the host on the side stream while the predictor runs
+    CK(cudaEventRecord(c->side_ev[0], c->st), "event");
+    CK(cudaStreamWaitEvent(c->side, c->side_ev[0], 0), "stream wait");
+    const int N = c->N;
+    for (int m = 0; m < 2; ++m) {
+      const size_t w = (size_t)(N + (m == 0)) * sizeof(double), h = (size_t)(N + (m == 1));
+      CK(cudaMemcpy2DAsync(c->early_uprev[m], w, c->UP[m], c->pitch * sizeof(double), w, h, cudaMemcpyDeviceToHost,
+                           c->side),
+         "u_prev copy");
+    }
+    CK(cudaEventRecord(c->side_ev[1], c->side), "event");
+    c->early_uprev = nullptr;
+  }
   int countIter = 0;
   double normError = 1.e9;
   while (normError > c->P.momentum_tolerance) {
@@ -1445,19 +1463,38 @@ int ns_step_host(ns_ctx* c, double* const* u, double* const* u_prev, double* p, 
   if (!c || !u || !u_prev || !p) return NS_ERR_ARG;
   const double t = c->time;
   const bool two_d = c->P.dim == 2;
+  // 2D: the outgoing u_prev (the incoming u, which the step leaves in place)
+  // is copied back on a side stream while the step runs
+  bool overlap = false;
+  if (two_d) {
+    if (!c->side) {
+      if (cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess) c->side = nullptr;
+      for (auto& e : c->side_ev)
+        if (c->side && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) e = nullptr;
+    }
+    overlap = c->side && c->side_ev[0] && c->side_ev[1];
+  }
   if (c->ev_ok) cudaEventRecord(c->ev[4], c->st);
   int r = two_d ? set_state_async(c, u, u_prev, p, t) : ns_set_state(c, u, u_prev, p, t);
   if (r != NS_OK) return r;
   if (c->ev_ok) cudaEventRecord(c->ev[5], c->st);
   ns_step_stats s;
   std::memset(&s, 0, sizeof(s));
+  c->early_uprev = overlap ? u_prev : nullptr;
   const int st = ns_step(c, &s);
+  c->early_uprev = nullptr;
+  if (overlap) {
+    // the side copy was enqueued after step begin: wait for it on the host
+    // (also on the error path, before the caller may reuse u_prev)
+    const cudaError_t e = cudaEventSynchronize(c->side_ev[1]);
+    if (st >= 0 && e != cudaSuccess) return cuda_check(c, e, "u_prev copy");
+  }
   if (st < 0) {
     if (stats) *stats = s;
     return st;
   }
   if (c->ev_ok) cudaEventRecord(c->ev[6], c->st);
-  r = two_d ? get_state_async(c, u, u_prev, p, nullptr) : ns_get_state(c, u, u_prev, p, nullptr);
+  r = two_d ? get_state_async(c, u, overlap ? nullptr : u_prev, p, nullptr) : ns_get_state(c, u, u_prev, p, nullptr);
   if (r != NS_OK) return r;
   if (c->ev_ok) cudaEventRecord(c->ev[7], c->st);
   r = ns_sync(c);

@@ -38,6 +38,7 @@ struct IncArgs {
   float vcoef[2];       // 1/(ren dx^2), 1/(ren dy^2)
   float c15;            // 1.5/dt
   int do_norm;
+  int rows;             // rows per strip (set by the launcher)
   float2* part;         // float-float block partials of the norm
   unsigned* counter;
   double* norm_out;

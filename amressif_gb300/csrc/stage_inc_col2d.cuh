@@ -1,7 +1,7 @@
 // FP32 increment stage, column-marching form (2D).
 //
 // dG(u_b; e_s) with the expanded QUICK flux difference (stage_inc2d.cuh).
-// One warp owns a strip of 64 columns and kIncH rows and marches up the rows
+// One warp owns a strip of 64 columns and A.rows rows and marches up the rows
 // with a 5-row register window of cell values (u_b and e_s, both components):
 // y neighbours are registers, x neighbours warp shuffles, and the raw face
 // rows stream through the per-warp cp.async ring of col2d.cuh. One lane owns
@@ -41,7 +41,12 @@
 namespace ns {
 
 constexpr int kIncOut = 58;    // output columns per warp
-constexpr int kIncH = 24;      // rows per strip (a 4096^2 sweep of 12..56 rows peaked at 24)
+// rows per strip (the launcher passes it as A.rows). A 4096^2 sweep of 12..56
+// rows peaked at 24. Strips are numbered x fastest, so the warps resident at
+// one time work on one band of rows; strips tall enough to run in a single
+// wave (164 rows at 4096^2) spread the resident warps over the whole grid
+// and took a launch from 0.209 to 0.297 ms.
+constexpr int kIncH = 24;
 // ring words per lane and row: 8 float2 pairs and 2 singles, plus the two lo
 // pairs of the base update
 __host__ __device__ constexpr int inc_words(bool base) { return base ? 22 : 18; }
@@ -67,12 +72,13 @@ __global__ void __launch_bounds__(NT, 384 / NT) k_inc_col2d(IncArgs A) {  // 12 
   const long P = g.pitch;
   const int lane = threadIdx.x & 31;
   const int nsx = (N + 1 + kIncOut - 1) / kIncOut;
-  const int nsy = (N + kIncH - 1) / kIncH;
+  const int H = A.rows;
+  const int nsy = (N + H - 1) / H;
   const int gw = blockIdx.x * (NT / 32) + (threadIdx.x >> 5);
   float n0 = 0.f, n1 = 0.f;
   if (gw < nsx * nsy) {  // warp-uniform
     const int sx = gw % nsx, sy = gw / nsx;
-    const int xs = sx * kIncOut, ys = sy * kIncH;
+    const int xs = sx * kIncOut, ys = sy * H;
     const int a = xs - 4 + 2 * lane;  // column of slot 0; slot 1 is a + 1
     const bool perx = g.periodic[0], pery = g.periodic[1];
     const float* __restrict__ shu = A.sh[0];
@@ -207,7 +213,7 @@ __global__ void __launch_bounds__(NT, 384 / NT) k_inc_col2d(IncArgs A) {  // 12 
     ColCells2 w[5];
     float2 ufb[3], ufe[3], vlb[3], vle[3], gqu[3], gqv[3], xb, xe;
     const int r_first = ys - 2;  // fy at face ys-1, then the totals of row ys-1
-    const int r_last = (ys + kIncH >= N) ? N : ys + kIncH - 1;
+    const int r_last = (ys + H >= N) ? N : ys + H - 1;
     k_next = r_first - 2;
     k_end = r_last + 2;
     for (int q = 0; q < kIncRing; ++q) {

@@ -104,7 +104,8 @@ typedef struct ns_step_stats {
   double ms_predictor, ms_poisson, ms_project; /* device time of the phases */
   int poisson_fp64_fallback; /* mixed solve: 1 if the float-float residual floor forced FP64 sweeps */
   double ms_h2d, ms_d2h;      /* ns_step_host: device time of the host->device copies of (u, u_prev, p) and
-                                 of the device->host copies of the result (0 for ns_step) */
+                                 of the device->host copies after the step (2D: u and p; u_prev is copied
+                                 while the step runs); 0 for ns_step */
 } ns_step_stats;
 
 typedef struct ns_ctx ns_ctx;
@@ -181,7 +182,11 @@ int ns_project(ns_ctx* c, double* divmax);                 /* main.cpp:1078-1164
 int ns_step(ns_ctx* c, ns_step_stats* stats);
 
 /* End-to-end host call: upload (u, u_prev, p) from host memory, advance one
- * step, download (u, p). The arrays are dense as in ns_set_state. */
+ * step, download (u, u_prev, p); the arrays are dense as in ns_set_state and
+ * are updated in place. The copies and the step are enqueued on the context's
+ * stream without intermediate waits; in 2D the outgoing u_prev (the incoming
+ * u, which the step does not change) is copied back on a second stream while
+ * the step runs. Use pinned buffers (ns_host_alloc) for full copy speed. */
 int ns_step_host(ns_ctx* c, double* const* u, double* const* u_prev, double* p, ns_step_stats* stats);
 
 /* Synchronise the context's stream. */
