@@ -3,7 +3,9 @@
 The CUDA translation units are compiled in parallel with nvcc and linked into
 amressif_gb300/libamressif_gb300.so; kernels_exact.cu is compiled with
 -fmad=false so that its kernels round every operation separately, in the
-reference's order.
+reference's order. The same units compiled with -DNS_BOUNDS_CHECK make the
+bounds-check build libamressif_gb300_check.so (bounds.cuh), a debugging
+library that the tests load beside the normal one.
 """
 import os
 import subprocess
@@ -15,6 +17,7 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libamressif_gb300.so")
+LIB_CHECK = os.path.join(PKG, "libamressif_gb300_check.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xptxas", "-warn-spills"]
 
@@ -47,14 +50,17 @@ def _run(cmd):
     return p.stdout
 
 
-def build_cuda(verbose=False):
-    os.makedirs(BUILD, exist_ok=True)
+def build_cuda(verbose=False, checked=False):
+    """The library; checked=True: the bounds-check build."""
+    out_dir = os.path.join(BUILD, "check") if checked else BUILD
+    os.makedirs(out_dir, exist_ok=True)
     nvcc = _nvcc()
     units = [u for u in UNITS if os.path.exists(os.path.join(CSRC, u))]
+    extra = ["-DNS_BOUNDS_CHECK"] if checked else []
 
     def one(u):
-        obj = os.path.join(BUILD, u.replace(".cu", ".o"))
-        cmd = [nvcc] + ARCH + NVCC_FLAGS + UNITS[u] + ["-c", os.path.join(CSRC, u), "-o", obj]
+        obj = os.path.join(out_dir, u.replace(".cu", ".o"))
+        cmd = [nvcc] + ARCH + NVCC_FLAGS + extra + UNITS[u] + ["-c", os.path.join(CSRC, u), "-o", obj]
         out = _run(cmd)
         if verbose and out.strip():
             sys.stdout.write(out)
@@ -62,8 +68,9 @@ def build_cuda(verbose=False):
 
     with ThreadPoolExecutor(max_workers=len(units)) as ex:
         objs = list(ex.map(one, units))
-    _run([nvcc] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"])
-    return LIB
+    lib = LIB_CHECK if checked else LIB
+    _run([nvcc] + ARCH + ["-shared", "-o", lib] + objs + ["-lcudart"])
+    return lib
 
 
 def build_oracle():
@@ -76,10 +83,11 @@ def build_oracle():
 
 
 def build(verbose=False):
-    with ThreadPoolExecutor(max_workers=2) as ex:
+    with ThreadPoolExecutor(max_workers=3) as ex:
         a = ex.submit(build_cuda, verbose)
+        c = ex.submit(build_cuda, verbose, True)
         b = ex.submit(build_oracle)
-        return a.result(), b.result()
+        return a.result(), c.result(), b.result()
 
 
 if __name__ == "__main__":

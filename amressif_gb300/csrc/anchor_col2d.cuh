@@ -8,6 +8,7 @@
 // memory (kAncRing rows in flight), so the loads never stall the arithmetic.
 #pragma once
 #include "anchor_ff2d.cuh"
+#include "bounds.cuh"
 #include "ff.cuh"
 #include "col2d.cuh"
 
@@ -82,9 +83,17 @@ __global__ void __launch_bounds__(NT) k_anchor_col2d(AnchorFFArgs A) {
   auto slot_ptr = [&](int sl) { return ring + (size_t)sl * kAncWords * 32; };
   // words: 0-2 u face (ic): hi, lo, e4; 3-5 u face (ic+1); 6-8 v face (ic, kk);
   // 9-11 v face (ic, kk+1); 12-13 S_u (iface): hi, lo; 14-15 S_v (ic): hi, lo
+  unsigned long long* const chk = g.check;  // bounds-check build only (bounds.cuh)
+  (void)chk;
   auto issue_row = [&](int k, int sl) {
     const long r0 = (long)row_of(k) * P;
     float* d = slot_ptr(sl);
+    // every level-0 field is P x (N + 1) elements
+    if (!NS_BCHK(chk, r0 + ic, P, N + 1, N - 1, 21) || !NS_BCHK(chk, r0 + P + ic, P, N + 1, N, 22) ||
+        !NS_BCHK(chk, r0 + iface, P, N + 1, N, 23)) {
+      cp_async_commit();
+      return;
+    }
     cp_async4(d + 0 * 32, A.bh[0] + r0 + ic);
     cp_async4(d + 1 * 32, A.bl[0] + r0 + ic);
     cp_async4(d + 3 * 32, A.bh[0] + r0 + ic + 1);
@@ -112,6 +121,7 @@ __global__ void __launch_bounds__(NT) k_anchor_col2d(AnchorFFArgs A) {
     return u;
   };
   auto ubase_direct = [&](int m, long id) {
+    if (!NS_BCHK(chk, id, P, N + 1, N, 24)) return ff_make(0.f, 0.f);
     ff u = ff_make(A.bh[m][id], A.bl[m][id]);
     if (has_e) u = ff_add_f(u, A.e4[m][id]);
     return u;
@@ -193,7 +203,7 @@ __global__ void __launch_bounds__(NT) k_anchor_col2d(AnchorFFArgs A) {
       const ff t0 = visc0 - conv0, t1 = visc1 - conv1;
       const ff t0l = shfl_up_ff(t0, 1);
       if (r >= ys && out_lane) {
-        if (r < N && i >= 0 && i <= N) {  // u face (i, r)
+        if (r < N && i >= 0 && i <= N && NS_BCHK(chk, (long)r * P + i, P, N + 1, N, 25)) {  // u face (i, r)
           ff avg = ff_scale2(t0l + t0, 0.5f);
           if (fgx != kWrap && (i == 0 || i == N)) avg = (fgx == kReflect) ? zero : ff_scale2(i == 0 ? t0 : t0l, 0.5f);
           const long id = (long)r * P + i;
@@ -203,7 +213,7 @@ __global__ void __launch_bounds__(NT) k_anchor_col2d(AnchorFFArgs A) {
           A.obl[0][id] = u.lo;
           A.g0[0][id] = G.hi + G.lo;
         }
-        if (i >= 0 && i < N) {  // v face (i, r), r <= N
+        if (i >= 0 && i < N && NS_BCHK(chk, (long)r * P + i, P, N + 1, N, 26)) {  // v face (i, r), r <= N
           ff avg = ff_scale2(t1p + t1, 0.5f);
           if (fgy != kWrap && (r == 0 || r == N)) avg = (fgy == kReflect) ? zero : ff_scale2(r == 0 ? t1 : t1p, 0.5f);
           const long id = (long)r * P + i;

@@ -111,6 +111,8 @@ struct ns_ctx {
   cudaStream_t side = nullptr;
   cudaEvent_t side_ev[2] = {nullptr, nullptr};
   double* const* early_uprev = nullptr;
+  // bounds-check build: status words of the checked kernels (bounds.cuh)
+  unsigned long long* check = nullptr;
   // cell-velocity output of ns_get_cell_velocity (lazily allocated)
   double* cell_tmp = nullptr;
   // lid profile (one value per cell column) when controls are set

@@ -11,6 +11,7 @@
 // the coarsest level. T = double (plain FP64 solver) or float (V-cycles of the
 // mixed-precision defect correction).
 #pragma once
+#include "bounds.cuh"
 #include "ns_common.cuh"
 
 namespace ns {
@@ -37,6 +38,7 @@ struct MGLevels {
   T idg[kMaxLevels][9];
   int periodic[2];
   const double* fmean;            // subtracted from f at level 0 when non-null
+  unsigned long long* check;      // bounds-check build: status words (bounds.cuh); null otherwise
 };
 
 // Gauss-Seidel update of one cell from its four neighbours; w* = 0 removes an
@@ -102,7 +104,7 @@ __global__ void __launch_bounds__(256) k_mg_smooth(MGLevels<T> M, int l, int mod
     const int a = x0 - H + lx, b = y0 - H + ly;
     const bool in = (px || (a >= 0 && a < n)) && (py || (b >= 0 && b < n));
     T xv = (T)0, fv = (T)0;
-    if (in) {
+    if (in && NS_BCHK(M.check, (long)wrapi(b, n) * P + wrapi(a, n), P, n + 1, n - 1, 51)) {
       const int aa = wrapi(a, n), bb = wrapi(b, n);
       const long id = (long)bb * P + aa;
       if (!x_zero) xv = M.x[l][id];
@@ -116,6 +118,8 @@ __global__ void __launch_bounds__(256) k_mg_smooth(MGLevels<T> M, int l, int mod
         I2 = px ? wrapi(I2, nc) : min(max(I2, 0), nc - 1);
         J2 = py ? wrapi(J2, nc) : min(max(J2, 0), nc - 1);
         const T* xc = M.x[l + 1];
+        if (!NS_BCHK(M.check, (long)J * Pc + I, Pc, nc + 1, nc - 1, 52) || !NS_BCHK(M.check, (long)J2 * Pc + I2, Pc, nc + 1, nc - 1, 53))
+          continue;
         const T c00 = xc[(long)J * Pc + I], c10 = xc[(long)J * Pc + I2];
         const T c01 = xc[(long)J2 * Pc + I], c11 = xc[(long)J2 * Pc + I2];
         xv = prolong_add(xv, c00, c10, c01, c11);
@@ -149,7 +153,7 @@ __global__ void __launch_bounds__(256) k_mg_smooth(MGLevels<T> M, int l, int mod
   }
   for (int t = tid; t < TX * TY; t += NT) {
     const int a = x0 + t % TX, b = y0 + t / TX;
-    if (a < n && b < n) M.x2[l][(long)b * P + a] = sm.x[b - (y0 - H)][a - (x0 - H)];
+    if (a < n && b < n && NS_BCHK(M.check, (long)b * P + a, P, n + 1, n - 1, 54)) M.x2[l][(long)b * P + a] = sm.x[b - (y0 - H)][a - (x0 - H)];
   }
 }
 
@@ -183,6 +187,8 @@ __device__ __forceinline__ SmRow<T> sm_load_row(const MGLevels<T>& M, int l, int
   if (!cin || !(py || (r >= 0 && r < n))) return o;
   const int rr = wrapi(r, n), w0 = wrapi(c0, n);  // w0 even, w0 + 1 < n
   const long id = (long)rr * M.pitch[l] + w0;
+  // level arrays are pitch x (n + 1) elements (bounds-check build only)
+  if (!NS_BCHK(M.check, id, M.pitch[l], n + 1, n - 2, 41)) return o;
   if (!x_zero) { o.x0 = M.x[l][id]; o.x1 = M.x[l][id + 1]; }
   o.f0 = level_f(M, l, id);
   o.f1 = level_f(M, l, id + 1);
@@ -195,6 +201,9 @@ __device__ __forceinline__ SmRow<T> sm_load_row(const MGLevels<T>& M, int l, int
     Ip = px ? wrapi(Ip, nc) : min(Ip, nc - 1);
     J2 = py ? wrapi(J2, nc) : min(max(J2, 0), nc - 1);
     const T* xc = M.x[l + 1];
+    if (!NS_BCHK(M.check, (long)J * Pc + Im, Pc, nc + 1, nc - 1, 42) || !NS_BCHK(M.check, (long)J2 * Pc + Ip, Pc, nc + 1, nc - 1, 43) ||
+        !NS_BCHK(M.check, (long)J2 * Pc + Im, Pc, nc + 1, nc - 1, 44) || !NS_BCHK(M.check, (long)J * Pc + Ip, Pc, nc + 1, nc - 1, 44))
+      return o;
     const T c00 = xc[(long)J * Pc + I], c01 = xc[(long)J2 * Pc + I];
     const T cm0 = xc[(long)J * Pc + Im], cm1 = xc[(long)J2 * Pc + Im];  // column w0 - 1 side (w0 even)
     const T cp0 = xc[(long)J * Pc + Ip], cp1 = xc[(long)J2 * Pc + Ip];  // column w0 + 2 side (w0 + 1 odd)
@@ -260,7 +269,8 @@ __global__ void __launch_bounds__(128) k_mg_smooth_col(MGLevels<T> M, int l, int
       }
     }
     const int ro = t - 3;
-    if (out_lane && c0 >= 0 && c1 < n && ro >= y0 && ro < y0 + kColSmH && ro < n) {  // real cells only
+    if (out_lane && c0 >= 0 && c1 < n && ro >= y0 && ro < y0 + kColSmH && ro < n &&
+        NS_BCHK(M.check, (long)ro * P + c0, P, n + 1, n - 2, 45)) {  // real cells only
       const long id = (long)ro * P + c0;
       M.x2[l][id] = xw[1][0];
       M.x2[l][id + 1] = xw[1][1];

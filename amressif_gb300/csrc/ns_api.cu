@@ -121,6 +121,7 @@ void free_all(ns_ctx* c) {
   F(c->Pp); F(c->F);
   F(c->lid_col);
   F(c->cell_tmp);
+  F(c->check);
   free3d(c);
   for (double* v : c->gm_v) F(v);
   F(c->gm_w); F(c->gm_z); F(c->gm_b); F(c->gm_part); F(c->gm_dev);
@@ -150,6 +151,7 @@ int alloc_levels(ns_ctx* c, MGLevels<T>& M, bool own_level0) {
   M.periodic[0] = c->g.periodic[0];
   M.periodic[1] = c->g.periodic[1];
   M.fmean = nullptr;
+  M.check = c->check;
   double hx = c->g.dx[0], hy = c->g.dx[1];
   while (true) {
     const int l = M.L;
@@ -337,6 +339,15 @@ int ns_ctx_create(const ns_params* p, void* stream, ns_ctx** out) {
   // dt rule of main.cpp:285-294
   double coeff = 1.0 / (g.dx[0] * g.dx[0]) + 1.0 / (g.dx[1] * g.dx[1]);
   if (D == 3) coeff += 1.0 / (g.dx[2] * g.dx[2]);
+#ifdef NS_BOUNDS_CHECK
+  if (cudaMalloc(&c->check, 4 * sizeof(unsigned long long)) != cudaSuccess ||
+      cudaMemset(c->check, 0, 4 * sizeof(unsigned long long)) != cudaSuccess) {
+    if (c->check) cudaFree(c->check);
+    delete c;
+    return NS_ERR_NOMEM;
+  }
+  g.check = c->check;
+#endif
   c->dt = p->fixed_dt != -1.0 ? p->fixed_dt : p->cfl / (2.0 * coeff);
   g.dt = c->dt;
   g.ren = p->ren;
@@ -1547,6 +1558,21 @@ int ns_profile_read(ns_ctx* c, double* ms, long long* counts, int nkinds, int re
 }
 
 long long ns_launch_count(const ns_ctx* c) { return c ? c->launches : -1; }
+
+int ns_bounds_check_read(ns_ctx* c, unsigned long long* status, int reset) {
+  if (!c || !status) return NS_ERR_ARG;
+#ifdef NS_BOUNDS_CHECK
+  CK(cudaStreamSynchronize(c->st), "stream sync");
+  unsigned long long h[3] = {0, 0, 0};
+  CK(cudaMemcpy(h, c->check, sizeof(h), cudaMemcpyDeviceToHost), "status read");
+  for (int k = 0; k < 3; ++k) status[k] = h[k];
+  if (reset) CK(cudaMemset(c->check, 0, sizeof(h)), "status reset");
+  return NS_OK;
+#else
+  status[0] = status[1] = status[2] = 0;
+  return NS_ERR_UNSUPPORTED;
+#endif
+}
 
 void* ns_host_alloc(unsigned long long bytes) {
   void* p = nullptr;

@@ -54,6 +54,9 @@ struct Geom {
   // column, device memory): the ghost becomes 2*lid_u[i] - q instead of
   // 2*inflow_waveform[0] - q (the controlled lid of the adjoint problem)
   const double* lid_u;
+  // bounds-check build only: the context's status words (failures, first
+  // failing index, its site); null otherwise
+  unsigned long long* check;
 };
 
 // periodic index in [0, n) for any a (tiles of small grids reach past one period)

@@ -33,6 +33,7 @@
 // slots swapped. Face-indexed words whose face is not the lane's cell column
 // (face N, the periodic image, wall faces) are loaded directly, per slot.
 #pragma once
+#include "bounds.cuh"
 #include "col2d.cuh"
 #include "ff.cuh"
 #include "ns_common.cuh"
@@ -131,22 +132,34 @@ __global__ void __launch_bounds__(NT, 384 / NT) k_inc_col2d(IncArgs A) {  // 12 
       int kk = k < 0 ? -k - 1 : 2 * N - 1 - k;
       return kk < 0 ? 0 : (kk >= N ? N - 1 : kk);
     };
+    // every level-0 field is P x (N + 1) elements; a pair at index q needs
+    // the column of q at most N - 1 (bounds-check build only, bounds.cuh)
+    unsigned long long* const chk = g.check;
+    (void)chk;
     auto issue_row = [&](int k, int sl) {
       const long r0 = (long)row_of(k) * P + pc;
-      cp_async8(reinterpret_cast<float*>(pair_ptr(sl, 0)), shu + r0);
-      cp_async8(reinterpret_cast<float*>(pair_ptr(sl, 1)), eu + r0);
-      cp_async8(reinterpret_cast<float*>(pair_ptr(sl, 2)), shv + r0);
-      cp_async8(reinterpret_cast<float*>(pair_ptr(sl, 3)), shv + r0 + P);
-      cp_async8(reinterpret_cast<float*>(pair_ptr(sl, 4)), ev + r0);
-      cp_async8(reinterpret_cast<float*>(pair_ptr(sl, 5)), ev + r0 + P);
-      cp_async8(reinterpret_cast<float*>(pair_ptr(sl, 6)), A.g0[0] + r0);
-      cp_async8(reinterpret_cast<float*>(pair_ptr(sl, 7)), A.g0[1] + r0);
-      cp_async4(single_ptr(sl, 0), shu + r0 + 2);
-      cp_async4(single_ptr(sl, 1), eu + r0 + 2);
+      if (NS_BCHK(chk, r0, P, N + 1, N - 1, 1)) {
+        cp_async8(reinterpret_cast<float*>(pair_ptr(sl, 0)), shu + r0);
+        cp_async8(reinterpret_cast<float*>(pair_ptr(sl, 1)), eu + r0);
+        cp_async8(reinterpret_cast<float*>(pair_ptr(sl, 2)), shv + r0);
+        cp_async8(reinterpret_cast<float*>(pair_ptr(sl, 4)), ev + r0);
+        cp_async8(reinterpret_cast<float*>(pair_ptr(sl, 6)), A.g0[0] + r0);
+        cp_async8(reinterpret_cast<float*>(pair_ptr(sl, 7)), A.g0[1] + r0);
+      }
+      if (NS_BCHK(chk, r0 + P, P, N + 1, N - 1, 2)) {
+        cp_async8(reinterpret_cast<float*>(pair_ptr(sl, 3)), shv + r0 + P);
+        cp_async8(reinterpret_cast<float*>(pair_ptr(sl, 5)), ev + r0 + P);
+      }
+      if (NS_BCHK(chk, r0 + 2, P, N + 1, N, 3)) {
+        cp_async4(single_ptr(sl, 0), shu + r0 + 2);
+        cp_async4(single_ptr(sl, 1), eu + r0 + 2);
+      }
       if constexpr (BASE) {
         const long r2 = (long)row_of(k - 2) * P + pc;
-        cp_async8(reinterpret_cast<float*>(pair_ptr(sl, 8)), A.bl[0] + r2);
-        cp_async8(reinterpret_cast<float*>(pair_ptr(sl, 9)), A.bl[1] + r2);
+        if (NS_BCHK(chk, r2, P, N + 1, N - 1, 4)) {
+          cp_async8(reinterpret_cast<float*>(pair_ptr(sl, 8)), A.bl[0] + r2);
+          cp_async8(reinterpret_cast<float*>(pair_ptr(sl, 9)), A.bl[1] + r2);
+        }
       }
       cp_async_commit();
     };
@@ -178,8 +191,12 @@ __global__ void __launch_bounds__(NT, 384 / NT) k_inc_col2d(IncArgs A) {  // 12 
       gu = GU;
       if (irr0 || irr1) {  // face N, the periodic image, wall faces: direct loads (edge lanes only)
         const long rr = (long)row_of(k) * P;
-        if (irr0) { ufb.x = shu[rr + iface[0]]; ufe.x = es * eu[rr + iface[0]]; gu.x = A.g0[0][rr + iface[0]]; }
-        if (irr1) { ufb.y = shu[rr + iface[1]]; ufe.y = es * eu[rr + iface[1]]; gu.y = A.g0[0][rr + iface[1]]; }
+        if (irr0 && NS_BCHK(chk, rr + iface[0], P, N + 1, N, 5)) {
+          ufb.x = shu[rr + iface[0]]; ufe.x = es * eu[rr + iface[0]]; gu.x = A.g0[0][rr + iface[0]];
+        }
+        if (irr1 && NS_BCHK(chk, rr + iface[1], P, N + 1, N, 5)) {
+          ufb.y = shu[rr + iface[1]]; ufe.y = es * eu[rr + iface[1]]; gu.y = A.g0[0][rr + iface[1]];
+        }
       }
       vlb = Vk;
       vle = p_mul(es2, Fk);
@@ -261,7 +278,7 @@ __global__ void __launch_bounds__(NT, 384 / NT) k_inc_col2d(IncArgs A) {  // 12 
       cell_row(r + 2, w[4], ufb[2], ufe[2], vlb[2], vle[2], gqu[2], gqv[2]);
       // y flux at face r+1 (rows r, r+1), cells r-1 .. r+2; face row N as stored
       float2 vfb = vlb[1], vfe = vle[1];
-      if (r + 1 == N) {
+      if (r + 1 == N && NS_BCHK(chk, (long)N * P + pc, P, N + 1, N - 1, 6)) {
         const long id = (long)N * P + pc;
         vfb = make_float2(shv[id], shv[id + 1]);
         vfe = p_mul(es2, make_float2(ev[id], ev[id + 1]));
@@ -307,7 +324,7 @@ __global__ void __launch_bounds__(NT, 384 / NT) k_inc_col2d(IncArgs A) {  // 12 
             const long id = (long)N * P + a;
 #pragma unroll
             for (int s = 0; s < 2; ++s) {
-              if (out_v[s]) {
+              if (out_v[s] && NS_BCHK(chk, id + s, P, N + 1, N, 7)) {
                 (s ? ecur.y : ecur.x) = es * ev[id + s];
                 (s ? gcur.y : gcur.x) = A.g0[1][id + s];
                 if constexpr (BASE) {
@@ -323,8 +340,9 @@ __global__ void __launch_bounds__(NT, 384 / NT) k_inc_col2d(IncArgs A) {  // 12 
           float2 nuh, nul, nvh, nvl;
           if constexpr (BASE) {
             float2 lo = blu;
-            if (irr0 && out_u[0] && r < N) lo.x = A.bl[0][(long)r * P + a];
-            if (irr1 && out_u[1] && r < N) lo.y = A.bl[0][(long)r * P + a + 1];
+            if (irr0 && out_u[0] && r < N && NS_BCHK(chk, (long)r * P + a, P, N + 1, N, 8)) lo.x = A.bl[0][(long)r * P + a];
+            if (irr1 && out_u[1] && r < N && NS_BCHK(chk, (long)r * P + a + 1, P, N + 1, N, 8))
+              lo.y = A.bl[0][(long)r * P + a + 1];
             ff_add_f2(ufb[0], lo, ufe[0], nuh, nul);
             ff_add_f2(bh, bo, ecur, nvh, nvl);
           }
@@ -332,7 +350,7 @@ __global__ void __launch_bounds__(NT, 384 / NT) k_inc_col2d(IncArgs A) {  // 12 
           for (int s = 0; s < 2; ++s) {
             const int i = a + s;
             const long id = (long)r * P + i;
-            if (out_u[s] && r < N) {  // u face (i, r)
+            if (out_u[s] && r < N && NS_BCHK(chk, id, P, N + 1, N, 9)) {  // u face (i, r)
               const float e = s ? eu2.y : eu2.x;
               A.eout[0][id] = e;
               n0 = fmaf(wgt_u[s] * e, e, n0);
@@ -341,7 +359,7 @@ __global__ void __launch_bounds__(NT, 384 / NT) k_inc_col2d(IncArgs A) {  // 12 
                 A.obl[0][id] = s ? nul.y : nul.x;
               }
             }
-            if (out_v[s]) {  // v face (i, r), r <= N
+            if (out_v[s] && NS_BCHK(chk, id, P, N + 1, N, 10)) {  // v face (i, r), r <= N
               const float e = s ? ev2.y : ev2.x;
               A.eout[1][id] = e;
               n1 = fmaf(edge_v ? 0.5f * e : e, e, n1);

@@ -250,6 +250,16 @@ int ns_profile_enable(ns_ctx* c, int on);
 int ns_profile_read(ns_ctx* c, double* ms, long long* counts, int nkinds, int reset);
 long long ns_launch_count(const ns_ctx* c);
 
+/* Bounds-check build (libamressif_gb300_check.so, compiled with
+ * -DNS_BOUNDS_CHECK; the counterpart of the reference's DEBUG=TRUE build,
+ * Exec/GNUmakefile:12): the column-marching predictor kernels and the
+ * multigrid smoothers test every index they form by hand against the array
+ * it addresses, skip a failing access and record it. status[0] = number of
+ * failed tests, status[1] = the first failing index, status[2] = its site
+ * (bounds.cuh). Waits for the stream; reset = 1 clears the words. The normal
+ * build returns NS_ERR_UNSUPPORTED (and zeros). */
+int ns_bounds_check_read(ns_ctx* c, unsigned long long* status, int reset);
+
 /* ---- Discrete adjoint of the time advance (2D wall / lid boxes) ----------
  *
  * The differentiated map is one converged step of main_main's loop
