@@ -102,6 +102,7 @@ class NsParams(ctypes.Structure):
         ("poisson_solver", ctypes.c_int),
         ("gmres_restart", ctypes.c_int),
         ("dc_residual", ctypes.c_int),
+        ("poisson_warm_start", ctypes.c_int),
     ]
 
 

@@ -77,6 +77,13 @@ struct ns_ctx {
   float* FFh = nullptr;
   float* FFl = nullptr;
   long long dc_fallbacks = 0;
+  // warm start of the mixed solve: the float-float phi buffer (PFh/PFl) that
+  // holds the last converged phi (-1: none, after a state was set), and the
+  // zero-guess residual max|f - mean f| of the current right-hand side
+  // (c15 * max|div u*| from ns_poisson_rhs; rhs_fmax_valid until the solve)
+  int pf_warm = -1;
+  double rhs_fmax = 0.0;
+  bool rhs_fmax_valid = false;
   // per-kernel timing (CUDA events around each launch) and launch count
   bool prof = false;
   std::vector<cudaEvent_t> evpool;

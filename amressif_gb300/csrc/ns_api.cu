@@ -242,6 +242,7 @@ void ns_params_default(ns_params* p) {
   p->poisson_solver = 0;
   p->gmres_restart = 30;
   p->dc_residual = 0;
+  p->poisson_warm_start = 0;
 }
 
 int ns_params_parse_file(ns_params* p, const char* path) {
@@ -306,6 +307,7 @@ int ns_ctx_create(const ns_params* p, void* stream, ns_ctx** out) {
   if (!(p->ren > 0)) return NS_ERR_ARG;
   if (p->dc_residual != 0 && p->dc_residual != 1) return NS_ERR_ARG;
   if (D == 3 && p->dc_residual == 1) return NS_ERR_UNSUPPORTED;  // the 3D defect correction is float-float
+  if (p->poisson_warm_start != 0 && p->poisson_warm_start != 1) return NS_ERR_ARG;
   ns_ctx* c = new ns_ctx();
   c->P = *p;
   const int N = p->n_cell;
@@ -522,7 +524,8 @@ int ns_get_box(ns_ctx* c, int field, int comp, double* data, const int lo[3], co
 }
 
 // the copies and resets of ns_set_state, enqueued without waiting (2D)
-static int set_state_async(ns_ctx* c, const double* const* u, const double* const* u_prev, const double* p, double time) {
+static int set_state_async(ns_ctx* c, const double* const* u, const double* const* u_prev, const double* p, double time,
+                           bool keep_warm = false) {
   const int N = c->N;
   for (int m = 0; m < 2; ++m) {
     const int lo[3] = {0, 0, 0};
@@ -539,6 +542,7 @@ static int set_state_async(ns_ctx* c, const double* const* u, const double* cons
   c->time = time;
   c->in_step = false;
   c->cart_pending = false;
+  if (!keep_warm) c->pf_warm = -1;  // no previous phi for a warm start
   return NS_OK;
 }
 
@@ -745,6 +749,10 @@ int ns_poisson_rhs(ns_ctx* c, double* divmax, double* sum) {
   if (r != NS_OK) return r;
   if (divmax) *divmax = c->red_h[kRedDivBefore];
   if (sum) *sum = c->red_h[kRedSum];
+  // max|f| = (1.5/dt) max|div u*| (the same rounding), the zero-guess
+  // residual of a warm-started mixed solve
+  c->rhs_fmax = c->g.c15 * c->red_h[kRedDivBefore];
+  c->rhs_fmax_valid = true;
   return NS_OK;
 }
 
@@ -1030,11 +1038,23 @@ int ns_poisson_solve(ns_ctx* c, int precision, int* cycles, double* res) {
     const bool ff_start = c->P.dc_residual == 0;
     int pf = 0;
     int pc = 0;
+    // warm start: the defect correction starts from the previous step's
+    // float-float phi (a zero correction added to it), with the tolerance
+    // relative to the zero-guess residual max|f - mean f|
+    const bool warm = ff_start && c->P.poisson_warm_start && c->pf_warm >= 0 && c->rhs_fmax_valid && c->rhs_fmax > 0;
     if (ff_start) {
       LAUNCH(NS_PROF_OTHER, "rhs split", launch_rhs_ff(c->N, c->pitch, c->F, c->red + kRedMean, c->FFh, c->FFl, c->st));
-      q.first = 1;
-      q.phin[0] = c->PFh[0]; q.phin[1] = c->PFl[0];
-      q.phout[0] = c->PFh[0]; q.phout[1] = c->PFl[0];
+      if (warm) {
+        CK(cudaMemsetAsync(c->M32.x[0], 0, (size_t)c->pitch * (c->N + 1) * sizeof(float), c->st), "memset e");
+        q.first = 0;
+        q.phin[0] = c->PFh[c->pf_warm]; q.phin[1] = c->PFl[c->pf_warm];
+        q.phout[0] = c->PFh[1 - c->pf_warm]; q.phout[1] = c->PFl[1 - c->pf_warm];
+        pf = 1 - c->pf_warm;
+      } else {
+        q.first = 1;
+        q.phin[0] = c->PFh[0]; q.phin[1] = c->PFl[0];
+        q.phout[0] = c->PFh[0]; q.phout[1] = c->PFl[0];
+      }
       LAUNCH(NS_PROF_DC_UPDATE, "dc update", launch_dc_update_ff(q, c->st));
     } else {
       // FP64 phi and residual from the first sweep: phi = 0, r = f - mean f
@@ -1045,8 +1065,9 @@ int ns_poisson_solve(ns_ctx* c, int precision, int* cycles, double* res) {
     }
     r = sync_red(c, kRedRes, 1);
     if (r != NS_OK) return r;
-    rnorm0 = c->red_h[kRedRes];
-    rn = rnorm0;
+    rn = c->red_h[kRedRes];
+    rnorm0 = warm ? c->rhs_fmax : rn;
+    c->rhs_fmax_valid = false;
     const double tol = std::max(c->P.poisson_tol_rel * rnorm0, 0.0);
     auto done = [&](double x) { return x <= tol && (div_tol_res <= 0 || x <= div_tol_res); };
     double best = rn;
@@ -1089,6 +1110,7 @@ int ns_poisson_solve(ns_ctx* c, int precision, int* cycles, double* res) {
     if (ffmode)
       LAUNCH(NS_PROF_OTHER, "phi to fp64", launch_ff_to_double(c->N, c->pitch, c->PFh[pf], c->PFl[pf], c->PHI[0], c->st));
     c->phi_cur = ffmode ? 0 : pc;
+    c->pf_warm = (ffmode && status == NS_OK) ? pf : -1;
   } else {
     c->phi_cur = 0;
     c->M64.x[0] = c->PHI[0];
@@ -1486,7 +1508,9 @@ int ns_step_host(ns_ctx* c, double* const* u, double* const* u_prev, double* p, 
     overlap = c->side && c->side_ev[0] && c->side_ev[1];
   }
   if (c->ev_ok) cudaEventRecord(c->ev[4], c->st);
-  int r = two_d ? set_state_async(c, u, u_prev, p, t) : ns_set_state(c, u, u_prev, p, t);
+  // a warm-started mixed solve keeps the previous step's phi as its initial
+  // guess: it meets the same tolerance whatever state the host uploads
+  int r = two_d ? set_state_async(c, u, u_prev, p, t, true) : ns_set_state(c, u, u_prev, p, t);
   if (r != NS_OK) return r;
   if (c->ev_ok) cudaEventRecord(c->ev[5], c->st);
   ns_step_stats s;

@@ -453,7 +453,7 @@ def bench_ours(args):
     n = args.n
     K, W = args.steps, args.warmup
     # ---- mixed precision (headline) ----
-    s = ns.Solver(workload_params(ns, n, ns.PREC_MIXED))
+    s = ns.Solver(workload_params(ns, n, ns.PREC_MIXED, poisson_warm_start=args.warm_start))
     s.init(ns.INIT_CAVITY)
     run_steps(s, W)
     # per-launch events only over the last Kp of the K timed steps: an event
@@ -591,6 +591,43 @@ def bench_ours(args):
             dc_ab["fp64_residual"]["vs_fp64_rel_l2"] = {"u": rel(udc[0], u64[0]), "v": rel(udc[1], u64[1]),
                                                         "p": rel(pdcs - pdcs.mean(), p64 - p64.mean())}
 
+    # ---- the mixed solver with a warm-started Poisson solve (the previous
+    # step's phi as the initial guess, the tolerance still relative to the
+    # zero-guess residual) on the same steps ----
+    warm_ab = None
+    if not args.no_warm_ab:
+        import numpy as np
+
+        alt = 0 if args.warm_start else 1
+        sw = ns.Solver(workload_params(ns, n, ns.PREC_MIXED, poisson_warm_start=alt))
+        sw.init(ns.INIT_CAVITY)
+        run_steps(sw, W)
+        sw.sync()
+        stw = run_steps(sw, K)
+        msw = sum(st["ms_predictor"] + st["ms_poisson"] + st["ms_project"] for st in stw) / K
+        uw, _, pws, _ = sw.get_state()
+        sw.close()
+        warm_ab = {
+            "poisson_warm_start_%d" % alt: {
+                "steps_per_s": 1e3 / msw, "ms_per_step": msw,
+                "poisson_ms_per_step": statistics.mean(st["ms_poisson"] for st in stw),
+                "poisson_cycles": [st["poisson_cycles"] for st in stw],
+                "pseudo_iters": [st["pseudo_iters"] for st in stw],
+                "div_after_max": max(st["div_after"] for st in stw)},
+            "poisson_warm_start_%d" % args.warm_start: {
+                "steps_per_s": value / world, "ms_per_step": ms_per_step,
+                "poisson_ms_per_step": statistics.mean(st["ms_poisson"] for st in stats),
+                "poisson_cycles": [st["poisson_cycles"] for st in stats],
+                "pseudo_iters": [st["pseudo_iters"] for st in stats],
+                "div_after_max": max(st["div_after"] for st in stats)},
+            "note": "the headline runs poisson_warm_start = %d; the other setting on the same steps" % args.warm_start,
+        }
+        if fp64 is not None:
+            def rel(a, b):
+                return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+            warm_ab["poisson_warm_start_%d" % alt]["vs_fp64_rel_l2"] = {
+                "u": rel(uw[0], u64[0]), "v": rel(uw[1], u64[1]), "p": rel(pws - pws.mean(), p64 - p64.mean())}
+
     # ---- roofline of the dominant kernel ----
     peak, peak_kind = measured_peak_hbm()
     dom = max(prof.items(), key=lambda kv: kv[1][1])
@@ -641,6 +678,7 @@ def bench_ours(args):
             "dtype": DTYPE_MIXED, "data": "synthetic (cavity from rest)",
             "config": bench_config(n, world),
             "window": "steps %d..%d of the run (W = %d untimed warm-up steps first)" % (W + 1, W + K, W),
+            "poisson_warm_start": args.warm_start,
             "pseudo_iters": [st["pseudo_iters"] for st in stats],
             "pseudo_iters_mean": statistics.mean(st["pseudo_iters"] for st in stats),
             "poisson_cycles_mean": statistics.mean(st["poisson_cycles"] for st in stats),
@@ -653,6 +691,7 @@ def bench_ours(args):
             "wall_ms_per_step": 1e3 * wall / K,
             "fp64_mg": fp64,
             "dc_residual_ab": dc_ab,
+            "poisson_warm_start_ab": warm_ab,
             "parity_4096_first_steps": parity,
             "adjoint_forward_ratio": adjoint["ratio"] if adjoint else None,
             "adjoint": adjoint,
@@ -710,6 +749,9 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-dc-ab", action="store_true", help="skip the FP64 defect-correction residual A/B")
+    ap.add_argument("--warm-start", type=int, default=0, choices=[0, 1],
+                    help="poisson_warm_start of the headline mixed solver")
+    ap.add_argument("--no-warm-ab", action="store_true", help="skip the warm-start A/B")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-cfg5", action="store_true")

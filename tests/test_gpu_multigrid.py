@@ -66,3 +66,35 @@ def test_mixed_step_is_deterministic(gpu_lib):
     assert np.array_equal(p1, p2)
     for a, b in zip(u1, u2):
         assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("n", [256, N])
+def test_warm_started_mixed_poisson_matches_fp64(gpu_lib, n):
+    """poisson_warm_start = 1: the defect correction starts from the previous
+    step's phi, with the tolerance still relative to max|f - mean f|. Over
+    several steps of the cavity it keeps the pseudo-iteration counts of the
+    FP64 solver, u and p within 1e-10 of it and max|div u| <= 1e-10, with no
+    more V-cycles than the cold start from zero."""
+    steps = 6 if n < N else 3
+    out = {}
+    for name, prec, warm in (("fp64", ns.PREC_FP64, 0), ("cold", ns.PREC_MIXED, 0), ("warm", ns.PREC_MIXED, 1)):
+        p = ns.default_params(n_cell=n, ren=1000.0, fixed_dt=0.5 / n, iter_num=100, momentum_tolerance=1e-10,
+                              max_grid_size=(n, n, n), precision=prec, poisson_tol_rel=1e-10, poisson_tol_div=1e-10,
+                              poisson_max_cycles=200, dtau_clip=1, poisson_warm_start=warm)
+        s = ns.Solver(p)
+        s.init(ns.INIT_CAVITY)
+        st = [s.step() for _ in range(steps)]
+        u, _, pp, _ = s.get_state()
+        out[name] = (st, u, pp)
+        s.close()
+    for name in ("cold", "warm"):
+        st, u, pp = out[name]
+        assert [x["pseudo_iters"] for x in st] == [x["pseudo_iters"] for x in out["fp64"][0]]
+        assert all(x["div_after"] <= 1e-10 for x in st)
+        for a, b in zip(u, out["fp64"][1]):
+            assert rel(a, b) <= 1e-10, (name, rel(a, b))
+        assert rel(pp - pp.mean(), out["fp64"][2] - out["fp64"][2].mean()) <= 1e-10
+    cold = [x["poisson_cycles"] for x in out["cold"][0]]
+    warm = [x["poisson_cycles"] for x in out["warm"][0]]
+    assert warm[0] == cold[0]  # the first step has no previous phi
+    assert sum(warm) <= sum(cold), (warm, cold)
