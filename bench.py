@@ -353,6 +353,122 @@ def adjoint_section(ns, args):
     return out
 
 
+def cpu_table_section(args):
+    """The CPU restatement (oracle/) on the host cores, all of them and one,
+    for the parity configurations (the benchmark's CPU table). Config 1 (128^2
+    cavity, 200 steps) runs in full; config 2 (1024^2 perturbed Taylor-Green)
+    and config 3 (4096^2 cavity from rest) are bounded samples: config 2 a few
+    steps, config 3 on one core the phases of step 1 (the four RK stages of
+    one pseudo-iteration, timed and multiplied by the step's K, plus the
+    Poisson right-hand side, solve and projection), all-core config 3 is the
+    bench's own cpu_baseline."""
+    import math
+
+    from amressif_gb300 import workloads as wl
+    from oracle.orc import Oracle
+
+    allc = os.cpu_count() or 1
+    out = {"host_cores": allc}
+    try:
+        out["cpu_model"] = [l.split(":", 1)[1].strip() for l in open("/proc/cpuinfo") if "model name" in l.lower()
+                            or l.startswith("CPU part")][0]
+    except Exception:
+        out["cpu_model"] = None
+
+    def cfg1(threads):
+        o = Oracle(128, ren=100.0, dt=0.5 / 128, iter_num=100, poisson_tol=1e-10, max_grid_size=(64, 64, 64),
+                   nthreads=threads)
+        o.init(0)
+        t0 = time.perf_counter()
+        ks = [o.step()["pseudo_iters"] for _ in range(200)]
+        dt = time.perf_counter() - t0
+        o.close()
+        return {"steps": 200, "seconds": dt, "steps_per_s": 200 / dt, "cell_updates_per_s": 200 * 128 * 128 / dt,
+                "pseudo_iters_mean": sum(ks) / len(ks)}
+
+    def cfg2(threads, steps):
+        n = 1024
+        h = 2 * math.pi / n
+        o = Oracle(n, ren=1000.0, dt=0.5 * h, iter_num=100, poisson_tol=1e-10, max_grid_size=(n, n, n),
+                   prob_hi=(2 * math.pi,) * 3, bc_lo=(111,) * 3, bc_hi=(111,) * 3, nthreads=threads)
+        o.set_state(*wl.tgv_perturbed_state(n, amp=1e-3, seed=0))
+        t0 = time.perf_counter()
+        ks = [o.step()["pseudo_iters"] for _ in range(steps)]
+        dt = time.perf_counter() - t0
+        o.close()
+        return {"steps": steps, "seconds": dt, "steps_per_s": steps / dt, "cell_updates_per_s": steps * n * n / dt,
+                "pseudo_iters": ks, "sample": "steps 1..%d of 500" % steps}
+
+    def cfg3_phases():
+        # one core: the first pseudo-iteration of step 1, then (from the
+        # converged u* of an all-core run of the same predictor) the Poisson
+        # right-hand side, solve and projection
+        from oracle.orc import FIELD_STAR
+
+        n = 4096
+        mk = lambda threads: Oracle(n, ren=1000.0, dt=0.5 / n, iter_num=100, dtau_clip=1, poisson_tol=1e-10,
+                                    max_grid_size=(n, n, n), nthreads=threads)
+        o1 = mk(1)
+        o1.init(0)
+        o1.step_begin()
+        t0 = time.perf_counter()
+        for sub in range(4):
+            o1.rk_stage(sub)
+        o1.pseudo_norm()
+        t_it = time.perf_counter() - t0
+        oa = mk(allc)
+        oa.init(0)
+        oa.step_begin()
+        k, norm = 0, 1e9
+        while norm > 1e-10 and k < 100:
+            for sub in range(4):
+                oa.rk_stage(sub)
+            norm = oa.pseudo_norm()
+            k += 1
+        for d in range(2):
+            o1.put_field(FIELD_STAR, d, oa.field(FIELD_STAR, d))
+        oa.close()
+        t0 = time.perf_counter()
+        o1.poisson_rhs()
+        o1.poisson_solve()
+        o1.project()
+        t_p = time.perf_counter() - t0
+        o1.close()
+        est = k * t_it + t_p
+        return {"pseudo_iteration_s": t_it, "pseudo_iters": k, "poisson_and_projection_s": t_p,
+                "step_s_estimate": est, "steps_per_s": 1.0 / est,
+                "sample": "step 1 from rest: one pseudo-iteration timed x K, plus the timed Poisson RHS, solve "
+                          "and projection from the converged u*"}
+
+    out["config1_cavity128_200_steps"] = {"all_cores": cfg1(allc), "one_core": cfg1(1)}
+    out["config2_tgv1024"] = {"all_cores": cfg2(allc, args.cpu_cfg2_steps), "one_core": cfg2(1, 1)}
+    out["config3_cavity4096_one_core"] = cfg3_phases()
+    return out
+
+
+def full_run_section(ns, args):
+    """The whole 1000-step 4096^2 cavity run from rest with the mixed
+    solver: steps/s over all steps, with the pseudo-iteration and V-cycle
+    counts of the first and the last steps (the timed window of the headline
+    sits at its start)."""
+    n = args.n
+    s = ns.Solver(workload_params(ns, n, ns.PREC_MIXED, poisson_warm_start=args.warm_start))
+    s.init(ns.INIT_CAVITY)
+    s.sync()
+    t0 = time.perf_counter()
+    st = [s.step() for _ in range(args.full_run_steps)]
+    s.sync()
+    wall = time.perf_counter() - t0
+    dev = sum(x["ms_predictor"] + x["ms_poisson"] + x["ms_project"] for x in st) / 1e3
+    s.close()
+    ks = [x["pseudo_iters"] for x in st]
+    cyc = [x["poisson_cycles"] for x in st]
+    return {"steps": len(st), "wall_s": wall, "device_s": dev, "steps_per_s": len(st) / dev,
+            "wall_steps_per_s": len(st) / wall, "pseudo_iters_first_last": [ks[:5], ks[-5:]],
+            "pseudo_iters_mean": sum(ks) / len(ks), "poisson_cycles_mean": sum(cyc) / len(cyc),
+            "div_after_max": max(x["div_after"] for x in st), "poisson_warm_start": args.warm_start}
+
+
 def cfg5_section(ns, args):
     """3D periodic Taylor-Green vortex on [0, 2 pi]^3, 256^3, Re = 1600, dt = 0.4 h
     (CFL 0.4 for unit velocity), with the seeded 1e-3 divergence-free
@@ -759,8 +875,11 @@ def main():
     ap.add_argument("--cfg5-steps", type=int, default=2)
     ap.add_argument("--no-cfg5-adjoint", action="store_true")
     ap.add_argument("--no-cfg5-fp64", action="store_true")
-    ap.add_argument("--section", default="all", choices=["all", "cfg5"],
-                    help="cfg5: run only the 3D Taylor-Green section and print it (profiling runs)")
+    ap.add_argument("--section", default="all", choices=["all", "cfg5", "cpu", "full-run"],
+                    help="cfg5: only the 3D Taylor-Green section (profiling runs); cpu: the CPU restatement on all "
+                         "host cores and on one, configs 1-3; full-run: the whole 1000-step 4096^2 run")
+    ap.add_argument("--cpu-cfg2-steps", type=int, default=5)
+    ap.add_argument("--full-run-steps", type=int, default=1000)
     ap.add_argument("--cfg5-adj-n", type=int, default=128)
     ap.add_argument("--cfg5-adj-steps", type=int, default=200)
     ap.add_argument("--cfg5-adj-snap", type=int, default=16)
@@ -773,7 +892,13 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
-    if args.section == "cfg5":
+    if args.section == "cpu":
+        print(json.dumps({"cpu_table": cpu_table_section(args)}))
+    elif args.section == "full-run":
+        import amressif_gb300 as ns
+
+        print(json.dumps({"full_run": full_run_section(ns, args)}))
+    elif args.section == "cfg5":
         import amressif_gb300 as ns
 
         out = cfg5_section(ns, args)
