@@ -213,18 +213,21 @@ __device__ __forceinline__ SmRow<T> sm_load_row(const MGLevels<T>& M, int l, int
   return o;
 }
 
-template <typename T>
-__global__ void __launch_bounds__(128) k_mg_smooth_col(MGLevels<T> M, int l, int mode, int x_zero) {
+// The climb of one warp. FAST: every column of the warp and every row of its
+// wavefront lies inside the domain away from the walls (or the direction is
+// periodic), so each update has all four neighbours and the diagonal entry of
+// a full stencil: the boundary weights, the diagonal-table index and the
+// domain tests drop out. The arithmetic (and so every bit of the result) is
+// that of gs_update with all weights set.
+template <typename T, bool FAST>
+__device__ __forceinline__ void smooth_col_march(const MGLevels<T>& M, int l, int mode, int x_zero, int xs, int y0,
+                                                 int lane) {
   constexpr unsigned FULL = 0xffffffffu;
   const int n = M.n[l];
   const long P = M.pitch[l];
-  const int lane = threadIdx.x & 31;
-  const int nsx = (n + kColSmOut - 1) / kColSmOut, nsy = (n + kColSmH - 1) / kColSmH;
-  const int gw = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  if (gw >= nsx * nsy) return;  // warp-uniform; the kernel has no block barrier
-  const int xs = (gw % nsx) * kColSmOut, y0 = (gw / nsx) * kColSmH;
   const bool px = M.periodic[0], py = M.periodic[1];
   const T ihx = M.ih[l][0], ihy = M.ih[l][1];
+  const T idg_full = M.idg[l][8];  // a + 3 b with two neighbours in each direction
   const int cfirst = (mode == 1) ? 1 : 0;
   const int c0 = xs - 4 + 2 * lane, c1 = c0 + 1;   // c0 even; both columns in or both out (n even)
   const bool cin = px || (c0 >= 0 && c1 < n);
@@ -237,7 +240,7 @@ __global__ void __launch_bounds__(128) k_mg_smooth_col(MGLevels<T> M, int l, int
   for (int k = 0; k < 6; ++k) xw[k][0] = xw[k][1] = (T)0;
 #pragma unroll
   for (int k = 0; k < 4; ++k) fw[k][0] = fw[k][1] = (T)0;
-  const int t0 = y0 - 3, t1 = y0 + kColSmH + 2;  // rows of half-sweep 0
+  const int t0 = y0 - 3, t1 = y0 + kColSmH + 2;  // rows of half-sweep 0; half-sweep s runs for t >= t0 + 2 s
   {
     const SmRow<T> a = sm_load_row(M, l, mode, x_zero, t0 - 1, c0, cin);
     const SmRow<T> b = sm_load_row(M, l, mode, x_zero, t0, c0, cin);
@@ -258,13 +261,25 @@ __global__ void __launch_bounds__(128) k_mg_smooth_col(MGLevels<T> M, int l, int
       const bool upd1 = ((r & 1) != color);  // c0 has the colour r & 1, c1 the other
       const T e_of_0 = __shfl_down_sync(FULL, xw[k][0], 1);  // column c1 + 1 (lane + 1's c0)
       const T w_of_1 = __shfl_up_sync(FULL, xw[k][1], 1);    // column c0 - 1 (lane - 1's c1)
-      const bool rok = r >= y0 - 3 + s && r <= y0 + kColSmH + 2 - s && (py || (r >= 0 && r < n)) && cin;
-      const bool wn = py || r + 1 < n, wsn = py || r > 0;
-      if (rok) {
-        if (!upd1) {
-          xw[k][0] = gs_update<T>(xw[k][1], w_of_1, xw[k + 1][0], xw[k - 1][0], we0, ww0, wn, wsn, ihx, ihy, fw[3 - s][0], M.idg[l]);
-        } else {
-          xw[k][1] = gs_update<T>(e_of_0, xw[k][0], xw[k + 1][1], xw[k - 1][1], we1, ww1, wn, wsn, ihx, ihy, fw[3 - s][1], M.idg[l]);
+      if constexpr (FAST) {
+        if (t >= t0 + 2 * s) {  // warp-uniform
+          const T xe = upd1 ? e_of_0 : xw[k][1], xwv = upd1 ? xw[k][0] : w_of_1;
+          const T xn = upd1 ? xw[k + 1][1] : xw[k + 1][0], xs_ = upd1 ? xw[k - 1][1] : xw[k - 1][0];
+          const T fv = upd1 ? fw[3 - s][1] : fw[3 - s][0];
+          const T sx = rn_mul(rn_add(xe, xwv), ihx), sy = rn_mul(rn_add(xn, xs_), ihy);
+          const T v = rn_mul(rn_add(rn_add(sx, sy), -fv), idg_full);
+          if (upd1) xw[k][1] = v;
+          else xw[k][0] = v;
+        }
+      } else {
+        const bool rok = r >= y0 - 3 + s && r <= y0 + kColSmH + 2 - s && (py || (r >= 0 && r < n)) && cin;
+        const bool wn = py || r + 1 < n, wsn = py || r > 0;
+        if (rok) {
+          if (!upd1) {
+            xw[k][0] = gs_update<T>(xw[k][1], w_of_1, xw[k + 1][0], xw[k - 1][0], we0, ww0, wn, wsn, ihx, ihy, fw[3 - s][0], M.idg[l]);
+          } else {
+            xw[k][1] = gs_update<T>(e_of_0, xw[k][0], xw[k + 1][1], xw[k - 1][1], we1, ww1, wn, wsn, ihx, ihy, fw[3 - s][1], M.idg[l]);
+          }
         }
       }
     }
@@ -282,6 +297,27 @@ __global__ void __launch_bounds__(128) k_mg_smooth_col(MGLevels<T> M, int l, int
     fw[3][0] = cur.f0;
     fw[3][1] = cur.f1;
   }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128) k_mg_smooth_col(MGLevels<T> M, int l, int mode, int x_zero) {
+  const int n = M.n[l];
+  const int lane = threadIdx.x & 31;
+  const int nsx = (n + kColSmOut - 1) / kColSmOut, nsy = (n + kColSmH - 1) / kColSmH;
+  const int gw = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (gw >= nsx * nsy) return;  // warp-uniform; the kernel has no block barrier
+  const int xs = (gw % nsx) * kColSmOut, y0 = (gw / nsx) * kColSmH;
+  const bool px = M.periodic[0], py = M.periodic[1];
+  // the fast climb needs both columns of every lane inside the domain with
+  // both x neighbours, and every row of the wavefront (y0 - 3 .. y0 + kColSmH
+  // + 2, plus the rows above and below it) inside with both y neighbours
+  const int c0 = xs - 4 + 2 * lane;
+  const bool lane_inner = px || (c0 >= 1 && c0 + 2 < n);
+  const bool rows_inner = py || (y0 - 3 >= 1 && y0 + kColSmH + 2 <= n - 2);
+  if (__all_sync(0xffffffffu, lane_inner) && rows_inner)
+    smooth_col_march<T, true>(M, l, mode, x_zero, xs, y0, lane);
+  else
+    smooth_col_march<T, false>(M, l, mode, x_zero, xs, y0, lane);
 }
 
 // residual at level l restricted (cell average) to the RHS of level l+1
