@@ -71,10 +71,6 @@ struct ns_ctx {
   float* SFl[2] = {nullptr, nullptr};
   int mb = 0;
   bool base_ff_valid = false, s_ff_valid = false;
-  // a pseudo-iteration head launched ahead of its iteration while the host
-  // waits for the norm: -1 none, 0 the incremental update, 1 the exact anchor
-  int spec_head = -1;
-  cudaEvent_t norm_ev = nullptr;  // the norm's read-back has landed
   // float-float phi (ping-pong) and RHS of the mixed Poisson solve
   float* PFh[2] = {nullptr, nullptr};
   float* PFl[2] = {nullptr, nullptr};

@@ -141,7 +141,6 @@ void free_all(ns_ctx* c) {
   if (c->own_stream && c->st) cudaStreamDestroy(c->st);
   for (auto& e : c->side_ev)
     if (e) cudaEventDestroy(e);
-  if (c->norm_ev) cudaEventDestroy(c->norm_ev);
   if (c->side) cudaStreamDestroy(c->side);
 }
 
@@ -414,7 +413,6 @@ int ns_ctx_create(const ns_params* p, void* stream, ns_ctx** out) {
     bool ok = true;
     for (auto& e : c->ev) ok = ok && cudaEventCreate(&e) == cudaSuccess;
     c->ev_ok = ok;
-    if (cudaEventCreateWithFlags(&c->norm_ev, cudaEventDisableTiming) != cudaSuccess) c->norm_ev = nullptr;
     c->M64.x[0] = c->PHI[0];
     c->M64.f[0] = c->F;
     c->M64.fmean = c->red + kRedMean;
@@ -659,7 +657,6 @@ int ns_step_begin(ns_ctx* c) {
   c->norm_ready = false;
   c->mix_pending = false;
   c->base_ff_valid = false;
-  c->spec_head = -1;  // a head launched ahead of an iteration that did not come
   c->s_ff_valid = false;
   return NS_OK;
 }
@@ -1187,27 +1184,47 @@ static void split_const(double x, float* out) {
   out[1] = (float)(x - (double)out[0]);
 }
 
-// exact anchors: at most kAnchorEvery iterations apart, and once the
-// pseudo-norm has fallen below kAnchorDrop times its value after the last one
+// One pseudo-iteration of the mixed-precision predictor: the anchor stage
+// evaluates G(u_base) in float-float arithmetic (after adding the pending
+// increment of the previous iteration), then three FP32 increment stages; the
+// fourth stage's increment e4 stays in E[0] and its norm is the
+// pseudo-increment norm of Error_Computation.
+// the anchor is evaluated exactly (float-float) on the first iteration, at
+// most kAnchorEvery iterations after the last exact one, and once the
+// pseudo-norm has fallen below kAnchorDrop times its value after the last
+// exact one; the others update it by an FP32 increment evaluation. Each
+// update rounds the stored G0 to FP32, an error relative to |G0| at that
+// iteration; the errors add up until the next exact anchor and shift the
+// converged u* by their sum over 1.5/dt, so the refresh on a falling norm
+// keeps that sum within a small multiple of the final norm however few
+// iterations the step takes.
 // (4096^2 cavity: a cap of 16 gives 5 exact anchors a step, 32 gives 3 and
-// 0.8% more steps/s)
+// 0.8% more steps/s.)
 constexpr int kAnchorEvery = 32;
 constexpr double kAnchorDrop = 1e-2;
 
-// The head of a pseudo-iteration from the current state (no host state
-// changes): the exact float-float anchor G(u_b), or the incremental update
-// G0 + dG(u_b; e4) by the FP32 increment kernel with rk = 1 (its rounding
-// error is relative to e4), whose launch also writes u_b + e4 in float-float
-// to the other base buffer. Both write only the other buffers of their pairs
-// (base hi/lo, and G0b for the update; the exact anchor's G0 is an input of
-// nothing after the iteration that launched it), so a head launched ahead of
-// its iteration can be dropped.
-static int launch_head(ns_ctx* c, bool exact) {
-  const int mb = c->mb, nb = 1 - c->mb;
+static int mixed_iteration(ns_ctx* c, double* norm) {
+  if (!c->s_ff_valid) {
+    const double* S[2] = {c->S[0], c->S[1]};
+    LAUNCH(NS_PROF_OTHER, "split S", launch_split_ff(c->g, S, c->SFh, c->SFl, c->st));
+    c->s_ff_valid = true;
+  }
+  if (!c->base_ff_valid) {
+    const double* B[2] = {face_ptr(c, c->base, 0), face_ptr(c, c->base, 1)};
+    LAUNCH(NS_PROF_OTHER, "split base", launch_split_ff(c->g, B, c->BH[0], c->BL[0], c->st));
+    c->mb = 0;
+    c->base_ff_valid = true;
+    c->mix_pending = false;
+  }
+  const bool exact = !c->mix_pending || c->mix_it - c->mix_last_exact >= kAnchorEvery ||
+                     !(c->mix_norm >= kAnchorDrop * c->mix_norm_exact);
+  if (exact) c->mix_last_exact = c->mix_it;
+  ++c->mix_it;
   if (exact) {
     AnchorFFArgs a;
     std::memset(&a, 0, sizeof(a));
     a.g = c->g;
+    const int mb = c->mb, nb = 1 - c->mb;
     for (int m = 0; m < 2; ++m) {
       a.bh[m] = c->BH[mb][m];
       a.bl[m] = c->BL[mb][m];
@@ -1222,75 +1239,39 @@ static int launch_head(ns_ctx* c, bool exact) {
     }
     split_const(c->g.c15, a.c15);
     LAUNCH(NS_PROF_ANCHOR, "anchor stage", launch_anchor_ff(a, c->st));
-    return NS_OK;
-  }
-  IncArgs u;
-  std::memset(&u, 0, sizeof(u));
-  u.g = c->g;
-  u.part = reinterpret_cast<float2*>(c->part);
-  u.counter = c->counter;
-  u.norm_out = c->red + kRedNorm;
-  for (int m = 0; m < 2; ++m) {
-    u.sh[m] = c->BH[mb][m];
-    u.g0[m] = c->G0[m];
-    u.ein[m] = c->E[0][m];
-    u.eout[m] = c->G0b[m];
-    u.bl[m] = c->BL[mb][m];
-    u.obh[m] = c->BH[nb][m];
-    u.obl[m] = c->BL[nb][m];
-    u.inv_dx[m] = (float)c->g.inv_dx[m];
-    u.vcoef[m] = (float)(1.0 / (c->g.ren * c->g.dx2[m]));
-  }
-  u.c15 = (float)c->g.c15;
-  u.rk_prev = 1.f;
-  u.rk = 1.f;
-  u.do_norm = 0;
-  LAUNCH(NS_PROF_INC, "anchor update", launch_inc_stage(u, c->st));
-  return NS_OK;
-}
-
-// One pseudo-iteration of the mixed-precision predictor: the head (exact
-// anchor or incremental update), then three FP32 increment stages; the fourth
-// stage's increment e4 stays in E[0] and its norm is the pseudo-increment norm
-// of Error_Computation. The anchor is evaluated exactly on the first
-// iteration, at most kAnchorEvery iterations after the last exact one, and
-// once the pseudo-norm has fallen below kAnchorDrop times its value after the
-// last exact one. Each incremental update rounds the stored G0 to FP32, an
-// error relative to |G0| at that iteration; the errors add up until the next
-// exact anchor and shift the converged u* by their sum over 1.5/dt, so the
-// refresh on a falling norm keeps that sum within a small multiple of the
-// final norm however few iterations the step takes.
-// While the host waits for the norm, the next iteration's head is already in
-// flight, launched with the decision the host can make before the norm
-// arrives (exact only when the cadence demands it): the GPU does not idle
-// through the read-back and the host's launches. When the norm asks for an
-// exact anchor instead, or the loop stops, that head is dropped.
-static int mixed_iteration(ns_ctx* c, double* norm) {
-  if (!c->s_ff_valid) {
-    const double* S[2] = {c->S[0], c->S[1]};
-    LAUNCH(NS_PROF_OTHER, "split S", launch_split_ff(c->g, S, c->SFh, c->SFl, c->st));
-    c->s_ff_valid = true;
-  }
-  if (!c->base_ff_valid) {
-    const double* B[2] = {face_ptr(c, c->base, 0), face_ptr(c, c->base, 1)};
-    LAUNCH(NS_PROF_OTHER, "split base", launch_split_ff(c->g, B, c->BH[0], c->BL[0], c->st));
-    c->mb = 0;
-    c->base_ff_valid = true;
-    c->mix_pending = false;
-    c->spec_head = -1;
-  }
-  const bool exact = !c->mix_pending || c->mix_it - c->mix_last_exact >= kAnchorEvery ||
-                     !(c->mix_norm >= kAnchorDrop * c->mix_norm_exact);
-  if (exact) c->mix_last_exact = c->mix_it;
-  ++c->mix_it;
-  if (c->spec_head != (exact ? 1 : 0)) {
-    const int r = launch_head(c, exact);
-    if (r != NS_OK) return r;
-  }
-  c->spec_head = -1;
-  if (!exact)
+    c->mb = nb;
+  } else {
+    // incremental anchor: G0 + dG(u_b; e4) by the FP32 increment kernel with
+    // rk = 1 (its rounding error is relative to e4); the same launch writes
+    // u_b + e4 in float-float to the other base buffer. The exact float-float
+    // anchor of the next kAnchorEvery-th iteration removes whatever these
+    // updates accumulated
+    const int mb = c->mb, nb = 1 - c->mb;
+    IncArgs u;
+    std::memset(&u, 0, sizeof(u));
+    u.g = c->g;
+    u.part = reinterpret_cast<float2*>(c->part);
+    u.counter = c->counter;
+    u.norm_out = c->red + kRedNorm;
+    for (int m = 0; m < 2; ++m) {
+      u.sh[m] = c->BH[mb][m];
+      u.g0[m] = c->G0[m];
+      u.ein[m] = c->E[0][m];
+      u.eout[m] = c->G0b[m];
+      u.bl[m] = c->BL[mb][m];
+      u.obh[m] = c->BH[nb][m];
+      u.obl[m] = c->BL[nb][m];
+      u.inv_dx[m] = (float)c->g.inv_dx[m];
+      u.vcoef[m] = (float)(1.0 / (c->g.ren * c->g.dx2[m]));
+    }
+    u.c15 = (float)c->g.c15;
+    u.rk_prev = 1.f;
+    u.rk = 1.f;
+    u.do_norm = 0;
+    LAUNCH(NS_PROF_INC, "anchor update", launch_inc_stage(u, c->st));
     for (int m = 0; m < 2; ++m) std::swap(c->G0[m], c->G0b[m]);
-  c->mb = 1 - c->mb;
+    c->mb = nb;
+  }
   const int nb = c->mb;  // the base of this iteration's increment stages
   IncArgs ia;
   std::memset(&ia, 0, sizeof(ia));
@@ -1317,18 +1298,8 @@ static int mixed_iteration(ns_ctx* c, double* norm) {
     LAUNCH(NS_PROF_INC, "increment stage", launch_inc_stage(ia, c->st));
   }
   c->mix_pending = true;
-  CK(cudaMemcpyAsync(c->red_h + kRedNorm, c->red + kRedNorm, sizeof(double), cudaMemcpyDeviceToHost, c->st),
-     "readback");
-  if (c->norm_ev) {
-    CK(cudaEventRecord(c->norm_ev, c->st), "event");
-    const bool guess = c->mix_it - c->mix_last_exact >= kAnchorEvery;
-    const int r = launch_head(c, guess);
-    if (r != NS_OK) return r;
-    c->spec_head = guess ? 1 : 0;
-    CK(cudaEventSynchronize(c->norm_ev), "norm wait");
-  } else {
-    CK(cudaStreamSynchronize(c->st), "stream sync");
-  }
+  int r = sync_red(c, kRedNorm, 1);
+  if (r != NS_OK) return r;
   *norm = c->red_h[kRedNorm];
   c->mix_norm = *norm;
   if (exact) c->mix_norm_exact = *norm;
