@@ -88,8 +88,7 @@ cudaError_t launch3i_cart(const Inc3& a, cudaStream_t s) {
 }
 cudaError_t launch3i_total(const Inc3& a, cudaStream_t s) {
   const int N = a.g.N;
-  k3i_flux<<<grid3(N + 1, N + 1, N + 1), 256, 0, s>>>(a);
-  k3i_total<<<grid3(N, N, N), 256, 0, s>>>(a);
+  k3i_fluxtot<<<dim3((N + 31) / 32, (N + 7) / 8, (N + kFtKZ - 1) / kFtKZ), 256, 0, s>>>(a);
   return cudaGetLastError();
 }
 cudaError_t launch3i_face(const Inc3& a, cudaStream_t s) {

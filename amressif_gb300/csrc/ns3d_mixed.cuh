@@ -272,62 +272,138 @@ __global__ void __launch_bounds__(256) k3i_cart(Inc3 A) {
 __device__ __forceinline__ float q3p(float x2, float x1, float x0) { return -0.125f * x2 + 0.75f * x1 + 0.375f * x0; }
 __device__ __forceinline__ float q3m(float x1, float x0, float xa) { return 0.375f * x1 + 0.75f * x0 - 0.125f * xa; }
 
-// flux increments of the three components at every face along the three
-// directions, each face once (the faces of k3_flux)
-__global__ void __launch_bounds__(256) k3i_flux(Inc3 A) {
-  const Geom& g = A.g;
-  const int N = g.N;
-  NS3_IJK(0, 0, 0)
-  if (i > N || j > N || k > N) return;
-  const long G1[3] = {1, N + 4, (long)(N + 4) * (N + 4)};
-  const long gc = gid3(N, i, j, k);
-  const long fc = id3(g, i, j, k);
-  const int c[3] = {i, j, k};
-  for (int d = 0; d < 3; ++d) {
-    bool ok = true;
-    for (int e = 0; e < 3; ++e)
-      if (e != d && c[e] >= N) ok = false;
-    if (!ok) continue;
-    const long s = G1[d];
-    const float ub = ldf(A.ub[d], fc);
-    const float e = inc_e(A, d, fc);
-    const float un = ub + e;
-    const float dpos = ub > 0.f ? (un > 0.f ? e : -ub) : fmaxf(un, 0.f);  // un+ - ub+
-    const float dneg = e - dpos;                                            // un- - ub-
-    const bool pos = un > 0.f;
-    for (int m = 0; m < 3; ++m) {
-      const float* pb = A.phb[m];
-      const float* pe = A.phe[m];
-      const float b2 = ldf(pb, gc - 2 * s), b1 = ldf(pb, gc - s), b0 = ldf(pb, gc), ba = ldf(pb, gc + s);
-      const float e1 = ldf(pe, gc - s), e0 = ldf(pe, gc);
-      const float qe = pos ? q3p(ldf(pe, gc - 2 * s), e1, e0) : q3m(e1, e0, ldf(pe, gc + s));
-      A.dfl[d][m][fc] = dpos * q3p(b2, b1, b0) + dneg * q3m(b1, b0, ba) + un * qe;
-    }
-  }
+// Flux increments and cell totals in one pass (dt_m = nu lap(phi_e,m) -
+// div dF_m): the QUICK flux increments of the three components at every face
+// along the three directions, then the cell totals, without the nine
+// face-flux arrays between two passes (36 B/cell of stores and more of loads). A block owns a 32 x 8 tile of
+// cells and climbs kFtKZ planes of it. Per plane it stages the ghosted cell
+// velocities of the tile and a halo (x: -2..+33, y: -2..+9) in shared memory,
+// forms the x and y face fluxes of the tile (33 x 8 and 32 x 9 faces) there,
+// and each thread carries its column's z window (cells k-1 .. k+2) and its
+// bottom z-face flux in registers, so every face flux is formed once.
+constexpr int kFtKZ = 16;
+struct FtSmem {
+  float pb[3][12][36];  // phi_b (ghosted cell velocity of u_b), plane k, tile + halo
+  float pe[3][12][36];  // phi_e (of the increment)
+  float fx[3][8][33];   // x-face flux increments of the tile's rows
+  float fy[3][9][32];   // y-face flux increments of the tile's columns
+};
+
+__device__ __forceinline__ float flux_inc(float ub, float e, float b2, float b1, float b0, float ba, float e2, float e1,
+                                          float e0, float ea) {
+  const float un = ub + e;
+  const float dpos = ub > 0.f ? (un > 0.f ? e : -ub) : fmaxf(un, 0.f);  // un+ - ub+
+  const float dneg = e - dpos;                                            // un- - ub-
+  const float qe = un > 0.f ? q3p(e2, e1, e0) : q3m(e1, e0, ea);
+  return dpos * q3p(b2, b1, b0) + dneg * q3m(b1, b0, ba) + un * qe;
 }
 
-// dt_m = nu lap(phi_e,m) - div dF_m at the cells
-__global__ void __launch_bounds__(256) k3i_total(Inc3 A) {
+__global__ void __launch_bounds__(256) k3i_fluxtot(Inc3 A) {
+  __shared__ FtSmem sm;
   const Geom& g = A.g;
   const int N = g.N;
-  NS3_IJK(0, 0, 0)
-  if (i >= N || j >= N || k >= N) return;
-  const long G1[3] = {1, N + 4, (long)(N + 4) * (N + 4)};
-  const long gc = gid3(N, i, j, k);
-  const long fc = id3(g, i, j, k);
-  const long fstride[3] = {1, g.pitch, g.plane};
-  for (int m = 0; m < 3; ++m) {
-    const float* ph = A.phe[m];
-    const float p0 = ldf(ph, gc);
-    float conv = 0.f, visc = 0.f;
-    for (int d = 0; d < 3; ++d) {
-      const long s = G1[d];
-      const float* F = A.dfl[d][m];
-      conv += (ldf(F, fc + fstride[d]) - ldf(F, fc)) * A.inv_dx[d];
-      visc += (ldf(ph, gc + s) - 2.f * p0 + ldf(ph, gc - s)) * A.vcoef[d];
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const int i0 = blockIdx.x * 32, j0 = blockIdx.y * 8, k0 = blockIdx.z * kFtKZ;
+  const int k1 = min(k0 + kFtKZ, N);
+  const int i = i0 + tx, j = j0 + ty;
+  const bool cell = i < N && j < N;
+  const long G1 = 1, G2 = N + 4, G3 = (long)(N + 4) * (N + 4);
+  // the column's z window: zb[m][q] / ze[m][q] = phi at plane k - 1 + q
+  float zb[3][4], ze[3][4], fzb[3];
+  auto zload = [&](int m, int kk, float& b, float& e) {
+    const long gi = gid3(N, i, j, kk);
+    b = ldf(A.phb[m], gi);
+    e = ldf(A.phe[m], gi);
+  };
+  if (cell) {
+    // the bottom z-face flux of the chunk's first plane (cells k0-2 .. k0+1)
+    float b2[3], e2[3];
+    for (int m = 0; m < 3; ++m) {
+      zload(m, k0 - 2, b2[m], e2[m]);
+      for (int q = 0; q < 3; ++q) zload(m, k0 - 1 + q, zb[m][q], ze[m][q]);
     }
-    A.dt[m][fc] = visc - conv;
+    const long fz = id3(g, i, j, k0);
+    const float ubz = ldf(A.ub[2], fz), ez = inc_e(A, 2, fz);
+    for (int m = 0; m < 3; ++m)
+      fzb[m] = flux_inc(ubz, ez, b2[m], zb[m][0], zb[m][1], zb[m][2], e2[m], ze[m][0], ze[m][1], ze[m][2]);
   }
+  for (int k = k0; k < k1; ++k) {
+    __syncthreads();  // the previous plane's shared values are consumed
+    for (int t = threadIdx.x; t < 12 * 36; t += 256) {
+      const int sx = t % 36, sy = t / 36;
+      const int a = i0 - 2 + sx, b = j0 - 2 + sy;
+      const bool in = a <= N + 1 && b <= N + 1;  // the ghosted array spans -2 .. N + 1
+      const long gi = in ? gid3(N, a, b, k) : 0;
+      for (int m = 0; m < 3; ++m) {
+        sm.pb[m][sy][sx] = in ? ldf(A.phb[m], gi) : 0.f;
+        sm.pe[m][sy][sx] = in ? ldf(A.phe[m], gi) : 0.f;
+      }
+    }
+    if (cell)
+      for (int m = 0; m < 3; ++m) zload(m, k + 2, zb[m][3], ze[m][3]);
+    __syncthreads();
+    // x faces (i0 .. i0 + 32) x rows (j0 .. j0 + 7)
+    for (int t = threadIdx.x; t < 33 * 8; t += 256) {
+      const int ii = t % 33, jj = t / 33;
+      const int a = i0 + ii, b = j0 + jj;
+      if (a > N || b >= N) continue;
+      const long fc = id3(g, a, b, k);
+      const float ub = ldf(A.ub[0], fc), e = inc_e(A, 0, fc);
+      const int sx = ii + 2, sy = jj + 2;
+      for (int m = 0; m < 3; ++m) {
+        const float(*pb)[36] = sm.pb[m];
+        const float(*pe)[36] = sm.pe[m];
+        sm.fx[m][jj][ii] = flux_inc(ub, e, pb[sy][sx - 2], pb[sy][sx - 1], pb[sy][sx], pb[sy][sx + 1], pe[sy][sx - 2],
+                                    pe[sy][sx - 1], pe[sy][sx], pe[sy][sx + 1]);
+      }
+    }
+    // y faces (j0 .. j0 + 8) x columns (i0 .. i0 + 31)
+    for (int t = threadIdx.x; t < 32 * 9; t += 256) {
+      const int ii = t % 32, jj = t / 32;
+      const int a = i0 + ii, b = j0 + jj;
+      if (a >= N || b > N) continue;
+      const long fc = id3(g, a, b, k);
+      const float ub = ldf(A.ub[1], fc), e = inc_e(A, 1, fc);
+      const int sx = ii + 2, sy = jj + 2;
+      for (int m = 0; m < 3; ++m) {
+        const float(*pb)[36] = sm.pb[m];
+        const float(*pe)[36] = sm.pe[m];
+        sm.fy[m][jj][ii] = flux_inc(ub, e, pb[sy - 2][sx], pb[sy - 1][sx], pb[sy][sx], pb[sy + 1][sx], pe[sy - 2][sx],
+                                    pe[sy - 1][sx], pe[sy][sx], pe[sy + 1][sx]);
+      }
+    }
+    __syncthreads();
+    if (cell) {
+      // the top z-face flux (cells k-1 .. k+2) and the totals of cell (i, j, k)
+      const long fz = id3(g, i, j, k + 1);
+      const float ubz = ldf(A.ub[2], fz), ez = inc_e(A, 2, fz);
+      const long fc = id3(g, i, j, k);
+      const int sx = tx + 2, sy = ty + 2;
+      for (int m = 0; m < 3; ++m) {
+        const float fzt =
+            flux_inc(ubz, ez, zb[m][0], zb[m][1], zb[m][2], zb[m][3], ze[m][0], ze[m][1], ze[m][2], ze[m][3]);
+        const float(*pe)[36] = sm.pe[m];
+        const float p0 = pe[sy][sx];
+        float conv = 0.f, visc = 0.f;
+        conv += (sm.fx[m][ty][tx + 1] - sm.fx[m][ty][tx]) * A.inv_dx[0];
+        visc += (pe[sy][sx + 1] - 2.f * p0 + pe[sy][sx - 1]) * A.vcoef[0];
+        conv += (sm.fy[m][ty + 1][tx] - sm.fy[m][ty][tx]) * A.inv_dx[1];
+        visc += (pe[sy + 1][sx] - 2.f * p0 + pe[sy - 1][sx]) * A.vcoef[1];
+        conv += (fzt - fzb[m]) * A.inv_dx[2];
+        visc += (ze[m][2] - 2.f * p0 + ze[m][0]) * A.vcoef[2];
+        A.dt[m][fc] = visc - conv;
+        fzb[m] = fzt;
+      }
+      for (int m = 0; m < 3; ++m)
+        for (int q = 0; q < 3; ++q) {
+          zb[m][q] = zb[m][q + 1];
+          ze[m][q] = ze[m][q + 1];
+        }
+    }
+  }
+  (void)G1;
+  (void)G2;
+  (void)G3;
 }
 
 __device__ __forceinline__ float t_along_inc(const Inc3& A, int m, int a, long base, long st) {
