@@ -122,6 +122,19 @@ cudaError_t launch3_mg_bottom(const MG3<T>& M, int l, int sweeps, cudaStream_t s
   return cudaGetLastError();
 }
 template <typename T>
+cudaError_t launch3_mg_coarse(const MG3<T>& M, int lb, cudaStream_t s) {
+  const size_t smem = mg3_bottom_smem(M, lb);
+  static bool attr_set = false;
+  if (!attr_set) {
+    const cudaError_t e = cudaFuncSetAttribute(k3_mg_coarse<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    if (e != cudaSuccess) return e;
+    attr_set = true;
+  }
+  if (smem > 200 * 1024) return cudaErrorInvalidValue;
+  k3_mg_coarse<T><<<1, 1024, smem, s>>>(M, lb);
+  return cudaGetLastError();
+}
+template <typename T>
 cudaError_t launch3_mg_resnorm(const MG3<T>& M, double* part, unsigned* counter, double* out, cudaStream_t s) {
   const int n = M.n[0];
   k3_mg_resnorm<T><<<grid3(n, n, n), 256, 0, s>>>(M, part, counter, out);
@@ -133,6 +146,7 @@ cudaError_t launch3_mg_resnorm(const MG3<T>& M, double* part, unsigned* counter,
   template cudaError_t launch3_mg_restrict<T>(const MG3<T>&, int, cudaStream_t);                  \
   template cudaError_t launch3_mg_prolong<T>(const MG3<T>&, int, cudaStream_t);                   \
   template cudaError_t launch3_mg_bottom<T>(const MG3<T>&, int, int, cudaStream_t);               \
+  template cudaError_t launch3_mg_coarse<T>(const MG3<T>&, int, cudaStream_t);                    \
   template cudaError_t launch3_mg_resnorm<T>(const MG3<T>&, double*, unsigned*, double*, cudaStream_t);
 NS3_INST(double)
 NS3_INST(float)

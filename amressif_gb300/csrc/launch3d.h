@@ -27,7 +27,7 @@ cudaError_t launch3_dcff(const DCff3& a, cudaStream_t s);
 cudaError_t launch3_rhs_ff(int n, long pitch, long plane, const double* f, const double* mean, float2* out, cudaStream_t s);
 cudaError_t launch3_ff_cells(int n, long pitch, long plane, const float2* in, double* out, cudaStream_t s);
 cudaError_t launch3i_cart(const Inc3& a, cudaStream_t s);
-cudaError_t launch3i_total(const Inc3& a, cudaStream_t s);  // flux increments, then cell totals
+cudaError_t launch3i_total(const Inc3& a, cudaStream_t s);  // flux increments and cell totals, one pass
 cudaError_t launch3i_face(const Inc3& a, cudaStream_t s);
 
 template <typename T>
@@ -38,6 +38,8 @@ template <typename T>
 cudaError_t launch3_mg_prolong(const MG3<T>& M, int l, cudaStream_t s);
 template <typename T>
 cudaError_t launch3_mg_bottom(const MG3<T>& M, int l, int sweeps, cudaStream_t s);
+template <typename T>
+cudaError_t launch3_mg_coarse(const MG3<T>& M, int lb, cudaStream_t s);  // levels lb..L-1 in one block
 template <typename T>
 cudaError_t launch3_mg_resnorm(const MG3<T>& M, double* part, unsigned* counter, double* out, cudaStream_t s);
 

@@ -300,6 +300,9 @@ struct MG3 {
   const double* fmean;   // subtracted from f at level 0 when non-null
 };
 
+// levels with n <= kBottom3N run in the persistent coarse block (k3_mg_coarse)
+constexpr int kBottom3N = 16;
+
 #ifndef NS_3D_ARGS_ONLY
 
 template <typename T>
@@ -416,6 +419,209 @@ __global__ void __launch_bounds__(1024) k3_mg_bottom(MG3<T> M, int l, int sweeps
       if (dg > (T)0) M.x[l][id] = (s - mg3_f(M, l, id)) / dg;
     }
     __syncthreads();
+  }
+}
+
+// ---- the coarse levels (n <= kBottom3N) in one persistent block ------------------------
+// The levels lb .. L-1 of a V-cycle in shared memory: on each the two
+// red-black pre-sweeps and the restriction of its residual, on the coarsest a
+// conjugate-gradient solve of L x = f - mean f (the constant mode projected
+// out: every 3D box here is all-Neumann or periodic, so L is singular), then
+// upward the trilinear prolongation and the two post-sweeps: the arithmetic of
+// k3_mg_rb, k3_mg_restrict and k3_mg_prolong, with the coarsest level solved
+// instead of swept 50 times. One launch in place of ten per level. The result
+// replaces x at level lb in global memory.
+
+template <typename T>
+__device__ __forceinline__ T k3_block_sum(T v, T* red) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  T s = (T)0;
+  if (threadIdx.x == 0) {
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w];
+    red[0] = s;
+  }
+  __syncthreads();
+  s = red[0];
+  __syncthreads();
+  return s;
+}
+
+// shared-memory bytes of the persistent coarse block from level lb
+template <typename T>
+inline size_t mg3_bottom_smem(const MG3<T>& M, int lb) {
+  size_t cells = 0;
+  for (int l = lb; l < M.L; ++l) cells += (size_t)M.n[l] * M.n[l] * M.n[l];
+  const size_t nc = (size_t)M.n[M.L - 1] * M.n[M.L - 1] * M.n[M.L - 1];
+  return (3 * cells + 3 * nc) * sizeof(T);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(1024) k3_mg_coarse(MG3<T> M, int lb) {
+  extern __shared__ __align__(16) unsigned char mg3c_smem[];
+  __shared__ T red[32];
+  __shared__ int off[kMaxLevels3];
+  const int tid = threadIdx.x, NT = blockDim.x;
+  const bool px = M.periodic[0], py = M.periodic[1], pz = M.periodic[2];
+  int cells = 0;
+  for (int l = lb; l < M.L; ++l) cells += M.n[l] * M.n[l] * M.n[l];
+  const int Lc = M.L - 1;
+  const int ncc = M.n[Lc] * M.n[Lc] * M.n[Lc];
+  T* sx = reinterpret_cast<T*>(mg3c_smem);
+  T* sf = sx + cells;
+  T* sr = sf + cells;
+  T* pcg = sr + cells;
+  T* qcg = pcg + ncc;
+  T* rcg = qcg + ncc;
+  if (tid == 0) {
+    int o = 0;
+    for (int l = lb; l < M.L; ++l) { off[l] = o; o += M.n[l] * M.n[l] * M.n[l]; }
+  }
+  __syncthreads();
+  {
+    const int n = M.n[lb];
+    for (int t = tid; t < n * n * n; t += NT) {
+      const int i = t % n, j = (t / n) % n, k = t / (n * n);
+      const long id = (long)k * M.plane[lb] + (long)j * M.pitch[lb] + i;
+      sf[off[lb] + t] = mg3_f(M, lb, id);
+      sx[off[lb] + t] = M.x[lb][id];  // zero below the finest level (the restriction clears it)
+    }
+  }
+  __syncthreads();
+  // the neighbour sum and diagonal of mg3_lap_terms on a dense n^3 level
+  auto lap = [&](const T* x, int l, int i, int j, int k, T* dg) {
+    const int n = M.n[l];
+    const bool per[3] = {px, py, pz};
+    const int c[3] = {i, j, k};
+    const int st[3] = {1, n, n * n};
+    const int id = (k * n + j) * n + i;
+    T s = (T)0, d = (T)0;
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      const T h = M.ih[l][q];
+      if (per[q] || c[q] + 1 < n) {
+        s += x[id + ((c[q] + 1 < n) ? st[q] : -(n - 1) * st[q])] * h;
+        d += h;
+      }
+      if (per[q] || c[q] > 0) {
+        s += x[id + ((c[q] > 0) ? -st[q] : (n - 1) * st[q])] * h;
+        d += h;
+      }
+    }
+    *dg = d;
+    return s;
+  };
+  auto sweep = [&](int l, int color) {
+    const int n = M.n[l];
+    T* x = sx + off[l];
+    const T* f = sf + off[l];
+    for (int t = tid; t < n * n * n; t += NT) {
+      const int i = t % n, j = (t / n) % n, k = t / (n * n);
+      if (((i + j + k) & 1) != color) continue;
+      T dg;
+      const T s = lap(x, l, i, j, k, &dg);
+      if (dg > (T)0) x[t] = (s - f[t]) / dg;
+    }
+    __syncthreads();
+  };
+  for (int l = lb; l < Lc; ++l) {
+    for (int s = 0; s < 4; ++s) sweep(l, s & 1);
+    const int n = M.n[l], nc = M.n[l + 1];
+    const T* x = sx + off[l];
+    const T* f = sf + off[l];
+    for (int t = tid; t < nc * nc * nc; t += NT) {
+      const int I = t % nc, J = (t / nc) % nc, K = t / (nc * nc);
+      T acc = (T)0;
+      for (int c = 0; c < 8; ++c) {
+        const int i = 2 * I + (c & 1), j = 2 * J + ((c >> 1) & 1), k = 2 * K + (c >> 2);
+        const int id = (k * n + j) * n + i;
+        T dg;
+        const T s = lap(x, l, i, j, k, &dg);
+        acc += f[id] - (s - dg * x[id]);
+      }
+      sf[off[l + 1] + t] = acc * (T)0.125;
+      sx[off[l + 1] + t] = (T)0;
+    }
+    __syncthreads();
+  }
+  {  // coarsest: CG on -L x = -(f - mean f)
+    const int n = M.n[Lc], nn = ncc;
+    T* x = sx + off[Lc];
+    const T* b = sf + off[Lc];
+    auto negL = [&](const T* in, T* out) {
+      for (int t = tid; t < nn; t += NT) {
+        const int i = t % n, j = (t / n) % n, k = t / (n * n);
+        T dg;
+        const T s = lap(in, Lc, i, j, k, &dg);
+        out[t] = dg * in[t] - s;  // -L in
+      }
+    };
+    T part = (T)0;
+    for (int t = tid; t < nn; t += NT) part += b[t];
+    const T mean = k3_block_sum<T>(part, red) / (T)nn;
+    for (int t = tid; t < nn; t += NT) { rcg[t] = -(b[t] - mean); x[t] = (T)0; pcg[t] = rcg[t]; }
+    __syncthreads();
+    part = (T)0;
+    for (int t = tid; t < nn; t += NT) part += rcg[t] * rcg[t];
+    T rr = k3_block_sum<T>(part, red);
+    const T rr0 = rr;
+    const T eps = sizeof(T) == 8 ? (T)1e-28 : (T)1e-12;
+    for (int it = 0; it < 4 * nn && rr > eps * rr0 && rr > (T)0; ++it) {
+      negL(pcg, qcg);
+      __syncthreads();
+      part = (T)0;
+      for (int t = tid; t < nn; t += NT) part += pcg[t] * qcg[t];
+      const T pq = k3_block_sum<T>(part, red);
+      if (!(pq > (T)0)) break;
+      const T alpha = rr / pq;
+      for (int t = tid; t < nn; t += NT) { x[t] += alpha * pcg[t]; rcg[t] -= alpha * qcg[t]; }
+      __syncthreads();
+      part = (T)0;
+      for (int t = tid; t < nn; t += NT) part += rcg[t] * rcg[t];
+      const T rr2 = k3_block_sum<T>(part, red);
+      const T beta = rr2 / rr;
+      rr = rr2;
+      for (int t = tid; t < nn; t += NT) pcg[t] = rcg[t] + beta * pcg[t];
+      __syncthreads();
+    }
+  }
+  for (int l = Lc - 1; l >= lb; --l) {
+    const int n = M.n[l], nc = M.n[l + 1];
+    const T* xc = sx + off[l + 1];
+    T* x = sx + off[l];
+    const bool per[3] = {px, py, pz};
+    for (int t = tid; t < n * n * n; t += NT) {
+      const int c[3] = {t % n, (t / n) % n, t / (n * n)};
+      int C[3], Nb[3];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        C[d] = c[d] >> 1;
+        const int o = (c[d] & 1) ? 1 : -1;
+        int nb = C[d] + o;
+        if (nb < 0 || nb >= nc) nb = per[d] ? wrapi(nb, nc) : C[d];
+        Nb[d] = nb;
+      }
+      T v = (T)0;
+#pragma unroll
+      for (int s = 0; s < 8; ++s) {
+        const int a = (s & 1) ? Nb[0] : C[0], b = ((s >> 1) & 1) ? Nb[1] : C[1], e = (s >> 2) ? Nb[2] : C[2];
+        const T w = (T)(((s & 1) ? 0.25 : 0.75) * (((s >> 1) & 1) ? 0.25 : 0.75) * ((s >> 2) ? 0.25 : 0.75));
+        v += w * xc[(e * nc + b) * nc + a];
+      }
+      x[t] += v;
+    }
+    __syncthreads();
+    for (int s = 0; s < 4; ++s) sweep(l, (s + 1) & 1);
+  }
+  {
+    const int n = M.n[lb];
+    for (int t = tid; t < n * n * n; t += NT) {
+      const int i = t % n, j = (t / n) % n, k = t / (n * n);
+      M.x[lb][(long)k * M.plane[lb] + (long)j * M.pitch[lb] + i] = sx[off[lb] + t];
+    }
   }
 }
 

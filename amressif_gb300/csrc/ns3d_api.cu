@@ -99,8 +99,31 @@ int pick3(int base, int in) {
   return -2;
 }
 
+// the first level from which the V-cycle runs in the persistent coarse block
+// (n <= kBottom3N down to the coarsest); M.L when the coarsest level is larger
+template <typename T>
+int coarse_level3(const MG3<T>& M) {
+  int lb = 0;
+  while (lb < M.L && M.n[lb] > kBottom3N) ++lb;
+  return lb;
+}
+
 template <typename T>
 int vcycle3(ns_ctx* c, MG3<T>& M) {
+  const int lb = coarse_level3(M);
+  if (lb < M.L) {
+    // levels above lb as launches, lb and below in one block
+    for (int l = 0; l < lb; ++l) {
+      for (int s = 0; s < 4; ++s) LAUNCH(l == 0 ? NS_PROF_MG_SMOOTH0 : NS_PROF_MG_SMOOTH, "mg3 smooth", launch3_mg_rb<T>(M, l, s & 1, c->st));
+      LAUNCH(l == 0 ? NS_PROF_MG_RESTRICT0 : NS_PROF_MG_RESTRICT, "mg3 restrict", launch3_mg_restrict<T>(M, l, c->st));
+    }
+    LAUNCH(NS_PROF_MG_BOTTOM, "mg3 coarse levels", launch3_mg_coarse<T>(M, lb, c->st));
+    for (int l = lb - 1; l >= 0; --l) {
+      LAUNCH(NS_PROF_MG_SMOOTH, "mg3 prolong", launch3_mg_prolong<T>(M, l, c->st));
+      for (int s = 0; s < 4; ++s) LAUNCH(l == 0 ? NS_PROF_MG_SMOOTH0 : NS_PROF_MG_SMOOTH, "mg3 smooth", launch3_mg_rb<T>(M, l, (s + 1) & 1, c->st));
+    }
+    return NS_OK;
+  }
   for (int l = 0; l + 1 < M.L; ++l) {
     for (int s = 0; s < 4; ++s) LAUNCH(l == 0 ? NS_PROF_MG_SMOOTH0 : NS_PROF_MG_SMOOTH, "mg3 smooth", launch3_mg_rb<T>(M, l, s & 1, c->st));
     LAUNCH(l == 0 ? NS_PROF_MG_RESTRICT0 : NS_PROF_MG_RESTRICT, "mg3 restrict", launch3_mg_restrict<T>(M, l, c->st));
