@@ -114,7 +114,7 @@ def test_3d_mixed_predictor_matches_fp64(gpu_lib, name):
     n, kw, tgv = CASES3_MIXED[name]
     dt = dt_of(n, kw)
     out = {}
-    tol = 1e-13 if n < 64 else 1e-12  # the FP64 multigrid's floor rises with n
+    tol = 1e-13 if n < 64 else 1e-12  # at 64^3 the mixed solve's floor is above 1e-13
     for prec in (ns.PREC_FP64, ns.PREC_MIXED):
         p = ns.default_params(dim=3, n_cell=n, fixed_dt=dt, iter_num=100, precision=prec, poisson_tol_rel=tol,
                               max_grid_size=(n, n, n), **kw)
