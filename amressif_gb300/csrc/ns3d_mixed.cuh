@@ -292,7 +292,7 @@ struct FtSmem {
 __device__ __forceinline__ float flux_inc(float ub, float e, float b2, float b1, float b0, float ba, float e2, float e1,
                                           float e0, float ea) {
   const float un = ub + e;
-  const float dpos = ub > 0.f ? (un > 0.f ? e : -ub) : fmaxf(un, 0.f);  // un+ - ub+
+  const float dpos = fmaxf(e, -ub) + fminf(ub, 0.f);  // un+ - ub+ (quick_sign2 of stage_inc2d.cuh)
   const float dneg = e - dpos;                                            // un- - ub-
   const float qe = un > 0.f ? q3p(e2, e1, e0) : q3m(e1, e0, ea);
   return dpos * q3p(b2, b1, b0) + dneg * q3m(b1, b0, ba) + un * qe;

@@ -66,10 +66,13 @@ __device__ __forceinline__ void ff_add_f2(float2 h, float2 l, float2 y, float2& 
 
 // Upwind split of the new advecting velocity un = ub + e and its change
 // against ub (fn_flux_calc.cpp:66-68): udn = max(un, 0) and upn = min(un, 0)
-// (formed as un - udn, exact); dud = udn - max(ub, 0) without a subtraction
-// (eb while both are positive, -ub after a sign change, max(eb, -ub) covers
-// both); dup = eb - dud (exact except after a sign change from negative to
-// positive, where it differs from -ub by one rounding).
+// (formed as un - udn, exact); dud = udn - max(ub, 0) without subtracting
+// nearly equal numbers: max(eb, -ub) + min(ub, 0), which is eb while both are
+// positive, -ub after a sign change to negative, and for ub <= 0 the sum
+// eb + ub = un (rounded as un is) or -ub + ub = 0, i.e. udn; dup = eb - dud
+// (exact except after a sign change from negative to positive, where it
+// differs from -ub by one rounding). The min / max form needs no compare and
+// select (two fewer ALU instructions per column pair).
 struct QSign2 {
   float2 udn, upn, dud, dup;
 };
@@ -79,7 +82,7 @@ __device__ __forceinline__ QSign2 quick_sign2(float2 ub, float2 eb) {
   const float2 un = p_add(ub, eb);
   q.udn = make_float2(fmaxf(un.x, 0.f), fmaxf(un.y, 0.f));
   q.upn = p_sub(un, q.udn);
-  q.dud = make_float2(ub.x > 0.f ? fmaxf(eb.x, -ub.x) : q.udn.x, ub.y > 0.f ? fmaxf(eb.y, -ub.y) : q.udn.y);
+  q.dud = p_add(make_float2(fmaxf(eb.x, -ub.x), fmaxf(eb.y, -ub.y)), make_float2(fminf(ub.x, 0.f), fminf(ub.y, 0.f)));
   q.dup = p_sub(eb, q.dud);
   return q;
 }
