@@ -33,6 +33,7 @@
 // slots swapped. Face-indexed words whose face is not the lane's cell column
 // (face N, the periodic image, wall faces) are loaded directly, per slot.
 #pragma once
+#include <type_traits>
 #include "bounds.cuh"
 #include "col2d.cuh"
 #include "ff.cuh"
@@ -168,8 +169,14 @@ __global__ void __launch_bounds__(NT, 384 / NT) k_inc_col2d(IncArgs A) {  // 12 
     float2 blu = make_float2(0.f, 0.f), blv = make_float2(0.f, 0.f);  // base lo of the u / v faces of row k - 2
     // consume row k: cell values of both columns (with ghosts), the u face
     // (iface), the lower v face and G0 at the lane's faces; put the next row in flight
-    auto cell_row = [&](int k, ColCells2& c, float2& ufb, float2& ufe, float2& vlb, float2& vle, float2& gu,
-                        float2& gv) {
+    // FAST (a strip whose columns and rows all lie inside the domain, away
+    // from every wall and the periodic seam): no ghost, image column or face
+    // row N case can occur, so those branches are compiled out and the row
+    // body is one block of straight-line code; the operations that remain are
+    // the same, so are the bits
+    auto cell_row = [&](auto fast_c, int k, ColCells2& c, float2& ufb, float2& ufe, float2& vlb, float2& vle,
+                        float2& gu, float2& gv) {
+      constexpr bool FAST = decltype(fast_c)::value;
       cp_async_wait<kIncRing - 1>();
       const float2 U = *pair_ptr(slot, 0), E = *pair_ptr(slot, 1), Vk = *pair_ptr(slot, 2), Vk1 = *pair_ptr(slot, 3);
       const float2 Fk = *pair_ptr(slot, 4), Fk1 = *pair_ptr(slot, 5), GU = *pair_ptr(slot, 6), GV = *pair_ptr(slot, 7);
@@ -189,7 +196,7 @@ __global__ void __launch_bounds__(NT, 384 / NT) k_inc_col2d(IncArgs A) {  // 12 
       ufb = U;
       ufe = p_mul(es2, E);
       gu = GU;
-      if (irr0 || irr1) {  // face N, the periodic image, wall faces: direct loads (edge lanes only)
+      if (!FAST && (irr0 || irr1)) {  // face N, the periodic image, wall faces: direct loads (edge lanes only)
         const long rr = (long)row_of(k) * P;
         if (irr0 && NS_BCHK(chk, rr + iface[0], P, N + 1, N, 5)) {
           ufb.x = shu[rr + iface[0]]; ufe.x = es * eu[rr + iface[0]]; gu.x = A.g0[0][rr + iface[0]];
@@ -201,7 +208,7 @@ __global__ void __launch_bounds__(NT, 384 / NT) k_inc_col2d(IncArgs A) {  // 12 
       vlb = Vk;
       vle = p_mul(es2, Fk);
       gv = GV;
-      if (warp_xghost) {  // x ghosts: the mirror pair's values (slots swapped) under the side's rule
+      if (!FAST && warp_xghost) {  // x ghosts: the mirror pair's values (slots swapped) under the side's rule
         const float q00 = __shfl_sync(FULL, c.p0.y, src_lane), q01 = __shfl_sync(FULL, c.p0.x, src_lane);
         const float q10 = __shfl_sync(FULL, c.p1.y, src_lane), q11 = __shfl_sync(FULL, c.p1.x, src_lane);
         const float s00 = __shfl_sync(FULL, c.e0.y, src_lane), s01 = __shfl_sync(FULL, c.e0.x, src_lane);
@@ -213,7 +220,7 @@ __global__ void __launch_bounds__(NT, 384 / NT) k_inc_col2d(IncArgs A) {  // 12 
           c.e1 = make_float2(cart_ghost_f(bx, 1, s10, true), cart_ghost_f(bx, 1, s11, true));
         }
       }
-      if (!pery && (k < 0 || k >= N)) {  // y ghosts from the mirror row; the lid profile on the north u
+      if (!FAST && !pery && (k < 0 || k >= N)) {  // y ghosts from the mirror row; the lid profile on the north u
         const CartBC& by = g.bc[k < 0 ? 2 : 3];
         if (k >= N && by.rule[0] == kInlet) {
           c.p0 = make_float2(lid[0] - c.p0.x, lid[1] - c.p0.y);
@@ -226,6 +233,8 @@ __global__ void __launch_bounds__(NT, 384 / NT) k_inc_col2d(IncArgs A) {  // 12 
       }
     };
 
+    auto march = [&](auto fast_c) {
+    constexpr bool FAST = decltype(fast_c)::value;
     // w[0..4]: cell rows r-2 .. r+2; uf*/vl*/gq*[0..2]: faces of rows r .. r+2
     ColCells2 w[5];
     float2 ufb[3], ufe[3], vlb[3], vle[3], gqu[3], gqv[3], xb, xe;
@@ -238,10 +247,10 @@ __global__ void __launch_bounds__(NT, 384 / NT) k_inc_col2d(IncArgs A) {  // 12 
       else cp_async_commit();
       ++k_next;
     }
-    cell_row(r_first - 2, w[0], xb, xe, xb, xe, xb, xe);
-    cell_row(r_first - 1, w[1], xb, xe, xb, xe, xb, xe);
-    cell_row(r_first, w[2], ufb[0], ufe[0], vlb[0], vle[0], gqu[0], gqv[0]);
-    cell_row(r_first + 1, w[3], ufb[1], ufe[1], vlb[1], vle[1], gqu[1], gqv[1]);
+    cell_row(fast_c, r_first - 2, w[0], xb, xe, xb, xe, xb, xe);
+    cell_row(fast_c, r_first - 1, w[1], xb, xe, xb, xe, xb, xe);
+    cell_row(fast_c, r_first, w[2], ufb[0], ufe[0], vlb[0], vle[0], gqu[0], gqv[0]);
+    cell_row(fast_c, r_first + 1, w[3], ufb[1], ufe[1], vlb[1], vle[1], gqu[1], gqv[1]);
     const float2 idx2 = p_splat(A.inv_dx[0]), idy2 = p_splat(A.inv_dx[1]);
     const float2 vx2 = p_splat(A.vcoef[0]), vy2 = p_splat(A.vcoef[1]), m2 = p_splat(-2.f);
     const float2 mc15 = p_splat(-A.c15), rk2 = p_splat(A.rk);
@@ -275,10 +284,10 @@ __global__ void __launch_bounds__(NT, 384 / NT) k_inc_col2d(IncArgs A) {  // 12 
     // base-update loop is not unrolled
 #pragma unroll (BASE ? 1 : 2)
     for (int r = r_first; r <= r_last; ++r) {
-      cell_row(r + 2, w[4], ufb[2], ufe[2], vlb[2], vle[2], gqu[2], gqv[2]);
+      cell_row(fast_c, r + 2, w[4], ufb[2], ufe[2], vlb[2], vle[2], gqu[2], gqv[2]);
       // y flux at face r+1 (rows r, r+1), cells r-1 .. r+2; face row N as stored
       float2 vfb = vlb[1], vfe = vle[1];
-      if (r + 1 == N && NS_BCHK(chk, (long)N * P + pc, P, N + 1, N - 1, 6)) {
+      if (!FAST && r + 1 == N && NS_BCHK(chk, (long)N * P + pc, P, N + 1, N - 1, 6)) {
         const long id = (long)N * P + pc;
         vfb = make_float2(shv[id], shv[id + 1]);
         vfe = p_mul(es2, make_float2(ev[id], ev[id + 1]));
@@ -309,18 +318,20 @@ __global__ void __launch_bounds__(NT, 384 / NT) k_inc_col2d(IncArgs A) {  // 12 
         if (r >= ys) {  // warp-uniform
           // u faces (a, r), (b, r); r < N
           float2 avg = p_mul(half2, p_add(t0l, t0));
-          if (rule_u[0]) avg.x = (fgx == kReflect) ? 0.f : 0.5f * (a == 0 ? t0.x : t0l.x);
-          if (rule_u[1]) avg.y = (fgx == kReflect) ? 0.f : 0.5f * (a + 1 == 0 ? t0.y : t0l.y);
+          if (!FAST && rule_u[0]) avg.x = (fgx == kReflect) ? 0.f : 0.5f * (a == 0 ? t0.x : t0l.x);
+          if (!FAST && rule_u[1]) avg.y = (fgx == kReflect) ? 0.f : 0.5f * (a + 1 == 0 ? t0.y : t0l.y);
           const float2 eu2 = p_mul(rk2, p_add(gqu[0], p_fma(ufe[0], mc15, avg)));
           // v faces (a, r), (b, r); r <= N
-          const bool edge_v = (r == 0 || r == N);
+          const bool edge_v = !FAST && (r == 0 || r == N);
           float2 avgv = p_mul(half2, p_add(t1p, t1));
           if (fgy != kWrap && edge_v) {
             avgv.x = (fgy == kReflect) ? 0.f : 0.5f * (r == 0 ? t1.x : t1p.x);
             avgv.y = (fgy == kReflect) ? 0.f : 0.5f * (r == 0 ? t1.y : t1p.y);
           }
           float2 ecur = vle[0], gcur = gqv[0], bh = vlb[0], bo = blv;
-          if (r == N) {  // face row N as stored
+          (void)bh;
+          (void)bo;
+          if (!FAST && r == N) {  // face row N as stored
             const long id = (long)N * P + a;
 #pragma unroll
             for (int s = 0; s < 2; ++s) {
@@ -338,10 +349,14 @@ __global__ void __launch_bounds__(NT, 384 / NT) k_inc_col2d(IncArgs A) {  // 12 
           // new float-float base u_b + e_s of both columns (BASE); u face words
           // off the pair loads come directly
           float2 nuh, nul, nvh, nvl;
+          (void)nuh;
+          (void)nul;
+          (void)nvh;
+          (void)nvl;
           if constexpr (BASE) {
             float2 lo = blu;
-            if (irr0 && out_u[0] && r < N && NS_BCHK(chk, (long)r * P + a, P, N + 1, N, 8)) lo.x = A.bl[0][(long)r * P + a];
-            if (irr1 && out_u[1] && r < N && NS_BCHK(chk, (long)r * P + a + 1, P, N + 1, N, 8))
+            if (!FAST && irr0 && out_u[0] && r < N && NS_BCHK(chk, (long)r * P + a, P, N + 1, N, 8)) lo.x = A.bl[0][(long)r * P + a];
+            if (!FAST && irr1 && out_u[1] && r < N && NS_BCHK(chk, (long)r * P + a + 1, P, N + 1, N, 8))
               lo.y = A.bl[0][(long)r * P + a + 1];
             ff_add_f2(ufb[0], lo, ufe[0], nuh, nul);
             ff_add_f2(bh, bo, ecur, nvh, nvl);
@@ -350,16 +365,16 @@ __global__ void __launch_bounds__(NT, 384 / NT) k_inc_col2d(IncArgs A) {  // 12 
           for (int s = 0; s < 2; ++s) {
             const int i = a + s;
             const long id = (long)r * P + i;
-            if (out_u[s] && r < N && NS_BCHK(chk, id, P, N + 1, N, 9)) {  // u face (i, r)
+            if ((FAST ? out_lane : (out_u[s] && r < N)) && NS_BCHK(chk, id, P, N + 1, N, 9)) {  // u face (i, r)
               const float e = s ? eu2.y : eu2.x;
               A.eout[0][id] = e;
-              n0 = fmaf(wgt_u[s] * e, e, n0);
+              n0 = fmaf((FAST ? 1.f : wgt_u[s]) * e, e, n0);
               if constexpr (BASE) {  // u_b + e_s at u face (i, r)
                 A.obh[0][id] = s ? nuh.y : nuh.x;
                 A.obl[0][id] = s ? nul.y : nul.x;
               }
             }
-            if (out_v[s] && NS_BCHK(chk, id, P, N + 1, N, 10)) {  // v face (i, r), r <= N
+            if ((FAST ? out_lane : out_v[s]) && NS_BCHK(chk, id, P, N + 1, N, 10)) {  // v face (i, r), r <= N
               const float e = s ? ev2.y : ev2.x;
               A.eout[1][id] = e;
               n1 = fmaf(edge_v ? 0.5f * e : e, e, n1);
@@ -381,6 +396,10 @@ __global__ void __launch_bounds__(NT, 384 / NT) k_inc_col2d(IncArgs A) {  // 12 
         vlb[q] = vlb[q + 1]; vle[q] = vle[q + 1];
       }
     }
+    };
+    const bool fast = xs >= 4 && xs + 60 <= N && ys >= 4 && ys + H + 2 <= N;
+    if (fast) march(std::true_type{});
+    else march(std::false_type{});
     cp_async_wait<0>();
   }
   if (A.do_norm) {
