@@ -7,6 +7,7 @@
 // the raw face rows streamed through a per-warp cp.async ring in shared
 // memory (kAncRing rows in flight), so the loads never stall the arithmetic.
 #pragma once
+#include <type_traits>
 #include "anchor_ff2d.cuh"
 #include "bounds.cuh"
 #include "ff.cuh"
@@ -130,13 +131,18 @@ __global__ void __launch_bounds__(NT) k_anchor_col2d(AnchorFFArgs A) {
   int rslot = 0;  // ring slot of the next row to read
   // consume row k: cell velocities (with ghosts), the u face (iface, k), the
   // lower v face (ic, k) and S at the lane's faces
-  auto cell_row = [&](int k, CellFF& c, ff& uf, ff& vl, ff& su, ff& sv) {
+  // FAST (a strip whose columns and rows all lie inside the domain, away
+  // from every wall and the periodic seam): the ghost, image-column and face
+  // row N branches are compiled out; the remaining operations, and so the
+  // bits, are the same
+  auto cell_row = [&](auto fast_c, int k, CellFF& c, ff& uf, ff& vl, ff& su, ff& sv) {
+    constexpr bool FAST = decltype(fast_c)::value;
     cp_async_wait<kAncRing - 1>();
     const float* d = slot_ptr(rslot);
     const ff ua = ubase(d, 0), ub = ubase(d, 3), va = ubase(d, 6), vb = ubase(d, 9);
     su = ff_make(d[12 * 32], d[13 * 32]);
     sv = ff_make(d[14 * 32], d[15 * 32]);
-    if (iface != ic) uf = ubase_direct(0, (long)row_of(k) * P + iface);  // boundary / periodic lanes only
+    if (!FAST && iface != ic) uf = ubase_direct(0, (long)row_of(k) * P + iface);  // boundary / periodic lanes only
     else uf = ua;
     vl = va;
     if (k_next <= k_end) issue_row(k_next, rslot);
@@ -145,14 +151,14 @@ __global__ void __launch_bounds__(NT) k_anchor_col2d(AnchorFFArgs A) {
     rslot = (rslot == kAncRing - 1) ? 0 : rslot + 1;
     c.p0 = ff_scale2(ua + ub, 0.5f);
     c.p1 = ff_scale2(va + vb, 0.5f);
-    if (warp_xghost) {
+    if (!FAST && warp_xghost) {
       const ff q0 = shfl_ff(c.p0, src_lane), q1 = shfl_ff(c.p1, src_lane);
       if (xghost) {
         c.p0 = cart_ghost_ff(bx, 0, q0);
         c.p1 = cart_ghost_ff(bx, 1, q1);
       }
     }
-    if (!pery && (k < 0 || k >= N)) {
+    if (!FAST && !pery && (k < 0 || k >= N)) {
       const CartBC& by = g.bc[k < 0 ? 2 : 3];
       if (k >= N && by.rule[0] == kInlet) c.p0 = lid - c.p0;
       else c.p0 = cart_ghost_ff(by, 0, c.p0);
@@ -161,6 +167,8 @@ __global__ void __launch_bounds__(NT) k_anchor_col2d(AnchorFFArgs A) {
   };
 
   const int r_first = ys - 2, r_last = (ys + H >= N) ? N : ys + H - 1;
+  auto march = [&](auto fast_c) {
+  constexpr bool FAST = decltype(fast_c)::value;
   k_next = r_first - 2;
   k_end = r_last + 2;
   for (int q = 0; q < kAncRing; ++q) {
@@ -170,10 +178,10 @@ __global__ void __launch_bounds__(NT) k_anchor_col2d(AnchorFFArgs A) {
   }
   CellFF w[5];
   ff uf[3], vl[3], su[3], sv[3], xa, xb, xc, xd;
-  cell_row(r_first - 2, w[0], xa, xb, xc, xd);
-  cell_row(r_first - 1, w[1], xa, xb, xc, xd);
-  cell_row(r_first, w[2], uf[0], vl[0], su[0], sv[0]);
-  cell_row(r_first + 1, w[3], uf[1], vl[1], su[1], sv[1]);
+  cell_row(fast_c, r_first - 2, w[0], xa, xb, xc, xd);
+  cell_row(fast_c, r_first - 1, w[1], xa, xb, xc, xd);
+  cell_row(fast_c, r_first, w[2], uf[0], vl[0], su[0], sv[0]);
+  cell_row(fast_c, r_first + 1, w[3], uf[1], vl[1], su[1], sv[1]);
   const ff idx_ = ff_make(A.inv_dx[0][0], A.inv_dx[0][1]), idy_ = ff_make(A.inv_dx[1][0], A.inv_dx[1][1]);
   const ff vx = ff_make(A.vcoef[0][0], A.vcoef[0][1]), vy = ff_make(A.vcoef[1][0], A.vcoef[1][1]);
   const ff c15 = ff_make(A.c15[0], A.c15[1]);
@@ -182,10 +190,10 @@ __global__ void __launch_bounds__(NT) k_anchor_col2d(AnchorFFArgs A) {
   const bool out_lane = lane >= 3 && lane < 3 + kAncOut;
   ff fyp0 = zero, fyp1 = zero, t1p = zero;
   for (int r = r_first; r <= r_last; ++r) {
-    cell_row(r + 2, w[4], uf[2], vl[2], su[2], sv[2]);
+    cell_row(fast_c, r + 2, w[4], uf[2], vl[2], su[2], sv[2]);
     // y flux at face r+1 (rows r, r+1); face row N as stored
     ff vf = vl[1];
-    if (r + 1 == N) vf = ubase_direct(1, (long)N * P + ic);
+    if (!FAST && r + 1 == N) vf = ubase_direct(1, (long)N * P + ic);
     const ff fy0 = quick_flux_ff(vf, w[4].p0, w[3].p0, w[2].p0, w[1].p0);
     const ff fy1 = quick_flux_ff(vf, w[4].p1, w[3].p1, w[2].p1, w[1].p1);
     if (r >= ys - 1) {
@@ -203,9 +211,9 @@ __global__ void __launch_bounds__(NT) k_anchor_col2d(AnchorFFArgs A) {
       const ff t0 = visc0 - conv0, t1 = visc1 - conv1;
       const ff t0l = shfl_up_ff(t0, 1);
       if (r >= ys && out_lane) {
-        if (r < N && i >= 0 && i <= N && NS_BCHK(chk, (long)r * P + i, P, N + 1, N, 25)) {  // u face (i, r)
+        if ((FAST || (r < N && i >= 0 && i <= N)) && NS_BCHK(chk, (long)r * P + i, P, N + 1, N, 25)) {  // u face (i, r)
           ff avg = ff_scale2(t0l + t0, 0.5f);
-          if (fgx != kWrap && (i == 0 || i == N)) avg = (fgx == kReflect) ? zero : ff_scale2(i == 0 ? t0 : t0l, 0.5f);
+          if (!FAST && fgx != kWrap && (i == 0 || i == N)) avg = (fgx == kReflect) ? zero : ff_scale2(i == 0 ? t0 : t0l, 0.5f);
           const long id = (long)r * P + i;
           const ff u = uf[0];
           const ff G = (su[0] - c15 * u) + avg;
@@ -213,12 +221,12 @@ __global__ void __launch_bounds__(NT) k_anchor_col2d(AnchorFFArgs A) {
           A.obl[0][id] = u.lo;
           A.g0[0][id] = G.hi + G.lo;
         }
-        if (i >= 0 && i < N && NS_BCHK(chk, (long)r * P + i, P, N + 1, N, 26)) {  // v face (i, r), r <= N
+        if ((FAST || (i >= 0 && i < N)) && NS_BCHK(chk, (long)r * P + i, P, N + 1, N, 26)) {  // v face (i, r), r <= N
           ff avg = ff_scale2(t1p + t1, 0.5f);
-          if (fgy != kWrap && (r == 0 || r == N)) avg = (fgy == kReflect) ? zero : ff_scale2(r == 0 ? t1 : t1p, 0.5f);
+          if (!FAST && fgy != kWrap && (r == 0 || r == N)) avg = (fgy == kReflect) ? zero : ff_scale2(r == 0 ? t1 : t1p, 0.5f);
           const long id = (long)r * P + i;
-          const ff u = (r == N) ? ubase_direct(1, id) : vl[0];  // face row N as stored
-          const ff S = (r == N) ? ff_make(A.Sh[1][id], A.Sl[1][id]) : sv[0];
+          const ff u = (!FAST && r == N) ? ubase_direct(1, id) : vl[0];  // face row N as stored
+          const ff S = (!FAST && r == N) ? ff_make(A.Sh[1][id], A.Sl[1][id]) : sv[0];
           const ff G = (S - c15 * u) + avg;
           A.obh[1][id] = u.hi;
           A.obl[1][id] = u.lo;
@@ -235,6 +243,10 @@ __global__ void __launch_bounds__(NT) k_anchor_col2d(AnchorFFArgs A) {
     su[0] = su[1]; su[1] = su[2];
     sv[0] = sv[1]; sv[1] = sv[2];
   }
+  };
+  const bool fast = xs >= 3 && xs + 29 <= N && ys >= 4 && ys + H + 2 <= N;
+  if (fast) march(std::true_type{});
+  else march(std::false_type{});
   cp_async_wait<0>();
 }
 
