@@ -167,6 +167,8 @@ __global__ void __launch_bounds__(NT) k_anchor_col2d(AnchorFFArgs A) {
   };
 
   const int r_first = ys - 2, r_last = (ys + H >= N) ? N : ys + H - 1;
+  // the strip's row march, instantiated once for fast strips and once for
+  // the others (the choice at its end)
   auto march = [&](auto fast_c) {
   constexpr bool FAST = decltype(fast_c)::value;
   k_next = r_first - 2;

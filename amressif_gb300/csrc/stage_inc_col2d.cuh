@@ -233,6 +233,8 @@ __global__ void __launch_bounds__(NT, 384 / NT) k_inc_col2d(IncArgs A) {  // 12 
       }
     };
 
+    // the strip's row march, instantiated once for fast strips and once for
+    // the others (the choice at its end)
     auto march = [&](auto fast_c) {
     constexpr bool FAST = decltype(fast_c)::value;
     // w[0..4]: cell rows r-2 .. r+2; uf*/vl*/gq*[0..2]: faces of rows r .. r+2
