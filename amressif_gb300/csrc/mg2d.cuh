@@ -11,6 +11,7 @@
 // the coarsest level. T = double (plain FP64 solver) or float (V-cycles of the
 // mixed-precision defect correction).
 #pragma once
+#include <type_traits>
 #include "bounds.cuh"
 #include "ns_common.cuh"
 
@@ -99,13 +100,19 @@ __global__ void __launch_bounds__(256) k_mg_smooth(MGLevels<T> M, int l, int mod
   const int tid = threadIdx.x, NT = blockDim.x;
   const bool px = M.periodic[0], py = M.periodic[1];
   const T ihx = M.ih[l][0], ihy = M.ih[l][1];
+  // FAST: the tile and its halo (and, for the prolongation, every coarse
+  // neighbour) lie at least two cells inside the domain, so no wrap, wall
+  // weight or range test is needed; the remaining operations, and the bits,
+  // are those of the general path
+  auto body = [&](auto fast_c) {
+  constexpr bool FAST = decltype(fast_c)::value;
   for (int t = tid; t < SM::W * SM::HH; t += NT) {
     const int lx = t % SM::W, ly = t / SM::W;
     const int a = x0 - H + lx, b = y0 - H + ly;
-    const bool in = (px || (a >= 0 && a < n)) && (py || (b >= 0 && b < n));
+    const bool in = FAST || ((px || (a >= 0 && a < n)) && (py || (b >= 0 && b < n)));
     T xv = (T)0, fv = (T)0;
-    if (in && NS_BCHK(M.check, (long)wrapi(b, n) * P + wrapi(a, n), P, n + 1, n - 1, 51)) {
-      const int aa = wrapi(a, n), bb = wrapi(b, n);
+    if (in && NS_BCHK(M.check, (long)(FAST ? b : wrapi(b, n)) * P + (FAST ? a : wrapi(a, n)), P, n + 1, n - 1, 51)) {
+      const int aa = FAST ? a : wrapi(a, n), bb = FAST ? b : wrapi(b, n);
       const long id = (long)bb * P + aa;
       if (!x_zero) xv = M.x[l][id];
       fv = level_f(M, l, id);
@@ -115,8 +122,10 @@ __global__ void __launch_bounds__(256) k_mg_smooth(MGLevels<T> M, int l, int mod
         const long Pc = M.pitch[l + 1];
         const int I = aa >> 1, J = bb >> 1;
         int I2 = I + ((aa & 1) ? 1 : -1), J2 = J + ((bb & 1) ? 1 : -1);
-        I2 = px ? wrapi(I2, nc) : min(max(I2, 0), nc - 1);
-        J2 = py ? wrapi(J2, nc) : min(max(J2, 0), nc - 1);
+        if (!FAST) {
+          I2 = px ? wrapi(I2, nc) : min(max(I2, 0), nc - 1);
+          J2 = py ? wrapi(J2, nc) : min(max(J2, 0), nc - 1);
+        }
         const T* xc = M.x[l + 1];
         if (!NS_BCHK(M.check, (long)J * Pc + I, Pc, nc + 1, nc - 1, 52) || !NS_BCHK(M.check, (long)J2 * Pc + I2, Pc, nc + 1, nc - 1, 53))
           continue;
@@ -141,11 +150,11 @@ __global__ void __launch_bounds__(256) k_mg_smooth(MGLevels<T> M, int l, int mod
       const int a0 = x0 - r;
       const int a = a0 + 2 * (t % w2) + (((a0 + b) & 1) != color ? 1 : 0);
       if (a >= a0 + w) continue;
-      if (!px && (a < 0 || a >= n)) continue;
-      if (!py && (b < 0 || b >= n)) continue;
+      if (!FAST && !px && (a < 0 || a >= n)) continue;
+      if (!FAST && !py && (b < 0 || b >= n)) continue;
       const int lx = a - (x0 - H), ly = b - (y0 - H);
-      const bool we = px || a + 1 < n, ww = px || a > 0;
-      const bool wn = py || b + 1 < n, wsn = py || b > 0;
+      const bool we = FAST || px || a + 1 < n, ww = FAST || px || a > 0;
+      const bool wn = FAST || py || b + 1 < n, wsn = FAST || py || b > 0;
       sm.x[ly][lx] = gs_update<T>(sm.x[ly][lx + 1], sm.x[ly][lx - 1], sm.x[ly + 1][lx], sm.x[ly - 1][lx],
                                   we, ww, wn, wsn, ihx, ihy, sm.f[ly][lx], M.idg[l]);
     }
@@ -153,8 +162,12 @@ __global__ void __launch_bounds__(256) k_mg_smooth(MGLevels<T> M, int l, int mod
   }
   for (int t = tid; t < TX * TY; t += NT) {
     const int a = x0 + t % TX, b = y0 + t / TX;
-    if (a < n && b < n && NS_BCHK(M.check, (long)b * P + a, P, n + 1, n - 1, 54)) M.x2[l][(long)b * P + a] = sm.x[b - (y0 - H)][a - (x0 - H)];
+    if ((FAST || (a < n && b < n)) && NS_BCHK(M.check, (long)b * P + a, P, n + 1, n - 1, 54)) M.x2[l][(long)b * P + a] = sm.x[b - (y0 - H)][a - (x0 - H)];
   }
+  };
+  const bool fast = x0 - H >= 2 && x0 + TX + H <= n - 2 && y0 - H >= 2 && y0 + TY + H <= n - 2;
+  if (fast) body(std::true_type{});
+  else body(std::false_type{});
 }
 
 // ---------------------------------------------------------------------------
@@ -332,20 +345,27 @@ __global__ void __launch_bounds__(256) k_mg_restrict(MGLevels<T> M, int l) {
   const bool px = M.periodic[0], py = M.periodic[1];
   const T ihx = M.ih[l][0], ihy = M.ih[l][1];
   const T* x = M.x[l];
-  T s = (T)0;
+  // FAST: the four fine cells and their neighbours lie inside the domain
+  // (no wrap, no wall); the same operations, and the same bits
+  auto body = [&](auto fast_c) {
+    constexpr bool FAST = decltype(fast_c)::value;
+    T s = (T)0;
 #pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    const int a = 2 * I + (q & 1), b = 2 * J + (q >> 1);
-    const long id = (long)b * P + a;
-    const T xc = x[id];
-    T lap = (T)0;
-    if (px || a + 1 < n) lap += (x[(long)b * P + wrapi(a + 1, n)] - xc) * ihx;
-    if (px || a > 0) lap += (x[(long)b * P + wrapi(a - 1, n)] - xc) * ihx;
-    if (py || b + 1 < n) lap += (x[(long)wrapi(b + 1, n) * P + a] - xc) * ihy;
-    if (py || b > 0) lap += (x[(long)wrapi(b - 1, n) * P + a] - xc) * ihy;
-    s += level_f(M, l, id) - lap;
-  }
-  M.f[l + 1][(long)J * M.pitch[l + 1] + I] = (T)0.25 * s;
+    for (int q = 0; q < 4; ++q) {
+      const int a = 2 * I + (q & 1), b = 2 * J + (q >> 1);
+      const long id = (long)b * P + a;
+      const T xc = x[id];
+      T lap = (T)0;
+      if (FAST || px || a + 1 < n) lap += (x[(long)b * P + (FAST ? a + 1 : wrapi(a + 1, n))] - xc) * ihx;
+      if (FAST || px || a > 0) lap += (x[(long)b * P + (FAST ? a - 1 : wrapi(a - 1, n))] - xc) * ihx;
+      if (FAST || py || b + 1 < n) lap += (x[(long)(FAST ? b + 1 : wrapi(b + 1, n)) * P + a] - xc) * ihy;
+      if (FAST || py || b > 0) lap += (x[(long)(FAST ? b - 1 : wrapi(b - 1, n)) * P + a] - xc) * ihy;
+      s += level_f(M, l, id) - lap;
+    }
+    M.f[l + 1][(long)J * M.pitch[l + 1] + I] = (T)0.25 * s;
+  };
+  if (I >= 1 && 2 * I + 2 < n && J >= 1 && 2 * J + 2 < n) body(std::true_type{});
+  else body(std::false_type{});
 }
 
 // max |f - L x| at level 0 (plain solver convergence check); red_out[0]
