@@ -57,6 +57,11 @@ struct ns_ctx {
   unsigned* counter = nullptr;
   double* red = nullptr;    // device scalars
   double* red_h = nullptr;  // pinned mirror
+  // the pseudo-norm as the reducing increment launch writes it straight into
+  // mapped pinned host memory: (norm, sequence number); null if unavailable
+  double* note_h = nullptr;
+  double* note_d = nullptr;
+  double note_seq = 0.0;
   cudaEvent_t ev[8];  // 0..3: phases of ns_step; 4..7: the copies of ns_step_host
   bool ev_ok = false;
   // mixed iteration: E[0] holds an increment not yet added to the base

@@ -42,6 +42,8 @@ struct IncArgs {
   float2* part;         // float-float block partials of the norm
   unsigned* counter;
   double* norm_out;
+  double* note;         // nullable: mapped host pair (norm, note_seq) written after norm_out
+  double note_seq;
 };
 
 // Packed FP32 pairs (the add / mul / fma f32x2 instructions of sm_100 and
