@@ -355,7 +355,7 @@ def adjoint_section(ns, args):
 
 def cpu_table_section(args):
     """The CPU restatement (oracle/) on the host cores, all of them and one,
-    for the parity configurations (the benchmark's CPU table). Config 1 (128^2
+    for the parity configurations (the CPU baseline table). Config 1 (128^2
     cavity, 200 steps) runs in full; config 2 (1024^2 perturbed Taylor-Green)
     and config 3 (4096^2 cavity from rest) are bounded samples: config 2 a few
     steps, config 3 on one core the phases of step 1 (the four RK stages of
