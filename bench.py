@@ -355,13 +355,13 @@ def adjoint_section(ns, args):
 
 def cpu_table_section(args):
     """The CPU restatement (oracle/) on the host cores, all of them and one,
-    for the parity configurations (the CPU baseline table). Config 1 (128^2
-    cavity, 200 steps) runs in full; config 2 (1024^2 perturbed Taylor-Green)
-    and config 3 (4096^2 cavity from rest) are bounded samples: config 2 a few
-    steps, config 3 on one core the phases of step 1 (the four RK stages of
+    for the parity workloads (the CPU baseline table). The 128^2 four-box
+    cavity (200 steps) runs in full; the 1024^2 perturbed Taylor-Green and the
+    4096^2 cavity from rest are bounded samples: the Taylor-Green a few steps,
+    the 4096^2 cavity on one core the phases of step 1 (the four RK stages of
     one pseudo-iteration, timed and multiplied by the step's K, plus the
-    Poisson right-hand side, solve and projection), all-core config 3 is the
-    bench's own cpu_baseline."""
+    Poisson right-hand side, solve and projection); the all-core 4096^2 figure
+    is the bench's own cpu_baseline."""
     import math
 
     from amressif_gb300 import workloads as wl
@@ -375,7 +375,7 @@ def cpu_table_section(args):
     except Exception:
         out["cpu_model"] = None
 
-    def cfg1(threads):
+    def cavity128(threads):
         o = Oracle(128, ren=100.0, dt=0.5 / 128, iter_num=100, poisson_tol=1e-10, max_grid_size=(64, 64, 64),
                    nthreads=threads)
         o.init(0)
@@ -386,7 +386,7 @@ def cpu_table_section(args):
         return {"steps": 200, "seconds": dt, "steps_per_s": 200 / dt, "cell_updates_per_s": 200 * 128 * 128 / dt,
                 "pseudo_iters_mean": sum(ks) / len(ks)}
 
-    def cfg2(threads, steps):
+    def tgv1024(threads, steps):
         n = 1024
         h = 2 * math.pi / n
         o = Oracle(n, ren=1000.0, dt=0.5 * h, iter_num=100, poisson_tol=1e-10, max_grid_size=(n, n, n),
@@ -399,7 +399,7 @@ def cpu_table_section(args):
         return {"steps": steps, "seconds": dt, "steps_per_s": steps / dt, "cell_updates_per_s": steps * n * n / dt,
                 "pseudo_iters": ks, "sample": "steps 1..%d of 500" % steps}
 
-    def cfg3_phases():
+    def cavity4096_phases():
         # one core: the first pseudo-iteration of step 1, then (from the
         # converged u* of an all-core run of the same predictor) the Poisson
         # right-hand side, solve and projection
@@ -440,9 +440,9 @@ def cpu_table_section(args):
                 "sample": "step 1 from rest: one pseudo-iteration timed x K, plus the timed Poisson RHS, solve "
                           "and projection from the converged u*"}
 
-    out["config1_cavity128_200_steps"] = {"all_cores": cfg1(allc), "one_core": cfg1(1)}
-    out["config2_tgv1024"] = {"all_cores": cfg2(allc, args.cpu_cfg2_steps), "one_core": cfg2(1, 1)}
-    out["config3_cavity4096_one_core"] = cfg3_phases()
+    out["cavity128_4boxes_200_steps"] = {"all_cores": cavity128(allc), "one_core": cavity128(1)}
+    out["tgv1024"] = {"all_cores": tgv1024(allc, args.cpu_tgv1024_steps), "one_core": tgv1024(1, 1)}
+    out["cavity4096_one_core"] = cavity4096_phases()
     return out
 
 
@@ -469,7 +469,7 @@ def full_run_section(ns, args):
             "div_after_max": max(x["div_after"] for x in st), "poisson_warm_start": args.warm_start}
 
 
-def cfg5_section(ns, args):
+def tgv3d_section(ns, args):
     """3D periodic Taylor-Green vortex on [0, 2 pi]^3, 256^3, Re = 1600, dt = 0.4 h
     (CFL 0.4 for unit velocity), with the seeded 1e-3 divergence-free
     perturbation; one warm-up step, then timed steps of the mixed-precision
@@ -481,12 +481,12 @@ def cfg5_section(ns, args):
     import numpy as np
     from amressif_gb300 import workloads as wl
 
-    n, k = args.cfg5_n, args.cfg5_steps
+    n, k = args.tgv3d_n, args.tgv3d_steps
     h = 2 * math.pi / n
     out = {"workload": "3D periodic Taylor-Green %d^3, Re=1600, dt=0.4h, seeded 1e-3 perturbation, steps 2..%d"
                        % (n, k + 1)}
     state = wl.tgv3d_perturbed_state(n, amp=1e-3, seed=0)
-    precs = [("mixed", ns.PREC_MIXED)] + ([] if args.no_cfg5_fp64 else [("fp64", ns.PREC_FP64)])
+    precs = [("mixed", ns.PREC_MIXED)] + ([] if args.no_tgv3d_fp64 else [("fp64", ns.PREC_FP64)])
     for name, prec in precs:
         p = ns.default_params(dim=3, n_cell=n, ren=1600.0, fixed_dt=0.4 * h, iter_num=100, precision=prec,
                               prob_hi=(2 * math.pi,) * 3, bc_lo=(111,) * 3, bc_hi=(111,) * 3, fix_quirks=1,
@@ -512,20 +512,20 @@ def cfg5_section(ns, args):
     return out
 
 
-def cfg5_adjoint_section(ns, args):
+def tgv3d_adjoint_section(ns, args):
     """Adjoint of the final enstrophy E = 1/2 sum |curl u|^2 dV of the 3D
     Taylor-Green run with respect to the initial velocity (u^{-1} = u^0):
     Re = 1600, dt = 0.4 h, the seeded 1e-3 perturbation, the mixed-precision
     solver, binomial checkpointing with 16 snapshots. Times the plain
     forward run (ns_step) and the ns_step_adjoint_fwd / ns_step_adjoint_bwd
     pair (wall clock, synchronised); the grid defaults to 128^3 so that the
-    section takes about a minute (--cfg5-adj-n 256 for the full grid)."""
+    section takes about a minute (--tgv3d-adj-n 256 for the full grid)."""
     import math
 
     import numpy as np
     from amressif_gb300 import workloads as wl
 
-    n, L, nsnap = args.cfg5_adj_n, args.cfg5_adj_steps, args.cfg5_adj_snap
+    n, L, nsnap = args.tgv3d_adj_n, args.tgv3d_adj_steps, args.tgv3d_adj_snap
     h = 2 * math.pi / n
     state = wl.tgv3d_perturbed_state(n, amp=1e-3, seed=0)
 
@@ -781,11 +781,11 @@ def bench_ours(args):
     adjoint = None
     if rank == 0 and not args.no_adjoint:
         adjoint = adjoint_section(ns, args)
-    cfg5 = None
-    if rank == 0 and not args.no_cfg5:
-        cfg5 = cfg5_section(ns, args)
-        if not args.no_cfg5_adjoint:
-            cfg5["adjoint"] = cfg5_adjoint_section(ns, args)
+    tgv3d = None
+    if rank == 0 and not args.no_tgv3d:
+        tgv3d = tgv3d_section(ns, args)
+        if not args.no_tgv3d_adjoint:
+            tgv3d["adjoint"] = tgv3d_adjoint_section(ns, args)
 
     if rank == 0:
         line = {
@@ -811,7 +811,7 @@ def bench_ours(args):
             "parity_4096_first_steps": parity,
             "adjoint_forward_ratio": adjoint["ratio"] if adjoint else None,
             "adjoint": adjoint,
-            "taylor_green_3d": cfg5,
+            "taylor_green_3d": tgv3d,
             "e2e": e2e,
             "gpu_launches": launches,
             "roofline": roofline,
@@ -870,19 +870,19 @@ def main():
     ap.add_argument("--no-warm-ab", action="store_true", help="skip the warm-start A/B")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
-    ap.add_argument("--no-cfg5", action="store_true")
-    ap.add_argument("--cfg5-n", type=int, default=256)
-    ap.add_argument("--cfg5-steps", type=int, default=2)
-    ap.add_argument("--no-cfg5-adjoint", action="store_true")
-    ap.add_argument("--no-cfg5-fp64", action="store_true")
-    ap.add_argument("--section", default="all", choices=["all", "cfg5", "cpu", "full-run"],
-                    help="cfg5: only the 3D Taylor-Green section (profiling runs); cpu: the CPU restatement on all "
-                         "host cores and on one, configs 1-3; full-run: the whole 1000-step 4096^2 run")
-    ap.add_argument("--cpu-cfg2-steps", type=int, default=5)
+    ap.add_argument("--no-tgv3d", action="store_true")
+    ap.add_argument("--tgv3d-n", type=int, default=256)
+    ap.add_argument("--tgv3d-steps", type=int, default=2)
+    ap.add_argument("--no-tgv3d-adjoint", action="store_true")
+    ap.add_argument("--no-tgv3d-fp64", action="store_true")
+    ap.add_argument("--section", default="all", choices=["all", "tgv3d", "cpu", "full-run"],
+                    help="tgv3d: only the 3D Taylor-Green section (profiling runs); cpu: the CPU restatement on all "
+                         "host cores and on one (the 128^2 four-box cavity, the 1024^2 Taylor-Green, the 4096^2 cavity); full-run: the whole 1000-step 4096^2 run")
+    ap.add_argument("--cpu-tgv1024-steps", type=int, default=5)
     ap.add_argument("--full-run-steps", type=int, default=1000)
-    ap.add_argument("--cfg5-adj-n", type=int, default=128)
-    ap.add_argument("--cfg5-adj-steps", type=int, default=200)
-    ap.add_argument("--cfg5-adj-snap", type=int, default=16)
+    ap.add_argument("--tgv3d-adj-n", type=int, default=128)
+    ap.add_argument("--tgv3d-adj-steps", type=int, default=200)
+    ap.add_argument("--tgv3d-adj-snap", type=int, default=16)
     ap.add_argument("--adj-n", type=int, default=512)
     ap.add_argument("--adj-steps", type=int, default=400)
     ap.add_argument("--adj-snap", type=int, default=20)
@@ -898,12 +898,12 @@ def main():
         import amressif_gb300 as ns
 
         print(json.dumps({"full_run": full_run_section(ns, args)}))
-    elif args.section == "cfg5":
+    elif args.section == "tgv3d":
         import amressif_gb300 as ns
 
-        out = cfg5_section(ns, args)
-        if not args.no_cfg5_adjoint:
-            out["adjoint"] = cfg5_adjoint_section(ns, args)
+        out = tgv3d_section(ns, args)
+        if not args.no_tgv3d_adjoint:
+            out["adjoint"] = tgv3d_adjoint_section(ns, args)
         print(json.dumps({"taylor_green_3d": out}))
     elif args.impl == "reference":
         bench_reference(args)

@@ -4,7 +4,7 @@ The reference splits the domain into boxes of max_grid_size (main.cpp:317-324)
 and keeps every field in ghosted FArrayBoxes (main.cpp:330-383); a host hands
 the library each valid box through MultiFab::array(mfi), i.e. a pointer to
 the box's lo corner inside a ghosted buffer, with the buffer's own jstride
-and kstride. These tests place config 1's four 64^2 boxes of a 128^2 cavity
+and kstride. These tests place the four 64^2 boxes of a 128^2 cavity
 (and eight 8^3 boxes of a 16^3 cavity) in ghosted host buffers whose ghost
 cells hold NaN, move them in box by box, and require the next step to be
 bitwise identical to the one of a context filled with ns_set_state; ns_get_box

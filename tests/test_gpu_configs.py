@@ -1,18 +1,18 @@
-"""The benchmark configurations over their stated lengths (main.cpp:875-1202).
+"""The benchmark workloads over their stated lengths (main.cpp:875-1202).
 
-Config 1 (128^2 cavity in four 64^2 boxes, Re 100, dt = 0.5 dx, 200 steps):
+The 128^2 cavity in four 64^2 boxes (Re 100, dt = 0.5 dx, 200 steps):
 the plain FP64 path runs all 200 steps free-running beside the oracle, with
 identical pseudo-iteration counts K and a relative L2 <= 1e-10 in u, v and p
 (p modulo its constant) after every step.
 
-Config 2 (perturbed Taylor-Green 1024^2, Re 1000, dt = 0.5 dx, parity mode):
+The perturbed Taylor-Green vortex at 1024^2 (Re 1000, dt = 0.5 dx, parity mode):
 20 steps resynced to the oracle (same K, <= 1e-10 per step), and all 500
 steps free-running against the oracle's committed per-step history
 (tests/golden/tgv1024_parity_history.json, made by make_tgv1024_history.py):
 the same K at every step and the kinetic energy, Taylor-Green amplitude and
 field norms within 1e-9 relative.
 
-Config 4 (512^2 cavity, Re 400, 400 steps, 256 lid controls, 20 snapshots):
+The 512^2 lid-control cavity (Re 400, 400 steps, 256 lid controls, 20 snapshots):
 the adjoint gradient against central differences (eps = 1e-6) along the 8
 seeded unit directions, to 1e-6 relative, and against the tangent-linear
 model (ns_step_jvp chained over the 400 steps) along one seeded direction,
@@ -51,7 +51,7 @@ def compare(s, o, what, tol=1e-10):
     return errs
 
 
-def test_config1_cavity128_200_steps(gpu_lib, oracle_lib):
+def test_cavity128_4boxes_200_steps(gpu_lib, oracle_lib):
     n, dt = 128, 0.5 / 128
     o = Oracle(n, ren=100.0, dt=dt, iter_num=100, poisson_tol=1e-13, max_grid_size=(64, 64, 64))
     o.init(0)
@@ -81,7 +81,7 @@ def tgv_solver():
     return ns.Solver(prm)
 
 
-def test_config2_tgv1024_20_resynced_steps(gpu_lib, oracle_lib):
+def test_tgv1024_20_resynced_steps(gpu_lib, oracle_lib):
     u, up, p = wl.tgv_perturbed_state(N2, amp=1e-3, seed=0)
     o = Oracle(N2, ren=1000.0, dt=DT2, iter_num=100, poisson_tol=1e-13, max_grid_size=(N2, N2, N2), **PER)
     o.set_state(u, up, p)
@@ -108,7 +108,7 @@ def history_scalars(u, v, p, h):
             "norm_p": float(np.linalg.norm(p - p.mean()))}
 
 
-def test_config2_tgv1024_500_steps_against_oracle_history(gpu_lib):
+def test_tgv1024_500_steps_against_oracle_history(gpu_lib):
     path = os.path.join(HERE, "golden", "tgv1024_parity_history.json")
     with open(path) as f:
         ref = json.load(f)
@@ -132,7 +132,7 @@ def test_config2_tgv1024_500_steps_against_oracle_history(gpu_lib):
     s.close()
 
 
-# ---- config 4 ----------------------------------------------------------------
+# ---- the 512^2 lid-control cavity ----------------------------------------------
 
 N4, L4, NSEG, SNAP = 512, 400, 256, 20
 
@@ -147,7 +147,7 @@ def cavity4(tol=1e-13):
 
 def quarter_ke_tangent(u, du, n):
     """dJ = sum over the cells of [0, 1/2]^2 of (phi . dphi) dx dy, phi the
-    cell average of the faces (the linearisation of the config-4 objective)"""
+    cell average of the faces (the linearisation of the lid-control cavity's objective)"""
     hh = n // 2
     dx = 1.0 / n
     cu = 0.5 * (u[0][:hh, :hh] + u[0][:hh, 1:hh + 1])
@@ -157,7 +157,7 @@ def quarter_ke_tangent(u, du, n):
     return float(np.sum(cu * dcu + cv * dcv)) * dx * dx
 
 
-def test_config4_adjoint_full_size(gpu_lib):
+def test_lid_control_adjoint_full_size(gpu_lib):
     rng = np.random.default_rng(0)
     c = 1.0 + 0.05 * rng.standard_normal(NSEG)
     s = cavity4()

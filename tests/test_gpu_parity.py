@@ -32,7 +32,7 @@ CASES = {
     # name: (n, oracle kwargs, gpu kwargs, init case)
     "cavity32": (32, dict(ren=100.0, dt=1e-3, max_grid_size=(32, 16, 16)), dict(ren=100.0, fixed_dt=1e-3), 0),
     "cavity40_partial_tiles": (40, dict(ren=100.0, dt=2e-3, max_grid_size=(40, 40, 40)), dict(ren=100.0, fixed_dt=2e-3), 0),
-    "cavity128_cfg1": (128, dict(ren=100.0, dt=0.5 / 128, max_grid_size=(64, 64, 64)),
+    "cavity128_4boxes": (128, dict(ren=100.0, dt=0.5 / 128, max_grid_size=(64, 64, 64)),
                        dict(ren=100.0, fixed_dt=0.5 / 128, max_grid_size=(64, 64, 64)), 0),
     "tgv64_parity": (64, dict(ren=1000.0, dt=0.5 * 2 * math.pi / 64, prob_hi=(2 * math.pi,) * 3,
                               bc_lo=(111,) * 3, bc_hi=(111,) * 3),
@@ -67,7 +67,7 @@ def sync_state(o, s):
     o.set_state(u, up, p)
 
 
-@pytest.mark.parametrize("name", ["cavity32", "cavity40_partial_tiles", "cavity128_cfg1", "tgv64_parity", "tgv64_fixed",
+@pytest.mark.parametrize("name", ["cavity32", "cavity40_partial_tiles", "cavity128_4boxes", "tgv64_parity", "tgv64_fixed",
                                   "tgv40_partial_tiles"])
 def test_rk_stages_bit_exact(gpu_lib, oracle_lib, name):
     o, s = make_pair(name)
@@ -119,7 +119,7 @@ def test_explicit_predictor_bit_exact(gpu_lib, oracle_lib):
 
 
 @pytest.mark.parametrize("precision", [ns.PREC_FP64, ns.PREC_MIXED])
-@pytest.mark.parametrize("name", ["cavity128_cfg1", "tgv64_fixed"])
+@pytest.mark.parametrize("name", ["cavity128_4boxes", "tgv64_fixed"])
 def test_poisson_and_projection(gpu_lib, oracle_lib, name, precision):
     o, s = make_pair(name, precision=ns.PREC_FP64_EXACT, tol=1e-12)
     for _ in range(2):
@@ -154,7 +154,7 @@ def test_poisson_and_projection(gpu_lib, oracle_lib, name, precision):
     assert relp(p, po) <= TOL_STEP
 
 
-@pytest.mark.parametrize("name,nsteps", [("cavity32", 11), ("cavity128_cfg1", 6), ("tgv64_parity", 6), ("tgv64_fixed", 6)])
+@pytest.mark.parametrize("name,nsteps", [("cavity32", 11), ("cavity128_4boxes", 6), ("tgv64_parity", 6), ("tgv64_fixed", 6)])
 def test_steps_resynced(gpu_lib, oracle_lib, name, nsteps):
     """Per-step parity: both sides start every step from the oracle's state."""
     o, s = make_pair(name)
@@ -188,7 +188,7 @@ def test_free_running_matches_golden(gpu_lib):
         assert relp(pp, g["p_%d" % step]) <= TOL_STEP
 
 
-@pytest.mark.parametrize("name", ["cavity128_cfg1", "tgv64_parity", "tgv64_fixed", "cavity40_partial_tiles",
+@pytest.mark.parametrize("name", ["cavity128_4boxes", "tgv64_parity", "tgv64_fixed", "cavity40_partial_tiles",
                                   "tgv40_partial_tiles"])
 def test_mixed_predictor_matches_fp64(gpu_lib, name):
     """Float-float anchor + FP32 increments reproduce the FP64 iterates.
@@ -222,7 +222,7 @@ def test_mixed_predictor_matches_fp64(gpu_lib, name):
 
 @pytest.mark.parametrize("precision", [ns.PREC_FP64, ns.PREC_MIXED])
 def test_fast_modes_track_oracle(gpu_lib, oracle_lib, precision):
-    o, s = make_pair("cavity128_cfg1", precision=precision)
+    o, s = make_pair("cavity128_4boxes", precision=precision)
     for step in range(4):
         sync_state(o, s)
         so = o.step()
@@ -285,7 +285,7 @@ def test_east_slip_code_m135_unsupported_in_parity_mode(gpu_lib):
         ns.Solver(p)
 
 
-@pytest.mark.parametrize("name", ["cavity32", "cavity128_cfg1", "tgv64_parity", "tgv64_fixed"])
+@pytest.mark.parametrize("name", ["cavity32", "cavity128_4boxes", "tgv64_parity", "tgv64_fixed"])
 def test_gmres_option_resynced(gpu_lib, oracle_lib, name):
     """The GMRES option of the Poisson solve (GMRES_Poisson.cpp:56-131, here
     with one V-cycle as the right preconditioner) reaches the same discrete
