@@ -2,9 +2,10 @@
 
 The reference ships no golden vectors, so the oracle is checked against
 (a) an independent numpy restatement of the RK stage (bit-exact),
-(b) a spectral (DCT / FFT) solve of the same discrete Poisson problem,
+(b) a spectral (DCT / FFT) solve of the same discrete Poisson problem, in 2D
+and in 3D (the 7-point operator),
 (c) the known answers of the reference's own formulas: zero discrete
-divergence after projection, zero wall-normal velocity, the analytic
+divergence after projection, zero wall-normal velocity (2D and 3D), the analytic
 Taylor-Green decay u0 exp(-2 nu t) with second-order convergence, and the
 BDF2 fixed point of the converged pseudo-time loop,
 (d) the committed golden fixtures (regression pin across x86 and Arm builds).
@@ -185,3 +186,71 @@ def test_golden_fixtures(oracle_lib):
             np.testing.assert_allclose(u[1], g["v_%d" % step], rtol=0, atol=1e-13)
             pc = p - p.mean()
             np.testing.assert_allclose(pc, g["p_%d" % step], rtol=0, atol=1e-11)
+
+
+# ---- the 3D restatement ----------------------------------------------------------------
+
+
+def test_poisson_3d_matches_dct_solution_walls(oracle_lib):
+    """The 7-point cell-centred Laplacian with homogeneous Neumann walls, solved
+    by the oracle's 3D multigrid + CG, against the exact solution of the same
+    discrete problem by a type-2 DCT (eigenvalues summed over the three axes)."""
+    from scipy.fft import dctn, idctn
+
+    n = 16
+    o = Oracle(n, dim=3, ren=100.0, dt=1e-3, bc_lo=(135, 135, 135), bc_hi=(135, 165, 135))
+    rng = np.random.default_rng(2)
+    f = rng.standard_normal((n, n, n))
+    phi, it, res = o.solve_poisson(f)
+    assert res <= 1e-12
+    h = 1.0 / n
+    e = _neumann_eigs(n, h)
+    lam = e[:, None, None] + e[None, :, None] + e[None, None, :]
+    lam[0, 0, 0] = 1.0
+    ph = dctn(f - f.mean(), type=2, norm="ortho") / lam
+    ph[0, 0, 0] = 0.0
+    ref = idctn(ph, type=2, norm="ortho")
+    err = np.abs((phi - phi.mean()) - (ref - ref.mean())).max() / np.abs(ref).max()
+    assert err <= 1e-11
+    o.close()
+
+
+def test_poisson_3d_matches_fft_solution_periodic(oracle_lib):
+    """The same on a periodic box, against the 3D FFT solution."""
+    n = 16
+    L = 2 * math.pi
+    o = Oracle(n, dim=3, prob_hi=(L, L, L), ren=100.0, dt=0.01, bc_lo=(111, 111, 111), bc_hi=(111, 111, 111))
+    rng = np.random.default_rng(3)
+    f = rng.standard_normal((n, n, n))
+    phi, it, res = o.solve_poisson(f)
+    h = L / n
+    k = np.arange(n)
+    e = -(4.0 / h ** 2) * np.sin(np.pi * k / n) ** 2
+    lam = e[:, None, None] + e[None, :, None] + e[None, None, :]
+    lam[0, 0, 0] = 1.0
+    ph = np.fft.fftn(f - f.mean()) / lam
+    ph[0, 0, 0] = 0.0
+    ref = np.real(np.fft.ifftn(ph))
+    err = np.abs((phi - phi.mean()) - (ref - ref.mean())).max() / np.abs(ref).max()
+    assert err <= 1e-11
+    o.close()
+
+
+def test_cavity3d_invariants(oracle_lib):
+    """Three steps of the 16^3 lid cavity: zero discrete divergence after the
+    projection, the wall-normal velocities exactly zero on every wall (quirk
+    Q4), and the lid (north face, +x) dragging the top layer of u forward."""
+    n = 16
+    o = Oracle(n, dim=3, ren=100.0, dt=0.4 / n, iter_num=100, bc_lo=(135, 135, 135), bc_hi=(135, 165, 135))
+    o.init(0)
+    stats = run_steps(o, 3)
+    u, up, p, phi = o.get_state()
+    for s in stats:
+        assert s["div_after"] <= 1e-12
+        assert 1 <= s["pseudo_iters"] <= 101
+    # arrays are (z, y, x) with x fastest: u has n+1 x-faces, v n+1 y-faces, w n+1 z-faces
+    assert np.all(u[0][:, :, 0] == 0) and np.all(u[0][:, :, -1] == 0)
+    assert np.all(u[1][:, 0, :] == 0) and np.all(u[1][:, -1, :] == 0)
+    assert np.all(u[2][0, :, :] == 0) and np.all(u[2][-1, :, :] == 0)
+    assert u[0][1:-1, -1, 1:-1].min() > 0
+    o.close()
