@@ -254,3 +254,48 @@ def test_cavity3d_invariants(oracle_lib):
     assert np.all(u[2][0, :, :] == 0) and np.all(u[2][-1, :, :] == 0)
     assert u[0][1:-1, -1, 1:-1].min() > 0
     o.close()
+
+
+@pytest.mark.parametrize("case", ["cavity", "mixed_walls", "tgv_parity", "tgv_fixed"])
+def test_stage_3d_matches_numpy_restatement(oracle_lib, case):
+    """One 3D RK pseudo-stage of the oracle against the independent numpy
+    restatement (tests/npstage3.py), bit for bit: the lid cavity (walls on
+    every side, the lid on the north face); a box with a west inlet, slip walls
+    south, bottom and top, the east code 1 that the reference reads as slip and
+    the lid; and the perturbed periodic Taylor-Green box in the reference's
+    parity mode and in the physical mode."""
+    from amressif_gb300 import workloads as wl
+    from tests import npstage3
+
+    n = 12
+    if case in ("cavity", "mixed_walls"):
+        bc_lo, bc_hi = ((135, 135, 135), (135, 165, 135)) if case == "cavity" else ((-165, -135, -135), (1, 165, -135))
+        o = Oracle(n, dim=3, ren=100.0, dt=0.4 / n, bc_lo=bc_lo, bc_hi=bc_hi)
+        o.init(0)
+        per, fq = (False, False, False), 0
+        h = 1.0 / n
+    else:
+        L = 2 * math.pi
+        fq = 1 if case == "tgv_fixed" else 0
+        o = Oracle(n, dim=3, prob_hi=(L, L, L), ren=1600.0, dt=0.4 * L / n, bc_lo=(111,) * 3, bc_hi=(111,) * 3,
+                   fix_quirks=fq)
+        o.set_state(*wl.tgv3d_perturbed_state(n, amp=1e-3, seed=0))
+        bc_lo, bc_hi, per = (111,) * 3, (111,) * 3, (True, True, True)
+        h = L / n
+    run_steps(o, 2)
+    u, up, p, _ = o.get_state()
+    o.set_state(u, up, p)
+    o.step_begin()
+    un = [o.field(2, d) for d in range(3)]
+    du = [o.field(3, d) for d in range(3)]
+    us = [o.field(FIELD_STAR, d) for d in range(3)]
+    ub = [o.field(FIELD_BASE, d) for d in range(3)]
+    dt = o.params.dt
+    rk = 0.4 * dt * 0.25
+    ref, rhs = npstage3.stage3(us, ub, un, du, p, n, (h, h, h), dt, o.params.ren, rk, bc_lo, bc_hi, (1.0, 0.0, 0.0),
+                               per, reflect_periodic=(fq == 0))
+    o.rk_stage(0)
+    for d in range(3):
+        np.testing.assert_array_equal(o.field(FIELD_MRHS, d), rhs[d])
+        np.testing.assert_array_equal(o.field(FIELD_STAR, d), ref[d])
+    o.close()
