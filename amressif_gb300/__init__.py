@@ -30,6 +30,7 @@ NS_ERR_UNSUPPORTED = -7
 NS_ERR_NONFINITE = -8
 
 PREC_FP64_EXACT, PREC_FP64, PREC_MIXED = 0, 1, 2
+CONV_NEW_QUICK, CONV_QUICK, CONV_UMIST_FORM = 0, 1, 2  # ns_params.conv_scheme
 INIT_CAVITY, INIT_TGV = 0, 1
 FIELD_VEL, FIELD_VEL_PREV, FIELD_PRESSURE, FIELD_PHI, FIELD_VEL_STAR, FIELD_POISSON_RHS, FIELD_CART = range(7)
 
@@ -103,6 +104,7 @@ class NsParams(ctypes.Structure):
         ("gmres_restart", ctypes.c_int),
         ("dc_residual", ctypes.c_int),
         ("poisson_warm_start", ctypes.c_int),
+        ("conv_scheme", ctypes.c_int),
     ]
 
 

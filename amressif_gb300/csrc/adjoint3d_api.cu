@@ -99,6 +99,8 @@ int need3(ns_ctx* c) {
     if (!g.periodic[d] || g.flux_ghost[d] != kWrap || g.ctx_mirror[d] != 0)
       return fail(c, NS_ERR_UNSUPPORTED, "3D adjoint: periodic boxes in the physical mode (fix_quirks = 1) only");
   if (c->P.pseudo_timestepping == 0) return fail(c, NS_ERR_UNSUPPORTED, "3D adjoint: the explicit predictor is not built");
+  if (c->P.conv_scheme != NS_CONV_NEW_QUICK)
+    return fail(c, NS_ERR_UNSUPPORTED, "3D adjoint: differentiates the QUICK predictor (conv_scheme 0) only");
   return NS_OK;
 }
 

@@ -182,6 +182,8 @@ int get_cells(ns_ctx* c, const double* d, double* h) {
 
 int check_supported(ns_ctx* c) {
   if (c->P.dim == 3) return fail(c, NS_ERR_UNSUPPORTED, "adjoint: 2D only");
+  if (c->P.conv_scheme != NS_CONV_NEW_QUICK)
+    return fail(c, NS_ERR_UNSUPPORTED, "adjoint: differentiates the QUICK predictor (conv_scheme 0) only");
   if (c->g.periodic[0] || c->g.periodic[1])
     return fail(c, NS_ERR_UNSUPPORTED, "adjoint: periodic boxes are not supported");
   if (c->P.pseudo_timestepping == 0)

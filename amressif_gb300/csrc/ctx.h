@@ -37,6 +37,7 @@ struct ns_ctx {
   double* PHI[2] = {nullptr, nullptr};
   double* F = nullptr;
   double* CART[2] = {nullptr, nullptr};
+  double* CONV[2] = {nullptr, nullptr};  // NS_CONV_QUICK: cell convective term of the stage
   bool cart_pending = false;
   // pseudo-iteration state: buffer ids, -1 = UP, 0..2 = B[i]
   int base = -1, cur = -1;

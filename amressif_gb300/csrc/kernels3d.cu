@@ -14,7 +14,8 @@ cudaError_t launch3_cart(const Arg3& a, cudaStream_t s) {
 }
 cudaError_t launch3_total(const Arg3& a, cudaStream_t s) {
   const int N = a.g.N;
-  k3_flux<<<grid3(N + 1, N + 1, N + 1), 256, 0, s>>>(a);
+  // convective_flux_calc (conv_scheme 2) adds no convective term: no fluxes
+  if (a.g.conv_scheme == 0) k3_flux<<<grid3(N + 1, N + 1, N + 1), 256, 0, s>>>(a);
   k3_total<<<grid3(N, N, N), 256, 0, s>>>(a);
   return cudaGetLastError();
 }

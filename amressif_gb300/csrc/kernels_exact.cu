@@ -1,5 +1,6 @@
 // Exact-arithmetic instantiations: compiled with -fmad=false so that every
 // product and sum is rounded separately, in the reference's order.
+#include "conv_alt2d.cuh"  // its kernel is not a template: this unit alone includes it
 #include "launch.h"
 
 namespace ns {
@@ -15,6 +16,12 @@ cudaError_t launch_stage_exact(int mode, const StageArgs& a, cudaStream_t s) {
     k_stage2d<ArithExact, kExplicit, kStageTX, kStageTY><<<stage_grid(a.g), 256, 0, s>>>(a);
   else
     return cudaErrorInvalidValue;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_conv_quick_exact(const StageArgs& a, cudaStream_t s) {
+  const int N = a.g.N;
+  k_conv_quick2d<<<dim3((N + 31) / 32, (N + 7) / 8, 1), dim3(32, 8, 1), 0, s>>>(a);
   return cudaGetLastError();
 }
 

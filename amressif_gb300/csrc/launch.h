@@ -17,6 +17,7 @@ cudaError_t launch_stage_exact(int mode, const StageArgs& a, cudaStream_t s);
 cudaError_t launch_step_begin_exact(const ProjArgs& a, cudaStream_t s);
 cudaError_t launch_poisson_rhs_exact(const ProjArgs& a, cudaStream_t s);
 cudaError_t launch_project_exact(const ProjArgs& a, cudaStream_t s);
+cudaError_t launch_conv_quick_exact(const StageArgs& a, cudaStream_t s);  // writes a.conv[0..1]
 
 // kernels_fast.cu
 cudaError_t launch_stage_fast(int mode, const StageArgs& a, cudaStream_t s);

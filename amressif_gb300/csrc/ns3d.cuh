@@ -7,7 +7,8 @@
 //             ghosts, utilities.cpp:16-350) on [-2, N+1]^3,
 //   k3_flux   QUICK fluxes of the three components at every face along the
 //             three directions, each face once (fn_flux_calc.cpp:66-76),
-//   k3_total  t_m = visc - conv at the cells (central viscous term),
+//   k3_total  t_m = visc - conv at the cells (central viscous term; conv = 0
+//             for convective_flux_calc, which never updates the total flux),
 //   k3_face   G = S - (1.5/dt) u* + avg(t) with the flux-ghost rule of the
 //             normal component (main.cpp:945-1014), the RK update and the
 //             pseudo-norm of Error_Computation (utilities.cpp:421-493);
@@ -139,7 +140,7 @@ __global__ void __launch_bounds__(256) k3_total(Arg3 A) {
     for (int d = 0; d < 3; ++d) {
       const long s = G1[d];
       const double* F = A.fl[d][m];
-      conv += (F[fc + fstride[d]] - F[fc]) * g.inv_dx[d];
+      if (g.conv_scheme == 0) conv += (F[fc + fstride[d]] - F[fc]) * g.inv_dx[d];
       visc += (ph[gc + s] - 2.0 * p0 + ph[gc - s]) * g.inv_dx2[d];
     }
     A.t[m][fc] = visc * g.inv_ren - conv;

@@ -135,7 +135,7 @@ long round_up(long x, long a) { return (x + a - 1) / a * a; }
 void free_all(ns_ctx* c) {
   auto F = [](void* p) { if (p) cudaFree(p); };
   for (int m = 0; m < 2; ++m) {
-    F(c->U[m]); F(c->UP[m]); F(c->DU[m]); F(c->S[m]); F(c->CART[m]); F(c->PHI[m]);
+    F(c->U[m]); F(c->UP[m]); F(c->DU[m]); F(c->S[m]); F(c->CART[m]); F(c->PHI[m]); F(c->CONV[m]);
     for (int i = 0; i < 3; ++i) F(c->B[i][m]);
     F(c->SH[m]); F(c->G0[m]); F(c->G0b[m]); F(c->E[0][m]); F(c->E[1][m]);
     F(c->BH[0][m]); F(c->BH[1][m]); F(c->BL[0][m]); F(c->BL[1][m]); F(c->SFh[m]); F(c->SFl[m]);
@@ -268,6 +268,7 @@ void ns_params_default(ns_params* p) {
   p->gmres_restart = 30;
   p->dc_residual = 0;
   p->poisson_warm_start = 0;
+  p->conv_scheme = NS_CONV_NEW_QUICK;
 }
 
 int ns_params_parse_file(ns_params* p, const char* path) {
@@ -333,6 +334,13 @@ int ns_ctx_create(const ns_params* p, void* stream, ns_ctx** out) {
   if (p->dc_residual != 0 && p->dc_residual != 1) return NS_ERR_ARG;
   if (D == 3 && p->dc_residual == 1) return NS_ERR_UNSUPPORTED;  // the 3D defect correction is float-float
   if (p->poisson_warm_start != 0 && p->poisson_warm_start != 1) return NS_ERR_ARG;
+  if (p->conv_scheme < NS_CONV_NEW_QUICK || p->conv_scheme > NS_CONV_UMIST_FORM) return NS_ERR_ARG;
+  if (p->conv_scheme != NS_CONV_NEW_QUICK && p->precision == NS_PREC_MIXED) return NS_ERR_UNSUPPORTED;
+  // convective_flux_calc_quick reads face 0 from boxes that do not hold it,
+  // and in 3D writes component k of a one-component fab
+  if (p->conv_scheme == NS_CONV_QUICK &&
+      (D == 3 || p->max_grid_size[0] < p->n_cell || p->max_grid_size[1] < p->n_cell))
+    return NS_ERR_UNSUPPORTED;
   ns_ctx* c = new ns_ctx();
   c->P = *p;
   const int N = p->n_cell;
@@ -355,6 +363,7 @@ int ns_ctx_create(const ns_params* p, void* stream, ns_ctx** out) {
     else
       g.flux_ghost[d] = (g.periodic[d] && p->fix_quirks) ? kWrap : kReflect;
     g.ctx_mirror[d] = (g.periodic[d] && p->fix_quirks) ? 0 : 1;
+    g.conv_scheme = p->conv_scheme;
     for (int side = 0; side < 2; ++side) {
       const int r = make_cart_bc(*p, d, side, g.bc[2 * d + side]);
       if (r != NS_OK) {
@@ -417,6 +426,8 @@ int ns_ctx_create(const ns_params* p, void* stream, ns_ctx** out) {
     if (r == NS_OK) r = alloc_field(c, &c->PHI[m]);
     for (int i = 0; i < 3 && r == NS_OK; ++i) r = alloc_field(c, &c->B[i][m]);
   }
+  for (int m = 0; m < 2 && r == NS_OK && D == 2 && p->conv_scheme == NS_CONV_QUICK; ++m)
+    r = alloc_field(c, &c->CONV[m]);
   if (r == NS_OK && D == 2) r = alloc_field(c, &c->Pp);
   if (r == NS_OK && D == 2) r = alloc_field(c, &c->F);
   if (r == NS_OK && D == 2) r = alloc_levels<double>(c, c->M64, false);
@@ -695,6 +706,15 @@ int ns_step_begin(ns_ctx* c) {
   return NS_OK;
 }
 
+// convective_flux_calc_quick: its cell convective term is formed first, into
+// CONV, and the stage reads it (stage2d.cuh)
+static int launch_conv_alt(ns_ctx* c, StageArgs& a) {
+  if (c->P.conv_scheme != NS_CONV_QUICK) return NS_OK;
+  for (int m = 0; m < 2; ++m) a.conv[m] = c->CONV[m];
+  LAUNCH(NS_PROF_OTHER, "convective_flux_calc_quick", launch_conv_quick_exact(a, c->st));
+  return NS_OK;
+}
+
 static int launch_rk(ns_ctx* c, int sub, bool use_cart) {
   const int in = c->cur;
   const int outb = pick_out(c->base, in);
@@ -707,6 +727,8 @@ static int launch_rk(ns_ctx* c, int sub, bool use_cart) {
   }
   a.rk = c->rk[sub];
   a.do_norm = (sub == 3);
+  int rc = launch_conv_alt(c, a);
+  if (rc != NS_OK) return rc;
   const int mode = (c->P.precision == NS_PREC_FP64_EXACT) ? kExactRK : kFastRK;
   LAUNCH(mode == kExactRK ? NS_PROF_STAGE_EXACT : NS_PROF_STAGE_FAST, "rk stage",
          (mode == kExactRK) ? launch_stage_exact(mode, a, c->st) : launch_stage_fast(mode, a, c->st));
@@ -751,6 +773,8 @@ int ns_explicit_predictor(ns_ctx* c, double* norm) {
     a.cart[m] = c->cart_pending ? c->CART[m] : nullptr;
   }
   a.do_norm = 1;
+  int rc = launch_conv_alt(c, a);
+  if (rc != NS_OK) return rc;
   LAUNCH(NS_PROF_EXPLICIT, "explicit stage", launch_stage_exact(kExplicit, a, c->st));
   c->cart_pending = false;
   c->cur = outb;

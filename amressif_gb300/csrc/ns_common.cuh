@@ -49,6 +49,7 @@ struct Geom {
   int periodic[3];
   int flux_ghost[3];  // per direction: kReflect (quirk Q1), kWrap, kZero
   int ctx_mirror[3];  // 1: p/phi ghosts mirrored (quirk Q2), 0: periodic wrap
+  int conv_scheme;    // NS_CONV_*: 0 QUICK, 1 convective_flux_calc_quick (CONV arrays), 2 no convective term
   CartBC bc[6];       // xlo, xhi, ylo, yhi, zlo, zhi
   // optional lid profile of the north inlet (u component, one value per cell
   // column, device memory): the ghost becomes 2*lid_u[i] - q instead of

@@ -19,6 +19,11 @@
 //              e4, and G0 = G(u_base) is written in FP32 with an FP32 copy of
 //              u_base for the FP32 increment stages.
 //   kExplicit  PSEUDO_TIMESTEPPING = 0 (momentum.cpp:96-192).
+//
+// Geom::conv_scheme selects the convective routine: QUICK as above; the
+// cell term of convective_flux_calc_quick read from StageArgs::conv
+// (conv_alt2d.cuh forms it); or none (convective_flux_calc leaves the total
+// flux at the 0 of its setVal, so total = 0 - 0 + visc keeps the bits).
 #pragma once
 #include "ns_common.cuh"
 
@@ -36,6 +41,7 @@ struct StageArgs {
   const double* S[2];     // step-constant source (fast / anchor)
   const double* cart[2];  // optional cell velocity override (first stage of a run), cells
   const float* e4[2];     // anchor: increment added to us to form u_base
+  double* conv[2];        // conv_scheme 1: cell convective term, cells
   double* out[2];         // new u* (or u_base for the anchor)
   float* g0[2];           // anchor: G(u_base) in FP32
   float* shadow[2];       // anchor: FP32 copy of u_base
@@ -149,6 +155,7 @@ __global__ void __launch_bounds__(256) k_stage2d(StageArgs A) {
 
   // ---- 2. half-node fluxes ----------------------------------------------
   // x-faces a in [x0-1, x0+TX+1], rows b in [y0-1, y0+TY]
+  if (g.conv_scheme == 0) {
   for (int t = tid; t < SM::FXW * SM::FXH; t += NT) {
     const int fx = t % SM::FXW, fyy = t / SM::FXW;
     const int a = x0 - 1 + fx, b = y0 - 1 + fyy;
@@ -188,6 +195,7 @@ __global__ void __launch_bounds__(256) k_stage2d(StageArgs A) {
     if (need_v)
       sm.fy[1][fyy][fx] = quick_flux(vcf, sm.c[1][ly + 1][lx], sm.c[1][ly][lx], sm.c[1][ly - 1][lx], sm.c[1][ly - 2][lx]);
   }
+  }
   __syncthreads();
 
   // ---- 3. total = -conv + visc at cells ----------------------------------
@@ -202,8 +210,12 @@ __global__ void __launch_bounds__(256) k_stage2d(StageArgs A) {
 #pragma unroll
     for (int m = 0; m < 2; ++m) {
       if (m == 0 ? !need_u : !need_v) continue;
-      double conv = AR::div(sm.fx[m][ty][tx + 1] - sm.fx[m][ty][tx], dx, idx_) +
-                    AR::div(sm.fy[m][ty + 1][tx] - sm.fy[m][ty][tx], dy, idy_);
+      double conv = 0.0;
+      if (g.conv_scheme == 0)
+        conv = AR::div(sm.fx[m][ty][tx + 1] - sm.fx[m][ty][tx], dx, idx_) +
+               AR::div(sm.fy[m][ty + 1][tx] - sm.fy[m][ty][tx], dy, idy_);
+      else if (g.conv_scheme == 1)  // the wrapped cell in periodic directions: FillBoundary's copy
+        conv = A.conv[m][(long)wrapi(b, N) * P + wrapi(a, N)];
       const double ce = sm.c[m][ly][lx];
       const double s = sm.c[m][ly - 1][lx], n = sm.c[m][ly + 1][lx];
       const double w = sm.c[m][ly][lx - 1], e = sm.c[m][ly][lx + 1];

@@ -95,7 +95,22 @@ typedef struct ns_params {
                                 The tolerance stays relative to the zero-guess residual max|f - mean f|,
                                 so the solve meets the same residual bound in fewer V-cycles. The result
                                 then depends on the previous step's phi at the tolerance level. 0 = off */
+  int conv_scheme;           /* convective flux routine of the predictor (NS_CONV_*). main_main calls
+                                convective_flux_calc_new_quick (main.cpp:909,936); the other two are the
+                                reference's alternatives, FP64 modes only (NS_PREC_MIXED and the adjoint
+                                give NS_ERR_UNSUPPORTED) */
 } ns_params;
+
+/* ns_params.conv_scheme */
+#define NS_CONV_NEW_QUICK 0  /* convective_flux_calc_new_quick (fn_flux_calc.cpp:11-202): QUICK; the default */
+#define NS_CONV_QUICK 1      /* convective_flux_calc_quick (fn_flux_calc.cpp:204-393) as written: its QUICK
+                                weight Real(1/8) is 0 (first-order upwind faces), face N copies face 0, and
+                                the y differences are taken at i+1 through the flat face fab. 2D, one box
+                                (max_grid_size >= n_cell in x and y): with more boxes and in 3D the routine
+                                reads and writes outside its fabs. Else NS_ERR_UNSUPPORTED */
+#define NS_CONV_UMIST_FORM 2 /* convective_flux_calc (fn_flux_calc.cpp:395-692): forms fluxConvect, which
+                                only Export_Fluxes reads, and never updates fluxTotal, so the predictor has
+                                no convective term. 2D and 3D */
 
 typedef struct ns_step_stats {
   int pseudo_iters;   /* K (countIter at exit) */

@@ -220,6 +220,64 @@ void convective_flux(orc_ctx* c) {
   });
 }
 
+// convective_flux_calc_quick (fn_flux_calc.cpp:204-393), 2D, one box. As
+// written it computes:
+// - face values upwinded on the sign of velStar, with the QUICK correction
+//   weighted by Real(1/8), an integer division that is 0: q_U + 0.0 * (...),
+//   the product kept (it decides the sign of a zero result);
+// - the faces over the cells only (face i is the west face of cell i); at
+//   the last cell of the domain face N takes face 0's value along x and y;
+// - conv_u from face-velocity products (conservative form), conv_v from the
+//   cell velocity times face differences (advective form), both taking the y
+//   differences at i+1 instead of j+1. The y-face arrays have no ghost cells,
+//   so at i = N-1 the (N, j) element of the flat fab is (0, j+1).
+void convective_flux_quick(orc_ctx* c) {
+  const int N = c->N;
+  const Arr &U = c->velStar[0], &V = c->velStar[1];
+  const Arr &q0 = c->cart[0], &q1 = c->cart[1];
+  const double w = 0.0;  // Real(1/8)
+  for (int j = 0; j < N; ++j)
+    for (int i = 0; i < N; ++i) {
+      for (int m = 0; m < 2; ++m) {
+        const Arr& q = c->cart[m];
+        Arr& fx = c->half[m][0];
+        if (U(i, j, 0) > 0)
+          fx(i, j, 0) = q(i - 1, j, 0) + w * (-q(i - 2, j, 0) - 2 * q(i - 1, j, 0) + 3 * q(i, j, 0));
+        else
+          fx(i, j, 0) = q(i, j, 0) + w * (3 * q(i - 1, j, 0) - 2 * q(i, j, 0) - q(i + 1, j, 0));
+        if (i == N - 1) fx(N, j, 0) = fx(0, j, 0);
+        Arr& fy = c->half[m][1];
+        if (V(i, j, 0) > 0)
+          fy(i, j, 0) = q(i, j - 1, 0) + w * (-q(i, j - 2, 0) - 2 * q(i, j - 1, 0) + 3 * q(i, j, 0));
+        else
+          fy(i, j, 0) = q(i, j, 0) + w * (3 * q(i, j - 1, 0) - 2 * q(i, j, 0) - q(i, j + 1, 0));
+        if (j == N - 1) fy(i, N, 0) = fy(i, 0, 0);
+      }
+    }
+  // element (i+1, j) of a y-face fab (x extent N, no ghosts)
+  auto yf = [N](const Arr& a, int i, int j) { return i + 1 < N ? a(i + 1, j, 0) : a(0, j + 1, 0); };
+  const double dx = c->dx[0], dy = c->dx[1];
+  par_cells(c, [&](int i, int j, int k) {
+    const Arr &ux = c->half[0][0], &uy = c->half[0][1], &vx = c->half[1][0], &vy = c->half[1][1];
+    c->conv[0](i, j, k) = (U(i + 1, j, 0) * ux(i + 1, j, 0) - U(i, j, 0) * ux(i, j, 0)) / dx +
+                          (yf(V, i, j) * yf(uy, i, j) - V(i, j, 0) * uy(i, j, 0)) / dy;
+    c->conv[1](i, j, k) = (q0(i, j, 0) * (vx(i + 1, j, 0) - vx(i, j, 0))) / dx +
+                          (q1(i, j, 0) * (yf(vy, i, j) - vy(i, j, 0))) / dy;
+  });
+  par_cells(c, [&](int i, int j, int k) {
+    for (int m = 0; m < 2; ++m) c->total[m](i, j, k) = c->total[m](i, j, k) - c->conv[m](i, j, k);
+  });
+}
+
+// The convective routine the predictor calls. convective_flux_calc
+// (fn_flux_calc.cpp:395-692) forms fluxConvect, which only Export_Fluxes
+// reads, and never updates fluxTotal: the predictor then carries no
+// convective term, and fluxTotal keeps the 0 of its setVal.
+void convective(orc_ctx* c) {
+  if (c->P.conv_scheme == 1) convective_flux_quick(c);
+  else if (c->P.conv_scheme == 0) convective_flux(c);
+}
+
 // viscous_flux_calc (fn_flux_calc.cpp:695-766)
 void viscous_flux(orc_ctx* c) {
   const double ren = c->P.ren;
@@ -722,6 +780,14 @@ int orc_create(const orc_params* p, orc_ctx** out) {
     if ((p->bc_lo[d] == 111) != (p->bc_hi[d] == 111)) { delete c; return ORC_ERR_BC; }
   }
   split_boxes(c);
+  // convective_flux_calc_quick reads and writes outside its fabs when there is
+  // more than one box (face 0 from a box that does not hold it) and in 3D
+  // (component k of a one-component fab)
+  if (p->conv_scheme < 0 || p->conv_scheme > 2 ||
+      (p->conv_scheme == 1 && (c->D != 2 || c->boxes.size() != 1))) {
+    delete c;
+    return ORC_ERR_ARG;
+  }
   for (int d = 0; d < c->D; ++d) {
     define_face(c, c->velCont[d], d); define_face(c, c->velContPrev[d], d);
     define_face(c, c->velContDiff[d], d); define_face(c, c->velStar[d], d);
@@ -893,7 +959,7 @@ int orc_rk_stage(orc_ctx* c, int sub) {
   // main.cpp:931-1017
   gradient_calc(c);
   for (int m = 0; m < c->D; ++m) c->total[m].setVal(0.0);
-  convective_flux(c);
+  convective(c);
   viscous_flux(c);
   flux_ghosts(c, true);
   momentum_rhs(c);
@@ -961,7 +1027,7 @@ int orc_explicit_predictor(orc_ctx* c, double* norm) {
   // main.cpp:902-925; no flux reflection in this mode (quirk Q3)
   gradient_calc(c);
   for (int m = 0; m < c->D; ++m) c->total[m].setVal(0.0);
-  convective_flux(c);
+  convective(c);
   viscous_flux(c);
   flux_ghosts(c, false);
   momentum_rhs(c);

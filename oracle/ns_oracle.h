@@ -46,6 +46,9 @@ typedef struct orc_params {
   double poisson_tol;      /* relative max-norm residual target of the exact solve (<= 1e-12) */
   int nthreads;            /* OpenMP threads (0 = runtime default) */
   int dtau_clip;           /* 1: clip dtau to 0.9 x the RK4 stability limit (grids where 0.4 dt is unstable) */
+  int conv_scheme;         /* convective flux routine the predictor calls: 0 convective_flux_calc_new_quick
+                              (main.cpp:909,936), 1 convective_flux_calc_quick (fn_flux_calc.cpp:204-393; 2D,
+                              one box), 2 convective_flux_calc (fn_flux_calc.cpp:395-692) */
 } orc_params;
 
 typedef struct orc_step_stats {

@@ -35,6 +35,7 @@ class OrcParams(ctypes.Structure):
         ("poisson_tol", ctypes.c_double),
         ("nthreads", ctypes.c_int),
         ("dtau_clip", ctypes.c_int),
+        ("conv_scheme", ctypes.c_int),
     ]
 
 
@@ -104,7 +105,7 @@ class Oracle:
     def __init__(self, n_cell, dim=2, max_grid_size=None, prob_lo=(0.0, 0.0, 0.0), prob_hi=(1.0, 1.0, 1.0),
                  ren=100.0, dt=1e-3, iter_num=100, momentum_tolerance=1e-10, pseudo_timestepping=1,
                  bc_lo=(135, 135, 135), bc_hi=(135, 165, 135), inflow=(1.0, 0.0, 0.0), fix_quirks=0,
-                 poisson_tol=1e-13, nthreads=0, dtau_clip=0):
+                 poisson_tol=1e-13, nthreads=0, dtau_clip=0, conv_scheme=0):
         p = OrcParams()
         p.dim, p.n_cell = dim, n_cell
         mgs = max_grid_size or (n_cell, n_cell, n_cell)
@@ -117,6 +118,7 @@ class Oracle:
         p.momentum_tolerance, p.pseudo_timestepping = momentum_tolerance, pseudo_timestepping
         p.fix_quirks, p.poisson_tol, p.nthreads = fix_quirks, poisson_tol, nthreads
         p.dtau_clip = dtau_clip
+        p.conv_scheme = conv_scheme
         self.params = p
         self.dim, self.n = dim, n_cell
         h = ctypes.c_void_p()

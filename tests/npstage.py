@@ -63,11 +63,46 @@ def quick(ucf, A, B, C, E):
     return up * (0.125 * (-A - 2 * B + 3 * C) + B) + ud * (0.125 * (-E - 2 * C + 3 * B) + C)
 
 
-def stage(us, ub, un, du, p, n, dx, dy, dt, ren, rk, bc_lo, bc_hi, inflow, periodic, cart=None):
-    """One RK pseudo-stage; returns (new u*, momentum rhs)."""
+def conv_quick_int(u, v, c, n, dx, dy):
+    """Convective term of convective_flux_calc_quick (fn_flux_calc.cpp:204-393)
+    on one box: first-order upwind face values plus 0.0 times the QUICK
+    correction (its weight Real(1/8) is an integer division), face n a copy of
+    face 0, and the y differences taken at i+1 through the flat y-face fab,
+    whose element (i+1, j) is (0, j+1) at the last column."""
+    g = 2
+    I = np.arange(n)
+    X, Y = [], []
+    for m in range(2):
+        q = c[m]
+        r = q[g:-g]
+        vp = r[:, g - 1 + I] + 0.0 * (-r[:, g - 2 + I] - 2 * r[:, g - 1 + I] + 3 * r[:, g + I])
+        vm = r[:, g + I] + 0.0 * (3 * r[:, g - 1 + I] - 2 * r[:, g + I] - r[:, g + 1 + I])
+        x = np.where(u[:, :n] > 0, vp, vm)
+        X.append(np.hstack([x, x[:, :1]]))
+        col = q[:, g:-g]
+        vp = col[g - 1 + I, :] + 0.0 * (-col[g - 2 + I, :] - 2 * col[g - 1 + I, :] + 3 * col[g + I, :])
+        vm = col[g + I, :] + 0.0 * (3 * col[g - 1 + I, :] - 2 * col[g + I, :] - col[g + 1 + I, :])
+        y = np.where(v[:n, :] > 0, vp, vm)
+        Y.append(np.vstack([y, y[:1, :]]))
+    flat = I[:, None] * n + I[None, :] + 1  # element (i+1, j) of an (n+1) x n y-face fab
+
+    def nxt(a):
+        return a.ravel()[flat]
+
+    conv0 = (u[:, 1:] * X[0][:, 1:] - u[:, :-1] * X[0][:, :-1]) / dx + (nxt(v) * nxt(Y[0]) - v[:n] * Y[0][:n]) / dy
+    conv1 = (c[0][g:-g, g:-g] * (X[1][:, 1:] - X[1][:, :-1])) / dx + (c[1][g:-g, g:-g] * (nxt(Y[1]) - Y[1][:n])) / dy
+    return conv0, conv1
+
+
+def stage(us, ub, un, du, p, n, dx, dy, dt, ren, rk, bc_lo, bc_hi, inflow, periodic, cart=None, conv_scheme=0):
+    """One RK pseudo-stage; returns (new u*, momentum rhs). conv_scheme: the
+    convective routine (0 convective_flux_calc_new_quick, 1
+    convective_flux_calc_quick, 2 convective_flux_calc, which leaves the
+    total flux without a convective term)."""
     g = 2
     u, v = us
     c = cart if cart is not None else cont2cart(u, v, n, bc_lo, bc_hi, inflow, periodic)
+    alt = conv_quick_int(u, v, c, n, dx, dy) if conv_scheme == 1 else None
     total = []
     for m in range(2):
         q = c[m]
@@ -85,6 +120,10 @@ def stage(us, ub, un, du, p, n, dx, dy, dt, ren, rk, bc_lo, bc_hi, inflow, perio
         Ey = q[J - 2, g:-g]
         Fy = quick(v, Ay, By, Cy, Ey)
         conv = (Fx[:, 1:] - Fx[:, :-1]) / dx + (Fy[1:, :] - Fy[:-1, :]) / dy
+        if conv_scheme == 1:
+            conv = alt[m]
+        elif conv_scheme == 2:
+            conv = np.zeros((n, n))
         ce = q[g:-g, g:-g]
         visc = ((q[g:-g, g + 1:n + g + 1] - 2 * ce + q[g:-g, g - 1:n + g - 1]) / (dx * dx)
                 + (q[g + 1:n + g + 1, g:-g] - 2 * ce + q[g - 1:n + g - 1, g:-g]) / (dy * dy)) / ren

@@ -64,6 +64,56 @@ def test_stage_matches_numpy_restatement(oracle_lib, periodic):
         np.testing.assert_array_equal(o.field(FIELD_MRHS, d), rhs[d])
 
 
+@pytest.mark.parametrize("scheme", [1, 2])
+@pytest.mark.parametrize("periodic", [False, True])
+def test_stage_conv_variants_match_numpy_restatement(oracle_lib, scheme, periodic):
+    """The two convective routines that main_main does not call, one RK
+    pseudo-stage against the numpy restatement, bit for bit:
+    convective_flux_calc_quick (scheme 1, fn_flux_calc.cpp:204-393) and
+    convective_flux_calc (scheme 2, fn_flux_calc.cpp:395-692), on the lid
+    cavity and the periodic Taylor-Green box, one box each."""
+    n = 24
+    if periodic:
+        L = 2 * math.pi
+        o = Oracle(n, prob_hi=(L, L, L), ren=400.0, dt=0.5 * L / n, bc_lo=(111, 111, 111), bc_hi=(111, 111, 111),
+                   conv_scheme=scheme)
+        o.init(1)
+        bc_lo, bc_hi, per, dx = (111, 111), (111, 111), (True, True), L / n
+    else:
+        o = Oracle(n, ren=100.0, dt=1e-3, conv_scheme=scheme)
+        o.init(0)
+        bc_lo, bc_hi, per, dx = (135, 135), (135, 165), (False, False), 1.0 / n
+    run_steps(o, 3)
+    u, up, p, _ = o.get_state()
+    o.set_state(u, up, p)
+    o.step_begin()
+    un = [o.field(2, d) for d in range(2)]
+    du = [o.field(3, d) for d in range(2)]
+    us = [o.field(FIELD_STAR, d) for d in range(2)]
+    ub = [o.field(FIELD_BASE, d) for d in range(2)]
+    dt = o.params.dt
+    rk = 0.4 * dt * 0.25
+    ref, rhs = npstage.stage(us, ub, un, du, p, n, dx, dx, dt, o.params.ren, rk, bc_lo, bc_hi, (1.0, 0.0), per,
+                             conv_scheme=scheme)
+    o.rk_stage(0)
+    for d in range(2):
+        np.testing.assert_array_equal(o.field(FIELD_MRHS, d), rhs[d])
+        np.testing.assert_array_equal(o.field(FIELD_STAR, d), ref[d])
+    o.close()
+
+
+def test_conv_quick_variant_needs_one_2d_box(oracle_lib):
+    """convective_flux_calc_quick reads and writes outside its fabs with more
+    than one box and in 3D, so the oracle refuses those layouts."""
+    with pytest.raises(ValueError):
+        Oracle(32, max_grid_size=(16, 32, 32), conv_scheme=1)
+    with pytest.raises(ValueError):
+        Oracle(12, dim=3, conv_scheme=1)
+    with pytest.raises(ValueError):
+        Oracle(32, conv_scheme=3)
+    Oracle(12, dim=3, conv_scheme=2).close()
+
+
 def _neumann_eigs(n, h):
     k = np.arange(n)
     return -(4.0 / h ** 2) * np.sin(np.pi * k / (2 * n)) ** 2

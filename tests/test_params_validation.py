@@ -37,6 +37,15 @@ def create(gpu_lib, **kw):
     (dict(bc_lo=(135, 135, 135), bc_hi=(195, 165, 135)), ns.NS_ERR_BC),
     # east -135 in parity mode: the reference tests east slip as == 1 (quirk Q5)
     (dict(bc_lo=(135, 135, 135), bc_hi=(-135, 165, 135), fix_quirks=0), ns.NS_ERR_UNSUPPORTED),
+    # the convective routine: an unknown one; the alternatives with the mixed predictor;
+    # convective_flux_calc_quick with two boxes (the defaults split 32 x 32 into 32 x 16 boxes)
+    # and in 3D, where it reads and writes outside its fabs
+    (dict(conv_scheme=3), ns.NS_ERR_ARG),
+    (dict(conv_scheme=-1), ns.NS_ERR_ARG),
+    (dict(conv_scheme=ns.CONV_QUICK, precision=ns.PREC_MIXED, max_grid_size=(32, 32, 32)), ns.NS_ERR_UNSUPPORTED),
+    (dict(conv_scheme=ns.CONV_UMIST_FORM, precision=ns.PREC_MIXED), ns.NS_ERR_UNSUPPORTED),
+    (dict(conv_scheme=ns.CONV_QUICK), ns.NS_ERR_UNSUPPORTED),
+    (dict(dim=3, n_cell=16, conv_scheme=ns.CONV_QUICK, max_grid_size=(16, 16, 16)), ns.NS_ERR_UNSUPPORTED),
 ])
 def test_rejected_before_any_device_work(gpu_lib, kw, code):
     rc, h = create(gpu_lib, **kw)
