@@ -11,7 +11,7 @@
 // true and the tests compile away.
 //
 // Sites: 1-12 k_inc_col2d, 21-32 k_anchor_col2d, 41-46 k_mg_smooth_col,
-// 51-56 k_mg_smooth.
+// 51-56 k_mg_smooth, 61 k_conv_quick2d.
 #pragma once
 #include <cuda_runtime.h>
 

@@ -64,3 +64,32 @@ def test_checked_build_finds_no_out_of_range_index(gpu_lib, name, precision):
     for a, b in zip(out[0][1], out[1][1]):
         assert rel(b, a) <= 1e-12
     assert rel(out[1][2] - out[1][2].mean(), out[0][2] - out[0][2].mean()) <= 1e-12
+
+
+@pytest.mark.parametrize("periodic", [False, True])
+def test_checked_build_conv_quick_variant(gpu_lib, periodic):
+    """convective_flux_calc_quick's cell kernel reads the y-face fab through its
+    flat layout at the last column, element (0, j+1) (site 61): no failure on a
+    40^2 cavity or periodic box, and the normal build's steps."""
+    n = 40
+    kw = dict(ren=100.0, fixed_dt=0.25 * 2 * math.pi / n, fix_quirks=1, **PER) if periodic else \
+        dict(ren=100.0, fixed_dt=0.5 / n)
+    out = []
+    for checked in (False, True):
+        p = ns.default_params(n_cell=n, iter_num=100, precision=ns.PREC_FP64_EXACT, poisson_tol_rel=1e-12,
+                              max_grid_size=(n, n, n), conv_scheme=ns.CONV_QUICK, **kw)
+        s = ns.Solver(p, checked=checked)
+        if periodic:
+            s.set_state(*wl.tgv_perturbed_state(n, amp=1e-3, seed=0))
+        else:
+            s.init(ns.INIT_CAVITY)
+        ks = [s.step()["pseudo_iters"] for _ in range(2)]
+        if checked:
+            count, first, site = s.bounds_check()
+            assert count == 0, "out-of-range index %d at site %d (%d failures)" % (first, site, count)
+        u, _, pp, _ = s.get_state()
+        out.append((ks, u))
+        s.close()
+    assert out[0][0] == out[1][0]
+    for a, b in zip(out[0][1], out[1][1]):
+        assert rel(b, a) <= 1e-12
