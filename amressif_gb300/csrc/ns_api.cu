@@ -354,6 +354,7 @@ int ns_ctx_create(const ns_params* p, void* stream, ns_ctx** out) {
   g.pitch = c->pitch;
   g.plane = c->pitch * (N + 1);
   for (int d = 0; d < 3; ++d) g.dx[d] = (p->prob_hi[d] - p->prob_lo[d]) / (double)N;
+  g.conv_scheme = p->conv_scheme;
   for (int d = 0; d < D; ++d) {
     const bool lo111 = p->bc_lo[d] == 111, hi111 = p->bc_hi[d] == 111;
     if (lo111 != hi111) { delete c; return NS_ERR_BC; }
@@ -363,7 +364,6 @@ int ns_ctx_create(const ns_params* p, void* stream, ns_ctx** out) {
     else
       g.flux_ghost[d] = (g.periodic[d] && p->fix_quirks) ? kWrap : kReflect;
     g.ctx_mirror[d] = (g.periodic[d] && p->fix_quirks) ? 0 : 1;
-    g.conv_scheme = p->conv_scheme;
     for (int side = 0; side < 2; ++side) {
       const int r = make_cart_bc(*p, d, side, g.bc[2 * d + side]);
       if (r != NS_OK) {
