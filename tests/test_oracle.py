@@ -64,6 +64,45 @@ def test_stage_matches_numpy_restatement(oracle_lib, periodic):
         np.testing.assert_array_equal(o.field(FIELD_MRHS, d), rhs[d])
 
 
+# the RK coefficient vector that the reference's only test prints
+# (Tests/loop_test/forloopforvec.cpp:12-21); main.cpp:861-870 scales it by 0.4 dt
+RK_COEFFS = [1.0 / 4.0, 1.0 / 3.0, 1.0 / 2.0, 1.0]
+
+
+@pytest.mark.parametrize("periodic", [False, True])
+def test_rk_pseudo_iteration_matches_loop_test_coefficients(oracle_lib, periodic):
+    """All four RK stages of one pseudo-iteration against the numpy stage with
+    rk = 0.4 dt x the printed coefficient vector, bit for bit, each stage from
+    the oracle's previous u*."""
+    n = 24
+    if periodic:
+        L = 2 * math.pi
+        o = Oracle(n, prob_hi=(L, L, L), ren=400.0, dt=0.5 * L / n, bc_lo=(111, 111, 111), bc_hi=(111, 111, 111))
+        o.init(1)
+        bc_lo, bc_hi, per, dx = (111, 111), (111, 111), (True, True), L / n
+    else:
+        o = cavity(n)
+        o.init(0)
+        bc_lo, bc_hi, per, dx = (135, 135), (135, 165), (False, False), 1.0 / n
+    run_steps(o, 2)
+    u, up, p, _ = o.get_state()
+    o.set_state(u, up, p)
+    o.step_begin()
+    un = [o.field(2, d) for d in range(2)]
+    du = [o.field(3, d) for d in range(2)]
+    ub = [o.field(FIELD_BASE, d) for d in range(2)]
+    dt = o.params.dt
+    d_tau = 0.4 * dt
+    for sub, coef in enumerate(RK_COEFFS):
+        us = [o.field(FIELD_STAR, d) for d in range(2)]
+        ref, _ = npstage.stage(us, ub, un, du, p, n, dx, dx, dt, o.params.ren, d_tau * coef, bc_lo, bc_hi,
+                               (1.0, 0.0), per)
+        o.rk_stage(sub)
+        for d in range(2):
+            np.testing.assert_array_equal(o.field(FIELD_STAR, d), ref[d], err_msg="stage %d comp %d" % (sub, d))
+    o.close()
+
+
 @pytest.mark.parametrize("scheme", [1, 2])
 @pytest.mark.parametrize("periodic", [False, True])
 def test_stage_conv_variants_match_numpy_restatement(oracle_lib, scheme, periodic):
