@@ -8,9 +8,9 @@ solved until max|div u| <= 1e-10 (and the reference's relative 1e-10), started
 from rest (a 1000-step run). A "step" is one time step: the dual-time BDF2
 predictor, the pressure Poisson solve and the projection.
 
-Metric: steps/s of the mixed-precision solver (FP64 anchors + FP32 increment
-stages, FP32 V-cycles inside FP64 defect correction), with the plain FP64 GPU
-solver timed on the same steps beside it.
+Metric: steps/s of the mixed-precision solver (float-float anchors + FP32
+increment stages, FP32 V-cycles inside a float-float defect correction, FP64
+projection), with the plain FP64 GPU solver timed on the same steps beside it.
 
 `--impl reference` times the CPU restatement of the reference (oracle/) on all
 host cores on a bounded sample of the same workload.
@@ -39,7 +39,7 @@ ALGO_BYTES_PER_CELL = {
     "anchor": 64.0,        # read base hi/lo, e4, S hi/lo (f32); write base hi/lo, G0 (f32)
     "increment": 35.7,     # stage 1: read u_b, G0, write e (24); stages 2-3 also read e (32); the incremental
                            # anchor update also reads the base lo part and writes the new base hi/lo (56);
-                           # launch mix of 15 incremental + 1 exact anchor per 16 iterations
+                           # the launch mix of the timed steps replaces this figure (increment_bytes_per_cell)
     "explicit": 88.0,
     "step_begin": 56.0,    # read u, u_prev, p; write du, S
     "poisson_rhs": 24.0,   # read 2 faces, write f
@@ -47,6 +47,21 @@ ALGO_BYTES_PER_CELL = {
     "mg_smooth0": 12.0,    # FP32: read x, f; write x (level 0)
     "dc_update": 32.0,     # read phi, e (f32), f; write phi, r (f32)
 }
+
+
+def increment_bytes_per_cell(prof):
+    """Launch-weighted algorithmic bytes per cell of the increment kernel over
+    the profiled launches. A pseudo-iteration is one exact anchor or one
+    incremental anchor update (56 B), then stages 1 (24 B), 2 and 3 (32 B
+    each), so with A exact anchors and I increment launches the iterations are
+    K = (I + A) / 4 and the updates I - 3K."""
+    a = prof.get("anchor", (0, 0.0))[0]
+    i = prof.get("increment", (0, 0.0))[0]
+    k = (i + a) / 4.0
+    upd = i - 3.0 * k
+    if i <= 0 or k <= 0 or upd < 0:
+        return ALGO_BYTES_PER_CELL["increment"]
+    return (88.0 * k + 56.0 * upd) / i
 
 
 def clocks_sampler(stop, out):
@@ -217,7 +232,9 @@ def throughput_block(n, K, total_s, stats, prof, peak, stats_p):
     kmean = statistics.mean(st["pseudo_iters"] for st in stats)
     cycles = sum(st["poisson_cycles"] for st in stats_p)
     prof_s = sum(st["ms_predictor"] + st["ms_poisson"] + st["ms_project"] for st in stats_p) / 1e3
-    algo = sum(ALGO_BYTES_PER_CELL[k] * n * n * c for k, (c, _) in prof.items() if k in ALGO_BYTES_PER_CELL)
+    inc_bpc = increment_bytes_per_cell(prof)
+    algo = sum((inc_bpc if k == "increment" else ALGO_BYTES_PER_CELL[k]) * n * n * c
+               for k, (c, _) in prof.items() if k in ALGO_BYTES_PER_CELL)
     mg_kinds = ("mg_smooth0", "mg_smooth", "mg_restrict0", "mg_restrict", "mg_bottom", "mg_cycle")
     mg_ms = sum(prof[k][1] for k in mg_kinds if k in prof)
     dc_c, dc_ms = prof.get("dc_update", (0, 0.0))
@@ -749,7 +766,7 @@ def bench_ours(args):
     dom = max(prof.items(), key=lambda kv: kv[1][1])
     kind, (cnt, kms) = dom
     per_launch_ms = kms / max(cnt, 1)
-    bpc = ALGO_BYTES_PER_CELL.get(kind)
+    bpc = increment_bytes_per_cell(prof) if kind == "increment" else ALGO_BYTES_PER_CELL.get(kind)
     roofline = None
     if bpc is not None and cnt > 0:
         algo = bpc * n * n

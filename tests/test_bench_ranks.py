@@ -73,3 +73,18 @@ def test_reference_arm_prints_on_rank_zero_only(oracle_lib):
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["cpu_baseline"]["kind"] == "port"
+
+
+def test_increment_bytes_follow_the_launch_mix():
+    """The dominant kernel's algorithmic bytes per cell: each pseudo-iteration
+    is one exact anchor or one incremental update (56 B) plus stages 1 (24 B),
+    2 and 3 (32 B each); the figure is weighted by the profiled launches."""
+    import bench
+
+    # 69 iterations with 3 exact anchors: 66 updates and 207 stage launches
+    assert abs(bench.increment_bytes_per_cell({"anchor": (3, 1.0), "increment": (273, 1.0)})
+               - (88 * 69 + 56 * 66) / 273) < 1e-12
+    # every iteration with an exact anchor: stages only, 88 / 3 B
+    assert abs(bench.increment_bytes_per_cell({"anchor": (5, 1.0), "increment": (15, 1.0)}) - 88 / 3) < 1e-12
+    # no profile: the fixed figure
+    assert bench.increment_bytes_per_cell({}) == bench.ALGO_BYTES_PER_CELL["increment"]
