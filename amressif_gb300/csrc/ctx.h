@@ -160,6 +160,7 @@ int step3d(ns_ctx* c, ns_step_stats* s);
 int step_begin3d(ns_ctx* c);
 int rk_stage3d(ns_ctx* c, int sub);
 int pseudo_norm3d(ns_ctx* c, double* norm);
+int explicit_predictor3d(ns_ctx* c, double* norm);
 int poisson_rhs3d(ns_ctx* c, double* divmax, double* sum);
 int poisson_solve3d(ns_ctx* c, int precision, int* cycles, double* res);
 int project3d(ns_ctx* c, double* divmax);

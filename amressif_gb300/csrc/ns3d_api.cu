@@ -3,8 +3,8 @@
 // ns3d_mixed.cuh (mixed-precision predictor). The 3D context supports the
 // whole-step API (ns_step, ns_set_state / ns_get_state, checkpoints), the
 // per-call-site building blocks (step begin, FP64 RK stage, pseudo-norm,
-// Poisson right-hand side and solve, projection; the explicit predictor is
-// not built in 3D), the box transfers and the adjoint (adjoint3d_api.cu).
+// explicit predictor, Poisson right-hand side and solve, projection), the box
+// transfers and the adjoint (adjoint3d_api.cu).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -588,6 +588,38 @@ int rk_stage3d(ns_ctx* c, int sub) {
   return NS_OK;
 }
 
+// explicit_time_marching (momentum.cpp:96-192, main.cpp:902-925): one pass
+// from u* = u^n (step begin leaves base and u* on u^n), R = -grad p +
+// avg(total) + du / (2 dt), u* += (dt / 1.5) R, then Error_Computation and
+// velCont <- velStar. With S = -grad p + (0.5/dt) du + (1.5/dt) u^n, R is the
+// face pass's S - (1.5/dt) u* + avg(total) at u* = u^n, so the RK passes run
+// once with rk = dt / 1.5. The flux ghosts of this mode are set when the
+// context is made: zero normal total at walls (no reflection, quirk Q3), the
+// periodic wrap otherwise.
+int explicit_predictor3d(ns_ctx* c, double* norm) {
+  State3D& S = *c->s3;
+  const int outb = pick3(S.base, S.cur);
+  Arg3 b = args(c);
+  for (int m = 0; m < 3; ++m) {
+    b.u[m] = face3(c, S.cur, m);
+    b.ub[m] = face3(c, S.cur, m);
+    b.S[m] = S.S[m];
+    b.out[m] = S.B[outb][m];
+  }
+  b.rk = c->dt / 1.5;
+  b.do_norm = 1;
+  b.red_out = c->red + kRedNorm;
+  LAUNCH(NS_PROF_EXPLICIT, "cart 3d", launch3_cart(b, c->st));
+  LAUNCH(NS_PROF_EXPLICIT, "total 3d", launch3_total(b, c->st));
+  LAUNCH(NS_PROF_EXPLICIT, "explicit face 3d", launch3_face(b, c->st));
+  S.cur = outb;
+  int r = sync_red(c, kRedNorm, 1);
+  if (r != NS_OK) return r;
+  if (norm) *norm = c->red_h[kRedNorm];
+  S.base = S.cur;
+  return NS_OK;
+}
+
 // Error_Computation and velCont <- velStar (main.cpp:1019-1026)
 int pseudo_norm3d(ns_ctx* c, double* norm) {
   State3D& S = *c->s3;
@@ -658,13 +690,19 @@ int predictor3d(ns_ctx* c, ns_step_stats* sp) {
   int r = step_begin3d(c);
   if (r != NS_OK) return r;
   // ---- dual-time pseudo-iterations (main.cpp:898-1040)
-  const bool mixed = c->P.precision == NS_PREC_MIXED;
+  const bool mixed = c->P.precision == NS_PREC_MIXED && c->P.pseudo_timestepping != 0;
   S.bf = -1;
   S.mix_it = 0;
   S.mix_last_exact = 0;
   int count = 0;
   double norm = 1.e9;
   while (norm > c->P.momentum_tolerance) {
+    if (c->P.pseudo_timestepping == 0) {  // one explicit pass, then break (main.cpp:902-925)
+      r = explicit_predictor3d(c, &norm);
+      if (r != NS_OK) return r;
+      count = 1;
+      break;
+    }
     if (mixed) {
       r = mixed_iteration3(c);
       if (r != NS_OK) return r;
@@ -693,7 +731,6 @@ int predictor3d(ns_ctx* c, ns_step_stats* sp) {
 }
 
 int step3d(ns_ctx* c, ns_step_stats* stats) {
-  if (c->P.pseudo_timestepping == 0) return fail(c, NS_ERR_UNSUPPORTED, "3D: the explicit predictor is not built");
   ns_step_stats s;
   std::memset(&s, 0, sizeof(s));
   if (c->ev_ok) cudaEventRecord(c->ev[0], c->st);

@@ -761,8 +761,8 @@ int ns_pseudo_norm(ns_ctx* c, double* norm) {
 
 int ns_explicit_predictor(ns_ctx* c, double* norm) {
   if (!c) return NS_ERR_ARG;
-  if (c->P.dim == 3) return fail(c, NS_ERR_UNSUPPORTED, "3D: the explicit predictor is not built");
   if (!c->in_step) return fail(c, NS_ERR_STATE, "explicit predictor before ns_step_begin");
+  if (c->P.dim == 3) return explicit_predictor3d(c, norm);
   const int in = c->cur;
   const int outb = pick_out(c->base, in);
   StageArgs a = base_stage_args(c);
