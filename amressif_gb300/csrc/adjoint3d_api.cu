@@ -624,6 +624,10 @@ int adjoint_fwd3(ns_ctx* c, const ns_adjoint_opts* opts, double* J, ns_adjoint_s
   int r = need3(c);
   if (r == NS_OK) r = ensure3(c);
   if (r != NS_OK) return r;
+  // the adjoint differentiates the step with cont2cart's cell velocity (its
+  // replays from the snapshots use it too): an analytic first-stage override
+  // from ns_init_fields is not applied
+  c->cart_pending = false;
   State3D& S = *c->s3;
   Adj3& A = *S.adj;
   CK(cudaStreamSynchronize(c->st), "stream sync");
@@ -738,6 +742,7 @@ static int prepare3(ns_ctx* c) {
   int r = need3(c);
   if (r == NS_OK) r = ensure3(c);
   if (r != NS_OK) return r;
+  c->cart_pending = false;  // as in adjoint_fwd3
   Adj3& A = *c->s3->adj;
   if (A.opts.lin_max_iters == 0) ns_adjoint_opts_default(&A.opts);
   A.have_fwd = false;

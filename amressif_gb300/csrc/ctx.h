@@ -161,6 +161,7 @@ int step_begin3d(ns_ctx* c);
 int rk_stage3d(ns_ctx* c, int sub);
 int pseudo_norm3d(ns_ctx* c, double* norm);
 int explicit_predictor3d(ns_ctx* c, double* norm);
+int ensure_cart3(ns_ctx* c);  // the cell arrays of NS_FIELD_CART
 int poisson_rhs3d(ns_ctx* c, double* divmax, double* sum);
 int poisson_solve3d(ns_ctx* c, int precision, int* cycles, double* res);
 int project3d(ns_ctx* c, double* divmax);

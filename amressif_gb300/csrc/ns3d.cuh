@@ -38,6 +38,7 @@ struct Arg3 {
   double* ph[3];         // ghosted cell velocity, (N+4)^3
   double* fl[3][3];      // face fluxes: fl[d][m] at the faces along d, component m
   double* t[3];          // cell totals
+  const double* cart[3];  // first stage after ns_init_fields(TGV): the analytic cell velocity (cells), else null
   double rk;
   int do_norm;
   double* part;
@@ -67,7 +68,9 @@ __device__ __forceinline__ double face_avg(const double* u, const Geom& g, int m
 }
 
 // ghosted cell velocity; only cells with at most one index outside [0, N)
-// are ever read by the stencils
+// are ever read by the stencils. The first stage after ns_init_fields(TGV)
+// takes the analytic cell velocity of hybrid_grid_init (fn_init.cpp:160-229)
+// in place of the face average, with the same ghost rules
 __global__ void __launch_bounds__(256) k3_cart(Arg3 A) {
   const Geom& g = A.g;
   const int N = g.N;
@@ -77,20 +80,24 @@ __global__ void __launch_bounds__(256) k3_cart(Arg3 A) {
   int out_d = -1, nout = 0;
   for (int d = 0; d < 3; ++d)
     if (c[d] < 0 || c[d] >= N) { out_d = d; ++nout; }
+  // the cell value: cont2cart's face average, or the analytic override
+  auto cell = [&](int m, int a, int b, int cc) {
+    return A.cart[0] != nullptr ? A.cart[m][id3(g, a, b, cc)] : face_avg(A.u[m], g, m, a, b, cc);
+  };
   for (int m = 0; m < 3; ++m) {
     double val = 0.0;
     if (nout == 0) {
-      val = face_avg(A.u[m], g, m, i, j, k);
+      val = cell(m, i, j, k);
     } else if (nout == 1) {
       const int d = out_d;
       int cm[3] = {i, j, k};
       const int side = c[d] < 0 ? 0 : 1;
       if (g.periodic[d]) {
         cm[d] = wrapi(c[d], N);
-        val = face_avg(A.u[m], g, m, cm[0], cm[1], cm[2]);
+        val = cell(m, cm[0], cm[1], cm[2]);
       } else {
         cm[d] = c[d] < 0 ? -c[d] - 1 : 2 * N - 1 - c[d];
-        const double q = face_avg(A.u[m], g, m, cm[0], cm[1], cm[2]);
+        const double q = cell(m, cm[0], cm[1], cm[2]);
         val = cart_ghost(g.bc[2 * d + side], m, q);
       }
     }

@@ -346,6 +346,7 @@ int set_state3d(ns_ctx* c, const double* const* u, const double* const* up, cons
   CK(cudaMemsetAsync(S.PHI, 0, S.fb, c->st), "memset phi");
   c->time = time;
   c->in_step = false;
+  c->cart_pending = false;
   return ns_sync(c);
 }
 
@@ -379,8 +380,19 @@ double* field_ptr3d(ns_ctx* c, int field, int comp, bool* is_face) {
     case NS_FIELD_PRESSURE: return S.Pp;
     case NS_FIELD_PHI: return S.PHI;
     case NS_FIELD_POISSON_RHS: return S.F;
+    case NS_FIELD_CART: return S.CART[comp];
     default: return nullptr;
   }
+}
+
+int ensure_cart3(ns_ctx* c) {
+  State3D& S = *c->s3;
+  for (int m = 0; m < 3; ++m)
+    if (!S.CART[m]) {
+      const int r = alloc3(c, &S.CART[m], S.fb);
+      if (r != NS_OK) return r;
+    }
+  return NS_OK;
 }
 
 int poisson3d(ns_ctx* c, int* cycles, double* res) {
@@ -580,9 +592,12 @@ int rk_stage3d(ns_ctx* c, int sub) {
   b.rk = c->rk[sub];
   b.do_norm = (sub == 3);
   b.red_out = c->red + kRedNorm;
+  const bool use_cart = c->cart_pending;
+  for (int m = 0; m < 3; ++m) b.cart[m] = use_cart ? S.CART[m] : nullptr;
   LAUNCH(NS_PROF_STAGE_FAST, "cart 3d", launch3_cart(b, c->st));
   LAUNCH(NS_PROF_STAGE_FAST, "total 3d", launch3_total(b, c->st));
   LAUNCH(NS_PROF_STAGE_FAST, "face 3d", launch3_face(b, c->st));
+  c->cart_pending = false;
   S.cur = outb;
   if (sub == 3) c->norm_ready = true;
   return NS_OK;
@@ -609,9 +624,11 @@ int explicit_predictor3d(ns_ctx* c, double* norm) {
   b.rk = c->dt / 1.5;
   b.do_norm = 1;
   b.red_out = c->red + kRedNorm;
+  for (int m = 0; m < 3; ++m) b.cart[m] = c->cart_pending ? S.CART[m] : nullptr;
   LAUNCH(NS_PROF_EXPLICIT, "cart 3d", launch3_cart(b, c->st));
   LAUNCH(NS_PROF_EXPLICIT, "total 3d", launch3_total(b, c->st));
   LAUNCH(NS_PROF_EXPLICIT, "explicit face 3d", launch3_face(b, c->st));
+  c->cart_pending = false;
   S.cur = outb;
   int r = sync_red(c, kRedNorm, 1);
   if (r != NS_OK) return r;
@@ -703,7 +720,10 @@ int predictor3d(ns_ctx* c, ns_step_stats* sp) {
       count = 1;
       break;
     }
-    if (mixed) {
+    if (mixed && !c->cart_pending) {
+      // the analytic first-stage cell velocity of ns_init_fields(TGV) is only
+      // consumed by the FP64 stages, so that iteration runs in FP64 (the next
+      // one starts its exact anchor from the FP64 base)
       r = mixed_iteration3(c);
       if (r != NS_OK) return r;
       r = sync_red(c, kRedNorm, 1);

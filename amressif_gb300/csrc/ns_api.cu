@@ -518,13 +518,16 @@ static int box_copy(ns_ctx* c, int field, int comp, double* data, const int lo[3
   const int D = c->P.dim;
   if (comp < 0 || comp >= D) return fail(c, NS_ERR_ARG, "box copy: component out of range");
   if (field == NS_FIELD_CART) {
-    if (D == 3) return fail(c, NS_ERR_UNSUPPORTED, "3D: no cell-velocity override (the first stage rebuilds it)");
     if (!put) return NS_ERR_ARG;
-    for (int m = 0; m < 2; ++m)
+    for (int m = 0; m < 2 && D == 2; ++m)
       if (!c->CART[m]) {
         int r = alloc_field(c, &c->CART[m]);
         if (r != NS_OK) return r;
       }
+    if (D == 3) {
+      const int r = ensure_cart3(c);
+      if (r != NS_OK) return r;
+    }
     c->cart_pending = true;
   }
   bool face = false;
@@ -624,13 +627,53 @@ int ns_get_state(ns_ctx* c, double* const* u, double* const* u_prev, double* p, 
 int ns_init_fields(ns_ctx* c, int init_case) {
   if (!c || (init_case != NS_INIT_CAVITY && init_case != NS_INIT_TGV)) return NS_ERR_ARG;
   if (c->P.dim == 3) {
-    // from rest; other 3D initial fields go through ns_set_state
-    if (init_case != NS_INIT_CAVITY) return fail(c, NS_ERR_UNSUPPORTED, "3D: set the initial field with ns_set_state");
-    const size_t N = c->N, nf = (N + 1) * N * N;
-    std::vector<double> z(nf, 0.0), zc(N * N * N, 0.0);
-    const double* u3[3] = {z.data(), z.data(), z.data()};
-    const int r = ns_set_state(c, u3, u3, zc.data(), 0.0);
-    if (r == NS_OK) c->step = 0;
+    // hybrid_grid_init of the AMREX_SPACEDIM = 3 build (fn_init.cpp:61-229,
+    // kn_init.H:8-37): the cavity from rest, or the Taylor-Green case that
+    // the source edit selects. Its z factors are commented out, so it is the
+    // 2D vortex in every z plane: u = sin x cos y, v = -cos x sin y, w = 0,
+    // u^{n-1} decayed by exp(-2 nu (t - dt)) with nu = 1 (1/Re with
+    // fix_quirks), p = (cos 2x + cos 2y) / 4, and the cell velocity set
+    // analytically (w = 0) for the first stage.
+    const size_t N = c->N, nf = (N + 1) * N * N, nc = N * N * N;
+    const double* lo = c->P.prob_lo;
+    const double dx = c->g.dx[0], dy = c->g.dx[1], dt = c->dt, t0 = 0.0;
+    const double nu_decay = c->P.fix_quirks ? 1.0 / c->P.ren : 1.0;
+    const bool tgv = init_case == NS_INIT_TGV;
+    const double decay = std::exp(-2.0 * nu_decay * (t0 - dt));
+    std::vector<double> u(nf, 0.0), v(nf, 0.0), w(nf, 0.0), up(nf, 0.0), vp(nf, 0.0);
+    std::vector<double> p(nc, 0.0), cu(nc, 0.0), cv(nc, 0.0), cw(nc, 0.0);
+    for (size_t k = 0; k < N && tgv; ++k) {
+      for (size_t j = 0; j < N; ++j)
+        for (size_t i = 0; i <= N; ++i) {  // x faces (i, j + 1/2)
+          const double x = lo[0] + (i + 0.0) * dx, y = lo[1] + (j + 0.5) * dy;
+          u[(k * N + j) * (N + 1) + i] = std::sin(x) * std::cos(y);
+          up[(k * N + j) * (N + 1) + i] = std::sin(x) * std::cos(y) * decay;
+        }
+      for (size_t j = 0; j <= N; ++j)
+        for (size_t i = 0; i < N; ++i) {  // y faces (i + 1/2, j)
+          const double x = lo[0] + (i + 0.5) * dx, y = lo[1] + (j + 0.0) * dy;
+          v[(k * (N + 1) + j) * N + i] = -std::cos(x) * std::sin(y);
+          vp[(k * (N + 1) + j) * N + i] = -std::cos(x) * std::sin(y) * decay;
+        }
+      for (size_t j = 0; j < N; ++j)
+        for (size_t i = 0; i < N; ++i) {
+          const double x = lo[0] + (i + 0.5) * dx, y = lo[1] + (j + 0.5) * dy;
+          const size_t id = (k * N + j) * N + i;
+          cu[id] = std::sin(x) * std::cos(y);
+          cv[id] = -std::cos(x) * std::sin(y);
+          p[id] = 0.25 * (std::cos(2.0 * x) + std::cos(2.0 * y));
+        }
+    }
+    const double* u3[3] = {u.data(), v.data(), w.data()};
+    const double* up3[3] = {up.data(), vp.data(), w.data()};
+    int r = ns_set_state(c, u3, up3, p.data(), 0.0);
+    if (r != NS_OK) return r;
+    c->step = 0;
+    if (!tgv) return NS_OK;
+    const int l0[3] = {0, 0, 0}, h0[3] = {(int)N - 1, (int)N - 1, (int)N - 1};
+    const double* cc[3] = {cu.data(), cv.data(), cw.data()};
+    for (int m = 0; m < 3 && r == NS_OK; ++m)
+      r = ns_put_box(c, NS_FIELD_CART, m, cc[m], l0, h0, (long long)N, (long long)(N * N), 0);
     return r;
   }
   // hybrid_grid_init (fn_init.cpp:61-229, kn_init.H:8-37), evaluated on the

@@ -22,6 +22,7 @@ struct State3D {
   double* PHI = nullptr;
   double* F = nullptr;
   double* PH[3] = {nullptr, nullptr, nullptr};  // ghosted cell velocity
+  double* CART[3] = {nullptr, nullptr, nullptr};  // analytic first-stage cell velocity (allocated on first use)
   double* T[3] = {nullptr, nullptr, nullptr};   // cell totals
   double* FL[3][3] = {};                         // face fluxes
   double* part = nullptr;

@@ -145,7 +145,11 @@ const char* ns_last_error(const ns_ctx* c);
 double ns_get_dt(const ns_ctx* c);
 double ns_get_time(const ns_ctx* c);
 
-/* hybrid_grid_init (fn_init.cpp:30-631) for init_case NS_INIT_*. */
+/* hybrid_grid_init (fn_init.cpp:30-631) for init_case NS_INIT_*. In 3D the
+ * Taylor-Green case is the reference's 2D vortex in every z plane (its z
+ * factors are commented out): w = 0, and w = 0 in the analytic cell velocity.
+ * Both dimensions give the first stage the analytic cell velocity, as the
+ * reference does; the adjoint replaces it by cont2cart's. */
 int ns_init_fields(ns_ctx* c, int init_case);
 
 /* Move one box of a field between the caller and the device
@@ -159,7 +163,8 @@ int ns_init_fields(ns_ctx* c, int init_case);
  * kstride below jstride times the box height; a 2D context takes only the
  * plane lo[2] = hi[2] = 0 (kstride unused). where_device = 1 if data is
  * device memory. ns_put_box from host memory and ns_get_box wait for the
- * stream before they return. NS_FIELD_CART is 2D only. */
+ * stream before they return. NS_FIELD_CART (put only) is the cell velocity of
+ * the next FP64 stage in place of cont2cart's; ns_set_state clears it. */
 int ns_put_box(ns_ctx* c, int field, int comp, const double* data, const int lo[3], const int hi[3],
                long long jstride, long long kstride, int where_device);
 int ns_get_box(ns_ctx* c, int field, int comp, double* data, const int lo[3], const int hi[3],

@@ -265,3 +265,81 @@ def test_3d_explicit_predictor_building_block(gpu_lib, oracle_lib):
         assert rel(s.get_field(ns.FIELD_VEL_STAR, d), o.field(FIELD_STAR, d)) <= 1e-13
     assert abs(eg - eo) <= 1e-9 * eo, (eg, eo)
     o.close()
+
+
+TGV3_INIT = {
+    # the reference's Taylor-Green init in the 3D build: the 2D vortex in every z plane
+    "tgv16_init_parity": (16, dict(ren=100.0, prob_hi=(L2PI,) * 3, bc_lo=(111,) * 3, bc_hi=(111,) * 3)),
+    "tgv16_init_fixed": (16, dict(ren=100.0, prob_hi=(L2PI,) * 3, bc_lo=(111,) * 3, bc_hi=(111,) * 3, fix_quirks=1)),
+}
+
+
+@pytest.mark.parametrize("name", sorted(TGV3_INIT))
+def test_3d_tgv_init_first_stage_and_steps(gpu_lib, oracle_lib, name):
+    """ns_init_fields(NS_INIT_TGV) on a 3D context against the oracle's
+    hybrid_grid_init (fn_init.cpp:61-229): the same initial state, the first
+    stage on the analytic cell velocity (w = 0) within 1e-13, and three
+    free-running FP64 steps within 1e-10 with the same pseudo-iteration
+    counts."""
+    from oracle.orc import FIELD_STAR, Oracle
+
+    n, kw = TGV3_INIT[name]
+    dt = dt_of(n, kw)
+    mk_o = lambda: Oracle(n, dim=3, dt=dt, iter_num=100, poisson_tol=1e-13, max_grid_size=(n, n, n), **kw)
+    mk_s = lambda: ns.Solver(ns.default_params(dim=3, n_cell=n, fixed_dt=dt, iter_num=100, precision=ns.PREC_FP64,
+                                               poisson_tol_rel=1e-12, max_grid_size=(n, n, n), **kw))
+    o, s = mk_o(), mk_s()
+    o.init(1)
+    s.init(ns.INIT_TGV)
+    ug, upg, pg, _ = s.get_state()
+    uo, upo, po, _ = o.get_state()
+    for d in range(3):
+        np.testing.assert_array_equal(ug[d], uo[d])
+        np.testing.assert_array_equal(upg[d], upo[d])
+    np.testing.assert_array_equal(pg, po)
+    o.step_begin()
+    s.step_begin()
+    o.rk_stage(0)
+    s.rk_stage(0)
+    for d in range(3):
+        assert rel(s.get_field(ns.FIELD_VEL_STAR, d), o.field(FIELD_STAR, d)) <= 1e-13 if d < 2 else \
+            np.abs(s.get_field(ns.FIELD_VEL_STAR, d)).max() <= 1e-14
+    o.close()
+    s.close()
+    o, s = mk_o(), mk_s()
+    o.init(1)
+    s.init(ns.INIT_TGV)
+    for step in range(3):
+        so = o.step()
+        sg = s.step()
+        assert sg["pseudo_iters"] == so["pseudo_iters"], (step, sg["pseudo_iters"], so["pseudo_iters"])
+        ug, _, pg, _ = s.get_state()
+        uo, _, po, _ = o.get_state()
+        ru = math.sqrt(sum(np.linalg.norm(ug[d] - uo[d]) ** 2 for d in range(3)) /
+                       sum(np.linalg.norm(uo[d]) ** 2 for d in range(3)))
+        assert ru <= 1e-10, (step, ru)
+        assert relp(pg, po) <= 1e-10, (step, relp(pg, po))
+    o.close()
+
+
+def test_3d_tgv_init_mixed_matches_fp64(gpu_lib):
+    """The mixed predictor after ns_init_fields(NS_INIT_TGV): its first
+    pseudo-iteration runs in FP64 on the analytic cell velocity, the rest in
+    mixed precision; three steps against the FP64 solver (same
+    pseudo-iteration counts, u and p within 1e-11)."""
+    n, kw = TGV3_INIT["tgv16_init_fixed"]
+    dt = dt_of(n, kw)
+    out = []
+    for prec in (ns.PREC_FP64, ns.PREC_MIXED):
+        s = ns.Solver(ns.default_params(dim=3, n_cell=n, fixed_dt=dt, iter_num=100, precision=prec,
+                                        poisson_tol_rel=1e-12, max_grid_size=(n, n, n), **kw))
+        s.init(ns.INIT_TGV)
+        ks = [s.step()["pseudo_iters"] for _ in range(3)]
+        u, _, p, _ = s.get_state()
+        out.append((ks, u, p))
+        s.close()
+    assert out[0][0] == out[1][0]
+    ru = math.sqrt(sum(np.linalg.norm(out[1][1][d] - out[0][1][d]) ** 2 for d in range(3)) /
+                   sum(np.linalg.norm(out[0][1][d]) ** 2 for d in range(3)))
+    assert ru <= 1e-11, ru
+    assert relp(out[1][2], out[0][2]) <= 1e-11

@@ -144,7 +144,7 @@ def test_box_arguments_are_validated(gpu_lib):
         (s2, 99, 0, (0, 0, 0), (8, 8, 0), 40, 0, ns.NS_ERR_ARG),               # unknown field
         (s3, ns.FIELD_VEL, 2, (0, 0, 0), (7, 7, 8), 8, 60, ns.NS_ERR_ARG),     # kstride below a plane (8 x 8)
         (s3, ns.FIELD_VEL, 2, (0, 0, 0), (7, 7, 17), 8, 64, ns.NS_ERR_ARG),    # z face box beyond face 16
-        (s3, ns.FIELD_CART, 0, (0, 0, 0), (7, 7, 7), 8, 64, ns.NS_ERR_UNSUPPORTED),
+        (s3, ns.FIELD_CART, 0, (0, 0, 0), (7, 7, 7), 8, 64, ns.NS_ERR_ARG),    # the cell-velocity override is put only
         (s3, ns.FIELD_VEL, 2, (0, 0, 0), (7, 7, 16), 8, 64, ns.NS_OK),         # the whole z extent of a box
         (s2, ns.FIELD_VEL, 1, (0, 0, 0), (31, 32, 0), 32, 0, ns.NS_OK),        # the whole v field
     ]
