@@ -162,6 +162,13 @@ int rk_stage3d(ns_ctx* c, int sub);
 int pseudo_norm3d(ns_ctx* c, double* norm);
 int explicit_predictor3d(ns_ctx* c, double* norm);
 int ensure_cart3(ns_ctx* c);  // the cell arrays of NS_FIELD_CART
+// the GMRES option of the Poisson solve (ns_api.cu), 2D and 3D: L phi = f - mean f
+int poisson_gmres(ns_ctx* c, double tol_rel, double div_tol_res, int maxc, int* cycles, double* rnorm0, double* rn);
+// its 3D parts (ns3d_api.cu): phi, f and the level-0 1/h^2; one FP64 V-cycle
+// from zero as the preconditioner; the max-norm residual into red[kRedRes]
+void gm3_fields(ns_ctx* c, double** phi, const double** f, double ih[3]);
+int gm3_precond(ns_ctx* c, const double* in, double* out);
+int gm3_resnorm(ns_ctx* c);
 int poisson_rhs3d(ns_ctx* c, double* divmax, double* sum);
 int poisson_solve3d(ns_ctx* c, int precision, int* cycles, double* res);
 int project3d(ns_ctx* c, double* divmax);

@@ -94,25 +94,32 @@ cudaError_t launch_gm_lap(int n, long P, int px, int py, double ihx, double ihy,
   return cudaGetLastError();
 }
 
-cudaError_t launch_gm_axpby(int n, long P, double a, const double* x, double b, const double* y, const double* sc, double c,
-                            double* out, cudaStream_t s) {
-  const dim3 grid((n + 31) / 32, (n + 7) / 8, 1);
-  k_gm_axpby<<<grid, 256, 0, s>>>(n, P, a, x, b, y, sc, c, out);
+cudaError_t launch_gm_lap3(const GmGrid& G, int px, int py, int pz, double ihx, double ihy, double ihz, const double* x,
+                           double* y, cudaStream_t s) {
+  const dim3 grid((G.n + 31) / 32, (G.n + 7) / 8, G.nz);
+  k_gm_lap3<<<grid, 256, 0, s>>>(G, px, py, pz, ihx, ihy, ihz, x, y);
   return cudaGetLastError();
 }
 
-cudaError_t launch_gm_mdot(int n, long P, int nv, const GmVecs& V, const double* w, double* part, unsigned* counter,
+cudaError_t launch_gm_axpby(const GmGrid& G, double a, const double* x, double b, const double* y, const double* sc,
+                            double c, double* out, cudaStream_t s) {
+  const dim3 grid((G.n + 31) / 32, (G.n + 7) / 8, G.nz);
+  k_gm_axpby<<<grid, 256, 0, s>>>(G, a, x, b, y, sc, c, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gm_mdot(const GmGrid& G, int nv, const GmVecs& V, const double* w, double* part, unsigned* counter,
                            double* out, cudaStream_t s) {
   if (nv < 1 || nv > kGmMaxV) return cudaErrorInvalidValue;
-  k_gm_mdot<256><<<kGmBlocks, 256, 0, s>>>(n, P, nv, V, w, part, counter, out);
+  k_gm_mdot<256><<<kGmBlocks, 256, 0, s>>>(G, nv, V, w, part, counter, out);
   return cudaGetLastError();
 }
 
-cudaError_t launch_gm_maxpy(int n, long P, int nv, const GmVecs& V, const double* coef, double s_, double* w,
+cudaError_t launch_gm_maxpy(const GmGrid& G, int nv, const GmVecs& V, const double* coef, double s_, double* w,
                             cudaStream_t s) {
   if (nv < 1 || nv > kGmMaxV) return cudaErrorInvalidValue;
-  const dim3 grid((n + 31) / 32, (n + 7) / 8, 1);
-  k_gm_maxpy<<<grid, 256, 0, s>>>(n, P, nv, V, coef, s_, w);
+  const dim3 grid((G.n + 31) / 32, (G.n + 7) / 8, G.nz);
+  k_gm_maxpy<<<grid, 256, 0, s>>>(G, nv, V, coef, s_, w);
   return cudaGetLastError();
 }
 

@@ -74,12 +74,15 @@ cudaError_t launch_lid_accum(int N, int nseg, const double* col, double coef, do
 
 // kernels_fast.cu: GMRES option of the Poisson solve
 struct GmVecs;
+struct GmGrid;
 cudaError_t launch_gm_lap(int n, long P, int px, int py, double ihx, double ihy, const double* x, double* y, cudaStream_t s);
-cudaError_t launch_gm_axpby(int n, long P, double a, const double* x, double b, const double* y, const double* sc, double c,
-                            double* out, cudaStream_t s);
-cudaError_t launch_gm_mdot(int n, long P, int nv, const GmVecs& V, const double* w, double* part, unsigned* counter,
+cudaError_t launch_gm_lap3(const GmGrid& G, int px, int py, int pz, double ihx, double ihy, double ihz, const double* x,
+                           double* y, cudaStream_t s);
+cudaError_t launch_gm_axpby(const GmGrid& G, double a, const double* x, double b, const double* y, const double* sc,
+                            double c, double* out, cudaStream_t s);
+cudaError_t launch_gm_mdot(const GmGrid& G, int nv, const GmVecs& V, const double* w, double* part, unsigned* counter,
                            double* out, cudaStream_t s);
-cudaError_t launch_gm_maxpy(int n, long P, int nv, const GmVecs& V, const double* coef, double s_, double* w,
+cudaError_t launch_gm_maxpy(const GmGrid& G, int nv, const GmVecs& V, const double* coef, double s_, double* w,
                             cudaStream_t s);
 
 struct DCArgs {

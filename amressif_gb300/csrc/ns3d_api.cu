@@ -196,6 +196,18 @@ int poisson3(ns_ctx* c, bool mixed, int* cycles, double* res, long long* fallbac
   CK(cudaMemsetAsync(S.PHI, 0, S.fb, c->st), "memset phi");
   const int maxc = std::max(1, c->P.poisson_max_cycles);
   const double div_tol_res = c->P.poisson_tol_div > 0 ? c->P.poisson_tol_div * 1.5 / c->dt : 0.0;
+  if (c->P.poisson_solver == 1) {
+    // restarted GMRES with one FP64 V-cycle as right preconditioner
+    // (GMRES_Poisson.cpp:56-131), in every precision mode as in 2D
+    double g0 = 0.0, gn = 0.0;
+    int its = 0;
+    const int st = poisson_gmres(c, c->P.poisson_tol_rel, div_tol_res, maxc, &its, &g0, &gn);
+    if (st != NS_OK && st != NS_ERR_MG_STALL) return st;
+    *cycles = its;
+    *res = g0 > 0 ? gn / g0 : 0.0;
+    if (st != NS_OK) c->err = "GMRES residual did not reach the tolerance";
+    return st;
+  }
   // mixed: phi as float-float pairs in PHF[pf]; each sweep adds the FP32
   // correction and recomputes the residual (k3_dcff), phi goes to FP64 at the end
   DCff3 dc;
@@ -398,6 +410,39 @@ int ensure_cart3(ns_ctx* c) {
 int poisson3d(ns_ctx* c, int* cycles, double* res) {
   long long fb = 0;
   return poisson3(c, c->P.precision == NS_PREC_MIXED, cycles, res, &fb);
+}
+
+void gm3_fields(ns_ctx* c, double** phi, const double** f, double ih[3]) {
+  State3D& S = *c->s3;
+  *phi = S.PHI;
+  *f = S.F;
+  for (int d = 0; d < 3; ++d) ih[d] = S.M64.ih[0][d];
+}
+
+int gm3_precond(ns_ctx* c, const double* in, double* out) {
+  State3D& S = *c->s3;
+  MG3<double>& M = S.M64;
+  double* x0 = M.x[0];
+  double* f0 = M.f[0];
+  const double* fm = M.fmean;
+  CK(cudaMemsetAsync(out, 0, S.fb, c->st), "memset");
+  M.x[0] = out;
+  M.f[0] = const_cast<double*>(in);
+  M.fmean = nullptr;
+  const int r = vcycle3<double>(c, M);
+  M.x[0] = x0;
+  M.f[0] = f0;
+  M.fmean = fm;
+  return r;
+}
+
+int gm3_resnorm(ns_ctx* c) {
+  State3D& S = *c->s3;
+  S.M64.x[0] = S.PHI;
+  S.M64.f[0] = S.F;
+  S.M64.fmean = c->red + kRedMean;
+  LAUNCH(NS_PROF_MG_RESNORM, "resnorm", launch3_mg_resnorm<double>(S.M64, S.part, c->counter, c->red + kRedRes, c->st));
+  return NS_OK;
 }
 
 }  // namespace nsh

@@ -963,12 +963,22 @@ static int gmres_precond(ns_ctx* c, const double* in, double* out) {
   return r;
 }
 
+// the cells of the context's fields for the GMRES vector kernels
+static GmGrid gm_grid(const ns_ctx* c) {
+  GmGrid G;
+  G.n = c->N;
+  G.P = c->pitch;
+  G.nz = c->P.dim == 3 ? c->N : 1;
+  G.PL = (long)c->pitch * (c->N + 1);
+  return G;
+}
+
 // out[k] = (w, V[k]) for k < nv, read back to c->gm_host
 static int gmres_dots(ns_ctx* c, const std::vector<double*>& V, int nv, const double* w) {
   GmVecs vv;
   std::memset(&vv, 0, sizeof(vv));
   for (int k = 0; k < nv; ++k) vv.v[k] = V[k];
-  LAUNCH(NS_PROF_OTHER, "gmres dots", launch_gm_mdot(c->N, c->pitch, nv, vv, w, c->gm_part, c->counter, c->gm_dev, c->st));
+  LAUNCH(NS_PROF_OTHER, "gmres dots", launch_gm_mdot(gm_grid(c), nv, vv, w, c->gm_part, c->counter, c->gm_dev, c->st));
   CK(cudaMemcpyAsync(c->gm_host, c->gm_dev, nv * sizeof(double), cudaMemcpyDeviceToHost, c->st), "readback");
   CK(cudaStreamSynchronize(c->st), "stream sync");
   return NS_OK;
@@ -980,30 +990,56 @@ static int gmres_update(ns_ctx* c, const std::vector<double*>& V, int nv, const 
   std::memset(&vv, 0, sizeof(vv));
   for (int k = 0; k < nv; ++k) vv.v[k] = V[k];
   CK(cudaMemcpyAsync(c->gm_dev + kGmMaxV, coef, nv * sizeof(double), cudaMemcpyHostToDevice, c->st), "coefficients");
-  LAUNCH(NS_PROF_OTHER, "gmres update", launch_gm_maxpy(c->N, c->pitch, nv, vv, c->gm_dev + kGmMaxV, s, w, c->st));
+  LAUNCH(NS_PROF_OTHER, "gmres update", launch_gm_maxpy(gm_grid(c), nv, vv, c->gm_dev + kGmMaxV, s, w, c->st));
   // the next host write of the coefficients must wait for this kernel
   CK(cudaStreamSynchronize(c->st), "stream sync");
   return NS_OK;
 }
 
-static int poisson_gmres(ns_ctx* c, double tol_rel, double div_tol_res, int maxc, int* cycles, double* rnorm0_out,
-                         double* rn_out) {
+// Restarted GMRES(m) with one FP64 V-cycle as right preconditioner on
+// L phi = f - mean f from phi = 0, stopped on the multigrid's max-norm test.
+// 2D and 3D: the operator, the preconditioner and the residual test are the
+// context's own; the Krylov vectors are whole fields.
+int nsh::poisson_gmres(ns_ctx* c, double tol_rel, double div_tol_res, int maxc, int* cycles, double* rnorm0_out,
+                       double* rn_out) {
   const int m = std::max(2, std::min(c->P.gmres_restart, kGmMaxV - 1));
   int r = gmres_alloc(c, m);
   if (r != NS_OK) return r;
+  const bool d3 = c->P.dim == 3;
+  const GmGrid G = gm_grid(c);
   const int N = c->N;
   const long P = c->pitch;
-  const int px = c->g.periodic[0], py = c->g.periodic[1];
-  const double ihx = c->M64.invh2[0][0], ihy = c->M64.invh2[0][1];
-  std::vector<double*>& V = c->gm_v;
+  const int px = c->g.periodic[0], py = c->g.periodic[1], pz = c->g.periodic[2];
+  double ih[3] = {c->M64.invh2[0][0], c->M64.invh2[0][1], 0.0};
   double* x = c->PHI[0];
-  c->phi_cur = 0;
-  c->M64.x[0] = c->PHI[0];
+  const double* F = c->F;
+  if (d3) {
+    gm3_fields(c, &x, &F, ih);
+  } else {
+    c->phi_cur = 0;
+    c->M64.x[0] = c->PHI[0];
+  }
+  std::vector<double*>& V = c->gm_v;
+  auto apply = [&](const double* in, double* out) -> int {
+    if (d3) LAUNCH(NS_PROF_OTHER, "gmres apply", launch_gm_lap3(G, px, py, pz, ih[0], ih[1], ih[2], in, out, c->st));
+    else LAUNCH(NS_PROF_OTHER, "gmres apply", launch_gm_lap(N, P, px, py, ih[0], ih[1], in, out, c->st));
+    return NS_OK;
+  };
+  auto precond = [&](const double* in, double* out) -> int {
+    return d3 ? gm3_precond(c, in, out) : gmres_precond(c, in, out);
+  };
+  auto resnorm = [&]() -> int {
+    if (d3) r = gm3_resnorm(c);
+    else {
+      LAUNCH(NS_PROF_MG_RESNORM, "resnorm", launch_mg_resnorm<double>(c->M64, c->part, c->counter, c->red + kRedRes, c->st));
+      r = NS_OK;
+    }
+    return r != NS_OK ? r : sync_red(c, kRedRes, 1);
+  };
   // b = f - mean(f); x = 0 (poisson.cpp:63)
-  LAUNCH(NS_PROF_OTHER, "gmres rhs", launch_gm_axpby(N, P, 1.0, c->F, 0.0, nullptr, c->red + kRedMean, -1.0, c->gm_b, c->st));
+  LAUNCH(NS_PROF_OTHER, "gmres rhs", launch_gm_axpby(G, 1.0, F, 0.0, nullptr, c->red + kRedMean, -1.0, c->gm_b, c->st));
   CK(cudaMemsetAsync(x, 0, c->fbytes, c->st), "memset phi");
-  LAUNCH(NS_PROF_MG_RESNORM, "resnorm", launch_mg_resnorm<double>(c->M64, c->part, c->counter, c->red + kRedRes, c->st));
-  r = sync_red(c, kRedRes, 1);
+  r = resnorm();
   if (r != NS_OK) return r;
   const double rnorm0 = c->red_h[kRedRes];
   double rn = rnorm0;
@@ -1015,20 +1051,21 @@ static int poisson_gmres(ns_ctx* c, double tol_rel, double div_tol_res, int maxc
   auto h = [&](int i, int j) -> double& { return H[(size_t)i * m + j]; };
   while (!done(rn) && rnorm0 > 0 && its < maxc) {
     // r0 = b - L x into V[0]; beta = |r0|
-    LAUNCH(NS_PROF_OTHER, "gmres apply", launch_gm_lap(N, P, px, py, ihx, ihy, x, c->gm_w, c->st));
-    LAUNCH(NS_PROF_OTHER, "gmres r0", launch_gm_axpby(N, P, 1.0, c->gm_b, -1.0, c->gm_w, nullptr, 0.0, V[0], c->st));
+    r = apply(x, c->gm_w);
+    if (r != NS_OK) return r;
+    LAUNCH(NS_PROF_OTHER, "gmres r0", launch_gm_axpby(G, 1.0, c->gm_b, -1.0, c->gm_w, nullptr, 0.0, V[0], c->st));
     r = gmres_dots(c, V, 1, V[0]);
     if (r != NS_OK) return r;
     const double beta = std::sqrt(c->gm_host[0]);
     if (!(beta > 0)) break;
-    LAUNCH(NS_PROF_OTHER, "gmres scale", launch_gm_axpby(N, P, 1.0 / beta, V[0], 0.0, nullptr, nullptr, 0.0, V[0], c->st));
+    LAUNCH(NS_PROF_OTHER, "gmres scale", launch_gm_axpby(G, 1.0 / beta, V[0], 0.0, nullptr, nullptr, 0.0, V[0], c->st));
     std::fill(g.begin(), g.end(), 0.0);
     g[0] = beta;
     int k = 0;
     for (int j = 0; j < m && its < maxc; ++j) {
       ++its;
-      r = gmres_precond(c, V[j], c->gm_z);
-      if (r == NS_OK) LAUNCH(NS_PROF_OTHER, "gmres apply", launch_gm_lap(N, P, px, py, ihx, ihy, c->gm_z, c->gm_w, c->st));
+      r = precond(V[j], c->gm_z);
+      if (r == NS_OK) r = apply(c->gm_z, c->gm_w);
       if (r != NS_OK) return r;
       for (int i = 0; i <= j; ++i) h(i, j) = 0.0;
       for (int pass = 0; pass < 2; ++pass) {  // classical Gram-Schmidt, twice
@@ -1056,7 +1093,7 @@ static int poisson_gmres(ns_ctx* c, double tol_rel, double div_tol_res, int maxc
       k = j + 1;
       if (hn > 0 && j + 1 < m)
         LAUNCH(NS_PROF_OTHER, "gmres scale",
-               launch_gm_axpby(N, P, 1.0 / hn, c->gm_w, 0.0, nullptr, nullptr, 0.0, V[j + 1], c->st));
+               launch_gm_axpby(G, 1.0 / hn, c->gm_w, 0.0, nullptr, nullptr, 0.0, V[j + 1], c->st));
       // the 2-norm estimate |g[j+1]| against the max-norm target (|r|_inf <= |r|_2)
       if (std::fabs(g[j + 1]) <= 0.5 * tol || hn == 0) break;
     }
@@ -1068,12 +1105,11 @@ static int poisson_gmres(ns_ctx* c, double tol_rel, double div_tol_res, int maxc
     }
     CK(cudaMemsetAsync(c->gm_w, 0, c->fbytes, c->st), "memset");
     r = gmres_update(c, V, k, y.data(), 1.0, c->gm_w);
-    if (r == NS_OK) r = gmres_precond(c, c->gm_w, c->gm_z);
-    if (r == NS_OK) LAUNCH(NS_PROF_OTHER, "gmres x", launch_gm_axpby(N, P, 1.0, x, 1.0, c->gm_z, nullptr, 0.0, x, c->st));
+    if (r == NS_OK) r = precond(c->gm_w, c->gm_z);
+    if (r == NS_OK) LAUNCH(NS_PROF_OTHER, "gmres x", launch_gm_axpby(G, 1.0, x, 1.0, c->gm_z, nullptr, 0.0, x, c->st));
     if (r != NS_OK) return r;
     // the true max-norm residual of the multigrid test
-    LAUNCH(NS_PROF_MG_RESNORM, "resnorm", launch_mg_resnorm<double>(c->M64, c->part, c->counter, c->red + kRedRes, c->st));
-    r = sync_red(c, kRedRes, 1);
+    r = resnorm();
     if (r != NS_OK) return r;
     rn = c->red_h[kRedRes];
   }
@@ -1098,7 +1134,7 @@ int ns_poisson_solve(ns_ctx* c, int precision, int* cycles, double* res) {
   int ncyc = 0;
   int status = NS_OK;
   if (c->P.poisson_solver == 1) {
-    status = poisson_gmres(c, c->P.poisson_tol_rel, div_tol_res, maxc, &ncyc, &rnorm0, &rn);
+    status = nsh::poisson_gmres(c, c->P.poisson_tol_rel, div_tol_res, maxc, &ncyc, &rnorm0, &rn);
     if (status != NS_OK && status != NS_ERR_MG_STALL) return status;
   } else if (precision == NS_PREC_MIXED) {
     // FP32 V-cycles inside an FP64 defect correction

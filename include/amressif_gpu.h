@@ -85,7 +85,8 @@ typedef struct ns_params {
   int poisson_max_cycles;    /* V-cycle / defect-correction cap (MLMG maxiter 2000) */
   int dtau_clip;             /* 0: dtau = 0.4 dt (main.cpp:861); 1: also clip to 0.9 x RK4 stability limit */
   int poisson_solver;        /* 0: multigrid V-cycles; 1: restarted GMRES with one FP64 V-cycle as right
-                                preconditioner (the GMRES option of GMRES_Poisson.cpp:56-131) */
+                                preconditioner (the GMRES option of GMRES_Poisson.cpp:56-131), 2D and 3D,
+                                FP64 in every precision mode */
   int gmres_restart;         /* Krylov vectors per GMRES cycle (<= 31) */
   int dc_residual;           /* NS_PREC_MIXED Poisson: the defect correction's residual and phi in
                                 0 = float-float (about 48 bits; FP64 once its floor is reached),

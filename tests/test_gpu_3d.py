@@ -343,3 +343,41 @@ def test_3d_tgv_init_mixed_matches_fp64(gpu_lib):
                    sum(np.linalg.norm(out[0][1][d]) ** 2 for d in range(3)))
     assert ru <= 1e-11, ru
     assert relp(out[1][2], out[0][2]) <= 1e-11
+
+
+@pytest.mark.parametrize("name", sorted(CASES3))
+def test_3d_gmres_option_resynced(gpu_lib, oracle_lib, name):
+    """poisson_solver = 1 in the 3D build (the GMRES option of
+    GMRES_Poisson.cpp:56-131, whose operator has a 7-point branch): restarted
+    GMRES with one FP64 V-cycle as right preconditioner, per step against the
+    oracle's exact solve (u, p within 1e-10, identical pseudo-iteration
+    counts), and against the V-cycle solver on the same state."""
+    from oracle.orc import Oracle
+
+    n, kw, tgv = CASES3[name]
+    dt = dt_of(n, kw)
+    o = Oracle(n, dim=3, dt=dt, iter_num=100, poisson_tol=1e-13, max_grid_size=(n, n, n), **kw)
+    mk = lambda solver: ns.Solver(ns.default_params(dim=3, n_cell=n, fixed_dt=dt, iter_num=100, precision=ns.PREC_FP64,
+                                                    poisson_tol_rel=1e-12, max_grid_size=(n, n, n),
+                                                    poisson_solver=solver, **kw))
+    s, t = mk(1), mk(0)
+    o.set_state(*state3(n, tgv))
+    for step in range(3):
+        uo, upo, po, _ = o.get_state()
+        s.set_state(uo, upo, po)
+        t.set_state(uo, upo, po)
+        so = o.step()
+        sg = s.step()
+        st = t.step()
+        assert sg["pseudo_iters"] == so["pseudo_iters"], (step, sg["pseudo_iters"], so["pseudo_iters"])
+        assert sg["poisson_cycles"] >= 1 and sg["poisson_res"] <= 1e-12
+        ug, _, pg, _ = s.get_state()
+        ut, _, pt, _ = t.get_state()
+        uo, _, po, _ = o.get_state()
+        for d in range(3):
+            assert rel(ug[d], uo[d]) <= 1e-10, (step, d, rel(ug[d], uo[d]))
+            assert rel(ug[d], ut[d]) <= 1e-10, (step, d, rel(ug[d], ut[d]))
+        assert relp(pg, po) <= 1e-10, (step, relp(pg, po))
+        if kw.get("fix_quirks") or not tgv:
+            assert sg["div_after"] <= 1e-10
+    o.close()
