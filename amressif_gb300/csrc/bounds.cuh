@@ -1,17 +1,18 @@
 // Bounds-check build (the reference's DEBUG=TRUE build, Exec/GNUmakefile:12).
 //
 // Compiled with -DNS_BOUNDS_CHECK (libamressif_gb300_check.so), the column-
-// marching kernels test every global index they form by hand (cp.async
-// sources, direct loads of face column / row N and of the periodic images,
-// stores, the multigrid rows) against the array it addresses: 0 <= index <
-// pitch * (rows), with the column (index mod pitch) at most ncol. A failed
+// marching kernels and the 3D tiled flux pass test every global index they
+// form by hand (cp.async sources, direct loads of face column / row N and of
+// the periodic images, stores, the multigrid rows, the halo tiles and z
+// windows) against the array it addresses: 0 <= index < pitch * (rows), with
+// the column (index mod pitch) at most ncol. A failed
 // test skips the access and records it in three status words the context
 // owns (Geom::check): the number of failures, the first failing index and its
 // site number. Nothing traps. In the normal build NS_BCHK is the constant
 // true and the tests compile away.
 //
 // Sites: 1-12 k_inc_col2d, 21-32 k_anchor_col2d, 41-46 k_mg_smooth_col,
-// 51-56 k_mg_smooth, 61 k_conv_quick2d.
+// 51-56 k_mg_smooth, 61 k_conv_quick2d, 71-73 k3i_fluxtot (3D).
 #pragma once
 #include <cuda_runtime.h>
 

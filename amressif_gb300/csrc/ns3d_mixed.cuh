@@ -20,6 +20,7 @@
 // pass but that store issues an FP64 arithmetic instruction (GB300 runs FP64
 // at 1/73 of the FP32 rate).
 #pragma once
+#include "bounds.cuh"
 #include "ff.cuh"
 #include "ns3d.cuh"
 
@@ -310,8 +311,12 @@ __global__ void __launch_bounds__(256) k3i_fluxtot(Inc3 A) {
   const long G1 = 1, G2 = N + 4, G3 = (long)(N + 4) * (N + 4);
   // the column's z window: zb[m][q] / ze[m][q] = phi at plane k - 1 + q
   float zb[3][4], ze[3][4], fzb[3];
+  // bounds-check build: the ghosted arrays are (N + 4)^3, rows of N + 4; the
+  // face arrays (N + 1) planes of N + 1 rows of pitch P
+  const long GR = (long)(N + 4) * (N + 4), FR = (long)(N + 1) * (N + 1);
   auto zload = [&](int m, int kk, float& b, float& e) {
     const long gi = gid3(N, i, j, kk);
+    if (!NS_BCHK(g.check, gi, N + 4, GR, N + 3, 71)) { b = e = 0.f; return; }
     b = ldf(A.phb[m], gi);
     e = ldf(A.phe[m], gi);
   };
@@ -332,7 +337,8 @@ __global__ void __launch_bounds__(256) k3i_fluxtot(Inc3 A) {
     for (int t = threadIdx.x; t < 12 * 36; t += 256) {
       const int sx = t % 36, sy = t / 36;
       const int a = i0 - 2 + sx, b = j0 - 2 + sy;
-      const bool in = a <= N + 1 && b <= N + 1;  // the ghosted array spans -2 .. N + 1
+      const bool in = a <= N + 1 && b <= N + 1 &&  // the ghosted array spans -2 .. N + 1
+                      NS_BCHK(g.check, gid3(N, a, b, k), N + 4, GR, N + 3, 72);
       const long gi = in ? gid3(N, a, b, k) : 0;
       for (int m = 0; m < 3; ++m) {
         sm.pb[m][sy][sx] = in ? ldf(A.phb[m], gi) : 0.f;
@@ -348,6 +354,7 @@ __global__ void __launch_bounds__(256) k3i_fluxtot(Inc3 A) {
       const int a = i0 + ii, b = j0 + jj;
       if (a > N || b >= N) continue;
       const long fc = id3(g, a, b, k);
+      if (!NS_BCHK(g.check, fc, g.pitch, FR, N, 73)) continue;
       const float ub = ldf(A.ub[0], fc), e = inc_e(A, 0, fc);
       const int sx = ii + 2, sy = jj + 2;
       for (int m = 0; m < 3; ++m) {
@@ -363,6 +370,7 @@ __global__ void __launch_bounds__(256) k3i_fluxtot(Inc3 A) {
       const int a = i0 + ii, b = j0 + jj;
       if (a >= N || b > N) continue;
       const long fc = id3(g, a, b, k);
+      if (!NS_BCHK(g.check, fc, g.pitch, FR, N, 73)) continue;
       const float ub = ldf(A.ub[1], fc), e = inc_e(A, 1, fc);
       const int sx = ii + 2, sy = jj + 2;
       for (int m = 0; m < 3; ++m) {

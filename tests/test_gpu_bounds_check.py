@@ -93,3 +93,36 @@ def test_checked_build_conv_quick_variant(gpu_lib, periodic):
     assert out[0][0] == out[1][0]
     for a, b in zip(out[0][1], out[1][1]):
         assert rel(b, a) <= 1e-12
+
+
+
+@pytest.mark.parametrize("name", ["cavity40_3d", "tgv24_3d_periodic"])
+def test_checked_build_3d_mixed_predictor(gpu_lib, name):
+    """The 3D tiled flux pass of the mixed predictor (k3i_fluxtot: halo tiles
+    of 36 x 12 cells, the z window of each column, the face loads; sites
+    71-73): no failure on a 40^3 cavity (two x tiles, one partial) and a 24^3
+    periodic box, and the normal build's steps."""
+    n = 40 if name == "cavity40_3d" else 24
+    if name == "cavity40_3d":
+        kw = dict(ren=100.0, fixed_dt=0.4 / n)
+    else:
+        kw = dict(ren=1600.0, fixed_dt=0.4 * 2 * math.pi / n, fix_quirks=1, **PER)
+    out = []
+    for checked in (False, True):
+        p = ns.default_params(dim=3, n_cell=n, iter_num=100, precision=ns.PREC_MIXED, poisson_tol_rel=1e-12,
+                              max_grid_size=(n, n, n), **kw)
+        s = ns.Solver(p, checked=checked)
+        if name == "cavity40_3d":
+            s.init(ns.INIT_CAVITY)
+        else:
+            s.set_state(*wl.tgv3d_perturbed_state(n, amp=1e-3, seed=0))
+        ks = [s.step()["pseudo_iters"] for _ in range(2)]
+        if checked:
+            count, first, site = s.bounds_check()
+            assert count == 0, "out-of-range index %d at site %d (%d failures)" % (first, site, count)
+        u, _, _, _ = s.get_state()
+        out.append((ks, u))
+        s.close()
+    assert out[0][0] == out[1][0]
+    for a, b in zip(out[0][1], out[1][1]):
+        assert rel(b, a) <= 1e-12
