@@ -412,6 +412,8 @@ __global__ void __launch_bounds__(256) k3i_fluxtot(Inc3 A) {
   (void)G1;
   (void)G2;
   (void)G3;
+  (void)GR;  // read by NS_BCHK in the bounds-check build only
+  (void)FR;
 }
 
 __device__ __forceinline__ float t_along_inc(const Inc3& A, int m, int a, long base, long st) {
