@@ -94,11 +94,15 @@ def conv_quick_int(u, v, c, n, dx, dy):
     return conv0, conv1
 
 
-def stage(us, ub, un, du, p, n, dx, dy, dt, ren, rk, bc_lo, bc_hi, inflow, periodic, cart=None, conv_scheme=0):
+def stage(us, ub, un, du, p, n, dx, dy, dt, ren, rk, bc_lo, bc_hi, inflow, periodic, cart=None, conv_scheme=0,
+          explicit=False):
     """One RK pseudo-stage; returns (new u*, momentum rhs). conv_scheme: the
     convective routine (0 convective_flux_calc_new_quick, 1
     convective_flux_calc_quick, 2 convective_flux_calc, which leaves the
-    total flux without a convective term)."""
+    total flux without a convective term). explicit=True: the explicit
+    predictor instead (PSEUDO_TIMESTEPPING = 0, main.cpp:902-925,
+    momentum.cpp:96-192): no reflection of the normal flux (quirk Q3),
+    R += du / (2 dt), u* += (dt / 1.5) R."""
     g = 2
     u, v = us
     c = cart if cart is not None else cont2cart(u, v, n, bc_lo, bc_hi, inflow, periodic)
@@ -139,10 +143,11 @@ def stage(us, ub, un, du, p, n, dx, dy, dt, ren, rk, bc_lo, bc_hi, inflow, perio
         if periodic[1]:
             t[0, :] = t[n, :]
             t[n + 1, :] = t[1, :]
-    total[0][:, 0] = -total[0][:, 1]
-    total[0][:, n + 1] = -total[0][:, n]
-    total[1][0, :] = -total[1][1, :]
-    total[1][n + 1, :] = -total[1][n, :]
+    if not explicit:
+        total[0][:, 0] = -total[0][:, 1]
+        total[0][:, n + 1] = -total[0][:, n]
+        total[1][0, :] = -total[1][1, :]
+        total[1][n + 1, :] = -total[1][n, :]
     # pressure with mirrored ghosts
     pp = np.zeros((n + 2, n + 2))
     pp[1:-1, 1:-1] = p
@@ -157,6 +162,11 @@ def stage(us, ub, un, du, p, n, dx, dy, dt, ren, rk, bc_lo, bc_hi, inflow, perio
     out = []
     rhs = []
     for r, s, b, pn, d in ((rx, u, ub[0], un[0], du[0]), (ry, v, ub[1], un[1], du[1])):
+        if explicit:
+            r = r + (1.0 / (2.0 * dt)) * d
+            rhs.append(r)
+            out.append(s + ((dt / 1.5) * r))
+            continue
         r = r - (1.5 / dt) * (s - pn) + (0.5 / dt) * d
         rhs.append(r)
         out.append(b + (rk * r))

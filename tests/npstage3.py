@@ -51,10 +51,13 @@ def cont2cart3(u, n, bc_lo, bc_hi, inflow, periodic):
     return c
 
 
-def stage3(us, ub, un, du, p, n, h, dt, ren, rk, bc_lo, bc_hi, inflow, periodic, reflect_periodic=True):
+def stage3(us, ub, un, du, p, n, h, dt, ren, rk, bc_lo, bc_hi, inflow, periodic, reflect_periodic=True,
+           explicit=False):
     """One 3D RK pseudo-stage; returns (new u*, momentum rhs). h = (dx, dy, dz).
     reflect_periodic=False skips the normal-flux reflection and keeps the
-    pressure ghosts' periodic wrap in periodic directions (fix_quirks = 1)."""
+    pressure ghosts' periodic wrap in periodic directions (fix_quirks = 1).
+    explicit=True: the explicit predictor (momentum.cpp:96-192) with no
+    normal-flux reflection at all (quirk Q3)."""
     c = cont2cart3(us, n, bc_lo, bc_hi, inflow, periodic)
     inner = slice(G, G + n)
     total = []
@@ -87,7 +90,7 @@ def stage3(us, ub, un, du, p, n, h, dt, ren, rk, bc_lo, bc_hi, inflow, periodic,
                 total[m][_box(0, a, box1)] = total[m][_box(n, a, box1)]
                 total[m][_box(n + 1, a, box1)] = total[m][_box(1, a, box1)]
     for d in range(3):
-        if periodic[d] and not reflect_periodic:
+        if explicit or (periodic[d] and not reflect_periodic):
             continue
         a = _axis(d)
         total[d][_box(0, a, box1)] = -total[d][_box(1, a, box1)]
@@ -104,6 +107,11 @@ def stage3(us, ub, un, du, p, n, h, dt, ren, rk, bc_lo, bc_hi, inflow, periodic,
         gp = (pp[_box(slice(1, n + 2), a, box1)] - pp[_box(slice(0, n + 1), a, box1)]) / h[d]
         t = total[d]
         r = -gp + 0.5 * (t[_box(slice(0, n + 1), a, box1)] + t[_box(slice(1, n + 2), a, box1)])
+        if explicit:
+            r = r + (1.0 / (2.0 * dt)) * du[d]
+            rhs.append(r)
+            out.append(us[d] + ((dt / 1.5) * r))
+            continue
         r = r - (1.5 / dt) * (us[d] - un[d]) + (0.5 / dt) * du[d]
         rhs.append(r)
         out.append(ub[d] + (rk * r))

@@ -388,3 +388,50 @@ def test_stage_3d_matches_numpy_restatement(oracle_lib, case):
         np.testing.assert_array_equal(o.field(FIELD_MRHS, d), rhs[d])
         np.testing.assert_array_equal(o.field(FIELD_STAR, d), ref[d])
     o.close()
+
+
+@pytest.mark.parametrize("dim,periodic", [(2, False), (2, True), (3, False), (3, True)])
+def test_explicit_predictor_matches_numpy_restatement(oracle_lib, dim, periodic):
+    """The explicit predictor (PSEUDO_TIMESTEPPING = 0, main.cpp:902-925,
+    explicit_time_marching momentum.cpp:96-192) of the oracle against the
+    numpy stage in its explicit mode, bit for bit: no normal-flux reflection
+    (quirk Q3), R += du / (2 dt), u* += (dt / 1.5) R; the lid cavity and the
+    periodic box, 2D and 3D."""
+    from amressif_gb300 import workloads as wl
+    from tests import npstage3
+
+    n = 24 if dim == 2 else 12
+    L = 2 * math.pi
+    if periodic:
+        kw = dict(prob_hi=(L, L, L), bc_lo=(111,) * 3, bc_hi=(111,) * 3)
+        h, per = L / n, (True,) * dim
+        bc_lo, bc_hi = (111,) * 3, (111,) * 3
+    else:
+        kw = dict(bc_lo=(135, 135, 135), bc_hi=(135, 165, 135))
+        h, per = 1.0 / n, (False,) * dim
+        bc_lo, bc_hi = (135, 135, 135), (135, 165, 135)
+    o = Oracle(n, dim=dim, ren=100.0, dt=0.25 * h, pseudo_timestepping=0, **kw)
+    if dim == 3 and periodic:
+        o.set_state(*wl.tgv3d_perturbed_state(n, amp=1e-3, seed=0))
+    else:
+        o.init(1 if periodic else 0)
+    run_steps(o, 2)
+    u, up, p, _ = o.get_state()
+    o.set_state(u, up, p)
+    o.step_begin()
+    un = [o.field(2, d) for d in range(dim)]
+    du = [o.field(3, d) for d in range(dim)]
+    us = [o.field(FIELD_STAR, d) for d in range(dim)]
+    ub = [o.field(FIELD_BASE, d) for d in range(dim)]
+    dt = o.params.dt
+    if dim == 2:
+        ref, rhs = npstage.stage(us, ub, un, du, p, n, h, h, dt, 100.0, 0.0, bc_lo[:2], bc_hi[:2], (1.0, 0.0), per,
+                                 explicit=True)
+    else:
+        ref, rhs = npstage3.stage3(us, ub, un, du, p, n, (h, h, h), dt, 100.0, 0.0, bc_lo, bc_hi, (1.0, 0.0, 0.0),
+                                   per, explicit=True)
+    o.explicit_predictor()
+    for d in range(dim):
+        np.testing.assert_array_equal(o.field(FIELD_MRHS, d), rhs[d])
+        np.testing.assert_array_equal(o.field(FIELD_STAR, d), ref[d])
+    o.close()
