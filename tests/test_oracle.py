@@ -16,7 +16,7 @@ import os
 import numpy as np
 import pytest
 
-from oracle.orc import FIELD_BASE, FIELD_MRHS, FIELD_STAR, Oracle
+from oracle.orc import FIELD_BASE, FIELD_MRHS, FIELD_P, FIELD_PRHS, FIELD_STAR, Oracle
 from tests import npstage
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
@@ -434,4 +434,104 @@ def test_explicit_predictor_matches_numpy_restatement(oracle_lib, dim, periodic)
     for d in range(dim):
         np.testing.assert_array_equal(o.field(FIELD_MRHS, d), rhs[d])
         np.testing.assert_array_equal(o.field(FIELD_STAR, d), ref[d])
+    o.close()
+
+
+@pytest.mark.parametrize("dim,case", [(2, "cavity"), (2, "tgv_parity"), (2, "tgv_fixed"),
+                                      (3, "cavity"), (3, "tgv_parity"), (3, "tgv_fixed")])
+def test_poisson_rhs_and_projection_match_numpy(oracle_lib, dim, case):
+    """poisson_righthand_side_calc (fn_rhs.cpp:71-125: the divergence, then
+    times 1.5/dt) and update_solution (poisson.cpp:192-310: u = u* -
+    (grad phi dt)/1.5 with the phi ghosts mirrored (quirk Q2) or, with
+    fix_quirks in periodic directions, wrapped; p += phi) of the oracle
+    against numpy, bit for bit, after the oracle's own solve."""
+    from amressif_gb300 import workloads as wl
+
+    n = 24 if dim == 2 else 12
+    L = 2 * math.pi
+    fq = 1 if case == "tgv_fixed" else 0
+    if case == "cavity":
+        kw = dict(bc_lo=(135, 135, 135), bc_hi=(135, 165, 135))
+        h, per = 1.0 / n, False
+    else:
+        kw = dict(prob_hi=(L, L, L), bc_lo=(111,) * 3, bc_hi=(111,) * 3)
+        h, per = L / n, True
+    o = Oracle(n, dim=dim, ren=100.0, dt=0.25 * h, fix_quirks=fq, **kw)
+    if dim == 3 and per:
+        o.set_state(*wl.tgv3d_perturbed_state(n, amp=1e-3, seed=0))
+    elif dim == 2 and per:
+        o.set_state(*wl.tgv_perturbed_state(n, amp=1e-3, seed=0))
+    else:
+        o.init(0)
+    run_steps(o, 2)
+    u, up, p, _ = o.get_state()
+    o.set_state(u, up, p)
+    o.step_begin()
+    for sub in range(4):
+        o.rk_stage(sub)
+    o.pseudo_norm()
+    us = [o.field(FIELD_STAR, d) for d in range(dim)]
+    dt = o.params.dt
+    ax = [dim - 1 - d for d in range(dim)]  # arrays are [(k,) j, i]
+    div = None
+    for d in range(dim):
+        t = np.diff(us[d], axis=ax[d]) / h
+        div = t if div is None else div + t
+    o.poisson_rhs()
+    np.testing.assert_array_equal(o.field(FIELD_PRHS), (1.5 / dt) * div)
+    o.poisson_solve()
+    p0 = o.field(FIELD_P)
+    o.project()
+    ug, _, pg, phi = o.get_state()  # the solve's phi, copied into userCtx comp 1 by the projection
+    for d in range(dim):
+        wrap = per and fq == 1
+        pad = [(1, 1) if e == ax[d] else (0, 0) for e in range(dim)]
+        pp = np.pad(phi, pad, mode="wrap" if wrap else "edge")
+        g = np.diff(pp, axis=ax[d]) / h
+        np.testing.assert_array_equal(ug[d], us[d] - (g * dt) / 1.5, err_msg="component %d" % d)
+    np.testing.assert_array_equal(pg, p0 + phi)
+    o.close()
+
+
+@pytest.mark.parametrize("mgs", [(24, 24), (8, 12), (7, 10), (5, 24)])
+def test_pseudo_norm_matches_numpy(oracle_lib, mgs):
+    """Error_Computation (utilities.cpp:421-493 with StagL2Norm, :669-778):
+    e_d = sqrt(sum over each box's faces of w (u_base - u*)^2) / sqrt(N^2),
+    w = 1/2 on the first and last face of every box, the max over d. Summed
+    over the boxes of any maxSize split the weight of a face is 1/2 at the two
+    domain-boundary faces and 1 elsewhere (a face between two boxes gets 1/2
+    from each), so only the summation order depends on the split: the
+    oracle's value for each split against the split-free numpy sum, 1e-13.
+    The perturbed periodic box in the physical mode, where the boundary faces
+    carry nonzero increments (on a cavity's walls the normal velocity and its
+    increment are 0, and the unperturbed Taylor-Green u vanishes at x = 0 and
+    2 pi by symmetry)."""
+    from amressif_gb300 import workloads as wl
+
+    n = 24
+    L = 2 * math.pi
+    o = Oracle(n, ren=100.0, dt=0.25 * L / n, max_grid_size=(mgs[0], mgs[1], 1), prob_hi=(L, L, L),
+               bc_lo=(111,) * 3, bc_hi=(111,) * 3, fix_quirks=1)
+    o.set_state(*wl.tgv_perturbed_state(n, amp=1e-2, seed=0))
+    run_steps(o, 2)
+    u, up, p, _ = o.get_state()
+    o.set_state(u, up, p)
+    o.step_begin()
+    for sub in range(4):
+        o.rk_stage(sub)
+    ub = [o.field(FIELD_BASE, d) for d in range(2)]
+    us = [o.field(FIELD_STAR, d) for d in range(2)]
+    eo = o.pseudo_norm()
+    e = []
+    for d in range(2):
+        q2 = (ub[d] - us[d]) ** 2
+        w = np.ones(n + 1)
+        w[0] = w[n] = 0.5
+        q2 = q2 * (w[None, :] if d == 0 else w[:, None])
+        e.append(math.sqrt(q2.sum()) / math.sqrt(n * n))
+    assert eo > 0
+    assert abs(eo - max(e)) <= 1e-13 * eo, (eo, max(e))
+    # the half weights matter here: weight 1 on every face gives another value
+    e1 = max(math.sqrt(((ub[d] - us[d]) ** 2).sum()) / math.sqrt(n * n) for d in range(2))
+    assert abs(e1 - eo) > 1e-6 * eo
     o.close()
