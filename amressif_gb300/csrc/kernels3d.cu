@@ -74,6 +74,10 @@ cudaError_t launch3_dcff(const DCff3& a, cudaStream_t s) {
   k3_dcff<<<grid3(a.n, a.n, a.n), 256, 0, s>>>(a);
   return cudaGetLastError();
 }
+cudaError_t launch3_dc64(const DCff3& a, cudaStream_t s) {
+  k3_dc64<<<grid3(a.n, a.n, a.n), 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
 cudaError_t launch3_rhs_ff(int n, long pitch, long plane, const double* f, const double* mean, float2* out, cudaStream_t s) {
   k3_rhs_ff<<<grid3(n, n, n), 256, 0, s>>>(n, pitch, plane, f, mean, out);
   return cudaGetLastError();

@@ -24,6 +24,7 @@ cudaError_t launch3f_total(const AncFF& a, cudaStream_t s);  // fluxes, then cel
 cudaError_t launch3f_face(const AncFF& a, cudaStream_t s);
 cudaError_t launch3f_store(const Geom& g, const float2* const* in, double* const* out, cudaStream_t s);
 cudaError_t launch3_dcff(const DCff3& a, cudaStream_t s);
+cudaError_t launch3_dc64(const DCff3& a, cudaStream_t s);  // dc_residual = 1
 cudaError_t launch3_rhs_ff(int n, long pitch, long plane, const double* f, const double* mean, float2* out, cudaStream_t s);
 cudaError_t launch3_ff_cells(int n, long pitch, long plane, const float2* in, double* out, cudaStream_t s);
 cudaError_t launch3i_cart(const Inc3& a, cudaStream_t s);

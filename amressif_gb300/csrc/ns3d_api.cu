@@ -209,10 +209,14 @@ int poisson3(ns_ctx* c, bool mixed, int* cycles, double* res, long long* fallbac
     return st;
   }
   // mixed: phi as float-float pairs in PHF[pf]; each sweep adds the FP32
-  // correction and recomputes the residual (k3_dcff), phi goes to FP64 at the end
+  // correction and recomputes the residual (k3_dcff), phi goes to FP64 at the
+  // end. dc_residual = 1: phi and the residual in FP64 from the first sweep
+  // (k3_dc64), phi in P64[pf]
   DCff3 dc;
   std::memset(&dc, 0, sizeof(dc));
   int pf = 0;
+  const bool dc64 = mixed && c->P.dc_residual == 1;
+  double* P64[2] = {S.PHI, S.PHI2};
   if (mixed) {
     dc.n = c->N;
     dc.pitch = c->pitch;
@@ -227,15 +231,23 @@ int poisson3(ns_ctx* c, bool mixed, int* cycles, double* res, long long* fallbac
     dc.part = S.part;
     dc.counter = c->counter;
     dc.red_out = c->red + kRedRes;
-    LAUNCH(NS_PROF_DC_UPDATE, "f - mean (ff)", launch3_rhs_ff(c->N, dc.pitch, dc.plane, S.F, c->red + kRedMean, S.FF, c->st));
+    if (dc64) {
+      dc.f64 = S.F;
+      dc.fmean = c->red + kRedMean;
+      for (int d = 0; d < 3; ++d) dc.ih64[d] = S.M64.ih[0][d];
+    } else {
+      LAUNCH(NS_PROF_DC_UPDATE, "f - mean (ff)", launch3_rhs_ff(c->N, dc.pitch, dc.plane, S.F, c->red + kRedMean, S.FF, c->st));
+    }
   }
   auto residual = [&](bool first) -> int {
     if (mixed) {
       dc.first = first;
       dc.phin = S.PHF[pf];
       dc.phout = S.PHF[first ? pf : 1 - pf];
+      dc.phin64 = P64[pf];
+      dc.phout64 = P64[first ? pf : 1 - pf];
       dc.e = first ? nullptr : S.M32.x[0];
-      LAUNCH(NS_PROF_DC_UPDATE, "dc update", launch3_dcff(dc, c->st));
+      LAUNCH(NS_PROF_DC_UPDATE, "dc update", dc64 ? launch3_dc64(dc, c->st) : launch3_dcff(dc, c->st));
       if (!first) pf = 1 - pf;
     } else {
       LAUNCH(NS_PROF_MG_RESNORM, "resnorm", launch3_mg_resnorm<double>(S.M64, S.part, c->counter, c->red + kRedRes, c->st));
@@ -263,7 +275,11 @@ int poisson3(ns_ctx* c, bool mixed, int* cycles, double* res, long long* fallbac
     rn = c->red_h[kRedRes];
     if (rn < 0.5 * best) { best = rn; stall = 0; } else if (++stall >= 6) { status = NS_ERR_MG_STALL; break; }
   }
-  if (mixed) LAUNCH(NS_PROF_DC_UPDATE, "phi to FP64", launch3_ff_cells(c->N, dc.pitch, dc.plane, S.PHF[pf], S.PHI, c->st));
+  if (dc64) {
+    if (P64[pf] != S.PHI) CK(cudaMemcpyAsync(S.PHI, P64[pf], S.fb, cudaMemcpyDeviceToDevice, c->st), "phi copy");
+  } else if (mixed) {
+    LAUNCH(NS_PROF_DC_UPDATE, "phi to FP64", launch3_ff_cells(c->N, dc.pitch, dc.plane, S.PHF[pf], S.PHI, c->st));
+  }
   (void)fallbacks;
   *cycles = ncyc;
   *res = r0 > 0 ? rn / r0 : 0.0;
@@ -341,6 +357,7 @@ int create3d(ns_ctx* c) {
     }
     for (int b = 0; b < 2 && r == NS_OK; ++b) r = alloc3(c, &S.PHF[b], S.fb);
     if (r == NS_OK) r = alloc3(c, &S.FF, S.fb);
+    if (r == NS_OK && c->P.dc_residual == 1) r = alloc3(c, &S.PHI2, S.fb);
   }
   return r;
 }

@@ -82,6 +82,12 @@ struct DCff3 {
   double* part;
   unsigned* counter;
   double* red_out;     // max |r|
+  // dc_residual = 1 (k3_dc64): phi and the residual in FP64
+  const double* phin64;
+  double* phout64;
+  const double* f64;   // f; the kernel subtracts *fmean
+  const double* fmean;
+  double ih64[3];      // the FP64 level-0 1/h^2
 };
 
 #ifndef NS_3D_ARGS_ONLY
@@ -502,6 +508,42 @@ __global__ void __launch_bounds__(256) k3_dcff(DCff3 A) {
     const ff r = ld2(A.f, id) - lap;
     st2(A.phout, id, xc);
     const float r1 = ff_round(r);
+    A.r32[id] = r1;
+    v[0] = fabsf(r1);
+  }
+  double out[1];
+  if (grid_reduce_last_f<1, 256>(v, reinterpret_cast<float2*>(A.part), A.counter, 1u, out) && threadIdx.x == 0)
+    A.red_out[0] = out[0];
+}
+
+// ---- FP64 defect correction (dc_residual = 1) ---------------------------------------------
+// phi_out = phi_in + e (FP64 + FP32), r = (f - mean f) - L phi_out in FP64,
+// r32 = float(r), max |r|: the same sweep as k3_dcff with an FP64 phi
+__device__ __forceinline__ double dc64_val(const DCff3& A, long id) {
+  if (A.first) return 0.0;
+  const double v = __ldg(A.phin64 + id);
+  return A.e ? v + (double)ldf(A.e, id) : v;
+}
+
+__global__ void __launch_bounds__(256) k3_dc64(DCff3 A) {
+  const int n = A.n;
+  const int i = blockIdx.x * 32 + (threadIdx.x & 31), j = blockIdx.y * 8 + (threadIdx.x >> 5), k = blockIdx.z;
+  float v[1] = {0.f};
+  if (i < n && j < n && k < n) {
+    const long id = (long)k * A.plane + (long)j * A.pitch + i;
+    const int c[3] = {i, j, k};
+    const long st[3] = {1, A.pitch, A.plane};
+    const double xc = dc64_val(A, id);
+    double lap = 0.0;
+    for (int d = 0; d < 3; ++d) {
+      double s = 0.0;
+      if (A.periodic[d] || c[d] + 1 < n) s += dc64_val(A, id + ((c[d] + 1 < n) ? st[d] : -(long)(n - 1) * st[d])) - xc;
+      if (A.periodic[d] || c[d] > 0) s += dc64_val(A, id + ((c[d] > 0) ? -st[d] : (long)(n - 1) * st[d])) - xc;
+      lap += A.ih64[d] * s;
+    }
+    const double r = (__ldg(A.f64 + id) - *A.fmean) - lap;
+    A.phout64[id] = xc;
+    const float r1 = (float)r;
     A.r32[id] = r1;
     v[0] = fabsf(r1);
   }

@@ -332,7 +332,6 @@ int ns_ctx_create(const ns_params* p, void* stream, ns_ctx** out) {
   }
   if (!(p->ren > 0)) return NS_ERR_ARG;
   if (p->dc_residual != 0 && p->dc_residual != 1) return NS_ERR_ARG;
-  if (D == 3 && p->dc_residual == 1) return NS_ERR_UNSUPPORTED;  // the 3D defect correction is float-float
   if (p->poisson_warm_start != 0 && p->poisson_warm_start != 1) return NS_ERR_ARG;
   if (p->conv_scheme < NS_CONV_NEW_QUICK || p->conv_scheme > NS_CONV_UMIST_FORM) return NS_ERR_ARG;
   if (p->conv_scheme != NS_CONV_NEW_QUICK && p->precision == NS_PREC_MIXED) return NS_ERR_UNSUPPORTED;

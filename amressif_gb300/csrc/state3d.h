@@ -20,6 +20,7 @@ struct State3D {
   double* B[3][3] = {};
   double* Pp = nullptr;
   double* PHI = nullptr;
+  double* PHI2 = nullptr;  // dc_residual = 1: the other FP64 phi of the defect correction
   double* F = nullptr;
   double* PH[3] = {nullptr, nullptr, nullptr};  // ghosted cell velocity
   double* CART[3] = {nullptr, nullptr, nullptr};  // analytic first-stage cell velocity (allocated on first use)

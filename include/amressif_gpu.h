@@ -90,7 +90,7 @@ typedef struct ns_params {
   int gmres_restart;         /* Krylov vectors per GMRES cycle (<= 31) */
   int dc_residual;           /* NS_PREC_MIXED Poisson: the defect correction's residual and phi in
                                 0 = float-float (about 48 bits; FP64 once its floor is reached),
-                                1 = FP64 from the first sweep (2D; NS_ERR_UNSUPPORTED in 3D) */
+                                1 = FP64 from the first sweep (2D and 3D) */
   int poisson_warm_start;    /* NS_PREC_MIXED Poisson (2D, float-float defect correction): 1 = start from
                                 the previous step's phi instead of zero (poisson.cpp:63 starts from zero).
                                 The tolerance stays relative to the zero-guess residual max|f - mean f|,

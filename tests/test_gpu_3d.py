@@ -76,14 +76,19 @@ def test_3d_steps_resynced(gpu_lib, oracle_lib, name):
     o.close()
 
 
-def test_3d_mixed_poisson_matches_fp64(gpu_lib):
+@pytest.mark.parametrize("dc_residual", [0, 1])
+def test_3d_mixed_poisson_matches_fp64(gpu_lib, dc_residual):
+    """The mixed solve (FP32 V-cycles inside the defect correction; its
+    residual and phi in float-float, dc_residual 0, or FP64, 1) against the
+    FP64 solver over three steps: the same pseudo-iteration counts, u and p
+    within 1e-10."""
     n = 32
     kw = dict(ren=1600.0, prob_hi=(L2PI,) * 3, bc_lo=(111,) * 3, bc_hi=(111,) * 3, fix_quirks=1)
     dt = dt_of(n, kw)
     out = {}
     for prec in (ns.PREC_FP64, ns.PREC_MIXED):
         p = ns.default_params(dim=3, n_cell=n, fixed_dt=dt, iter_num=100, precision=prec, poisson_tol_rel=1e-12,
-                              poisson_tol_div=1e-10, max_grid_size=(n, n, n), **kw)
+                              poisson_tol_div=1e-10, max_grid_size=(n, n, n), dc_residual=dc_residual, **kw)
         s = ns.Solver(p)
         s.set_state(*wl.tgv3d_perturbed_state(n, amp=1e-3, seed=0))
         ks = [s.step()["pseudo_iters"] for _ in range(3)]

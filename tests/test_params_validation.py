@@ -24,7 +24,6 @@ def create(gpu_lib, **kw):
     (dict(ren=0.0), ns.NS_ERR_ARG),
     (dict(ren=float("nan")), ns.NS_ERR_ARG),
     (dict(dc_residual=2), ns.NS_ERR_ARG),
-    (dict(dim=3, n_cell=16, dc_residual=1), ns.NS_ERR_UNSUPPORTED),
     (dict(dim=4), ns.NS_ERR_UNSUPPORTED),
     # periodic on one side only: the reference makes a direction periodic only when both
     # codes are 111 (main.cpp:160-162) yet gives the 111 side an interior BC type
