@@ -31,6 +31,9 @@ L2PI = 2 * math.pi
 CASES3 = {
     # name: (n, kwargs shared by the oracle and the GPU, periodic TGV input)
     "cavity16": (16, dict(ren=100.0, bc_lo=(135, 135, 135), bc_hi=(135, 165, 135)), False),
+    # a west inlet (-165), slip walls south, bottom and top, the east code 1 that the reference
+    # reads as slip, and the lid: every ghost rule of cont2cart (utilities.cpp:62-349) in 3D
+    "walls16": (16, dict(ren=100.0, bc_lo=(-165, -135, -135), bc_hi=(1, 165, -135)), False),
     "tgv16_parity": (16, dict(ren=1600.0, prob_hi=(L2PI,) * 3, bc_lo=(111,) * 3, bc_hi=(111,) * 3), True),
     "tgv24_fixed": (24, dict(ren=1600.0, prob_hi=(L2PI,) * 3, bc_lo=(111,) * 3, bc_hi=(111,) * 3, fix_quirks=1), True),
 }
@@ -159,6 +162,10 @@ def test_3d_building_blocks(gpu_lib, oracle_lib, name):
         x.set_state(uo, upo, po)
     o.step_begin()
     s.step_begin()
+    # the pseudo-increments near convergence (norm ~1e-11) carry the round-off of
+    # the velocities, which the GPU's FMA and the oracle's separate roundings make
+    # differently: the norms agree to 1e-9 relative or to eps max|u| absolute
+    floor = 2.2e-16 * max(float(np.abs(a).max()) for a in uo)
     K = 0
     while True:
         for sub in range(4):
@@ -168,7 +175,7 @@ def test_3d_building_blocks(gpu_lib, oracle_lib, name):
             for d in range(3):
                 assert rel(s.get_field(ns.FIELD_VEL_STAR, d), o.field(FIELD_STAR, d)) <= 1e-13
         eo, eg = o.pseudo_norm(), s.pseudo_norm()
-        assert abs(eg - eo) <= 1e-9 * eo, (K, eg, eo)
+        assert abs(eg - eo) <= 1e-9 * eo + floor, (K, eg, eo)
         K += 1
         if eo <= 1e-10 or K > 100:
             break
