@@ -13,7 +13,12 @@
  * known answers the reference's own formulas give: the discrete Taylor-Green
  * decay, zero discrete divergence after projection, zero wall-normal velocity,
  * the BDF2 fixed-point identity of the pseudo-time loop, and an independent
- * DCT/FFT solve of the same discrete Poisson problem (see tests/).
+ * DCT/FFT solve of the same discrete Poisson problem; against the RK
+ * coefficient vector that the reference's only test prints
+ * (Tests/loop_test/forloopforvec.cpp); and, bit for bit, against independent
+ * vectorised restatements of the RK stage (2D and 3D, every ghost rule and
+ * convective routine), the explicit predictor, the Poisson right-hand side,
+ * the projection and the box-weighted pseudo-norm (see tests/).
  *
  * Field exchange layout (all arrays dense, x fastest, no ghosts):
  *   face array of direction d : extent N+1 along d, N along the others
