@@ -21,7 +21,7 @@ constexpr int kMaxLevels = 16;
 // levels with n <= kBottomN live in the bottom CTA: x, f, r of each level and
 // the coarsest level's CG vectors in dynamic shared memory, at most 43 KB in
 // FP64 (a lone 30^2 coarsest level), within the default 48 KB. The 64^2 level
-// in the block as well made the 4096^2 V-cycle slower (0.4855 against 0.476 ms)
+// in the block as well made the 4096^2 V-cycle slower (0.4855 against 0.476 ms).
 constexpr int kBottomN = 32;
 
 template <typename T>
