@@ -9,6 +9,11 @@ cavity32_exec_inputs.npz: the shipped inputs-file physics (n_cell 32, boxes
 32x16, Re 100, fixed_dt 1e-3, 11 steps, lid u = 1), every step: u, v, p
 (mean removed) and the pseudo-iteration count K.
 
+cavity16_3d.npz: the lid cavity in the AMREX_SPACEDIM = 3 build (16^3 cells,
+one box, Re 100, fixed_dt 0.4 dx, lid u = 1), 5 steps from rest: K of each
+step, the kinetic energy of each step, and the final u, v, w and p (mean
+removed).
+
 Run: python tests/golden/make_golden.py
 """
 import os
@@ -38,6 +43,22 @@ def cavity32():
     np.savez_compressed(os.path.join(HERE, "cavity32_exec_inputs.npz"), **out)
 
 
+def cavity16_3d():
+    n = 16
+    o = Oracle(n, dim=3, max_grid_size=(n, n, n), ren=100.0, dt=0.4 / n, iter_num=100, poisson_tol=1e-13,
+               bc_lo=(135, 135, 135), bc_hi=(135, 165, 135))
+    o.init(0)
+    K, E = [], []
+    for _ in range(5):
+        s = o.step()
+        K.append(s["pseudo_iters"])
+        u, _, p, _ = o.get_state()
+        E.append(0.5 * sum(float((a * a).sum()) for a in u) / n ** 3)
+    out = {"nsteps": 5, "K": np.array(K), "energy": np.array(E), "u": u[0], "v": u[1], "w": u[2], "p": p - p.mean()}
+    np.savez_compressed(os.path.join(HERE, "cavity16_3d.npz"), **out)
+
+
 if __name__ == "__main__":
     cavity32()
+    cavity16_3d()
     print("ok")

@@ -393,3 +393,26 @@ def test_3d_gmres_option_resynced(gpu_lib, oracle_lib, name):
         if kw.get("fix_quirks") or not tgv:
             assert sg["div_after"] <= 1e-10
     o.close()
+
+
+
+def test_3d_free_running_matches_golden(gpu_lib):
+    """The committed 3D fixture (the oracle's 16^3 lid cavity, 5 free-running
+    steps from rest) against the FP64 3D path: the same pseudo-iteration
+    counts, the final velocity (all components) and p within 1e-10."""
+    import os
+
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "cavity16_3d.npz"))
+    n = 16
+    s = ns.Solver(ns.default_params(dim=3, n_cell=n, fixed_dt=0.4 / n, iter_num=100, precision=ns.PREC_FP64,
+                                    poisson_tol_rel=1e-13, max_grid_size=(n, n, n), ren=100.0,
+                                    bc_lo=(135, 135, 135), bc_hi=(135, 165, 135)))
+    s.init(ns.INIT_CAVITY)
+    for step in range(int(g["nsteps"])):
+        st = s.step()
+        assert st["pseudo_iters"] == int(g["K"][step]), (step, st["pseudo_iters"])
+    u, _, p, _ = s.get_state()
+    ru = math.sqrt(sum(np.linalg.norm(u[d] - g[k]) ** 2 for d, k in enumerate("uvw")) /
+                   sum(np.linalg.norm(g[k]) ** 2 for k in "uvw"))
+    assert ru <= 1e-10, ru
+    assert relp(p, g["p"]) <= 1e-10

@@ -280,6 +280,28 @@ def test_golden_fixtures(oracle_lib):
 # ---- the 3D restatement ----------------------------------------------------------------
 
 
+def test_golden_fixture_3d(oracle_lib):
+    """The committed 3D fixture (tests/golden/make_golden.py: the 16^3 lid
+    cavity, 5 steps from rest) against this build of the oracle: the same
+    pseudo-iteration counts, kinetic energies and final state."""
+    path = os.path.join(GOLDEN, "cavity16_3d.npz")
+    g = np.load(path)
+    n = 16
+    o = Oracle(n, dim=3, max_grid_size=(n, n, n), ren=100.0, dt=0.4 / n, iter_num=100, poisson_tol=1e-13,
+               bc_lo=(135, 135, 135), bc_hi=(135, 165, 135))
+    o.init(0)
+    for step in range(int(g["nsteps"])):
+        s = o.step()
+        assert s["pseudo_iters"] == int(g["K"][step])
+        u, _, p, _ = o.get_state()
+        e = 0.5 * sum(float((a * a).sum()) for a in u) / n ** 3
+        assert abs(e - g["energy"][step]) <= 1e-13 * g["energy"][step]
+    for d, key in enumerate("uvw"):
+        np.testing.assert_allclose(u[d], g[key], rtol=0, atol=1e-13)
+    np.testing.assert_allclose(p - p.mean(), g["p"], rtol=0, atol=1e-11)
+    o.close()
+
+
 def test_poisson_3d_matches_dct_solution_walls(oracle_lib):
     """The 7-point cell-centred Laplacian with homogeneous Neumann walls, solved
     by the oracle's 3D multigrid + CG, against the exact solution of the same
