@@ -266,8 +266,11 @@ DTYPE_MIXED = ("mixed: float-float anchors and fp32 increment stages in the pred
 def bench_config(n, world):
     """The `config` of both arms (the same dict, so that the two lines name
     the same workload); the window of timed steps is a key of its own."""
+    field_mb = (n + 1) * n * 4 / 1e6  # the smallest field: one FP32 face array
+    l2 = ("inputs larger than L2 (every field is >=%.0f MB, the step touches >1 GB)" % field_mb if field_mb * 10 > 129
+          else "inputs smaller than L2 at this size (%.2f MB a field): no flush" % field_mb)
     return {"workload": WORKLOAD % (n, n), "n_cell": n, "parallelism": "replicas" if world > 1 else "single GPU",
-            "l2_flush": "inputs larger than L2 (every field is >=67 MB, the step touches >1 GB)"}
+            "l2_flush": l2}
 
 
 def run_steps(s, k):
