@@ -588,3 +588,37 @@ def test_stage_wall_rules_match_numpy_restatement(oracle_lib, bc_lo, bc_hi):
         np.testing.assert_array_equal(o.field(FIELD_MRHS, d), rhs[d])
         np.testing.assert_array_equal(o.field(FIELD_STAR, d), ref[d])
     o.close()
+
+
+@pytest.mark.parametrize("dim,fq", [(2, 0), (2, 1), (3, 0), (3, 1)])
+def test_tgv_init_matches_analytic_fields(oracle_lib, dim, fq):
+    """hybrid_grid_init's Taylor-Green case (fn_init.cpp:61-229, kn_init.H:8-37)
+    in the oracle against the formulas: u = sin x cos y at the x faces
+    (i dx, (j + 1/2) dy), v = -cos x sin y at the y faces, w = 0 (the 3D build
+    keeps the 2D vortex: its z factors are commented out), p = (cos 2x +
+    cos 2y) / 4 at the cells, and u^{n-1} = u exp(2 nu dt) with nu = 1 (quirk
+    Q6) or 1/Re (fix_quirks). NumPy's sin / cos may differ from the C
+    library's in the last bit: 1e-15."""
+    n = 16
+    L = 2 * math.pi
+    ren, dt = 100.0, 0.1
+    o = Oracle(n, dim=dim, ren=ren, dt=dt, prob_hi=(L, L, L), bc_lo=(111,) * 3, bc_hi=(111,) * 3, fix_quirks=fq)
+    o.init(1)
+    u, up, p, _ = o.get_state()
+    h = L / n
+    nu = 1.0 / ren if fq else 1.0
+    decay = math.exp(-2.0 * nu * (0.0 - dt))
+    fi, ci = np.arange(n + 1) * h, (np.arange(n) + 0.5) * h  # face and cell coordinates
+    ref_u = np.sin(fi)[None, :] * np.cos(ci)[:, None]          # [j, i], x faces
+    ref_v = -np.cos(ci)[None, :] * np.sin(fi)[:, None]         # [j, i], y faces
+    ref_p = 0.25 * (np.cos(2 * ci)[None, :] + np.cos(2 * ci)[:, None])
+    if dim == 3:
+        ref_u, ref_v, ref_p = (np.broadcast_to(a, (n,) + a.shape) for a in (ref_u, ref_v, ref_p))
+        np.testing.assert_array_equal(u[2], 0.0)
+        np.testing.assert_array_equal(up[2], 0.0)
+    np.testing.assert_allclose(u[0], ref_u, rtol=0, atol=1e-15)
+    np.testing.assert_allclose(u[1], ref_v, rtol=0, atol=1e-15)
+    np.testing.assert_allclose(up[0], ref_u * decay, rtol=0, atol=1e-15)
+    np.testing.assert_allclose(up[1], ref_v * decay, rtol=0, atol=1e-15)
+    np.testing.assert_allclose(p, ref_p, rtol=0, atol=1e-15)
+    o.close()
